@@ -1,0 +1,190 @@
+/*
+ * spectral_rbc.h -- C ABI of the GB300 spectral Rayleigh-Benard library.
+ *
+ * Drop-in boundary for rustpde's pseudo-spectral RBC time step.  The
+ * reference exposes Rust traits, not an FFI; every entry point below states
+ * the reference item it replaces (paths relative to the rustpde repository).
+ *
+ * Conventions
+ *  - Every function returns an int status: RBC_OK (0) or a negative error
+ *    code; rbc_last_error() returns the message of the last failure on the
+ *    calling thread.  No call aborts the process or traps on the device.
+ *  - Arrays are row-major (x, y) with y contiguous, like the reference's
+ *    ndarray default.  Complex spectral arrays are interleaved (re, im)
+ *    doubles, the memory layout of num_complex::Complex<f64>.
+ *  - A case handle is not thread-safe; different handles may be used from
+ *    different threads.  Each case owns a CUDA stream; stepping calls are
+ *    asynchronous and every state/diagnostic call synchronises that stream.
+ *  - `stream` arguments are cudaStream_t values passed as void* (NULL: the
+ *    legacy default stream).
+ */
+#ifndef SPECTRAL_RBC_H
+#define SPECTRAL_RBC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define RBC_OK 0
+#define RBC_ERR_INVALID (-1)     /* bad argument: size mismatch, null pointer, range */
+#define RBC_ERR_CUDA (-2)        /* CUDA runtime failure */
+#define RBC_ERR_NUMERIC (-3)     /* non-finite value detected in the state */
+#define RBC_ERR_UNSUPPORTED (-4) /* valid request the library does not implement */
+#define RBC_ERR_NOMEM (-5)       /* device allocation failed / budget exceeded */
+
+/* ---- enums -------------------------------------------------------------- */
+/* case kinds: Navier2D::new(adiabatic=true/false), Navier2D::new_periodic */
+#define RBC_BOX_ADIABATIC 0
+#define RBC_BOX_CONDUCTING 1
+#define RBC_PERIODIC 2
+/* arithmetic of the time step */
+#define RBC_PREC_FP64 0
+#define RBC_PREC_MIXED 1
+/* fields (Navier2D public fields, src/navier/navier.rs:153-170) */
+#define RBC_TEMP 0
+#define RBC_UX 1
+#define RBC_UY 2
+#define RBC_PRES 3        /* pres[0] */
+#define RBC_PSEUDO_PRES 4 /* pres[1] */
+#define RBC_FIELDBC 5     /* fieldbc (read only) */
+/* diagnostics */
+#define RBC_NU 0       /* eval_nu       src/navier/functions.rs:12-36 */
+#define RBC_NUVOL 1    /* eval_nuvol    functions.rs:42-75 */
+#define RBC_RE 2       /* eval_re       functions.rs:82-101 */
+#define RBC_KE 3       /* <(ux^2+uy^2)/2> with the volume weights of Field2::average */
+#define RBC_DIV_NORM 4 /* ||divergence||_2, the quantity Navier2D::exit tests (navier.rs:855-862) */
+
+typedef struct RbcParams {
+  int nx, ny;       /* modes in x and y */
+  double ra, pr;    /* Rayleigh and Prandtl numbers */
+  double dt;        /* time step */
+  double aspect;    /* aspect ratio L/H */
+  int kind;         /* RBC_BOX_ADIABATIC / RBC_BOX_CONDUCTING / RBC_PERIODIC */
+  int precision;    /* RBC_PREC_FP64 (RBC_PREC_MIXED: see rbc_batch_*) */
+} RbcParams;
+
+typedef struct RbcCase RbcCase;
+
+const char* rbc_last_error(void);
+/* library version string */
+const char* rbc_version(void);
+
+/* ---- case lifecycle ------------------------------------------------------
+ * Replaces Navier2D::new (navier.rs:219-307) and Navier2D::new_periodic
+ * (navier.rs:384-467).  The state starts at zero; the reference's unseeded
+ * random_disturbance(0.1) is available seeded as rbc_random_disturbance. */
+int rbc_create(const RbcParams* params, RbcCase** out);
+int rbc_destroy(RbcCase* c);
+/* nu, ka, ra, pr, dt, scale_x, scale_y (navier.rs:46-55 get_nu/get_ka) */
+int rbc_get_params(const RbcCase* c, double out[7]);
+
+/* ---- initial conditions ---------------------------------------------------
+ * set_velocity navier.rs:927-931, set_temperature :934-936,
+ * random_disturbance :939-948 (seeded: splitmix64, row-major draws). */
+int rbc_set_velocity(RbcCase* c, double amp, double m, double n);
+int rbc_set_temperature(RbcCase* c, double amp, double m, double n);
+int rbc_random_disturbance(RbcCase* c, double amp, uint64_t seed);
+/* temperature = amp*(2u-1) at interior points (0 on walls), u ~ splitmix64(seed) */
+int rbc_set_temperature_noise(RbcCase* c, double amp, uint64_t seed);
+
+/* ---- stepping -------------------------------------------------------------
+ * rbc_step: Integrate::update (src/lib.rs:137, navier.rs:737-765), nsteps
+ * times, enqueued on the case stream (asynchronous). */
+int rbc_step(RbcCase* c, int nsteps);
+int rbc_synchronize(RbcCase* c);
+int rbc_get_time(const RbcCase* c, double* t);   /* Integrate::get_time lib.rs:139 */
+int rbc_set_time(RbcCase* c, double t);          /* Navier2D::reset_time navier.rs:951 */
+int rbc_get_dt(const RbcCase* c, double* dt);    /* Integrate::get_dt lib.rs:141 */
+/* bit 0: a non-finite value was written to the state since creation */
+int rbc_status(RbcCase* c, int* status);
+/* Integrate::exit (navier.rs:855-862): *stop = 1 if ||div|| is NaN */
+int rbc_exit(RbcCase* c, int* stop);
+/* integrate() (lib.rs:155-187): step until max_time; call cb(case, time, user)
+ * whenever time % save_intervall is within dt/2 (save_intervall <= 0: never);
+ * a non-zero return of cb stops the loop.  steps_done may be NULL. */
+typedef int (*rbc_callback)(RbcCase* c, double time, void* user);
+int rbc_integrate(RbcCase* c, double max_time, double save_intervall, rbc_callback cb, void* user,
+                  long* steps_done);
+
+/* ---- state ----------------------------------------------------------------
+ * The spectral arrays (Field2::vhat).  n_doubles must equal the array size
+ * in doubles (complex arrays count 2 per element). */
+int rbc_field_shape(const RbcCase* c, int field, int* n0, int* n1, int* is_complex);
+int rbc_get_state(RbcCase* c, int field, double* host, size_t n_doubles);
+int rbc_set_state(RbcCase* c, int field, const double* host, size_t n_doubles);
+/* Field2::backward of a field (physical nx x ny values) */
+int rbc_get_physical(RbcCase* c, int field, double* host, size_t n_doubles);
+/* Field2 grid coordinates of a field (scaled by the aspect ratio as
+ * Navier2D::_scale does for temp/ux/uy/pres) */
+int rbc_get_coords(const RbcCase* c, int field, double* x, double* y);
+/* diagnostics: RBC_NU, RBC_NUVOL, RBC_RE, RBC_KE, RBC_DIV_NORM */
+int rbc_eval(RbcCase* c, int what, double* out);
+int rbc_get_stream(RbcCase* c, void** stream);
+/* device bytes held by the case (state, scratch, operators) */
+int rbc_device_bytes(const RbcCase* c, size_t* bytes);
+
+/* Time the kernels of the step individually: runs nsteps steps launching each
+ * stage on the case stream between CUDA events; stage_ms[k] receives the mean
+ * duration of stage k (at most max_stages entries), *nstages the count. */
+int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, int* nstages);
+/* name of stage k of the step (static string) */
+const char* rbc_stage_name(const RbcCase* c, int k);
+
+/* ---- device memory helpers (callers that do not link the CUDA runtime) ---- */
+int rbc_host_alloc_pinned(void** ptr, size_t bytes);
+int rbc_host_free_pinned(void* ptr);
+int rbc_dev_alloc(void** ptr, size_t bytes);
+int rbc_dev_free(void* ptr);
+int rbc_memcpy_h2d(void* dst, const void* src, size_t bytes);
+int rbc_memcpy_d2h(void* dst, const void* src, size_t bytes);
+int rbc_device_synchronize(void);
+
+/* ---- funspace primitives on device buffers ---------------------------------
+ * Space2::new(base0, base1) (funspace/src/space2.rs:37-50) with bases
+ * chebyshev / cheb_dirichlet / cheb_neumann / cheb_dirichlet_bc /
+ * cheb_neumann_bc / fourier_r2c (funspace/src/lib.rs:230-345).  Fourier is
+ * supported along axis 0 (the reference's R2c x R2r space). */
+#define FS_CHEBYSHEV 0
+#define FS_CHEB_DIRICHLET 1
+#define FS_CHEB_NEUMANN 2
+#define FS_CHEB_DIRICHLET_BC 3
+#define FS_CHEB_NEUMANN_BC 4
+#define FS_FOURIER_R2C 5
+/* shape selectors for fs_space_shape */
+#define FS_PHYSICAL 0
+#define FS_SPECTRAL 1
+#define FS_ORTHO 2
+
+typedef struct FsSpace FsSpace;
+int fs_space_create(int base0, int n0, int base1, int n1, FsSpace** out);
+int fs_space_destroy(FsSpace* s);
+int fs_space_shape(const FsSpace* s, int which, int* n0, int* n1, int* is_complex);
+/* Field2::forward / backward / to_ortho / from_ortho / gradient (src/field.rs:103-129) */
+int fs_forward(FsSpace* s, const double* d_phys, double* d_spec, void* stream);
+int fs_backward(FsSpace* s, const double* d_spec, double* d_phys, void* stream);
+int fs_to_ortho(FsSpace* s, const double* d_spec, double* d_ortho, void* stream);
+int fs_from_ortho(FsSpace* s, const double* d_ortho, double* d_spec, void* stream);
+/* scale: two doubles or NULL (None) */
+int fs_gradient(FsSpace* s, const double* d_spec, double* d_ortho, int deriv0, int deriv1, const double* scale,
+                void* stream);
+
+/* ---- solvers ----------------------------------------------------------------
+ * Hholtz::new (src/solver/hholtz.rs:42-76), HholtzAdi::new (hholtz_adi.rs:44-63),
+ * Poisson::new (poisson.rs:50-90); Solve::solve (src/solver.rs:56-64) maps an
+ * ortho-sized input to a spectral-sized output of the space. */
+#define SV_HHOLTZ 0
+#define SV_HHOLTZ_ADI 1
+#define SV_POISSON 2
+typedef struct SvSolver SvSolver;
+int sv_create(FsSpace* s, int kind, const double c[2], SvSolver** out);
+int sv_destroy(SvSolver* sv);
+int sv_solve(SvSolver* sv, const double* d_in, double* d_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPECTRAL_RBC_H */

@@ -1,0 +1,552 @@
+"""rustpde_gb300 -- GB300-native spectral Rayleigh-Benard time step.
+
+Python mirror of rustpde's public interface for the hot path, over the C ABI
+of ``libspectral_rbc.so`` (include/spectral_rbc.h):
+
+  * ``Navier2D.new`` / ``Navier2D.new_periodic`` / ``update`` / ``integrate``
+    (src/navier/navier.rs, src/lib.rs)
+  * ``Space2``, ``Field2`` with ``forward/backward/to_ortho/from_ortho/gradient``
+    and the bases ``chebyshev, cheb_dirichlet, cheb_neumann, cheb_dirichlet_bc,
+    cheb_neumann_bc, fourier_r2c`` (funspace, src/field.rs)
+  * ``Hholtz``, ``HholtzAdi``, ``Poisson`` solvers (src/solver/*.rs)
+
+All numerical work runs in the CUDA library; there is no CPU fallback.  If the
+library is not built, every entry point raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libspectral_rbc.so")
+
+RBC_OK = 0
+RBC_ERR_INVALID = -1
+RBC_ERR_CUDA = -2
+RBC_ERR_NUMERIC = -3
+RBC_ERR_UNSUPPORTED = -4
+RBC_ERR_NOMEM = -5
+
+BOX_ADIABATIC, BOX_CONDUCTING, PERIODIC = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+TEMP, UX, UY, PRES, PSEUDO_PRES, FIELDBC = 0, 1, 2, 3, 4, 5
+NU, NUVOL, RE, KE, DIV_NORM = 0, 1, 2, 3, 4
+CHEBYSHEV, CHEB_DIRICHLET, CHEB_NEUMANN, CHEB_DIRICHLET_BC, CHEB_NEUMANN_BC, FOURIER_R2C = range(6)
+HHOLTZ, HHOLTZ_ADI, POISSON = 0, 1, 2
+
+_lock = threading.Lock()
+_lib = None
+
+
+class RbcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class RbcParams(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("ra", ctypes.c_double), ("pr", ctypes.c_double),
+                ("dt", ctypes.c_double), ("aspect", ctypes.c_double), ("kind", ctypes.c_int),
+                ("precision", ctypes.c_int)]
+
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_SZ = ctypes.c_size_t
+CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, _P, _D, _P)
+
+_SIGNATURES = {
+    "rbc_last_error": (ctypes.c_char_p, []),
+    "rbc_version": (ctypes.c_char_p, []),
+    "rbc_create": (_I, [ctypes.POINTER(RbcParams), ctypes.POINTER(_P)]),
+    "rbc_destroy": (_I, [_P]),
+    "rbc_get_params": (_I, [_P, _DP]),
+    "rbc_set_velocity": (_I, [_P, _D, _D, _D]),
+    "rbc_set_temperature": (_I, [_P, _D, _D, _D]),
+    "rbc_random_disturbance": (_I, [_P, _D, ctypes.c_uint64]),
+    "rbc_set_temperature_noise": (_I, [_P, _D, ctypes.c_uint64]),
+    "rbc_step": (_I, [_P, _I]),
+    "rbc_synchronize": (_I, [_P]),
+    "rbc_get_time": (_I, [_P, _DP]),
+    "rbc_set_time": (_I, [_P, _D]),
+    "rbc_get_dt": (_I, [_P, _DP]),
+    "rbc_status": (_I, [_P, _IP]),
+    "rbc_exit": (_I, [_P, _IP]),
+    "rbc_integrate": (_I, [_P, _D, _D, CALLBACK, _P, ctypes.POINTER(ctypes.c_long)]),
+    "rbc_field_shape": (_I, [_P, _I, _IP, _IP, _IP]),
+    "rbc_get_state": (_I, [_P, _I, _DP, _SZ]),
+    "rbc_set_state": (_I, [_P, _I, _DP, _SZ]),
+    "rbc_get_physical": (_I, [_P, _I, _DP, _SZ]),
+    "rbc_get_coords": (_I, [_P, _I, _DP, _DP]),
+    "rbc_eval": (_I, [_P, _I, _DP]),
+    "rbc_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "rbc_device_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
+    "rbc_profile_step": (_I, [_P, _I, _DP, _I, _IP]),
+    "rbc_stage_name": (ctypes.c_char_p, [_P, _I]),
+    "rbc_host_alloc_pinned": (_I, [ctypes.POINTER(_P), _SZ]),
+    "rbc_host_free_pinned": (_I, [_P]),
+    "rbc_dev_alloc": (_I, [ctypes.POINTER(_P), _SZ]),
+    "rbc_dev_free": (_I, [_P]),
+    "rbc_memcpy_h2d": (_I, [_P, _P, _SZ]),
+    "rbc_memcpy_d2h": (_I, [_P, _P, _SZ]),
+    "rbc_device_synchronize": (_I, []),
+    "fs_space_create": (_I, [_I, _I, _I, _I, ctypes.POINTER(_P)]),
+    "fs_space_destroy": (_I, [_P]),
+    "fs_space_shape": (_I, [_P, _I, _IP, _IP, _IP]),
+    "fs_forward": (_I, [_P, _P, _P, _P]),
+    "fs_backward": (_I, [_P, _P, _P, _P]),
+    "fs_to_ortho": (_I, [_P, _P, _P, _P]),
+    "fs_from_ortho": (_I, [_P, _P, _P, _P]),
+    "fs_gradient": (_I, [_P, _P, _P, _I, _I, _DP, _P]),
+    "sv_create": (_I, [_P, _I, _DP, ctypes.POINTER(_P)]),
+    "sv_destroy": (_I, [_P]),
+    "sv_solve": (_I, [_P, _P, _P, _P]),
+}
+
+
+def lib():
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"{LIB_PATH} is missing: build it with python -m rustpde_gb300.build "
+                                   "(there is no CPU fallback)")
+            L = ctypes.CDLL(LIB_PATH)
+            for name, (res, args) in _SIGNATURES.items():
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != RBC_OK:
+        raise RbcError(rc, lib().rbc_last_error().decode())
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+# ---------------------------------------------------------------------------
+# device buffers (plain cudaMalloc through the C ABI)
+# ---------------------------------------------------------------------------
+class PinnedArray:
+    """A numpy view of page-locked host memory (cudaHostAlloc)."""
+
+    def __init__(self, shape, dtype=np.float64):
+        self.dtype = np.dtype(dtype)
+        n = int(np.prod(shape)) * self.dtype.itemsize
+        p = _P()
+        _check(lib().rbc_host_alloc_pinned(ctypes.byref(p), max(n, 16)))
+        self.ptr = p
+        buf = (ctypes.c_char * max(n, 16)).from_address(p.value)
+        self.array = np.frombuffer(buf, dtype=self.dtype, count=int(np.prod(shape))).reshape(shape)
+
+    def __del__(self):
+        p = getattr(self, "ptr", None)
+        if p is not None and _lib is not None:
+            self.array = None
+            _lib.rbc_host_free_pinned(p)
+            self.ptr = None
+
+
+class DeviceArray:
+    """A device array of float64 / complex128 values."""
+
+    def __init__(self, shape, complex_=False):
+        self.shape = tuple(int(s) for s in shape)
+        self.complex = bool(complex_)
+        self.nbytes = int(np.prod(self.shape)) * (16 if complex_ else 8)
+        p = _P()
+        _check(lib().rbc_dev_alloc(ctypes.byref(p), max(self.nbytes, 16)))
+        self.ptr = p
+
+    @classmethod
+    def from_host(cls, a):
+        a = np.ascontiguousarray(a)
+        cx = np.iscomplexobj(a)
+        a = a.astype(np.complex128 if cx else np.float64, copy=False)
+        d = cls(a.shape, cx)
+        _check(lib().rbc_memcpy_h2d(d.ptr, a.ctypes.data_as(_P), d.nbytes))
+        return d
+
+    def to_host(self):
+        out = np.empty(self.shape, dtype=np.complex128 if self.complex else np.float64)
+        _check(lib().rbc_memcpy_d2h(out.ctypes.data_as(_P), self.ptr, self.nbytes))
+        return out
+
+    def __del__(self):
+        p = getattr(self, "ptr", None)
+        if p is not None and _lib is not None:
+            _lib.rbc_dev_free(p)
+            self.ptr = None
+
+
+# ---------------------------------------------------------------------------
+# funspace: bases, Space2, Field2
+# ---------------------------------------------------------------------------
+class Base:
+    def __init__(self, kind, n):
+        self.kind = int(kind)
+        self.n = int(n)
+
+
+def chebyshev(n):
+    return Base(CHEBYSHEV, n)
+
+
+def cheb_dirichlet(n):
+    return Base(CHEB_DIRICHLET, n)
+
+
+def cheb_neumann(n):
+    return Base(CHEB_NEUMANN, n)
+
+
+def cheb_dirichlet_bc(n):
+    return Base(CHEB_DIRICHLET_BC, n)
+
+
+def cheb_neumann_bc(n):
+    return Base(CHEB_NEUMANN_BC, n)
+
+
+def fourier_r2c(n):
+    return Base(FOURIER_R2C, n)
+
+
+class Space2:
+    """Space2::new(base0, base1) (funspace/src/space2.rs)."""
+
+    def __init__(self, base0: Base, base1: Base):
+        h = _P()
+        _check(lib().fs_space_create(base0.kind, base0.n, base1.kind, base1.n, ctypes.byref(h)))
+        self._h = h
+        self.base0, self.base1 = base0, base1
+        self.physical = self._shape(0)[:2]
+        sp = self._shape(1)
+        self.spectral = sp[:2]
+        self.is_complex = bool(sp[2])
+        self.ortho = self._shape(2)[:2]
+
+    def _shape(self, which):
+        a, b, c = _I(), _I(), _I()
+        _check(lib().fs_space_shape(self._h, which, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.fs_space_destroy(h)
+            self._h = None
+
+    # device-buffer level (drop-in primitives)
+    def forward_dev(self, d_phys, d_spec, stream=None):
+        _check(lib().fs_forward(self._h, d_phys.ptr, d_spec.ptr, stream))
+
+    def backward_dev(self, d_spec, d_phys, stream=None):
+        _check(lib().fs_backward(self._h, d_spec.ptr, d_phys.ptr, stream))
+
+    def to_ortho_dev(self, d_spec, d_ortho, stream=None):
+        _check(lib().fs_to_ortho(self._h, d_spec.ptr, d_ortho.ptr, stream))
+
+    def from_ortho_dev(self, d_ortho, d_spec, stream=None):
+        _check(lib().fs_from_ortho(self._h, d_ortho.ptr, d_spec.ptr, stream))
+
+    def gradient_dev(self, d_spec, d_ortho, deriv, scale=None, stream=None):
+        sc = None
+        if scale is not None:
+            self._sc = np.asarray(scale, dtype=np.float64)
+            sc = _dptr(self._sc)
+        _check(lib().fs_gradient(self._h, d_spec.ptr, d_ortho.ptr, int(deriv[0]), int(deriv[1]), sc, stream))
+
+    # host-array convenience (copies in and out)
+    def _run(self, fn, a, out_shape, out_complex, *args):
+        d_in = DeviceArray.from_host(a)
+        d_out = DeviceArray(out_shape, out_complex)
+        fn(d_in, d_out, *args)
+        _check(lib().rbc_device_synchronize())
+        return d_out.to_host()
+
+    def forward(self, v):
+        return self._run(self.forward_dev, np.asarray(v, dtype=np.float64), self.spectral, self.is_complex)
+
+    def backward(self, vhat):
+        return self._run(self.backward_dev, self._spec(vhat), self.physical, False)
+
+    def to_ortho(self, vhat):
+        return self._run(self.to_ortho_dev, self._spec(vhat), self.ortho, self.is_complex)
+
+    def from_ortho(self, o):
+        return self._run(self.from_ortho_dev, self._spec(o), self.spectral, self.is_complex)
+
+    def gradient(self, vhat, deriv, scale=None):
+        return self._run(self.gradient_dev, self._spec(vhat), self.ortho, self.is_complex, deriv, scale)
+
+    def _spec(self, a):
+        return np.asarray(a, dtype=np.complex128 if self.is_complex else np.float64)
+
+
+class Field2:
+    """Field2 (src/field.rs:67-129): physical ``v`` and spectral ``vhat``."""
+
+    def __init__(self, space: Space2):
+        self.space = space
+        self.v = np.zeros(space.physical)
+        self.vhat = np.zeros(space.spectral, dtype=np.complex128 if space.is_complex else np.float64)
+
+    def forward(self):
+        self.vhat = self.space.forward(self.v)
+
+    def backward(self):
+        self.v = self.space.backward(self.vhat)
+
+    def to_ortho(self):
+        return self.space.to_ortho(self.vhat)
+
+    def from_ortho(self, o):
+        self.vhat = self.space.from_ortho(o)
+
+    def gradient(self, deriv, scale=None):
+        return self.space.gradient(self.vhat, deriv, scale)
+
+
+class _Solver:
+    kind = HHOLTZ
+
+    def __init__(self, field_or_space, c):
+        space = field_or_space.space if isinstance(field_or_space, Field2) else field_or_space
+        self.space = space
+        self._c = np.asarray(c, dtype=np.float64).reshape(2)
+        h = _P()
+        _check(lib().sv_create(space._h, self.kind, _dptr(self._c), ctypes.byref(h)))
+        self._h = h
+
+    def solve_dev(self, d_in, d_out, stream=None):
+        _check(lib().sv_solve(self._h, d_in.ptr, d_out.ptr, stream))
+
+    def solve(self, rhs):
+        rhs = np.asarray(rhs, dtype=np.complex128 if self.space.is_complex else np.float64)
+        d_in = DeviceArray.from_host(rhs)
+        d_out = DeviceArray(self.space.spectral, self.space.is_complex)
+        self.solve_dev(d_in, d_out)
+        _check(lib().rbc_device_synchronize())
+        return d_out.to_host()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.sv_destroy(h)
+            self._h = None
+
+
+class Hholtz(_Solver):
+    """Hholtz::new (src/solver/hholtz.rs:42-76)."""
+    kind = HHOLTZ
+
+
+class HholtzAdi(_Solver):
+    """HholtzAdi::new (src/solver/hholtz_adi.rs:44-63)."""
+    kind = HHOLTZ_ADI
+
+
+class Poisson(_Solver):
+    """Poisson::new (src/solver/poisson.rs:50-90)."""
+    kind = POISSON
+
+
+# ---------------------------------------------------------------------------
+# Navier2D
+# ---------------------------------------------------------------------------
+class Navier2D:
+    """Navier2D (src/navier/navier.rs) on the GPU.
+
+    ``Navier2D.new(nx, ny, ra, pr, dt, aspect, adiabatic)`` and
+    ``Navier2D.new_periodic(nx, ny, ra, pr, dt, aspect)`` mirror the reference
+    constructors, including the initial ``random_disturbance(0.1)``, which is
+    seeded here (``seed``) where the reference draws from an unseeded RNG.
+    """
+
+    def __init__(self, nx, ny, ra, pr, dt, aspect, kind, precision=PREC_FP64, seed=None):
+        p = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(aspect), int(kind), int(precision))
+        h = _P()
+        _check(lib().rbc_create(ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        self.kind = kind
+        self.periodic = kind == PERIODIC
+        self.nx, self.ny = int(nx), int(ny)
+        pv = np.zeros(7)
+        _check(lib().rbc_get_params(h, _dptr(pv)))
+        self.nu, self.ka, self.ra, self.pr, self.dt = (float(x) for x in pv[:5])
+        self.scale = pv[5:7].copy()
+        if seed is not None:
+            self.random_disturbance(0.1, seed)
+
+    @classmethod
+    def new(cls, nx, ny, ra, pr, dt, aspect, adiabatic=True, seed=0):
+        return cls(nx, ny, ra, pr, dt, aspect, BOX_ADIABATIC if adiabatic else BOX_CONDUCTING, seed=seed)
+
+    @classmethod
+    def new_periodic(cls, nx, ny, ra, pr, dt, aspect, seed=0):
+        return cls(nx, ny, ra, pr, dt, aspect, PERIODIC, seed=seed)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.rbc_destroy(h)
+            self._h = None
+
+    # --- Integrate trait (src/lib.rs:135-146)
+    def update(self, nsteps: int = 1):
+        _check(lib().rbc_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _check(lib().rbc_synchronize(self._h))
+
+    def get_time(self):
+        t = _D()
+        _check(lib().rbc_get_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    @property
+    def time(self):
+        return self.get_time()
+
+    def get_dt(self):
+        return self.dt
+
+    def reset_time(self):
+        _check(lib().rbc_set_time(self._h, 0.0))
+
+    def exit(self):
+        s = _I()
+        _check(lib().rbc_exit(self._h, ctypes.byref(s)))
+        return bool(s.value)
+
+    def status(self):
+        s = _I()
+        _check(lib().rbc_status(self._h, ctypes.byref(s)))
+        return s.value
+
+    def callback(self):
+        """Diagnostics of Navier2D::callback (navier.rs:775-853) without file I/O."""
+        return {"time": self.get_time(), "div": self.eval(DIV_NORM), "Nu": self.eval_nu(), "Nuvol": self.eval_nuvol(),
+                "Re": self.eval_re()}
+
+    # --- initial conditions
+    def set_velocity(self, amp, m, n):
+        _check(lib().rbc_set_velocity(self._h, float(amp), float(m), float(n)))
+
+    def set_temperature(self, amp, m, n):
+        _check(lib().rbc_set_temperature(self._h, float(amp), float(m), float(n)))
+
+    def random_disturbance(self, amp, seed=0):
+        _check(lib().rbc_random_disturbance(self._h, float(amp), ctypes.c_uint64(seed)))
+
+    def set_temperature_noise(self, amp, seed):
+        _check(lib().rbc_set_temperature_noise(self._h, float(amp), ctypes.c_uint64(seed)))
+
+    def zero_pressure(self):
+        for f in (PRES, PSEUDO_PRES):
+            self.set(f, np.zeros_like(self.get(f)))
+
+    # --- state
+    def shape(self, field):
+        a, b, c = _I(), _I(), _I()
+        _check(lib().rbc_field_shape(self._h, field, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return (a.value, b.value), bool(c.value)
+
+    def get(self, field):
+        sh, cx = self.shape(field)
+        out = np.empty(sh, dtype=np.complex128 if cx else np.float64)
+        _check(lib().rbc_get_state(self._h, field, out.ctypes.data_as(_DP), out.size * (2 if cx else 1)))
+        return out
+
+    def set(self, field, arr):
+        sh, cx = self.shape(field)
+        a = np.ascontiguousarray(arr, dtype=np.complex128 if cx else np.float64)
+        if a.shape != sh:
+            raise ValueError(f"shape mismatch: got {a.shape}, expected {sh}")
+        _check(lib().rbc_set_state(self._h, field, a.ctypes.data_as(_DP), a.size * (2 if cx else 1)))
+
+    def get_physical(self, field):
+        out = np.empty((self.nx, self.ny))
+        _check(lib().rbc_get_physical(self._h, field, _dptr(out), out.size))
+        return out
+
+    def coords(self, field=UX):
+        """Grid coordinates (x, y) of a field, scaled like Navier2D::_scale."""
+        x, y = np.zeros(self.nx), np.zeros(self.ny)
+        _check(lib().rbc_get_coords(self._h, field, _dptr(x), _dptr(y)))
+        return x, y
+
+    # --- diagnostics
+    def eval(self, what):
+        v = _D()
+        _check(lib().rbc_eval(self._h, what, ctypes.byref(v)))
+        return v.value
+
+    def eval_nu(self):
+        return self.eval(NU)
+
+    def eval_nuvol(self):
+        return self.eval(NUVOL)
+
+    def eval_re(self):
+        return self.eval(RE)
+
+    def eval_ke(self):
+        return self.eval(KE)
+
+    def div_norm(self):
+        return self.eval(DIV_NORM)
+
+    def profile_step(self, nsteps=10):
+        """Mean device time (ms) of each kernel of the step: {stage name: ms}."""
+        ms = np.zeros(64)
+        n = _I()
+        _check(lib().rbc_profile_step(self._h, int(nsteps), _dptr(ms), 64, ctypes.byref(n)))
+        return {lib().rbc_stage_name(self._h, k).decode(): float(ms[k]) for k in range(n.value)}
+
+    def stream(self):
+        s = _P()
+        _check(lib().rbc_get_stream(self._h, ctypes.byref(s)))
+        return s.value
+
+    def device_bytes(self):
+        b = _SZ()
+        _check(lib().rbc_device_bytes(self._h, ctypes.byref(b)))
+        return b.value
+
+
+def integrate(pde: Navier2D, max_time: float, save_intervall=None, callback=None):
+    """integrate() (src/lib.rs:155-187).  ``callback(pde)`` runs at each save
+    interval (Integrate::callback); returning True from it stops the loop."""
+    user_cb = callback if callback is not None else (lambda p: None)
+
+    def _cb(_h, _t, _u):
+        return 1 if user_cb(pde) else 0
+
+    cfun = CALLBACK(_cb)
+    steps = ctypes.c_long(0)
+    _check(lib().rbc_integrate(pde._h, float(max_time), float(save_intervall or 0.0), cfun, None,
+                               ctypes.byref(steps)))
+    return steps.value
+
+
+def standard_ic(nav: Navier2D, seed: int = 1, vel_amp: float = 0.2, temp_amp: float = 1e-3):
+    """Seeded initial condition of the benchmark configurations: set_velocity(vel_amp, 1, 1),
+    interior temperature noise temp_amp*(2u-1) from splitmix64(seed), zero pressure."""
+    nav.set_velocity(vel_amp, 1.0, 1.0)
+    nav.set_temperature_noise(temp_amp, seed)
+    nav.zero_pressure()

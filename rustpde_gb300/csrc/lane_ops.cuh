@@ -1,0 +1,412 @@
+// lane_ops.cuh -- CTA-cooperative 1-D operations on lanes held in shared memory.
+//
+// A "lane" is one 1-D line of a 2-D field along the axis being processed
+// (a row for y passes, a column for x passes).  Each function is executed by
+// all threads of the CTA (tid, nth) and ends with __syncthreads().  Lanes of
+// the same call are stored at base + l*ld.  T is double (real data) or
+// double2 (complex data, interleaved re/im).
+//
+// Operations and the reference code they restate:
+//   to_ortho / from_ortho   funspace/src/chebyshev/composite_stencil.rs:207-276, linalg.rs:14-57
+//   cheb_diff               funspace/src/chebyshev/ortho.rs:107-125
+//   matvec_pinv             src/solver/matvec.rs:172-193
+//   fdma_solve              src/solver/fdma.rs:101-118 (factors swept at set-up)
+//   dct1 (fwd/bwd)          funspace/src/chebyshev/ortho.rs:235-312 (DCT-I = REDFT00)
+//   c2r / r2c               funspace/src/fourier/r2c.rs:160-226 (1/n on the inverse)
+#pragma once
+#include <cuda_runtime.h>
+
+#include "rbc_dev.h"
+
+namespace rbc {
+namespace dev {
+
+// ------------------------------------------------------------------ scalars
+__device__ __forceinline__ double2 c2(double a, double b) { return make_double2(a, b); }
+__device__ __forceinline__ double2 operator+(double2 a, double2 b) { return c2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 operator-(double2 a, double2 b) { return c2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 operator*(double2 a, double s) { return c2(a.x * s, a.y * s); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 w) {
+  return c2(fma(a.x, w.x, -a.y * w.y), fma(a.x, w.y, a.y * w.x));
+}
+__device__ __forceinline__ double2 cmulc(double2 a, double2 w) {  // a * conj(w)
+  return c2(fma(a.x, w.x, a.y * w.y), fma(a.y, w.x, -a.x * w.y));
+}
+__device__ __forceinline__ double2 conj2(double2 a) { return c2(a.x, -a.y); }
+
+template <class T> __device__ __forceinline__ T zero_v();
+template <> __device__ __forceinline__ double zero_v<double>() { return 0.0; }
+template <> __device__ __forceinline__ double2 zero_v<double2>() { return c2(0.0, 0.0); }
+
+__device__ __forceinline__ double scal(double a, double s) { return a * s; }
+__device__ __forceinline__ double2 scal(double2 a, double s) { return c2(a.x * s, a.y * s); }
+// a - b*s, a + b*s (fused)
+__device__ __forceinline__ double fnms(double a, double b, double s) { return fma(-b, s, a); }
+__device__ __forceinline__ double2 fnms(double2 a, double2 b, double s) { return c2(fma(-b.x, s, a.x), fma(-b.y, s, a.y)); }
+__device__ __forceinline__ double fmas(double a, double b, double s) { return fma(b, s, a); }
+__device__ __forceinline__ double2 fmas(double2 a, double2 b, double s) { return c2(fma(b.x, s, a.x), fma(b.y, s, a.y)); }
+__device__ __forceinline__ bool finite_v(double a) { return isfinite(a); }
+__device__ __forceinline__ bool finite_v(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+
+// multiply by i*k / s  (Fourier derivative of order 1, then division by the scale)
+__device__ __forceinline__ double2 mul_ik(double2 a, double k) { return c2(-a.y * k, a.x * k); }
+
+// ------------------------------------------------------------------ stencils
+// composite -> ortho along a lane: p_i = diag_i c_i + low2_{i-2} c_{i-2}
+template <class T>
+__device__ __forceinline__ T stencil_at(const BasisDev& b, const T* c, int i) {
+  int n = b.n, m = b.m;
+  if (b.kind == 0 || b.kind == 5) return c[i];  // Chebyshev / Fourier: identity
+  if (b.kind == 3 || b.kind == 4) {             // boundary basis
+    if (i == 0) return fmas(scal(c[0], b.t0[0]), c[1], b.t0[1]);
+    if (i == 1) return fmas(scal(c[0], b.t1[0]), c[1], b.t1[1]);
+    return zero_v<T>();
+  }
+  T v = zero_v<T>();
+  if (i < m) v = scal(c[i], b.diag[i]);
+  if (i >= 2 && i - 2 < m) v = (i < m) ? fmas(v, c[i - 2], b.low2[i - 2]) : scal(c[i - 2], b.low2[i - 2]);
+  (void)n;
+  return v;
+}
+
+template <class T>
+static __device__ void to_ortho(const BasisDev& b, const T* in, int in_ld, T* out, int out_ld, int nl, int tid, int nth) {
+  int n = (b.kind == 5) ? b.m : b.n;
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l = idx / n, i = idx - l * n;
+    out[l * out_ld + i] = stencil_at(b, in + l * in_ld, i);
+  }
+  __syncthreads();
+}
+
+// ortho -> composite (least squares, stride-2 tridiagonal).  in and out may not alias.
+template <class T>
+static __device__ void from_ortho(const BasisDev& b, const T* in, int in_ld, T* out, int out_ld, int nl, int tid, int nth) {
+  int m = b.m;
+  if (b.kind == 0 || b.kind == 5) {
+    for (int idx = tid; idx < nl * m; idx += nth) {
+      int l = idx / m, i = idx - l * m;
+      out[l * out_ld + i] = in[l * in_ld + i];
+    }
+    __syncthreads();
+    return;
+  }
+  if (b.kind == 3 || b.kind == 4) {
+    for (int l = tid; l < nl; l += nth) {
+      const T* p = in + l * in_ld;
+      T c0 = fmas(scal(p[0], b.t0[0]), p[1], b.t1[0]);
+      T c1 = fmas(scal(p[0], b.t0[1]), p[1], b.t1[1]);
+      out[l * out_ld + 0] = fmas(scal(c0, b.bc_inv[0]), c1, b.bc_inv[1]);
+      out[l * out_ld + 1] = fmas(scal(c0, b.bc_inv[2]), c1, b.bc_inv[3]);
+    }
+    __syncthreads();
+    return;
+  }
+  for (int idx = tid; idx < nl * m; idx += nth) {
+    int l = idx / m, i = idx - l * m;
+    const T* p = in + l * in_ld;
+    out[l * out_ld + i] = fmas(scal(p[i], b.diag[i]), p[i + 2], b.low2[i]);
+  }
+  __syncthreads();
+  // one thread per (lane, parity) chain
+  for (int t = tid; t < 2 * nl; t += nth) {
+    int l = t >> 1, par = t & 1;
+    T* d = out + l * out_ld;
+    // forward: g_i = (d_i - a_{i-2} g_{i-2}) / den_i
+    T g = scal(d[par], b.fo_dinv[par]);
+    d[par] = g;
+    for (int i = par + 2; i < m; i += 2) {
+      g = scal(fnms(d[i], g, b.fo_off[i - 2]), b.fo_dinv[i]);
+      d[i] = g;
+    }
+    // backward: x_j = g_j - w_j x_{j+2}
+    int top = ((m - 1 - par) & 1) ? m - 2 : m - 1;  // highest index of this parity
+    T x = d[top];
+    for (int j = top - 2; j >= 0; j -= 2) {
+      x = fnms(d[j], x, b.fo_w[j]);
+      d[j] = x;
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ derivatives
+// Chebyshev derivative of order `times` (1 or 2) of ortho lanes: out = D^times in
+// (in and out may alias only if times == 0).
+template <class T>
+static __device__ void cheb_diff(const T* in, int in_ld, T* out, int out_ld, int n, int nl, int times, T* tmp, int tmp_ld,
+                          int tid, int nth) {
+  if (times == 0) {
+    if (in != out)
+      for (int idx = tid; idx < nl * n; idx += nth) {
+        int l = idx / n, i = idx - l * n;
+        out[l * out_ld + i] = in[l * in_ld + i];
+      }
+    __syncthreads();
+    return;
+  }
+  const T* src = in;
+  int src_ld = in_ld;
+  for (int t = 0; t < times; t++) {
+    T* dst = (t == times - 1) ? out : tmp;
+    int dst_ld = (t == times - 1) ? out_ld : tmp_ld;
+    // d_0 = a_1; d_i = 2(i+1) a_{i+1} (1 <= i <= n-2); d_{n-1} = 0
+    for (int idx = tid; idx < nl * n; idx += nth) {
+      int l = idx / n, i = idx - l * n;
+      const T* a = src + l * src_ld;
+      T v;
+      if (i == 0) v = a[1];
+      else if (i < n - 1) v = scal(a[i + 1], 2.0 * (double)(i + 1));
+      else v = zero_v<T>();
+      dst[l * dst_ld + i] = v;
+    }
+    __syncthreads();
+    // suffix recurrence d_i += d_{i+2} for i = n-3 .. 1, then d_0 += d_2 / 2
+    for (int q = tid; q < 2 * nl; q += nth) {
+      int l = q >> 1, par = q & 1;
+      T* d = dst + l * dst_ld;
+      int top = ((n - 3 - par) & 1) ? n - 4 : n - 3;
+      if (top >= 1) {
+        T acc = d[top + 2];
+        for (int i = top; i >= 1; i -= 2) {
+          acc = d[i] + acc;
+          d[i] = acc;
+        }
+      }
+      if (par == 0) d[0] = fmas(d[0], d[2], 0.5);
+    }
+    __syncthreads();
+    src = dst;
+    src_ld = dst_ld;
+  }
+}
+
+// ------------------------------------------------------------------ banded solvers
+// out (n-2 per lane) = pinv(n) * in (n per lane)
+template <class T>
+static __device__ void matvec_pinv(const PinvDev& p, const T* in, int in_ld, T* out, int out_ld, int nl, int tid, int nth) {
+  int m = p.n - 2;
+  for (int idx = tid; idx < nl * m; idx += nth) {
+    int l = idx / m, i = idx - l * m;
+    const T* a = in + l * in_ld;
+    T v = scal(a[i], p.dia[i]);
+    if (i < m - 2) v = fmas(v, a[i + 2], p.up1[i]);
+    if (i < m - 4) v = fmas(v, a[i + 4], p.up2[i]);
+    out[l * out_ld + i] = v;
+  }
+  __syncthreads();
+}
+
+// In-place banded solve with swept factors; lane l uses factor row
+// (row0 + l*lane_step) when f.rows > 1.  One thread per (lane, parity) chain.
+template <class T>
+static __device__ void fdma_solve(const FdmaDev& f, T* x, int ld, int nl, int row0, int lane_step, int tid, int nth) {
+  int m = f.m;
+  for (int t = tid; t < 2 * nl; t += nth) {
+    int l = t >> 1, par = t & 1;
+    size_t off = (f.rows > 1) ? (size_t)(row0 + l * lane_step) * f.stride : 0;
+    const double* low = f.low + off;
+    const double* dinv = f.dinv + off;
+    const double* up1 = f.up1 + off;
+    const double* up2 = f.up2 + off;
+    T* d = x + l * ld;
+    T prev = d[par];
+    for (int i = par + 2; i < m; i += 2) {
+      T v = fnms(d[i], prev, low[i - 2]);
+      d[i] = v;
+      prev = v;
+    }
+    int top = ((m - 1 - par) & 1) ? m - 2 : m - 1;
+    T x2 = zero_v<T>(), x4 = zero_v<T>();  // x_{i+2}, x_{i+4}
+    for (int i = top; i >= 0; i -= 2) {
+      T v = d[i];
+      if (i + 2 < m) v = fnms(v, x2, up1[i]);
+      if (i + 4 < m) v = fnms(v, x4, up2[i]);
+      v = scal(v, dinv[i]);
+      d[i] = v;
+      x4 = x2;
+      x2 = v;
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ FFT
+// Radix-4 (+ one radix-2) Stockham complex FFT of nl lanes of length L = 2^log2L
+// held in a (lane stride ld).  tw has length twL (multiple of L), tw[t] =
+// exp(-2 pi i t / twL).  Forward uses exp(-...), inverse exp(+...), both
+// unnormalised.  Returns the buffer (a or b) holding the result.
+__device__ __forceinline__ double2* fft_pow2(double2* a, double2* b, int L, int log2L, int nl, int ld,
+                                              const double2* __restrict__ tw, int twL, bool inv, int tid, int nth) {
+  int Ns = 1;
+  if (log2L & 1) {
+    int half = L >> 1;
+    for (int idx = tid; idx < nl * half; idx += nth) {
+      int l = idx >> (log2L - 1), j = idx & (half - 1);
+      double2 v0 = a[l * ld + j], v1 = a[l * ld + j + half];
+      b[l * ld + 2 * j] = v0 + v1;
+      b[l * ld + 2 * j + 1] = v0 - v1;
+    }
+    __syncthreads();
+    double2* t = a; a = b; b = t;
+    Ns = 2;
+  }
+  int quarter = L >> 2;
+  int lq = log2L - 2;
+  while (Ns < L) {
+    int tstep = twL / (Ns * 4);
+    for (int idx = tid; idx < nl * quarter; idx += nth) {
+      int l = idx >> lq, j = idx & (quarter - 1);
+      const double2* src = a + l * ld;
+      double2 v0 = src[j], v1 = src[j + quarter], v2 = src[j + 2 * quarter], v3 = src[j + 3 * quarter];
+      int jm = j & (Ns - 1);
+      if (jm) {
+        int e = jm * tstep;
+        double2 w1 = tw[e], w2 = tw[2 * e], w3 = tw[3 * e];
+        if (inv) { v1 = cmulc(v1, w1); v2 = cmulc(v2, w2); v3 = cmulc(v3, w3); }
+        else { v1 = cmul(v1, w1); v2 = cmul(v2, w2); v3 = cmul(v3, w3); }
+      }
+      double2 s0 = v0 + v2, d0 = v0 - v2, s1 = v1 + v3, d1 = v1 - v3;
+      // forward: d1 * (-i) ; inverse: d1 * (+i)
+      double2 r = inv ? c2(-d1.y, d1.x) : c2(d1.y, -d1.x);
+      double2* dst = b + l * ld + (j - jm) * 4 + jm;
+      dst[0] = s0 + s1;
+      dst[Ns] = d0 + r;
+      dst[2 * Ns] = s0 - s1;
+      dst[3 * Ns] = d0 - r;
+    }
+    __syncthreads();
+    double2* t = a; a = b; b = t;
+    Ns <<= 2;
+  }
+  return a;
+}
+
+// ------------------------------------------------------------------ Chebyshev transforms
+// pre/post factors of ortho.rs:235-312 for index k of length n (N = n-1)
+__device__ __forceinline__ double cheb_fwd_post(int k, int n) {
+  double s = ((k & 1) ? -1.0 : 1.0) * (1.0 / (double)(n - 1));
+  return (k == 0 || k == n - 1) ? s * 0.5 : s;
+}
+__device__ __forceinline__ double cheb_bwd_pre(int k, int n) {
+  double s = ((k & 1) ? -1.0 : 1.0) / 2.0;
+  return (k == 0 || k == n - 1) ? s * 2.0 : s;
+}
+
+// Complex lanes, FFT variant: out = DCT-I(pre .* in) .* post
+// wa, wb: work lanes of length >= L with stride wld.
+static __device__ void dct1_fft_c(const ChebXformDev& cx, bool forward, const double2* in, int in_ld, double2* out,
+                           int out_ld, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  int n = cx.n, N = n - 1, L = cx.L;
+  for (int idx = tid; idx < nl * L; idx += nth) {
+    int l = idx >> cx.log2L, j = idx & (L - 1);
+    int src = j <= N ? j : L - j;
+    double2 v = in[l * in_ld + src];
+    if (!forward) v = v * cheb_bwd_pre(src, n);
+    wa[l * wld + j] = v;
+  }
+  __syncthreads();
+  double2* r = fft_pow2(wa, wb, L, cx.log2L, nl, wld, cx.tw, L, false, tid, nth);
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l = idx / n, k = idx - l * n;
+    double2 v = r[l * wld + k];
+    out[l * out_ld + k] = forward ? v * cheb_fwd_post(k, n) : v;
+  }
+  __syncthreads();
+}
+
+// Real lanes, FFT variant: two real lanes per complex FFT.
+static __device__ void dct1_fft_r(const ChebXformDev& cx, bool forward, const double* in, int in_ld, double* out, int out_ld,
+                           int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  int n = cx.n, N = n - 1, L = cx.L;
+  int np = (nl + 1) >> 1;
+  for (int idx = tid; idx < np * L; idx += nth) {
+    int q = idx >> cx.log2L, j = idx & (L - 1);
+    int src = j <= N ? j : L - j;
+    double pre = forward ? 1.0 : cheb_bwd_pre(src, n);
+    double re = in[(2 * q) * in_ld + src] * pre;
+    double im = (2 * q + 1 < nl) ? in[(2 * q + 1) * in_ld + src] * pre : 0.0;
+    wa[q * wld + j] = c2(re, im);
+  }
+  __syncthreads();
+  double2* r = fft_pow2(wa, wb, L, cx.log2L, np, wld, cx.tw, L, false, tid, nth);
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l = idx / n, k = idx - l * n;
+    double2 v = r[(l >> 1) * wld + k];
+    double s = (l & 1) ? v.y : v.x;
+    out[l * out_ld + k] = forward ? s * cheb_fwd_post(k, n) : s;
+  }
+  __syncthreads();
+}
+
+// Dense variant (any n): out[k] = sum_j M[k][j] in[j]
+template <class T>
+static __device__ void dct1_dense(const ChebXformDev& cx, bool forward, const T* in, int in_ld, T* out, int out_ld, int nl,
+                           int tid, int nth) {
+  int n = cx.n;
+  const double* __restrict__ M = forward ? cx.fwd : cx.bwd;
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l = idx / n, k = idx - l * n;
+    const T* a = in + l * in_ld;
+    const double* row = M + (size_t)k * n;
+    T acc = zero_v<T>();
+    for (int j = 0; j < n; j++) acc = fmas(acc, a[j], __ldg(row + j));
+    out[l * out_ld + k] = acc;
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ Fourier (x)
+// c2r: in = M+1 complex per lane (DC imag and Nyquist imag ignored), out = 2M reals.
+// Lane l reads in[l*in_ld + k*in_stride].
+static __device__ void c2r(const FourierXformDev& fx, const double2* in, int in_ld, int in_stride, double* out, int out_ld,
+                    int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  int M = fx.M;
+  for (int idx = tid; idx < nl * M; idx += nth) {
+    int l = idx >> fx.log2M, k = idx & (M - 1);
+    const double2* X = in + l * in_ld;
+    double2 xk = X[k * in_stride];
+    double2 xm = X[(M - k) * in_stride];
+    if (k == 0) { xk.y = 0.0; xm.y = 0.0; }
+    double2 xc = conj2(xm);
+    double2 d = xk - xc;
+    double2 t = cmulc(d, fx.tw[k]);  // e^{+2 pi i k / n} (xk - xc)
+    wa[l * wld + k] = c2(xk.x + xc.x - t.y, xk.y + xc.y + t.x);
+  }
+  __syncthreads();
+  double2* r = fft_pow2(wa, wb, M, fx.log2M, nl, wld, fx.tw, fx.n, true, tid, nth);
+  double s = 1.0 / (double)fx.n;
+  for (int idx = tid; idx < nl * M; idx += nth) {
+    int l = idx >> fx.log2M, k = idx & (M - 1);
+    double2 v = r[l * wld + k];
+    out[l * out_ld + 2 * k] = v.x * s;
+    out[l * out_ld + 2 * k + 1] = v.y * s;
+  }
+  __syncthreads();
+}
+
+// r2c: in = 2M reals per lane, out = first `keep` (<= M+1) complex values;
+// lane l writes out[l*out_ld + k*out_stride].
+static __device__ void r2c(const FourierXformDev& fx, const double* in, int in_ld, double2* out, int out_ld, int out_stride,
+                    int keep, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  int M = fx.M;
+  for (int idx = tid; idx < nl * M; idx += nth) {
+    int l = idx >> fx.log2M, k = idx & (M - 1);
+    wa[l * wld + k] = c2(in[l * in_ld + 2 * k], in[l * in_ld + 2 * k + 1]);
+  }
+  __syncthreads();
+  double2* r = fft_pow2(wa, wb, M, fx.log2M, nl, wld, fx.tw, fx.n, false, tid, nth);
+  for (int idx = tid; idx < nl * keep; idx += nth) {
+    int l = idx / keep, k = idx - l * keep;
+    double2 zk = r[l * wld + (k & (M - 1))];
+    double2 zc = conj2(r[l * wld + ((M - k) & (M - 1))]);
+    double2 e = (zk + zc) * 0.5;
+    double2 dd = zk - zc;
+    double2 o = c2(dd.y * 0.5, -dd.x * 0.5);  // (zk - zc) / (2i)
+    out[l * out_ld + k * out_stride] = e + cmul(o, fx.tw[k]);
+  }
+  __syncthreads();
+}
+
+}  // namespace dev
+}  // namespace rbc

@@ -1,0 +1,120 @@
+// rbc_dev.h -- device-resident descriptors of one RBC case (shared by host and
+// device code).  All pointers are device pointers into the case's arena.
+//
+// Layout in HBM: row-major (x, y) arrays with y contiguous, as the reference's
+// ndarray default; complex spectral data interleaved (re, im) = double2.
+#pragma once
+#include <cstdint>
+
+namespace rbc {
+
+// One basis along one axis (tables built by host_ops.cpp make_basis).
+struct BasisDev {
+  int kind;   // BaseKind
+  int n;      // physical / ortho length (Fourier: physical length)
+  int m;      // spectral length
+  int pad_;
+  const double* diag;     // composite stencil diag (m)
+  const double* low2;     // composite stencil low2 (m)
+  const double* fo_off;   // from_ortho tdma off-diagonal (m-2)
+  const double* fo_w;     // from_ortho tdma ratios (m-2)
+  const double* fo_dinv;  // from_ortho tdma 1/denominators (m)
+  double t0[2], t1[2];    // boundary stencil
+  double bc_inv[4];       // boundary least-squares inverse
+};
+
+// Rows of peye*laplace_inv for ortho length n (n-2 rows, entries at i, i+2, i+4).
+struct PinvDev {
+  int n;
+  int pad_;
+  const double* dia;
+  const double* up1;
+  const double* up2;
+};
+
+// Swept banded factors (offsets -2,0,2,4) of length m; `rows` > 1 means one
+// factorisation per lane (row i at offset i*stride).
+struct FdmaDev {
+  int m;
+  int rows;
+  int stride;
+  int pad_;
+  const double* low;   // swept low (m-2)
+  const double* dinv;  // 1/dia (m)
+  const double* up1;   // swept up1 (m-2)
+  const double* up2;   // up2 (m-4)
+};
+
+// Chebyshev transform along an axis of length n: FFT (n = 2^p + 1) or dense.
+struct ChebXformDev {
+  int n;
+  int use_fft;        // 1: DCT-I via complex FFT of length L = 2(n-1)
+  int L;              // FFT length
+  int log2L;
+  const double2* tw;  // exp(-2 pi i t / L), t < L
+  const double* fwd;  // dense n x n forward matrix (row = output)
+  const double* bwd;  // dense n x n backward matrix
+};
+
+// Fourier r2c/c2r along x of physical length n (power of two).
+struct FourierXformDev {
+  int n;        // physical length
+  int M;        // n/2 (half-length complex FFT)
+  int log2M;
+  int pad_;
+  const double2* tw;  // exp(-2 pi i t / n), t < n
+};
+
+enum CaseKind { KIND_BOX_ADIABATIC = 0, KIND_BOX_CONDUCTING = 1, KIND_PERIODIC = 2 };
+
+// Everything the FP64 step kernels need for one case.
+struct CaseDev {
+  int kind;
+  int nx, ny;      // physical grid
+  int mx;          // spectral rows of ortho x arrays: box nx, periodic nx/2+1
+  int mxc;         // spectral rows of composite-x arrays: box nx-2, periodic nx/2+1
+  int myc;         // composite y length ny-2
+  int kx, ky;      // dealias: rows kept (ortho x), columns kept (ortho y)
+  double dt, nu, ka, aspect;
+  double inv_dt;
+
+  // bases: y (CD velocity/temp, CN pseudo pressure, CHEB pressure) and x
+  BasisDev ycd, ycn;
+  BasisDev xu;   // x basis of ux/uy (CD) or Fourier
+  BasisDev xt;   // x basis of temperature (CN adiabatic / CD conducting) or Fourier
+  BasisDev xp;   // x basis of pseudo pressure (CN) or Fourier
+  PinvDev pinv_y;   // length ny
+  PinvDev pinv_x;   // length nx (box)
+  ChebXformDev cy;  // Chebyshev along y (length ny)
+  ChebXformDev cx;  // Chebyshev along x (box)
+  FourierXformDev fx;  // Fourier along x (periodic)
+
+  // solvers
+  FdmaDev hu_y, hu_x;    // box ADI velocity (y, x); periodic: hu_y per row
+  FdmaDev ht_y, ht_x;    // box ADI temperature; periodic: per row
+  FdmaDev pois_y;        // per-row factors of the pressure Poisson solve
+  const double* pois_fwd;  // box: (mxc x mxc) eigenbasis forward, row-major
+  const double* pois_bwd;  // box: eigenbasis backward
+
+  // state (spectral): real (box) or double2 (periodic) elements
+  void* ux;   // mxc x myc
+  void* uy;   // mxc x myc
+  void* temp; // mxc x myc
+  void* p0;   // mx x ny
+  void* p1;   // mxc x myc (Neumann)
+
+  // constants derived from the temperature boundary field
+  const void* bc_ortho;   // mx x ny: to_ortho(fieldbc)
+  const void* bc_diff;    // mx x ny: dt*ka*(d2/dx2 + d2/dy2) fieldbc
+  const double* bc_dx;    // nx x ny physical d/dx fieldbc
+  const double* bc_dy;    // nx x ny physical d/dy fieldbc
+
+  // scratch (per case)
+  void* yw[6];   // y-pass outputs (Y0, Y1 for ux, uy, temp): mxc x ny
+  void* q[3];    // x-pass outputs (dealiased products, x transformed): kx x ny
+  void* s[8];    // further scratch for the box pass sequence
+  unsigned int* status;  // bit 0: non-finite value seen
+  double* accum;         // reductions
+};
+
+}  // namespace rbc

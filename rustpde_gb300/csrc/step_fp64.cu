@@ -1,0 +1,759 @@
+// step_fp64.cu -- the plain FP64 Rayleigh-Benard time step as fused lane passes.
+//
+// One call of Integrate::update (src/navier/navier.rs:737-765) is decomposed
+// into passes along y (lanes = rows, contiguous) and along x (lanes = columns).
+// Linear operators acting on different axes commute, so each pass applies all
+// the work that is local to its lanes; the reference's results are reproduced
+// up to floating-point reassociation.
+//
+//  periodic (FourierR2c x Chebyshev):  Y1 -> X -> Y2            (3 launches)
+//  box (Chebyshev x Chebyshev):        Y1 -> X1 -> Y2 -> X2 -> Y3 -> X3 -> Y4 -> X4 -> Y5
+//
+// Each launch takes a table of work items (case, first lane, lane count); a
+// batch of cases is the same launch with a longer table.
+#include "lane_ops.cuh"
+#include "step_fp64.h"
+
+#include <algorithm>
+
+namespace rbc {
+namespace dev {
+
+static __device__ __forceinline__ void flag_nonfinite(unsigned int* status) { atomicOr(status, 1u); }
+
+// load a lane set: lane l (0 <= l < 3*nr) = field (l / nr), row (r0 + l % nr)
+template <class T>
+__device__ void load_rows3(void* const f[3], int row_len, int r0, int nr, T* dst, int ld, int tid, int nth) {
+  for (int idx = tid; idx < 3 * nr * row_len; idx += nth) {
+    int l = idx / row_len, j = idx - l * row_len;
+    int fi = l / nr, r = l - fi * nr;
+    dst[l * ld + j] = static_cast<const T*>(f[fi])[(size_t)(r0 + r) * row_len + j];
+  }
+  __syncthreads();
+}
+
+// ============================================================================
+// Y1: Y0_f = Ty^-1 Sy f,  Y1_f = Ty^-1 Dy Sy f   for f in (ux, uy, temp)
+// ============================================================================
+template <class T>
+__global__ void __launch_bounds__(256) k_y1(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int r0 = w.y, nr = w.z;
+  const int ny = c.ny, myc = c.myc, ld = c.ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  extern __shared__ double2 smem[];
+  T* IN = reinterpret_cast<T*>(smem);
+  T* O = IN + 3 * nr * ld;   // 3nr ortho lanes, followed by
+  T* D = O + 3 * nr * ld;    // 3nr derivative lanes
+  T* TMP = D + 3 * nr * ld;
+  double2* WA = reinterpret_cast<double2*>(TMP + 3 * nr * ld + 2);
+  WA = reinterpret_cast<double2*>((reinterpret_cast<size_t>(WA) + 15) & ~size_t(15));
+  const int wld = c.cy.use_fft ? c.cy.L : 1;
+  double2* WB = WA + (size_t)3 * nr * wld;
+  void* f3[3] = {c.ux, c.uy, c.temp};
+  load_rows3<T>(f3, myc, r0, nr, IN, ld, tid, nth);
+  to_ortho<T>(c.ycd, IN, ld, O, ld, 3 * nr, tid, nth);
+  cheb_diff<T>(O, ld, D, ld, ny, 3 * nr, 1, TMP, ld, tid, nth);
+  // inverse Chebyshev transform of O and D (6nr lanes, O and D contiguous)
+  if (c.cy.use_fft) {
+    if constexpr (sizeof(T) == 16) {
+      dct1_fft_c(c.cy, false, (const double2*)O, ld, (double2*)O, ld, 3 * nr, WA, WB, wld, tid, nth);
+      dct1_fft_c(c.cy, false, (const double2*)D, ld, (double2*)D, ld, 3 * nr, WA, WB, wld, tid, nth);
+    } else {
+      dct1_fft_r(c.cy, false, (const double*)O, ld, (double*)O, ld, 6 * nr, WA, WB, wld, tid, nth);
+    }
+  } else {
+    dct1_dense<T>(c.cy, false, O, ld, TMP, ld, 3 * nr, tid, nth);
+    for (int idx = tid; idx < 3 * nr * ny; idx += nth) {
+      int l = idx / ny, k = idx - l * ny;
+      O[l * ld + k] = TMP[l * ld + k];
+    }
+    __syncthreads();
+    dct1_dense<T>(c.cy, false, D, ld, TMP, ld, 3 * nr, tid, nth);
+    for (int idx = tid; idx < 3 * nr * ny; idx += nth) {
+      int l = idx / ny, k = idx - l * ny;
+      D[l * ld + k] = TMP[l * ld + k];
+    }
+    __syncthreads();
+  }
+  // store: yw[2f] = O lanes, yw[2f+1] = D lanes; row stride ny
+  for (int idx = tid; idx < 6 * nr * ny; idx += nth) {
+    int l = idx / ny, k = idx - l * ny;
+    int which = l / (3 * nr), ll = l - which * 3 * nr;
+    int fi = ll / nr, r = ll - fi * nr;
+    const T* src = which ? D : O;
+    static_cast<T*>(c.yw[2 * fi + which])[(size_t)(r0 + r) * ny + k] = src[ll * ld + k];
+  }
+}
+
+size_t smem_y1(const CaseDev& c, int nr, bool cplx) {
+  size_t es = cplx ? 16 : 8;
+  size_t ld = c.ny + 1;
+  size_t base = 4 * 3 * nr * ld * es + 2 * 8 + 16;
+  size_t wld = c.cy.use_fft ? c.cy.L : 1;
+  return base + 2 * (size_t)3 * nr * wld * 16 + 64;
+}
+
+// ============================================================================
+// Periodic X pass: one column j of the Y arrays.
+//  u = F^-1 Y0_ux, v = F^-1 Y0_uy;  for f: a = F^-1 (ik/s Y0_f), b = F^-1 Y1_f
+//  P_f = u a + v b (+ u dbc/dx + v dbc/dy for temp);  Q_f = F P_f, rows < kx
+// ============================================================================
+__global__ void __launch_bounds__(256) k_per_x(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int j = w.y;
+  const int mx = c.mx, nx = c.nx, ny = c.ny, M = c.fx.M;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double inv_asp = 1.0 / c.aspect;
+  extern __shared__ double2 smem[];
+  const int ild = mx + 1;         // input lanes (complex)
+  double2* IN = smem;             // 8 lanes
+  double2* WA = IN + 8 * ild;     // 8 lanes of M
+  double2* WB = WA + 8 * M;
+  double* PH = reinterpret_cast<double*>(IN);  // physical lanes alias the inputs (8 x nx reals)
+  // lane order: Y0u, Y0v, ikY0u, Y1u, ikY0v, Y1v, ikY0t, Y1t
+  for (int idx = tid; idx < 8 * mx; idx += nth) {
+    int l = idx / mx, k = idx - l * mx;
+    int src = (l < 2) ? 2 * l : (l & 1 ? 2 * ((l - 2) >> 1) + 1 : 2 * ((l - 2) >> 1));
+    double2 v = static_cast<const double2*>(c.yw[src])[(size_t)k * ny + j];
+    if (l >= 2 && !(l & 1)) v = mul_ik(v, (double)k) * inv_asp;
+    IN[l * ild + k] = v;
+  }
+  __syncthreads();
+  c2r(c.fx, IN, ild, 1, PH, nx, 8, WA, WB, M, tid, nth);
+  // products into lanes 2, 4, 6
+  const double* bx = c.bc_dx;
+  const double* by = c.bc_dy;
+  for (int idx = tid; idx < 3 * nx; idx += nth) {
+    int f = idx / nx, x = idx - f * nx;
+    double u = PH[x], v = PH[nx + x];
+    double a = PH[(2 + 2 * f) * nx + x], b = PH[(3 + 2 * f) * nx + x];
+    double p = u * a + v * b;
+    if (f == 2) {
+      p = p + u * bx[(size_t)x * ny + j];
+      p = p + v * by[(size_t)x * ny + j];
+    }
+    PH[(2 + 2 * f) * nx + x] = p;
+  }
+  __syncthreads();
+  double2* q = static_cast<double2*>(c.q[0]);
+  r2c(c.fx, PH + 2 * nx, 2 * nx, q + j, c.kx * ny, ny, c.kx, 3, WA, WB, M, tid, nth);
+}
+
+size_t smem_per_x(const CaseDev& c) {
+  size_t ild = c.mx + 1;
+  size_t in_bytes = std::max((size_t)8 * ild * 16, (size_t)8 * c.nx * 8);
+  return in_bytes + 2 * 8 * (size_t)c.fx.M * 16 + 64;
+}
+
+// ============================================================================
+// Periodic Y2 pass: one row i.  Convection DCT, right-hand sides, Helmholtz
+// solves (Hholtz per row), divergence, Poisson row solve, projection and the
+// pressure update (navier.rs:622-721).
+// ============================================================================
+__global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y;
+  const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, mx = c.mx;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double dt = c.dt, nu = c.nu, inv_asp = 1.0 / c.aspect, ki = (double)i;
+  extern __shared__ double2 smem[];
+  double2* CV = smem;            // 3 lanes conv
+  double2* F = CV + 3 * ld;      // 3 lanes composite state (old, then new)
+  double2* O = F + 3 * ld;       // 3 lanes ortho of old state
+  double2* R = O + 3 * ld;       // 3 lanes rhs
+  double2* P = R + 3 * ld;       // p0 row
+  double2* G = P + ld;           // d/dy p0, later scratch
+  double2* X1 = G + ld;          // 3 scratch lanes
+  double2* TMP = X1 + 3 * ld;
+  double2* WA = TMP + 3 * ld;
+  const int wld = c.cy.use_fft ? c.cy.L : 1;
+  double2* WB = WA + 3 * wld;
+  (void)mx;
+
+  // 1. convection: forward Chebyshev transform of Q_f[i], dealiased
+  if (i < kx) {
+    const double2* q = static_cast<const double2*>(c.q[0]);
+    for (int idx = tid; idx < 3 * ny; idx += nth) {
+      int f = idx / ny, k = idx - f * ny;
+      CV[f * ld + k] = q[(size_t)f * kx * ny + (size_t)i * ny + k];
+    }
+    __syncthreads();
+    if (c.cy.use_fft) dct1_fft_c(c.cy, true, CV, ld, CV, ld, 3, WA, WB, wld, tid, nth);
+    else {
+      dct1_dense<double2>(c.cy, true, CV, ld, TMP, ld, 3, tid, nth);
+      for (int idx = tid; idx < 3 * ny; idx += nth) {
+        int f = idx / ny, k = idx - f * ny;
+        CV[f * ld + k] = TMP[f * ld + k];
+      }
+      __syncthreads();
+    }
+    for (int idx = tid; idx < 3 * ny; idx += nth) {
+      int f = idx / ny, k = idx - f * ny;
+      if (k >= ky) CV[f * ld + k] = c2(0.0, 0.0);
+    }
+  } else {
+    for (int idx = tid; idx < 3 * ny; idx += nth) CV[(idx / ny) * ld + idx % ny] = c2(0.0, 0.0);
+  }
+  // 2. right-hand sides
+  void* f3[3] = {c.ux, c.uy, c.temp};
+  for (int idx = tid; idx < 3 * myc; idx += nth) {
+    int f = idx / myc, k = idx - f * myc;
+    F[f * ld + k] = static_cast<const double2*>(f3[f])[(size_t)i * myc + k];
+  }
+  const double2* p0 = static_cast<const double2*>(c.p0);
+  for (int k = tid; k < ny; k += nth) P[k] = p0[(size_t)i * ny + k];
+  __syncthreads();
+  to_ortho<double2>(c.ycd, F, ld, O, ld, 3, tid, nth);
+  cheb_diff<double2>(P, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);
+  const double2* bco = static_cast<const double2*>(c.bc_ortho);
+  const double2* bcd = static_cast<const double2*>(c.bc_diff);
+  for (int k = tid; k < ny; k += nth) {
+    double2 gx = mul_ik(P[k], ki) * inv_asp;
+    double2 cu = CV[k], cvv = CV[ld + k], ct = CV[2 * ld + k];
+    R[k] = fnms(fnms(O[k], gx, dt), cu, dt);
+    double2 that = O[2 * ld + k] + bco[(size_t)i * ny + k];
+    R[ld + k] = fnms(fmas(fnms(O[ld + k], G[k], dt), that, dt), cvv, dt);
+    R[2 * ld + k] = fnms(O[2 * ld + k] + bcd[(size_t)i * ny + k], ct, dt);
+  }
+  __syncthreads();
+  // 3. Helmholtz: pinv_y then per-row banded solve
+  matvec_pinv<double2>(c.pinv_y, R, ld, F, ld, 3, tid, nth);
+  fdma_solve<double2>(c.hu_y, F, ld, 2, i, 0, tid, nth);
+  fdma_solve<double2>(c.ht_y, F + 2 * ld, ld, 1, i, 0, tid, nth);
+  // F now holds ux*, uy*, temp(new)
+  // 4. divergence = ik/s Sy ux* + Dy Sy uy*
+  to_ortho<double2>(c.ycd, F, ld, O, ld, 2, tid, nth);
+  cheb_diff<double2>(O + ld, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);
+  for (int k = tid; k < ny; k += nth) R[k] = mul_ik(O[k], ki) * inv_asp + G[k];  // R lane 0 = div
+  __syncthreads();
+  // 5. Poisson row solve -> pseudo pressure row
+  matvec_pinv<double2>(c.pinv_y, R, ld, X1, ld, 1, tid, nth);
+  fdma_solve<double2>(c.pois_y, X1, ld, 1, i, 0, tid, nth);
+  if (i == 0 && tid == 0) X1[0] = c2(0.0, 0.0);
+  __syncthreads();
+  double2* p1 = static_cast<double2*>(c.p1);
+  for (int k = tid; k < myc; k += nth) p1[(size_t)i * myc + k] = X1[k];
+  // 6. projection: O1 = Sy^N p1; dpdx = ik/s O1; dpdy = Dy O1
+  to_ortho<double2>(c.ycn, X1, ld, O, ld, 1, tid, nth);  // O lane 0 = O1
+  cheb_diff<double2>(O, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);  // G = dpdy
+  for (int k = tid; k < ny; k += nth) O[ld + k] = mul_ik(O[k], ki) * inv_asp;  // O lane 1 = dpdx
+  for (int k = tid; k < ny; k += nth) O[2 * ld + k] = G[k];                      // O lane 2 = dpdy
+  __syncthreads();
+  from_ortho<double2>(c.ycd, O + ld, ld, X1 + ld, ld, 2, tid, nth);  // X1 lanes 1, 2
+  // 7. pressure update and stores
+  double2* pw = static_cast<double2*>(c.p0);
+  for (int k = tid; k < ny; k += nth) {
+    double2 v = fnms(P[k], R[k], nu);
+    pw[(size_t)i * ny + k] = fmas(v, O[k], c.inv_dt);
+  }
+  double2* ux = static_cast<double2*>(c.ux);
+  double2* uy = static_cast<double2*>(c.uy);
+  double2* tt = static_cast<double2*>(c.temp);
+  bool bad = false;
+  for (int k = tid; k < myc; k += nth) {
+    double2 a = F[k] - X1[ld + k];
+    double2 b = F[ld + k] - X1[2 * ld + k];
+    double2 t = F[2 * ld + k];
+    ux[(size_t)i * myc + k] = a;
+    uy[(size_t)i * myc + k] = b;
+    tt[(size_t)i * myc + k] = t;
+    bad |= !(finite_v(a) && finite_v(b) && finite_v(t));
+  }
+  if (bad) flag_nonfinite(c.status);
+}
+
+size_t smem_per_y2(const CaseDev& c) {
+  size_t ld = c.ny + 1;
+  size_t wld = c.cy.use_fft ? c.cy.L : 1;
+  return (3 + 3 + 3 + 3 + 1 + 1 + 3 + 3) * ld * 16 + 2 * 3 * wld * 16 + 64;
+}
+
+// ============================================================================
+// Box passes (Chebyshev in x).  Real data.
+// ============================================================================
+// X1: columns j < ny.  x-backward of the y-transformed state, products,
+// x-forward of the products (rows < kx), and d/dx p0.
+__global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int j = w.y;
+  const int nx = c.nx, ny = c.ny, mxc = c.mxc, kx = c.kx;
+  const int ld = nx + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double inv_asp = 1.0 / c.aspect;
+  extern __shared__ double2 smem[];
+  double* IN = reinterpret_cast<double*>(smem);  // 8 lanes composite-x (mxc)
+  double* OR = IN + 8 * ld;                      // 8 ortho lanes (nx)
+  double* PH = OR + 8 * ld;                      // 8 physical lanes
+  double* TMP = PH + 8 * ld;                     // 8 lanes
+  double2* WA = reinterpret_cast<double2*>(TMP + 8 * ld + 2);
+  WA = reinterpret_cast<double2*>((reinterpret_cast<size_t>(WA) + 15) & ~size_t(15));
+  const int wld = c.cx.use_fft ? c.cx.L : 1;
+  double2* WB = WA + 4 * wld;
+  // lanes: 0 Y0u, 1 Y0v, 2 Y0u(dx), 3 Y1u, 4 Y0v(dx), 5 Y1v, 6 Y0t(dx), 7 Y1t
+  for (int idx = tid; idx < 8 * mxc; idx += nth) {
+    int l = idx / mxc, k = idx - l * mxc;
+    int src = (l < 2) ? 2 * l : (l & 1 ? 2 * ((l - 2) >> 1) + 1 : 2 * ((l - 2) >> 1));
+    IN[l * ld + k] = static_cast<const double*>(c.yw[src])[(size_t)k * ny + j];
+  }
+  __syncthreads();
+  // x stencils: lanes 0-5 use the velocity basis, 6-7 the temperature basis
+  to_ortho<double>(c.xu, IN, ld, OR, ld, 6, tid, nth);
+  to_ortho<double>(c.xt, IN + 6 * ld, ld, OR + 6 * ld, ld, 2, tid, nth);
+  // d/dx for lanes 2, 4, 6 (in place through TMP)
+  for (int f = 0; f < 3; f++) {
+    double* lane = OR + (2 + 2 * f) * ld;
+    cheb_diff<double>(lane, ld, TMP, ld, nx, 1, 1, TMP + ld, ld, tid, nth);
+    for (int k = tid; k < nx; k += nth) lane[k] = TMP[k] * inv_asp;
+    __syncthreads();
+  }
+  if (c.cx.use_fft) dct1_fft_r(c.cx, false, OR, ld, PH, ld, 8, WA, WB, wld, tid, nth);
+  else dct1_dense<double>(c.cx, false, OR, ld, PH, ld, 8, tid, nth);
+  // products (lanes 2, 4, 6)
+  for (int idx = tid; idx < 3 * nx; idx += nth) {
+    int f = idx / nx, x = idx - f * nx;
+    double u = PH[x], v = PH[ld + x];
+    double p = u * PH[(2 + 2 * f) * ld + x] + v * PH[(3 + 2 * f) * ld + x];
+    if (f == 2) {
+      p = p + u * c.bc_dx[(size_t)x * ny + j];
+      p = p + v * c.bc_dy[(size_t)x * ny + j];
+    }
+    TMP[f * ld + x] = p;
+  }
+  __syncthreads();
+  // forward x transform of the 3 products -> OR lanes 0..2
+  if (c.cx.use_fft) dct1_fft_r(c.cx, true, TMP, ld, OR, ld, 3, WA, WB, wld, tid, nth);
+  else dct1_dense<double>(c.cx, true, TMP, ld, OR, ld, 3, tid, nth);
+  double* q = static_cast<double*>(c.q[0]);
+  for (int idx = tid; idx < 3 * kx; idx += nth) {
+    int f = idx / kx, k = idx - f * kx;
+    q[(size_t)f * kx * ny + (size_t)k * ny + j] = OR[f * ld + k];
+  }
+  // d/dx p0 column / aspect -> s[0] (nx x ny)
+  const double* p0 = static_cast<const double*>(c.p0);
+  for (int k = tid; k < nx; k += nth) IN[k] = p0[(size_t)k * ny + j];
+  __syncthreads();
+  cheb_diff<double>(IN, ld, TMP, ld, nx, 1, 1, TMP + ld, ld, tid, nth);
+  double* gp = static_cast<double*>(c.s[0]);
+  for (int k = tid; k < nx; k += nth) gp[(size_t)k * ny + j] = TMP[k] * inv_asp;
+}
+
+size_t smem_box_x1(const CaseDev& c) {
+  size_t ld = c.nx + 1;
+  size_t wld = c.cx.use_fft ? c.cx.L : 1;
+  return 32 * ld * 8 + 2 * 4 * wld * 16 + 64;
+}
+
+// Y2: rows i < nx (ortho x).  conv (y forward, dealiased), rhs, pinv_y -> s[1..3]
+__global__ void __launch_bounds__(256) k_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y;
+  const int nx = c.nx, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, mxc = c.mxc;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double dt = c.dt;
+  extern __shared__ double2 smem[];
+  double* CV = reinterpret_cast<double*>(smem);  // 3 lanes
+  double* SX = CV + 3 * ld;   // 3 lanes: Sx f (composite y)
+  double* O = SX + 3 * ld;    // 3 lanes
+  double* R = O + 3 * ld;     // 3 lanes
+  double* P = R + 3 * ld;
+  double* G = P + ld;
+  double* TMP = G + ld;       // 3 lanes
+  double2* WA = reinterpret_cast<double2*>(TMP + 3 * ld + 2);
+  WA = reinterpret_cast<double2*>((reinterpret_cast<size_t>(WA) + 15) & ~size_t(15));
+  const int wld = c.cy.use_fft ? c.cy.L : 1;
+  double2* WB = WA + 2 * wld;
+  (void)nx;
+  if (i < kx) {
+    const double* q = static_cast<const double*>(c.q[0]);
+    for (int idx = tid; idx < 3 * ny; idx += nth) {
+      int f = idx / ny, k = idx - f * ny;
+      TMP[f * ld + k] = q[(size_t)f * kx * ny + (size_t)i * ny + k];
+    }
+    __syncthreads();
+    if (c.cy.use_fft) dct1_fft_r(c.cy, true, TMP, ld, CV, ld, 3, WA, WB, wld, tid, nth);
+    else dct1_dense<double>(c.cy, true, TMP, ld, CV, ld, 3, tid, nth);
+    for (int idx = tid; idx < 3 * ny; idx += nth) {
+      int f = idx / ny, k = idx - f * ny;
+      if (k >= ky) CV[f * ld + k] = 0.0;
+    }
+  } else {
+    for (int idx = tid; idx < 3 * ny; idx += nth) CV[(idx / ny) * ld + idx % ny] = 0.0;
+  }
+  // (Sx f)[i] = diag_i f[i] + low2_{i-2} f[i-2] for composite rows
+  void* f3[3] = {c.ux, c.uy, c.temp};
+  const BasisDev* xb[3] = {&c.xu, &c.xu, &c.xt};
+  for (int idx = tid; idx < 3 * myc; idx += nth) {
+    int f = idx / myc, k = idx - f * myc;
+    const double* a = static_cast<const double*>(f3[f]);
+    const BasisDev& b = *xb[f];
+    double v = 0.0;
+    bool has = false;
+    if (i < mxc) { v = a[(size_t)i * myc + k] * b.diag[i]; has = true; }
+    if (i >= 2 && i - 2 < mxc) {
+      double t = a[(size_t)(i - 2) * myc + k];
+      v = has ? fma(t, b.low2[i - 2], v) : t * b.low2[i - 2];
+    }
+    SX[f * ld + k] = v;
+  }
+  const double* p0 = static_cast<const double*>(c.p0);
+  for (int k = tid; k < ny; k += nth) P[k] = p0[(size_t)i * ny + k];
+  __syncthreads();
+  to_ortho<double>(c.ycd, SX, ld, O, ld, 3, tid, nth);
+  cheb_diff<double>(P, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);
+  const double* gpx = static_cast<const double*>(c.s[0]);
+  const double* bco = static_cast<const double*>(c.bc_ortho);
+  const double* bcd = static_cast<const double*>(c.bc_diff);
+  for (int k = tid; k < ny; k += nth) {
+    R[k] = fnms(fnms(O[k], gpx[(size_t)i * ny + k], dt), CV[k], dt);
+    double that = O[2 * ld + k] + bco[(size_t)i * ny + k];
+    R[ld + k] = fnms(fmas(fnms(O[ld + k], G[k], dt), that, dt), CV[ld + k], dt);
+    R[2 * ld + k] = fnms(O[2 * ld + k] + bcd[(size_t)i * ny + k], CV[2 * ld + k], dt);
+  }
+  __syncthreads();
+  matvec_pinv<double>(c.pinv_y, R, ld, O, ld, 3, tid, nth);
+  for (int idx = tid; idx < 3 * myc; idx += nth) {
+    int f = idx / myc, k = idx - f * myc;
+    static_cast<double*>(c.s[1 + f])[(size_t)i * myc + k] = O[f * ld + k];
+  }
+}
+
+size_t smem_box_y2(const CaseDev& c) {
+  size_t ld = c.ny + 1;
+  size_t wld = c.cy.use_fft ? c.cy.L : 1;
+  return 17 * ld * 8 + 2 * 2 * wld * 16 + 64;
+}
+
+// X2: columns j < myc.  pinv_x then the ADI x solve.  s[1..3] -> s[4..6] (mxc x myc)
+__global__ void __launch_bounds__(256) k_box_x2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int j = w.y;
+  const int nx = c.nx, myc = c.myc, mxc = c.mxc;
+  const int ld = nx + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  extern __shared__ double2 smem[];
+  double* IN = reinterpret_cast<double*>(smem);
+  double* OUT = IN + 3 * ld;
+  for (int idx = tid; idx < 3 * nx; idx += nth) {
+    int f = idx / nx, k = idx - f * nx;
+    IN[f * ld + k] = static_cast<const double*>(c.s[1 + f])[(size_t)k * myc + j];
+  }
+  __syncthreads();
+  matvec_pinv<double>(c.pinv_x, IN, ld, OUT, ld, 3, tid, nth);
+  fdma_solve<double>(c.hu_x, OUT, ld, 2, 0, 0, tid, nth);
+  fdma_solve<double>(c.ht_x, OUT + 2 * ld, ld, 1, 0, 0, tid, nth);
+  for (int idx = tid; idx < 3 * mxc; idx += nth) {
+    int f = idx / mxc, k = idx - f * mxc;
+    static_cast<double*>(c.s[4 + f])[(size_t)k * myc + j] = OUT[f * ld + k];
+  }
+}
+
+size_t smem_box_x2(const CaseDev& c) { return 6 * (size_t)(c.nx + 1) * 8 + 64; }
+
+// Y3: rows i < mxc.  ADI y solve -> ux*, uy*, temp(new); A = Sy ux*, B = Dy Sy uy*
+__global__ void __launch_bounds__(256) k_box_y3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y;
+  const int ny = c.ny, myc = c.myc;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  extern __shared__ double2 smem[];
+  double* F = reinterpret_cast<double*>(smem);
+  double* O = F + 3 * ld;
+  double* B = O + 2 * ld;
+  double* TMP = B + ld;
+  for (int idx = tid; idx < 3 * myc; idx += nth) {
+    int f = idx / myc, k = idx - f * myc;
+    F[f * ld + k] = static_cast<const double*>(c.s[4 + f])[(size_t)i * myc + k];
+  }
+  __syncthreads();
+  fdma_solve<double>(c.hu_y, F, ld, 2, 0, 0, tid, nth);
+  fdma_solve<double>(c.ht_y, F + 2 * ld, ld, 1, 0, 0, tid, nth);
+  to_ortho<double>(c.ycd, F, ld, O, ld, 2, tid, nth);
+  cheb_diff<double>(O + ld, ld, B, ld, ny, 1, 1, TMP, ld, tid, nth);
+  // ux*, uy* -> s[4], s[5] (in place);  temp -> state
+  bool bad = false;
+  double* tt = static_cast<double*>(c.temp);
+  for (int idx = tid; idx < 3 * myc; idx += nth) {
+    int f = idx / myc, k = idx - f * myc;
+    double v = F[f * ld + k];
+    if (f < 2) static_cast<double*>(c.s[4 + f])[(size_t)i * myc + k] = v;
+    else tt[(size_t)i * myc + k] = v;
+    bad |= !isfinite(v);
+  }
+  double* A = static_cast<double*>(c.s[1]);   // mxc x ny
+  double* Bs = static_cast<double*>(c.s[2]);  // mxc x ny
+  for (int k = tid; k < ny; k += nth) {
+    A[(size_t)i * ny + k] = O[k];
+    Bs[(size_t)i * ny + k] = B[k];
+  }
+  if (bad) flag_nonfinite(c.status);
+}
+
+size_t smem_box_y3(const CaseDev& c) { return 8 * (size_t)(c.ny + 1) * 8 + 64; }
+
+// X3: columns j < ny.  div = Dx Sx A / s + Sx B  (-> s[3], nx x ny);
+// Zf = fwd * pinv_x div  (-> s[1] reused? no: s[6], mxc x ny)
+__global__ void __launch_bounds__(256) k_box_x3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int j = w.y;
+  const int nx = c.nx, ny = c.ny, mxc = c.mxc;
+  const int ld = nx + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double inv_asp = 1.0 / c.aspect;
+  extern __shared__ double2 smem[];
+  double* IN = reinterpret_cast<double*>(smem);  // 2 lanes (mxc)
+  double* OR = IN + 2 * ld;                      // 2 lanes (nx)
+  double* DV = OR + 2 * ld;                      // div lane
+  double* Z = DV + ld;                           // pinv lane
+  double* TMP = Z + ld;                          // 2 lanes
+  const double* A = static_cast<const double*>(c.s[1]);
+  const double* B = static_cast<const double*>(c.s[2]);
+  for (int k = tid; k < mxc; k += nth) {
+    IN[k] = A[(size_t)k * ny + j];
+    IN[ld + k] = B[(size_t)k * ny + j];
+  }
+  __syncthreads();
+  to_ortho<double>(c.xu, IN, ld, OR, ld, 2, tid, nth);
+  cheb_diff<double>(OR, ld, TMP, ld, nx, 1, 1, TMP + ld, ld, tid, nth);
+  double* dv = static_cast<double*>(c.s[3]);
+  for (int k = tid; k < nx; k += nth) {
+    double v = TMP[k] * inv_asp + OR[ld + k];
+    DV[k] = v;
+    dv[(size_t)k * ny + j] = v;
+  }
+  __syncthreads();
+  matvec_pinv<double>(c.pinv_x, DV, ld, Z, ld, 1, tid, nth);
+  // dense eigenbasis forward along x
+  double* zf = static_cast<double*>(c.s[6]);
+  for (int r = tid; r < mxc; r += nth) {
+    const double* row = c.pois_fwd + (size_t)r * mxc;
+    double acc = 0.0;
+    for (int k = 0; k < mxc; k++) acc = fma(__ldg(row + k), Z[k], acc);
+    zf[(size_t)r * ny + j] = acc;
+  }
+}
+
+size_t smem_box_x3(const CaseDev& c) { return 8 * (size_t)(c.nx + 1) * 8 + 64; }
+
+// Y4: rows i < mxc.  pinv_y then the Poisson row solve (eigen row i) -> s[7] (mxc x myc)
+__global__ void __launch_bounds__(256) k_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y;
+  const int ny = c.ny, myc = c.myc;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  extern __shared__ double2 smem[];
+  double* IN = reinterpret_cast<double*>(smem);
+  double* OUT = IN + ld;
+  const double* zf = static_cast<const double*>(c.s[6]);
+  for (int k = tid; k < ny; k += nth) IN[k] = zf[(size_t)i * ny + k];
+  __syncthreads();
+  matvec_pinv<double>(c.pinv_y, IN, ld, OUT, ld, 1, tid, nth);
+  fdma_solve<double>(c.pois_y, OUT, ld, 1, i, 0, tid, nth);
+  double* wv = static_cast<double*>(c.s[7]);
+  for (int k = tid; k < myc; k += nth) wv[(size_t)i * myc + k] = OUT[k];
+}
+
+size_t smem_box_y4(const CaseDev& c) { return 2 * (size_t)(c.ny + 1) * 8 + 64; }
+
+// X4: columns j < myc.  p1 = bwd * W (p1[0][0] = 0).  E = Sx+ Dx Sx^N p1 / s,
+// Fv = Sx+ Sx^N p1 (-> s[1], s[2] as mxc x myc), Gp = Sx^N p1 (-> s[0], nx x myc)
+__global__ void __launch_bounds__(256) k_box_x4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int j = w.y;
+  const int nx = c.nx, myc = c.myc, mxc = c.mxc;
+  const int ld = nx + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double inv_asp = 1.0 / c.aspect;
+  extern __shared__ double2 smem[];
+  double* W = reinterpret_cast<double*>(smem);
+  double* PV = W + ld;
+  double* OR = PV + ld;       // Sx^N p1 (nx)
+  double* D = OR + ld;        // 2 lanes: Dx OR / s, OR copy
+  double* FO = D + 2 * ld;    // 2 lanes from_ortho
+  double* TMP = FO + 2 * ld;  // 2 lanes
+  const double* wv = static_cast<const double*>(c.s[7]);
+  for (int k = tid; k < mxc; k += nth) W[k] = wv[(size_t)k * myc + j];
+  __syncthreads();
+  double* p1 = static_cast<double*>(c.p1);
+  for (int r = tid; r < mxc; r += nth) {
+    const double* row = c.pois_bwd + (size_t)r * mxc;
+    double acc = 0.0;
+    for (int k = 0; k < mxc; k++) acc = fma(__ldg(row + k), W[k], acc);
+    if (j == 0 && r == 0) acc = 0.0;
+    PV[r] = acc;
+    p1[(size_t)r * myc + j] = acc;
+  }
+  __syncthreads();
+  to_ortho<double>(c.xp, PV, ld, OR, ld, 1, tid, nth);
+  cheb_diff<double>(OR, ld, TMP, ld, nx, 1, 1, TMP + ld, ld, tid, nth);
+  double* gp = static_cast<double*>(c.s[0]);
+  for (int k = tid; k < nx; k += nth) {
+    D[k] = TMP[k] * inv_asp;
+    D[ld + k] = OR[k];
+    gp[(size_t)k * myc + j] = OR[k];
+  }
+  __syncthreads();
+  from_ortho<double>(c.xu, D, ld, FO, ld, 2, tid, nth);
+  double* e = static_cast<double*>(c.s[1]);
+  double* fv = static_cast<double*>(c.s[2]);
+  for (int k = tid; k < mxc; k += nth) {
+    e[(size_t)k * myc + j] = FO[k];
+    fv[(size_t)k * myc + j] = FO[ld + k];
+  }
+}
+
+size_t smem_box_x4(const CaseDev& c) { return 9 * (size_t)(c.nx + 1) * 8 + 64; }
+
+// Y5: rows i < nx.  ux = ux* - Sy+ Sy^N E ; uy = uy* - Sy+ Dy Sy^N Fv ;
+// p0 = (p0 - nu div) + Sy^N Gp / dt
+__global__ void __launch_bounds__(256) k_box_y5(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y;
+  const int ny = c.ny, myc = c.myc, mxc = c.mxc;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  extern __shared__ double2 smem[];
+  double* IN = reinterpret_cast<double*>(smem);  // 3 lanes (myc): E, Fv, Gp
+  double* OR = IN + 3 * ld;                      // 3 lanes
+  double* D = OR + 3 * ld;                       // 2 lanes: dpdx, dpdy
+  double* FO = D + 2 * ld;                       // 2 lanes
+  double* TMP = FO + 2 * ld;
+  const double* e = static_cast<const double*>(c.s[1]);
+  const double* fv = static_cast<const double*>(c.s[2]);
+  const double* gp = static_cast<const double*>(c.s[0]);
+  for (int k = tid; k < myc; k += nth) {
+    if (i < mxc) {
+      IN[k] = e[(size_t)i * myc + k];
+      IN[ld + k] = fv[(size_t)i * myc + k];
+    }
+    IN[2 * ld + k] = gp[(size_t)i * myc + k];
+  }
+  __syncthreads();
+  if (i < mxc) {
+    to_ortho<double>(c.ycn, IN, ld, OR, ld, 2, tid, nth);
+    cheb_diff<double>(OR + ld, ld, D + ld, ld, ny, 1, 1, TMP, ld, tid, nth);
+    for (int k = tid; k < ny; k += nth) D[k] = OR[k];
+    __syncthreads();
+    from_ortho<double>(c.ycd, D, ld, FO, ld, 2, tid, nth);
+    double* ux = static_cast<double*>(c.ux);
+    double* uy = static_cast<double*>(c.uy);
+    const double* us = static_cast<const double*>(c.s[4]);
+    const double* vs = static_cast<const double*>(c.s[5]);
+    bool bad = false;
+    for (int k = tid; k < myc; k += nth) {
+      double a = us[(size_t)i * myc + k] - FO[k];
+      double b = vs[(size_t)i * myc + k] - FO[ld + k];
+      ux[(size_t)i * myc + k] = a;
+      uy[(size_t)i * myc + k] = b;
+      bad |= !(isfinite(a) && isfinite(b));
+    }
+    if (bad) flag_nonfinite(c.status);
+  }
+  to_ortho<double>(c.ycn, IN + 2 * ld, ld, OR + 2 * ld, ld, 1, tid, nth);
+  double* p0 = static_cast<double*>(c.p0);
+  const double* dv = static_cast<const double*>(c.s[3]);
+  for (int k = tid; k < ny; k += nth) {
+    double v = fnms(p0[(size_t)i * ny + k], dv[(size_t)i * ny + k], c.nu);
+    p0[(size_t)i * ny + k] = fmas(v, OR[2 * ld + k], c.inv_dt);
+  }
+}
+
+size_t smem_box_y5(const CaseDev& c) { return 12 * (size_t)(c.ny + 1) * 8 + 64; }
+
+}  // namespace dev
+
+// ---------------------------------------------------------------------------
+// host-side launch helpers
+// ---------------------------------------------------------------------------
+static inline size_t clamp_smem(size_t s) { return (s + 127) & ~size_t(127); }
+
+cudaError_t configure_step_kernels() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  const int big = 200 * 1024;
+  cudaError_t e;
+#define SET_ATTR(k)                                                                          \
+  e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, big);             \
+  if (e != cudaSuccess) return e;
+  SET_ATTR(dev::k_y1<double>);
+  SET_ATTR(dev::k_y1<double2>);
+  SET_ATTR(dev::k_per_x);
+  SET_ATTR(dev::k_per_y2);
+  SET_ATTR(dev::k_box_x1);
+  SET_ATTR(dev::k_box_y2);
+  SET_ATTR(dev::k_box_x2);
+  SET_ATTR(dev::k_box_y3);
+  SET_ATTR(dev::k_box_x3);
+  SET_ATTR(dev::k_box_y4);
+  SET_ATTR(dev::k_box_x4);
+  SET_ATTR(dev::k_box_y5);
+#undef SET_ATTR
+  done = true;
+  return cudaSuccess;
+}
+
+StepPlan build_step_plan(const CaseDev& c) {
+  StepPlan p;
+  bool per = c.kind == KIND_PERIODIC;
+  auto add = [&](int kernel, int lanes, size_t smem) {
+    StepLaunch L;
+    L.kernel = kernel;
+    L.smem = clamp_smem(smem);
+    for (int i = 0; i < lanes; i++) L.items.push_back(make_int4(0, i, 1, 0));
+    p.launches.push_back(L);
+  };
+  if (per) {
+    add(K_Y1_C, c.mxc, dev::smem_y1(c, 1, true));
+    add(K_PER_X, c.ny, dev::smem_per_x(c));
+    add(K_PER_Y2, c.mx, dev::smem_per_y2(c));
+  } else {
+    add(K_Y1_R, c.mxc, dev::smem_y1(c, 1, false));
+    add(K_BOX_X1, c.ny, dev::smem_box_x1(c));
+    add(K_BOX_Y2, c.nx, dev::smem_box_y2(c));
+    add(K_BOX_X2, c.myc, dev::smem_box_x2(c));
+    add(K_BOX_Y3, c.mxc, dev::smem_box_y3(c));
+    add(K_BOX_X3, c.ny, dev::smem_box_x3(c));
+    add(K_BOX_Y4, c.mxc, dev::smem_box_y4(c));
+    add(K_BOX_X4, c.myc, dev::smem_box_x4(c));
+    add(K_BOX_Y5, c.nx, dev::smem_box_y5(c));
+  }
+  return p;
+}
+
+cudaError_t launch_step_kernel(int kernel, int nblocks, size_t smem, cudaStream_t s, const CaseDev* cases,
+                               const int4* work) {
+  dim3 g(nblocks), b(256);
+  switch (kernel) {
+    case K_Y1_C: dev::k_y1<double2><<<g, b, smem, s>>>(cases, work); break;
+    case K_Y1_R: dev::k_y1<double><<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_X: dev::k_per_x<<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_Y2: dev::k_per_y2<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X1: dev::k_box_x1<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y2: dev::k_box_y2<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X2: dev::k_box_x2<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y3: dev::k_box_y3<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X3: dev::k_box_x3<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y4: dev::k_box_y4<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X4: dev::k_box_x4<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y5: dev::k_box_y5<<<g, b, smem, s>>>(cases, work); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace rbc

@@ -1,0 +1,174 @@
+"""Parity of the CUDA path against the CPU FP64 oracle (same seeded inputs).
+
+Tolerances: relative L2 per field <= 1e-10 after 10 steps; Nusselt number and
+kinetic energy <= 1e-9 relative after 100 steps (config 0); funspace
+primitives and solvers <= 1e-12 relative (single operations).
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = (O.TEMP, O.UX, O.UY, O.PRES0, O.PRES1)
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+@pytest.fixture(scope="module")
+def R():
+    from rustpde_gb300 import build
+    build.build()
+    import rustpde_gb300
+    return rustpde_gb300
+
+
+def pair(R, kind, nx, ny, ra, pr, dt, asp, seed=1):
+    o = O.Navier2D(nx, ny, ra, pr, dt, asp, kind)
+    O.standard_ic(o, seed)
+    g = R.Navier2D(nx, ny, ra, pr, dt, asp, kind, seed=None)
+    R.standard_ic(g, seed)
+    return o, g
+
+
+CASES = {
+    "box64": (O.BOX_ADIABATIC, 64, 64, 1e5, 1.0, 0.02, 1.0),
+    "box_cond33": (O.BOX_CONDUCTING, 33, 33, 1e5, 1.0, 0.01, 1.5),
+    "periodic64x33": (O.PERIODIC, 64, 33, 1e5, 1.0, 0.005, 1.0),
+    "periodic512x257": (O.PERIODIC, 512, 257, 1e7, 1.0, 1e-3, 2.0),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_initial_state_and_fieldbc(R, name):
+    o, g = pair(R, *CASES[name])
+    for f in FIELDS + (O.FIELDBC,):
+        a, b = g.get(f), o.get(f)
+        assert a.shape == b.shape
+        if np.linalg.norm(b) == 0:
+            assert np.linalg.norm(a) == 0
+        else:
+            assert rel(a, b) < 1e-12, (f, rel(a, b))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_ten_steps_per_field(R, name):
+    o, g = pair(R, *CASES[name])
+    o.update(10)
+    g.update(10)
+    for f in FIELDS:
+        e = rel(g.get(f), o.get(f))
+        assert e < 1e-10, (name, f, e)
+    assert g.status() == 0
+    assert abs(g.get_time() - o.time) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["box64", "periodic64x33"])
+def test_diagnostics(R, name):
+    o, g = pair(R, *CASES[name])
+    o.update(5)
+    g.update(5)
+    for what in (O.NU, O.NUVOL, O.RE, O.KE, O.DIVNORM):
+        a, b = g.eval(what), o.eval(what)
+        assert abs(a - b) <= 1e-10 * abs(b) + 1e-14, (what, a, b)
+
+
+def test_config0_100_steps_nu_ke(R):
+    o, g = pair(R, *CASES["box64"])
+    o.update(100)
+    g.update(100)
+    for what in (O.NU, O.KE):
+        a, b = g.eval(what), o.eval(what)
+        assert abs(a - b) <= 1e-9 * abs(b), (what, a, b)
+
+
+def test_step_is_deterministic(R):
+    _, g1 = pair(R, *CASES["periodic64x33"])
+    _, g2 = pair(R, *CASES["periodic64x33"])
+    g1.update(7)
+    g2.update(7)
+    for f in FIELDS:
+        assert np.array_equal(g1.get(f), g2.get(f))
+
+
+# ------------------------------------------------------------------ primitives
+SPACES = [
+    (O.CHEB, 16, O.CHEB, 12),
+    (O.CD, 17, O.CN, 12),
+    (O.CN, 20, O.CD, 33),
+    (O.CHEB, 9, O.CDBC, 17),
+    (O.FOURIER, 16, O.CD, 17),
+    (O.FOURIER, 32, O.CN, 12),
+    (O.FOURIER, 8, O.CHEB, 65),
+]
+
+
+@pytest.mark.parametrize("sp", SPACES)
+def test_funspace_primitives(R, sp):
+    k0, n0, k1, n1 = sp
+    os_ = O.Space2(k0, n0, k1, n1)
+    gs = R.Space2(R.Base(k0, n0), R.Base(k1, n1))
+    assert gs.physical == os_.phys and gs.spectral == os_.spec and gs.ortho == os_.ortho
+    rng = np.random.default_rng(n0 * 100 + n1)
+    v = rng.standard_normal(os_.phys)
+    vh_o = os_.forward(v)
+    vh_g = gs.forward(v)
+    assert rel(vh_g, vh_o) < 1e-12
+    assert rel(gs.backward(vh_o), os_.backward(vh_o)) < 1e-12
+    assert rel(gs.to_ortho(vh_o), os_.to_ortho(vh_o)) < 1e-13
+    orth = os_.to_ortho(vh_o)
+    assert rel(gs.from_ortho(orth), os_.from_ortho(orth)) < 1e-12
+    for d in ((1, 0), (0, 1), (2, 0), (0, 2), (1, 1)):
+        for scale in (None, (1.7, 0.8)):
+            a = gs.gradient(vh_o, d, scale)
+            b = os_.gradient(vh_o, d, scale)
+            assert rel(a, b) < 1e-12, (d, scale, rel(a, b))
+
+
+SOLVER_CASES = [
+    (O.CD, 16, O.CD, 12, O.HHOLTZ_ADI, (1e-3, 2e-3)),
+    (O.CN, 18, O.CD, 14, O.HHOLTZ_ADI, (0.5, 0.1)),
+    (O.CD, 16, O.CD, 12, O.HHOLTZ, (1e-2, 1e-2)),
+    (O.CN, 18, O.CN, 14, O.POISSON, (1.0, 1.0)),
+    (O.CD, 8, O.CD, 7, O.POISSON, (1.0, 1.0)),
+    (O.FOURIER, 16, O.CD, 17, O.HHOLTZ, (1e-3, 1e-3)),
+    (O.FOURIER, 32, O.CN, 17, O.POISSON, (0.25, 1.0)),
+    (O.FOURIER, 16, O.CD, 9, O.HHOLTZ_ADI, (1e-5, 1e-5)),
+]
+
+
+@pytest.mark.parametrize("case", SOLVER_CASES)
+def test_solvers(R, case):
+    k0, n0, k1, n1, kind, c = case
+    os_ = O.Space2(k0, n0, k1, n1)
+    gs = R.Space2(R.Base(k0, n0), R.Base(k1, n1))
+    rng = np.random.default_rng(7)
+    rhs = rng.standard_normal(os_.ortho)
+    if os_.cpx:
+        rhs = rhs + 1j * rng.standard_normal(os_.ortho)
+    xo = O.Solver(os_, kind, c).solve(rhs)
+    cls = {O.HHOLTZ: R.Hholtz, O.HHOLTZ_ADI: R.HholtzAdi, O.POISSON: R.Poisson}[kind]
+    xg = cls(gs, c).solve(rhs)
+    tol = 1e-9 if kind == O.POISSON else 1e-12
+    assert rel(xg, xo) < tol, rel(xg, xo)
+
+
+def test_reference_kat_hholtz_adi_2d(R, kats):
+    # src/solver/hholtz_adi.rs:175-207 through the GPU solver
+    gs = R.Space2(R.cheb_dirichlet(7), R.cheb_dirichlet(7))
+    b = np.tile(np.arange(1.0, 8.0), (7, 1))
+    x = R.HholtzAdi(gs, (1.0, 1.0)).solve(b)
+    exp = np.array(kats["hholtz_adi_2d"]["values"])
+    assert np.all(np.abs(x - exp) <= 5.1e-4 * np.abs(exp) + 1e-12)
+
+
+def test_reference_kat_poisson_2d(R, kats):
+    # src/solver/poisson.rs:207-240
+    gs = R.Space2(R.cheb_dirichlet(8), R.cheb_dirichlet(7))
+    b = np.tile(np.arange(1.0, 8.0), (8, 1))
+    x = R.Poisson(gs, (1.0, 1.0)).solve(b)
+    assert np.max(np.abs(x - np.array(kats["poisson_2d"]["values"]))) < 1e-6
