@@ -174,6 +174,13 @@ def run_ours(args, rank, world, local):
     # warm-up
     nav.update(args.warmup)
     nav.synchronize()
+    if args.quick:
+        t0 = time.perf_counter()
+        nav.update(args.steps)
+        nav.synchronize()
+        dt = time.perf_counter() - t0
+        return {"metric": METRIC, "value": GP * args.steps / dt, "unit": "grid-pt-steps/s", "steps": args.steps,
+                "warmup": args.warmup, "mode": "quick (host wall clock, no L2 flush)", "status": nav.status()}
 
     barrier = None
     if world > 1:
@@ -333,6 +340,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--quick", action="store_true",
+                    help="only warm-up + timed steps (profiling target); prints a reduced line")
     args = ap.parse_args()
     rank, world, local = dist_info()
     if world > 1 and args.impl == "ours":

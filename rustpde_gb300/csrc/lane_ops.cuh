@@ -16,10 +16,19 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "chain_scan.cuh"
 #include "rbc_dev.h"
 
 namespace rbc {
 namespace dev {
+
+
+// quotient of non-negative idx < 2^31/n by n through a multiply-high
+struct FastDiv {
+  unsigned c;
+  __device__ __forceinline__ explicit FastDiv(int n) : c(0xFFFFFFFFu / (unsigned)n + 1u) {}
+  __device__ __forceinline__ int operator()(int idx) const { return (int)__umulhi((unsigned)idx, c); }
+};
 
 // ------------------------------------------------------------------ scalars
 __device__ __forceinline__ double2 c2(double a, double b) { return make_double2(a, b); }
@@ -72,8 +81,9 @@ __device__ __forceinline__ T stencil_at(const BasisDev& b, const T* c, int i) {
 template <class T>
 static __device__ void to_ortho(const BasisDev& b, const T* in, int in_ld, T* out, int out_ld, int nl, int tid, int nth) {
   int n = (b.kind == 5) ? b.m : b.n;
+  const FastDiv dn(n);
   for (int idx = tid; idx < nl * n; idx += nth) {
-    int l = idx / n, i = idx - l * n;
+    int l = dn(idx), i = idx - l * n;
     out[l * out_ld + i] = stencil_at(b, in + l * in_ld, i);
   }
   __syncthreads();
@@ -102,31 +112,39 @@ static __device__ void from_ortho(const BasisDev& b, const T* in, int in_ld, T* 
     __syncthreads();
     return;
   }
+  const FastDiv dm(m);
   for (int idx = tid; idx < nl * m; idx += nth) {
-    int l = idx / m, i = idx - l * m;
+    int l = dm(idx), i = idx - l * m;
     const T* p = in + l * in_ld;
     out[l * out_ld + i] = fmas(scal(p[i], b.diag[i]), p[i + 2], b.low2[i]);
   }
   __syncthreads();
-  // one thread per (lane, parity) chain
-  for (int t = tid; t < 2 * nl; t += nth) {
-    int l = t >> 1, par = t & 1;
-    T* d = out + l * out_ld;
-    // forward: g_i = (d_i - a_{i-2} g_{i-2}) / den_i
-    T g = scal(d[par], b.fo_dinv[par]);
-    d[par] = g;
-    for (int i = par + 2; i < m; i += 2) {
-      g = scal(fnms(d[i], g, b.fo_off[i - 2]), b.fo_dinv[i]);
-      d[i] = g;
-    }
-    // backward: x_j = g_j - w_j x_{j+2}
-    int top = ((m - 1 - par) & 1) ? m - 2 : m - 1;  // highest index of this parity
-    T x = d[top];
-    for (int j = top - 2; j >= 0; j -= 2) {
-      x = fnms(d[j], x, b.fo_w[j]);
-      d[j] = x;
-    }
-  }
+  // forward g_i = (d_i - a_{i-2} g_{i-2}) / den_i, then x_j = g_j - w_j x_{j+2},
+  // one group of threads per (lane, parity) chain
+  const double* __restrict__ off = b.fo_off;
+  const double* __restrict__ dinv = b.fo_dinv;
+  const double* __restrict__ w = b.fo_w;
+  auto len_of = [&](int c) { return (m - (c & 1) + 1) >> 1; };
+  chains1<16, T>(
+      2 * nl, len_of,
+      [&](int c, int t, double& a, T& v) {
+        int i = (c & 1) + 2 * t;
+        T d = out[(c >> 1) * out_ld + i];
+        double q = dinv[i];
+        a = t ? -off[i - 2] * q : 0.0;
+        v = scal(d, q);
+      },
+      [&](int c, int t, T x) { out[(c >> 1) * out_ld + (c & 1) + 2 * t] = x; }, tid, nth);
+  __syncthreads();
+  auto top_of = [&](int c) { int par = c & 1; return ((m - 1 - par) & 1) ? m - 2 : m - 1; };
+  chains1<16, T>(
+      2 * nl, len_of,
+      [&](int c, int t, double& a, T& v) {
+        int j = top_of(c) - 2 * t;
+        v = out[(c >> 1) * out_ld + j];
+        a = t ? -w[j] : 0.0;
+      },
+      [&](int c, int t, T x) { out[(c >> 1) * out_ld + top_of(c) - 2 * t] = x; }, tid, nth);
   __syncthreads();
 }
 
@@ -151,8 +169,9 @@ static __device__ void cheb_diff(const T* in, int in_ld, T* out, int out_ld, int
     T* dst = (t == times - 1) ? out : tmp;
     int dst_ld = (t == times - 1) ? out_ld : tmp_ld;
     // d_0 = a_1; d_i = 2(i+1) a_{i+1} (1 <= i <= n-2); d_{n-1} = 0
+    const FastDiv dn(n);
     for (int idx = tid; idx < nl * n; idx += nth) {
-      int l = idx / n, i = idx - l * n;
+      int l = dn(idx), i = idx - l * n;
       const T* a = src + l * src_ld;
       T v;
       if (i == 0) v = a[1];
@@ -161,21 +180,26 @@ static __device__ void cheb_diff(const T* in, int in_ld, T* out, int out_ld, int
       dst[l * dst_ld + i] = v;
     }
     __syncthreads();
-    // suffix recurrence d_i += d_{i+2} for i = n-3 .. 1, then d_0 += d_2 / 2
-    for (int q = tid; q < 2 * nl; q += nth) {
-      int l = q >> 1, par = q & 1;
-      T* d = dst + l * dst_ld;
-      int top = ((n - 3 - par) & 1) ? n - 4 : n - 3;
-      if (top >= 1) {
-        T acc = d[top + 2];
-        for (int i = top; i >= 1; i -= 2) {
-          acc = d[i] + acc;
-          d[i] = acc;
-        }
-      }
-      if (par == 0) d[0] = fmas(d[0], d[2], 0.5);
+    // suffix sums d_i += d_{i+2} for i = n-3 .. 1 (per parity), then d_0 += d_2 / 2
+    {
+      T* dd = dst;
+      const int dl = dst_ld;
+      auto top2 = [&](int c) { int par = c & 1; return ((n - 3 - par) & 1) ? n - 2 : n - 1; };  // start element
+      auto len_of = [&](int c) {
+        int par = c & 1, st = top2(c), lo = par ? 1 : 2;
+        return st >= lo ? (st - lo) / 2 + 1 : 1;
+      };
+      chains1<16, T>(
+          2 * nl, len_of,
+          [&](int c, int t, double& a, T& v) {
+            v = dd[(c >> 1) * dl + top2(c) - 2 * t];
+            a = t ? 1.0 : 0.0;
+          },
+          [&](int c, int t, T x) { dd[(c >> 1) * dl + top2(c) - 2 * t] = x; }, tid, nth);
+      __syncthreads();
+      for (int l = tid; l < nl; l += nth) dd[l * dl] = fmas(dd[l * dl], dd[l * dl + 2], 0.5);
+      __syncthreads();
     }
-    __syncthreads();
     src = dst;
     src_ld = dst_ld;
   }
@@ -186,8 +210,9 @@ static __device__ void cheb_diff(const T* in, int in_ld, T* out, int out_ld, int
 template <class T>
 static __device__ void matvec_pinv(const PinvDev& p, const T* in, int in_ld, T* out, int out_ld, int nl, int tid, int nth) {
   int m = p.n - 2;
+  const FastDiv dm(m);
   for (int idx = tid; idx < nl * m; idx += nth) {
-    int l = idx / m, i = idx - l * m;
+    int l = dm(idx), i = idx - l * m;
     const T* a = in + l * in_ld;
     T v = scal(a[i], p.dia[i]);
     if (i < m - 2) v = fmas(v, a[i + 2], p.up1[i]);
@@ -197,38 +222,49 @@ static __device__ void matvec_pinv(const PinvDev& p, const T* in, int in_ld, T* 
   __syncthreads();
 }
 
-// In-place banded solve with swept factors; lane l uses factor row
-// (row0 + l*lane_step) when f.rows > 1.  One thread per (lane, parity) chain.
+// In-place banded solve with swept factors (offsets -2, 0, 2, 4; fdma.rs:101-118).
+// FdmaDev stores low = -low_swept, dinv = 1/dia, up1 = -up1/dia, up2 = -up2/dia.
+// Lanes l < split use factor set f0, the others f1; a factor set with rows > 1
+// gives lane l the row (row0 + l*lane_step).
 template <class T>
-static __device__ void fdma_solve(const FdmaDev& f, T* x, int ld, int nl, int row0, int lane_step, int tid, int nth) {
-  int m = f.m;
-  for (int t = tid; t < 2 * nl; t += nth) {
-    int l = t >> 1, par = t & 1;
-    size_t off = (f.rows > 1) ? (size_t)(row0 + l * lane_step) * f.stride : 0;
-    const double* low = f.low + off;
-    const double* dinv = f.dinv + off;
-    const double* up1 = f.up1 + off;
-    const double* up2 = f.up2 + off;
-    T* d = x + l * ld;
-    T prev = d[par];
-    for (int i = par + 2; i < m; i += 2) {
-      T v = fnms(d[i], prev, low[i - 2]);
-      d[i] = v;
-      prev = v;
-    }
-    int top = ((m - 1 - par) & 1) ? m - 2 : m - 1;
-    T x2 = zero_v<T>(), x4 = zero_v<T>();  // x_{i+2}, x_{i+4}
-    for (int i = top; i >= 0; i -= 2) {
-      T v = d[i];
-      if (i + 2 < m) v = fnms(v, x2, up1[i]);
-      if (i + 4 < m) v = fnms(v, x4, up2[i]);
-      v = scal(v, dinv[i]);
-      d[i] = v;
-      x4 = x2;
-      x2 = v;
-    }
-  }
+__device__ void fdma_solve2(const FdmaDev& f0, const FdmaDev& f1, int split, T* x, int ld, int nl, int row0,
+                            int lane_step, int tid, int nth) {
+  const int m = f0.m;
+  auto fac = [&](int l) -> const FdmaDev& { return l < split ? f0 : f1; };
+  auto offs = [&](int l) -> size_t {
+    const FdmaDev& f = fac(l);
+    return (f.rows > 1) ? (size_t)(row0 + l * lane_step) * f.stride : 0;
+  };
+  auto len_of = [&](int c) { return (m - (c & 1) + 1) >> 1; };
+  // forward elimination x_i -= low_{i-2} x_{i-2}
+  chains1<16, T>(
+      2 * nl, len_of,
+      [&](int c, int t, double& a, T& v) {
+        int l = c >> 1, i = (c & 1) + 2 * t;
+        v = x[l * ld + i];
+        a = t ? fac(l).low[offs(l) + i - 2] : 0.0;
+      },
+      [&](int c, int t, T v) { x[(c >> 1) * ld + (c & 1) + 2 * t] = v; }, tid, nth);
   __syncthreads();
+  // back substitution x_j = (x_j - up1_j x_{j+2} - up2_j x_{j+4}) / dia_j
+  auto top_of = [&](int c) { int par = c & 1; return ((m - 1 - par) & 1) ? m - 2 : m - 1; };
+  chains2<16, T>(
+      2 * nl, len_of,
+      [&](int c, int t, double& a, double& cc, T& v) {
+        int l = c >> 1, j = top_of(c) - 2 * t;
+        const FdmaDev& f = fac(l);
+        size_t o = offs(l);
+        v = scal(x[l * ld + j], f.dinv[o + j]);
+        a = t ? f.up1[o + j] : 0.0;
+        cc = t >= 2 ? f.up2[o + j] : 0.0;
+      },
+      [&](int c, int t, T v) { x[(c >> 1) * ld + top_of(c) - 2 * t] = v; }, tid, nth);
+  __syncthreads();
+}
+
+template <class T>
+__device__ void fdma_solve(const FdmaDev& f, T* x, int ld, int nl, int row0, int lane_step, int tid, int nth) {
+  fdma_solve2<T>(f, f, nl, x, ld, nl, row0, lane_step, tid, nth);
 }
 
 // ------------------------------------------------------------------ FFT
@@ -284,18 +320,18 @@ __device__ __forceinline__ double2* fft_pow2(double2* a, double2* b, int L, int 
 
 // ------------------------------------------------------------------ Chebyshev transforms
 // pre/post factors of ortho.rs:235-312 for index k of length n (N = n-1)
-__device__ __forceinline__ double cheb_fwd_post(int k, int n) {
-  double s = ((k & 1) ? -1.0 : 1.0) * (1.0 / (double)(n - 1));
+__device__ __forceinline__ double cheb_fwd_post(int k, int n, double inv_nm1) {
+  double s = (k & 1) ? -inv_nm1 : inv_nm1;
   return (k == 0 || k == n - 1) ? s * 0.5 : s;
 }
 __device__ __forceinline__ double cheb_bwd_pre(int k, int n) {
-  double s = ((k & 1) ? -1.0 : 1.0) / 2.0;
+  double s = (k & 1) ? -0.5 : 0.5;
   return (k == 0 || k == n - 1) ? s * 2.0 : s;
 }
 
-// Complex lanes, FFT variant: out = DCT-I(pre .* in) .* post
+// Complex lanes, FFT variant (length 2N, kept for reference): out = DCT-I(pre .* in) .* post
 // wa, wb: work lanes of length >= L with stride wld.
-static __device__ void dct1_fft_c(const ChebXformDev& cx, bool forward, const double2* in, int in_ld, double2* out,
+static __device__ void dct1_fft2_c(const ChebXformDev& cx, bool forward, const double2* in, int in_ld, double2* out,
                            int out_ld, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
   int n = cx.n, N = n - 1, L = cx.L;
   for (int idx = tid; idx < nl * L; idx += nth) {
@@ -310,13 +346,13 @@ static __device__ void dct1_fft_c(const ChebXformDev& cx, bool forward, const do
   for (int idx = tid; idx < nl * n; idx += nth) {
     int l = idx / n, k = idx - l * n;
     double2 v = r[l * wld + k];
-    out[l * out_ld + k] = forward ? v * cheb_fwd_post(k, n) : v;
+    out[l * out_ld + k] = forward ? v * cheb_fwd_post(k, n, cx.inv_nm1) : v;
   }
   __syncthreads();
 }
 
-// Real lanes, FFT variant: two real lanes per complex FFT.
-static __device__ void dct1_fft_r(const ChebXformDev& cx, bool forward, const double* in, int in_ld, double* out, int out_ld,
+// Real lanes, FFT variant (length 2N): two real lanes per complex FFT.
+static __device__ void dct1_fft2_r(const ChebXformDev& cx, bool forward, const double* in, int in_ld, double* out, int out_ld,
                            int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
   int n = cx.n, N = n - 1, L = cx.L;
   int np = (nl + 1) >> 1;
@@ -334,7 +370,121 @@ static __device__ void dct1_fft_r(const ChebXformDev& cx, bool forward, const do
     int l = idx / n, k = idx - l * n;
     double2 v = r[(l >> 1) * wld + k];
     double s = (l & 1) ? v.y : v.x;
-    out[l * out_ld + k] = forward ? s * cheb_fwd_post(k, n) : s;
+    out[l * out_ld + k] = forward ? s * cheb_fwd_post(k, n, cx.inv_nm1) : s;
+  }
+  __syncthreads();
+}
+
+// ---- DCT-I through a complex FFT of length N = n-1 (N a power of two).
+// For lanes z_0..z_N (complex, or two real lanes packed as re/im):
+//   Z_j = (z_j + z_{N-j}) - 2 sin(pi j/N) (z_j - z_{N-j}),   W = FFT_N(Z)
+//   C_{2k}   = (W_k + W_{N-k}) / 2                     k = 0 .. N/2
+//   C_{2k+1} = C_{2k-1} + (i/2) (W_k - W_{N-k})        k = 1 .. N/2-1
+//   C_1      = z_0 - z_N + 2 sum_{j=1}^{N-1} z_j cos(pi j/N)
+// (the pre-twiddled real-FFT route to REDFT00; the odd outputs are a prefix
+// sum computed with a warp scan).  cx.tw holds exp(-i pi t / N), t < 2N.
+struct DctLanesC {  // complex lanes
+  const double2* in;
+  int in_ld;
+  double2* out;
+  int out_ld;
+  __device__ double2 load(int l, int j) const { return in[l * in_ld + j]; }
+  __device__ void store(int l, int k, double2 v) const { out[l * out_ld + k] = v; }
+};
+struct DctLanesR {  // pairs of real lanes (2q, 2q+1) -> (re, im)
+  const double* in;
+  int in_ld;
+  double* out;
+  int out_ld;
+  int nl;  // real lanes
+  __device__ double2 load(int q, int j) const {
+    double a = in[(2 * q) * in_ld + j];
+    double b = (2 * q + 1 < nl) ? in[(2 * q + 1) * in_ld + j] : 0.0;
+    return c2(a, b);
+  }
+  __device__ void store(int q, int k, double2 v) const {
+    out[(2 * q) * out_ld + k] = v.x;
+    if (2 * q + 1 < nl) out[(2 * q + 1) * out_ld + k] = v.y;
+  }
+};
+
+template <class Lanes>
+static __device__ void dct1_half(const ChebXformDev& cx, bool forward, const Lanes& io, int nl, double2* wa,
+                                 double2* wb, int wld, int tid, int nth) {
+  const int n = cx.n, N = n - 1, lN = cx.log2L - 1, half = N >> 1;
+  const double2* __restrict__ tw = cx.tw;
+  const int lane_id = tid & 31, warp = tid >> 5, nwarp = nth >> 5;
+  // C_1 per lane (warp reduction), kept at wa[l*wld + N]
+  for (int l = warp; l < nl; l += nwarp) {
+    double2 acc = c2(0.0, 0.0);
+    for (int j = 1 + lane_id; j < N; j += 32) {
+      double2 v = io.load(l, j);
+      if (!forward) v = v * cheb_bwd_pre(j, n);
+      acc = fmas(acc, v, tw[j].x);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane_id == 0) {
+      double2 z0 = io.load(l, 0), zN = io.load(l, N);
+      if (!forward) { z0 = z0 * cheb_bwd_pre(0, n); zN = zN * cheb_bwd_pre(N, n); }
+      wa[l * wld + N] = (z0 - zN) + acc * 2.0;
+    }
+  }
+  for (int idx = tid; idx < nl * N; idx += nth) {
+    int l = idx >> lN, j = idx & (N - 1);
+    double2 a = io.load(l, j), b = io.load(l, N - j);
+    if (!forward) { a = a * cheb_bwd_pre(j, n); b = b * cheb_bwd_pre(N - j, n); }
+    double s2 = -2.0 * tw[j].y;  // 2 sin(pi j / N)
+    wa[l * wld + j] = fnms(a + b, a - b, s2);
+  }
+  __syncthreads();
+  double2* r = fft_pow2(wa, wb, N, lN, nl, wld, tw, 2 * N, false, tid, nth);
+  // even outputs
+  const FastDiv dh(half + 1);
+  for (int idx = tid; idx < nl * (half + 1); idx += nth) {
+    int l = dh(idx), k = idx - l * (half + 1);
+    double2 v = (r[l * wld + (k & (N - 1))] + r[l * wld + ((N - k) & (N - 1))]) * 0.5;
+    if (forward) v = v * cheb_fwd_post(2 * k, n, cx.inv_nm1);
+    io.store(l, 2 * k, v);
+  }
+  // odd outputs: prefix sum, one warp per lane
+  const int K = half - 1;
+  const int per = (K + 31) >> 5;
+  for (int l = warp; l < nl; l += nwarp) {
+    const double2* rl = r + l * wld;
+    int k0 = 1 + lane_id * per;
+    double2 loc = c2(0.0, 0.0);
+    for (int t = 0; t < per; t++) {
+      int k = k0 + t;
+      if (k <= K) {
+        double2 d = rl[k] - rl[N - k];
+        loc = loc + c2(-0.5 * d.y, 0.5 * d.x);
+      }
+    }
+    // exclusive warp scan of the chunk sums
+    double2 inc = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      double ux = __shfl_up_sync(0xffffffffu, inc.x, o);
+      double uy = __shfl_up_sync(0xffffffffu, inc.y, o);
+      if (lane_id >= o) { inc.x += ux; inc.y += uy; }
+    }
+    double2 run = wa[l * wld + N] + (inc - loc);  // C_1 + sum of the previous chunks
+    if (lane_id == 0) {
+      double2 c1 = wa[l * wld + N];
+      io.store(l, 1, forward ? c1 * cheb_fwd_post(1, n, cx.inv_nm1) : c1);
+    }
+    for (int t = 0; t < per; t++) {
+      int k = k0 + t;
+      if (k <= K) {
+        double2 d = rl[k] - rl[N - k];
+        run = run + c2(-0.5 * d.y, 0.5 * d.x);
+        io.store(l, 2 * k + 1, forward ? run * cheb_fwd_post(2 * k + 1, n, cx.inv_nm1) : run);
+      }
+    }
   }
   __syncthreads();
 }
@@ -408,5 +558,23 @@ static __device__ void r2c(const FourierXformDev& fx, const double* in, int in_l
   __syncthreads();
 }
 
+}  // namespace dev
+}  // namespace rbc
+
+namespace rbc {
+namespace dev {
+// DCT-I of complex / real lanes through the half-length FFT (n = 2^p + 1).
+// `in` and `out` may alias.  wa, wb: work lanes of length >= n with stride wld.
+static __device__ void dct1_fft_c(const ChebXformDev& cx, bool forward, const double2* in, int in_ld, double2* out,
+                                  int out_ld, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  // the outputs are written after every input has been read (C_1 and Z use a barrier)
+  DctLanesC io{in, in_ld, out, out_ld};
+  dct1_half(cx, forward, io, nl, wa, wb, wld, tid, nth);
+}
+static __device__ void dct1_fft_r(const ChebXformDev& cx, bool forward, const double* in, int in_ld, double* out,
+                                  int out_ld, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  DctLanesR io{in, in_ld, out, out_ld, nl};
+  dct1_half(cx, forward, io, (nl + 1) >> 1, wa, wb, wld, tid, nth);
+}
 }  // namespace dev
 }  // namespace rbc

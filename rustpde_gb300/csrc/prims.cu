@@ -63,6 +63,7 @@ ChebXformDev upload_cheb(Arena& a, int n) {
   std::memset(&d, 0, sizeof d);
   d.n = n;
   int N = n - 1;
+  d.inv_nm1 = 1.0 / (double)(n - 1);
   d.use_fft = (N >= 2 && is_pow2(N)) ? 1 : 0;
   if (d.use_fft) {
     d.L = 2 * N;
@@ -108,12 +109,14 @@ FdmaDev upload_fdma(Arena& a, const std::vector<Band4>& rows) {
   d.stride = m;
   std::vector<double> low((size_t)R * m, 0.0), dinv((size_t)R * m, 0.0), up1((size_t)R * m, 0.0),
       up2((size_t)R * m, 0.0);
+  // device form of the swept factors: low negated, 1/dia, and the upper
+  // diagonals divided by dia and negated (x_j = x_j/dia_j + up1' x_{j+2} + up2' x_{j+4})
   for (int r = 0; r < R; r++) {
     const Band4& f = rows[r];
-    for (size_t i = 0; i < f.low.size(); i++) low[(size_t)r * m + i] = f.low[i];
+    for (size_t i = 0; i < f.low.size(); i++) low[(size_t)r * m + i] = -f.low[i];
     for (int i = 0; i < m; i++) dinv[(size_t)r * m + i] = 1.0 / f.dia[i];
-    for (size_t i = 0; i < f.up1.size(); i++) up1[(size_t)r * m + i] = f.up1[i];
-    for (size_t i = 0; i < f.up2.size(); i++) up2[(size_t)r * m + i] = f.up2[i];
+    for (size_t i = 0; i < f.up1.size(); i++) up1[(size_t)r * m + i] = -f.up1[i] / f.dia[i];
+    for (size_t i = 0; i < f.up2.size(); i++) up2[(size_t)r * m + i] = -f.up2[i] / f.dia[i];
   }
   d.low = a.upload(low);
   d.dinv = a.upload(dinv);

@@ -39,10 +39,10 @@ struct FdmaDev {
   int rows;
   int stride;
   int pad_;
-  const double* low;   // swept low (m-2)
+  const double* low;   // -low of the swept factors (m-2)
   const double* dinv;  // 1/dia (m)
-  const double* up1;   // swept up1 (m-2)
-  const double* up2;   // up2 (m-4)
+  const double* up1;   // -up1/dia (m-2)
+  const double* up2;   // -up2/dia (m-4)
 };
 
 // Chebyshev transform along an axis of length n: FFT (n = 2^p + 1) or dense.
@@ -52,6 +52,7 @@ struct ChebXformDev {
   int L;              // FFT length
   int log2L;
   const double2* tw;  // exp(-2 pi i t / L), t < L
+  double inv_nm1;     // 1 / (n - 1)
   const double* fwd;  // dense n x n forward matrix (row = output)
   const double* bwd;  // dense n x n backward matrix
 };

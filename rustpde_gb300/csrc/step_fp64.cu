@@ -153,27 +153,53 @@ size_t smem_per_x(const CaseDev& c) {
 // solves (Hholtz per row), divergence, Poisson row solve, projection and the
 // pressure update (navier.rs:622-721).
 // ============================================================================
+// stage the factors of row `row` of a per-row banded solver into shared memory
+__device__ FdmaDev stage_fdma_row(const FdmaDev& f, int row, double* dst, int tid, int nth) {
+  const int m = f.m;
+  const size_t off = (f.rows > 1) ? (size_t)row * f.stride : 0;
+  for (int k = tid; k < m; k += nth) {
+    dst[k] = f.low[off + k];
+    dst[m + k] = f.dinv[off + k];
+    dst[2 * m + k] = f.up1[off + k];
+    dst[3 * m + k] = f.up2[off + k];
+  }
+  FdmaDev r = f;
+  r.rows = 1;
+  r.stride = 0;
+  r.low = dst;
+  r.dinv = dst + m;
+  r.up1 = dst + 2 * m;
+  r.up2 = dst + 3 * m;
+  return r;
+}
+
 __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
   const int i = w.y;
-  const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, mx = c.mx;
+  const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
   const int ld = ny + 1;
   const int tid = threadIdx.x, nth = blockDim.x;
   const double dt = c.dt, nu = c.nu, inv_asp = 1.0 / c.aspect, ki = (double)i;
   extern __shared__ double2 smem[];
-  double2* CV = smem;            // 3 lanes conv
-  double2* F = CV + 3 * ld;      // 3 lanes composite state (old, then new)
-  double2* O = F + 3 * ld;       // 3 lanes ortho of old state
-  double2* R = O + 3 * ld;       // 3 lanes rhs
-  double2* P = R + 3 * ld;       // p0 row
-  double2* G = P + ld;           // d/dy p0, later scratch
-  double2* X1 = G + ld;          // 3 scratch lanes
-  double2* TMP = X1 + 3 * ld;
-  double2* WA = TMP + 3 * ld;
+  double2* CV = smem;        // 3 lanes conv
+  double2* REG = CV + 3 * ld;
+  // during the convection transform REG holds the FFT work lanes; afterwards:
+  double2* F = REG;          // 3 lanes composite state (old, then new)
+  double2* O = F + 3 * ld;   // 3 lanes
+  double2* R = O + 3 * ld;   // 3 lanes rhs (lane 0 later: divergence)
+  double2* P = R + 3 * ld;   // p0 row
+  double2* G = P + ld;       // d/dy
+  double2* X1 = G + ld;      // 3 lanes
   const int wld = c.cy.use_fft ? c.cy.L : 1;
+  double2* WA = REG;
   double2* WB = WA + 3 * wld;
-  (void)mx;
+  const size_t reg_elems = max((size_t)14 * ld, (size_t)6 * wld);
+  double* FAC = reinterpret_cast<double*>(REG + reg_elems);
+  // per-row factors of the three banded solves
+  const FdmaDev fu = stage_fdma_row(c.hu_y, i, FAC, tid, nth);
+  const FdmaDev ft = stage_fdma_row(c.ht_y, i, FAC + 4 * myc, tid, nth);
+  const FdmaDev fp = stage_fdma_row(c.pois_y, i, FAC + 8 * myc, tid, nth);
 
   // 1. convection: forward Chebyshev transform of Q_f[i], dealiased
   if (i < kx) {
@@ -185,10 +211,10 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
     __syncthreads();
     if (c.cy.use_fft) dct1_fft_c(c.cy, true, CV, ld, CV, ld, 3, WA, WB, wld, tid, nth);
     else {
-      dct1_dense<double2>(c.cy, true, CV, ld, TMP, ld, 3, tid, nth);
+      dct1_dense<double2>(c.cy, true, CV, ld, REG, ld, 3, tid, nth);
       for (int idx = tid; idx < 3 * ny; idx += nth) {
         int f = idx / ny, k = idx - f * ny;
-        CV[f * ld + k] = TMP[f * ld + k];
+        CV[f * ld + k] = REG[f * ld + k];
       }
       __syncthreads();
     }
@@ -199,6 +225,7 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
   } else {
     for (int idx = tid; idx < 3 * ny; idx += nth) CV[(idx / ny) * ld + idx % ny] = c2(0.0, 0.0);
   }
+  __syncthreads();
   // 2. right-hand sides
   void* f3[3] = {c.ux, c.uy, c.temp};
   for (int idx = tid; idx < 3 * myc; idx += nth) {
@@ -209,7 +236,7 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
   for (int k = tid; k < ny; k += nth) P[k] = p0[(size_t)i * ny + k];
   __syncthreads();
   to_ortho<double2>(c.ycd, F, ld, O, ld, 3, tid, nth);
-  cheb_diff<double2>(P, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);
+  cheb_diff<double2>(P, ld, G, ld, ny, 1, 1, nullptr, ld, tid, nth);
   const double2* bco = static_cast<const double2*>(c.bc_ortho);
   const double2* bcd = static_cast<const double2*>(c.bc_diff);
   for (int k = tid; k < ny; k += nth) {
@@ -221,28 +248,29 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
     R[2 * ld + k] = fnms(O[2 * ld + k] + bcd[(size_t)i * ny + k], ct, dt);
   }
   __syncthreads();
-  // 3. Helmholtz: pinv_y then per-row banded solve
+  // 3. Helmholtz: pinv_y then the row's banded solve
   matvec_pinv<double2>(c.pinv_y, R, ld, F, ld, 3, tid, nth);
-  fdma_solve<double2>(c.hu_y, F, ld, 2, i, 0, tid, nth);
-  fdma_solve<double2>(c.ht_y, F + 2 * ld, ld, 1, i, 0, tid, nth);
-  // F now holds ux*, uy*, temp(new)
+  // ux*, uy* (factors fu) and temp (factors ft): 6 chains in one phase
+  fdma_solve2<double2>(fu, ft, 2, F, ld, 3, 0, 0, tid, nth);
   // 4. divergence = ik/s Sy ux* + Dy Sy uy*
   to_ortho<double2>(c.ycd, F, ld, O, ld, 2, tid, nth);
-  cheb_diff<double2>(O + ld, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);
+  cheb_diff<double2>(O + ld, ld, G, ld, ny, 1, 1, nullptr, ld, tid, nth);
   for (int k = tid; k < ny; k += nth) R[k] = mul_ik(O[k], ki) * inv_asp + G[k];  // R lane 0 = div
   __syncthreads();
   // 5. Poisson row solve -> pseudo pressure row
   matvec_pinv<double2>(c.pinv_y, R, ld, X1, ld, 1, tid, nth);
-  fdma_solve<double2>(c.pois_y, X1, ld, 1, i, 0, tid, nth);
+  fdma_solve<double2>(fp, X1, ld, 1, 0, 0, tid, nth);
   if (i == 0 && tid == 0) X1[0] = c2(0.0, 0.0);
   __syncthreads();
   double2* p1 = static_cast<double2*>(c.p1);
   for (int k = tid; k < myc; k += nth) p1[(size_t)i * myc + k] = X1[k];
   // 6. projection: O1 = Sy^N p1; dpdx = ik/s O1; dpdy = Dy O1
   to_ortho<double2>(c.ycn, X1, ld, O, ld, 1, tid, nth);  // O lane 0 = O1
-  cheb_diff<double2>(O, ld, G, ld, ny, 1, 1, TMP, ld, tid, nth);  // G = dpdy
-  for (int k = tid; k < ny; k += nth) O[ld + k] = mul_ik(O[k], ki) * inv_asp;  // O lane 1 = dpdx
-  for (int k = tid; k < ny; k += nth) O[2 * ld + k] = G[k];                      // O lane 2 = dpdy
+  cheb_diff<double2>(O, ld, G, ld, ny, 1, 1, nullptr, ld, tid, nth);  // G = dpdy
+  for (int k = tid; k < ny; k += nth) {
+    O[ld + k] = mul_ik(O[k], ki) * inv_asp;  // O lane 1 = dpdx
+    O[2 * ld + k] = G[k];                     // O lane 2 = dpdy
+  }
   __syncthreads();
   from_ortho<double2>(c.ycd, O + ld, ld, X1 + ld, ld, 2, tid, nth);  // X1 lanes 1, 2
   // 7. pressure update and stores
@@ -270,7 +298,8 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
 size_t smem_per_y2(const CaseDev& c) {
   size_t ld = c.ny + 1;
   size_t wld = c.cy.use_fft ? c.cy.L : 1;
-  return (3 + 3 + 3 + 3 + 1 + 1 + 3 + 3) * ld * 16 + 2 * 3 * wld * 16 + 64;
+  size_t reg = std::max((size_t)14 * ld, (size_t)6 * wld);
+  return (3 * ld + reg) * 16 + (size_t)12 * c.myc * 8 + 64;
 }
 
 // ============================================================================
