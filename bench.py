@@ -122,22 +122,34 @@ def fp64_peak_tflops():
 
 def stage_model(name):
     """Algorithmic HBM bytes and FP64 flops of one launch of a stage of the
-    periodic step (each array the stage must touch, read or written once)."""
+    periodic step.  Bytes: every array the stage must read or write, once.
+    Flops: conventional 5 N log2 N per complex FFT of length N plus the
+    element-wise work of the pass (stencils, derivatives, banded solves)."""
     import math
     mx, ny, nx, myc, kx = NX // 2 + 1, NY, NX, NY - 2, (NX // 2 + 1) * 2 // 3
     c16 = 16
-    L = 2 * (NY - 1)
-    M = NX // 2
-    fft = lambda n: 5.0 * n * math.log2(n)  # noqa: E731  conventional complex-FFT flop count
+    N = NY - 1  # DCT-I through a complex FFT of length ny-1
+    M = NX // 2  # r2c/c2r through a complex FFT of length nx/2
+    fft = lambda n: 5.0 * n * math.log2(n)  # noqa: E731
+    dct = fft(N) + 24.0 * N  # pre-twiddle, C_1, even/odd outputs (complex lane)
     if name == "y1_complex":
         b = 3 * mx * myc * c16 + 6 * mx * ny * c16
-        f = mx * 3 * 2 * fft(L)
+        f = mx * 3 * (2 * dct + 30 * ny)
     elif name == "periodic_x":
         b = 6 * mx * ny * c16 + 2 * nx * ny * 8 + 3 * kx * ny * c16
         f = ny * (11 * (fft(M) + 12 * M) + 3 * nx * 4)
     elif name == "periodic_y2":
-        b = 3 * kx * ny * c16 + 5 * mx * ny * c16 + 2 * mx * ny * c16 + 3 * 4 * mx * myc * 8
-        f = kx * 3 * fft(L) + mx * 12 * ny * 8
+        # q (3 fields) in; ux, uy, temp read and written; p1, p0 written;
+        # the boundary-field constants read; per-row solver factors read
+        b = (3 * kx * ny * c16 + 2 * 3 * mx * myc * c16 + mx * myc * c16 + mx * ny * c16
+             + 2 * mx * ny * c16 + 3 * 4 * mx * myc * 8)
+        f = kx * 3 * dct + mx * ny * 180
+    elif name == "periodic_y2a":
+        b = 3 * kx * ny * c16 + 2 * 3 * mx * myc * c16 + 4 * mx * ny * c16 + 3 * 4 * mx * myc * 8
+        f = kx * 3 * dct + mx * 3 * ny * 60
+    elif name == "periodic_y2b":
+        b = 2 * 2 * mx * myc * c16 + mx * myc * c16 + 2 * mx * ny * c16 + 4 * mx * myc * 8
+        f = mx * ny * 120
     else:
         b, f = 0, 0
     return b, f

@@ -134,6 +134,25 @@ int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, i
 /* name of stage k of the step (static string) */
 const char* rbc_stage_name(const RbcCase* c, int k);
 
+/* ---- batches --------------------------------------------------------------
+ * Many independent cases advanced together (no reference counterpart: the
+ * reference advances one Navier2D at a time).  Cases are grouped in buckets of
+ * equal (kind, nx, ny); each pass of the step is one launch per bucket whose
+ * work table covers the lanes of every case in the bucket, buckets run as
+ * parallel branches, and the whole batch step is one CUDA graph.  Case handles
+ * from rbc_batch_case are borrowed (do not destroy them); they share the batch
+ * stream, so their state/diagnostic calls are ordered after rbc_batch_step. */
+typedef struct RbcBatch RbcBatch;
+int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out);
+int rbc_batch_destroy(RbcBatch* b);
+int rbc_batch_size(const RbcBatch* b, int* ncases);
+int rbc_batch_case(RbcBatch* b, int i, RbcCase** c);
+int rbc_batch_step(RbcBatch* b, int nsteps);
+int rbc_batch_synchronize(RbcBatch* b);
+/* number of size buckets and of kernel launches per batch step */
+int rbc_batch_layout(const RbcBatch* b, int* nbuckets, int* launches_per_step);
+int rbc_batch_get_stream(RbcBatch* b, void** stream);
+
 /* ---- device memory helpers (callers that do not link the CUDA runtime) ---- */
 int rbc_host_alloc_pinned(void** ptr, size_t bytes);
 int rbc_host_free_pinned(void* ptr);

@@ -90,6 +90,14 @@ _SIGNATURES = {
     "rbc_device_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
     "rbc_profile_step": (_I, [_P, _I, _DP, _I, _IP]),
     "rbc_stage_name": (ctypes.c_char_p, [_P, _I]),
+    "rbc_batch_create": (_I, [ctypes.POINTER(RbcParams), _I, ctypes.POINTER(_P)]),
+    "rbc_batch_destroy": (_I, [_P]),
+    "rbc_batch_size": (_I, [_P, _IP]),
+    "rbc_batch_case": (_I, [_P, _I, ctypes.POINTER(_P)]),
+    "rbc_batch_step": (_I, [_P, _I]),
+    "rbc_batch_synchronize": (_I, [_P]),
+    "rbc_batch_layout": (_I, [_P, _IP, _IP]),
+    "rbc_batch_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "rbc_host_alloc_pinned": (_I, [ctypes.POINTER(_P), _SZ]),
     "rbc_host_free_pinned": (_I, [_P]),
     "rbc_dev_alloc": (_I, [ctypes.POINTER(_P), _SZ]),
@@ -377,10 +385,15 @@ class Navier2D:
     seeded here (``seed``) where the reference draws from an unseeded RNG.
     """
 
-    def __init__(self, nx, ny, ra, pr, dt, aspect, kind, precision=PREC_FP64, seed=None):
-        p = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(aspect), int(kind), int(precision))
-        h = _P()
-        _check(lib().rbc_create(ctypes.byref(p), ctypes.byref(h)))
+    def __init__(self, nx, ny, ra, pr, dt, aspect, kind, precision=PREC_FP64, seed=None, _borrowed=None):
+        if _borrowed is not None:
+            h = _P(_borrowed)
+            self._borrowed = True
+        else:
+            p = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(aspect), int(kind), int(precision))
+            h = _P()
+            _check(lib().rbc_create(ctypes.byref(p), ctypes.byref(h)))
+            self._borrowed = False
         self._h = h
         self.kind = kind
         self.periodic = kind == PERIODIC
@@ -402,9 +415,9 @@ class Navier2D:
 
     def __del__(self):
         h = getattr(self, "_h", None)
-        if h is not None and _lib is not None:
+        if h is not None and _lib is not None and not getattr(self, "_borrowed", False):
             _lib.rbc_destroy(h)
-            self._h = None
+        self._h = None
 
     # --- Integrate trait (src/lib.rs:135-146)
     def update(self, nsteps: int = 1):
@@ -527,6 +540,49 @@ class Navier2D:
         b = _SZ()
         _check(lib().rbc_device_bytes(self._h, ctypes.byref(b)))
         return b.value
+
+
+class Batch:
+    """Independent cases advanced together (rbc_batch_*).  ``params`` is a
+    list of (nx, ny, ra, pr, dt, aspect, kind) tuples; ``cases[i]`` is a
+    borrowed Navier2D handle of case i (initial conditions, state, diagnostics)."""
+
+    def __init__(self, params):
+        arr = (RbcParams * len(params))()
+        for i, (nx, ny, ra, pr, dt, asp, kind) in enumerate(params):
+            arr[i] = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(asp), int(kind), PREC_FP64)
+        h = _P()
+        _check(lib().rbc_batch_create(arr, len(params), ctypes.byref(h)))
+        self._h = h
+        self.cases = []
+        for i, (nx, ny, ra, pr, dt, asp, kind) in enumerate(params):
+            c = _P()
+            _check(lib().rbc_batch_case(h, i, ctypes.byref(c)))
+            self.cases.append(Navier2D(nx, ny, ra, pr, dt, asp, kind, _borrowed=c.value))
+
+    def update(self, nsteps=1):
+        _check(lib().rbc_batch_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _check(lib().rbc_batch_synchronize(self._h))
+
+    def layout(self):
+        a, b = _I(), _I()
+        _check(lib().rbc_batch_layout(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def stream(self):
+        s = _P()
+        _check(lib().rbc_batch_get_stream(self._h, ctypes.byref(s)))
+        return s.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            for c in getattr(self, "cases", []):
+                c._h = None
+            _lib.rbc_batch_destroy(h)
+            self._h = None
 
 
 def integrate(pde: Navier2D, max_time: float, save_intervall=None, callback=None):

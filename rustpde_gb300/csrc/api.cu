@@ -70,12 +70,14 @@ struct RbcCase {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   double time = 0.0;
+  bool own_stream = true;
+  bool in_batch = false;
   ~RbcCase() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     if (stream) {
       cudaStreamSynchronize(stream);
-      cudaStreamDestroy(stream);
+      if (own_stream) cudaStreamDestroy(stream);
     }
   }
   size_t spec_elem() const { return periodic ? 16 : 8; }
@@ -151,7 +153,7 @@ std::vector<double> get_dx(const std::vector<double>& x, bool periodic) {  // fi
   return dx;
 }
 
-void build_case(RbcCase* c) {
+void build_case(RbcCase* c, bool with_graph = true) {
   const RbcParams& p = c->p;
   Arena& A = c->arena;
   const int nx = p.nx, ny = p.ny;
@@ -292,6 +294,7 @@ void build_case(RbcCase* c) {
   // ---- step plan, work tables and the CUDA graph of one update()
   cuda_check(configure_step_kernels(), "configure step kernels");
   c->plan = build_step_plan(h);
+  if (!with_graph) return;
   for (auto& L : c->plan.launches) {
     int4* w = static_cast<int4*>(A.alloc(L.items.size() * sizeof(int4)));
     cuda_check(cudaMemcpy(w, L.items.data(), L.items.size() * sizeof(int4), cudaMemcpyHostToDevice), "work table");
@@ -417,11 +420,7 @@ extern "C" {
 const char* rbc_last_error(void) { return g_err.c_str(); }
 const char* rbc_version(void) { return "spectral_rbc 0.1 (sm_103a, FP64 step)"; }
 
-int rbc_create(const RbcParams* params, RbcCase** out) {
-  API_BEGIN
-  require(params != nullptr && out != nullptr, "rbc_create: null argument");
-  *out = nullptr;
-  const RbcParams& p = *params;
+static void validate_params(const RbcParams& p) {
   require(p.kind >= 0 && p.kind <= 2, "rbc_create: unknown kind");
   require(p.ra > 0 && p.pr > 0 && p.dt > 0 && p.aspect > 0, "rbc_create: ra, pr, dt, aspect must be positive");
   require(p.ny >= 8 && p.ny <= 4097, "rbc_create: ny must be in [8, 4097]");
@@ -430,6 +429,14 @@ int rbc_create(const RbcParams* params, RbcCase** out) {
   else require(p.nx >= 8 && p.nx <= 4097, "rbc_create: nx must be in [8, 4097]");
   if (p.precision != RBC_PREC_FP64)
     throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_create: single cases run in FP64; mixed precision is a batch form");
+}
+
+int rbc_create(const RbcParams* params, RbcCase** out) {
+  API_BEGIN
+  require(params != nullptr && out != nullptr, "rbc_create: null argument");
+  *out = nullptr;
+  const RbcParams& p = *params;
+  validate_params(p);
   cuda_check(configure_prim_kernels(), "configure kernels");
   std::unique_ptr<RbcCase> c(new RbcCase());
   c->p = p;
@@ -442,6 +449,7 @@ int rbc_create(const RbcParams* params, RbcCase** out) {
 
 int rbc_destroy(RbcCase* c) {
   API_BEGIN
+  require(c == nullptr || !c->in_batch, "rbc_destroy: the case belongs to a batch (destroy the batch)");
   delete c;
   API_END
 }
@@ -512,6 +520,7 @@ int rbc_random_disturbance(RbcCase* c, double amp, uint64_t seed) {
 int rbc_step(RbcCase* c, int nsteps) {
   API_BEGIN
   require(c != nullptr && nsteps >= 0, "rbc_step: invalid argument");
+  require(c->gexec != nullptr, "rbc_step: the case belongs to a batch (use rbc_batch_step)");
   for (int s = 0; s < nsteps; s++) {
     cuda_check(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
     c->time += c->p.dt;
@@ -570,6 +579,7 @@ int rbc_integrate(RbcCase* c, double max_time, double save_intervall, rbc_callba
   require(c != nullptr, "null case");
   const long MAX_TIMESTEP = 10000000;
   long timestep = 0;
+  require(c->gexec != nullptr, "rbc_integrate: the case belongs to a batch (use rbc_batch_step)");
   double dt = c->p.dt;
   double eps_dt = dt * 1e-4;
   while (true) {
@@ -673,9 +683,172 @@ int rbc_device_bytes(const RbcCase* c, size_t* bytes) {
   API_END
 }
 
+// ---------------------------------------------------------------- batches
+}  // extern "C"
+
+struct RbcBatch {
+  std::vector<RbcCase*> cases;
+  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> events;
+  Arena arena;
+  CaseDev* d_cases = nullptr;
+  struct Bucket {
+    int kind, nx, ny;
+    std::vector<int> members;
+    StepPlan plan;
+    std::vector<int4*> d_work;
+  };
+  std::vector<Bucket> buckets;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int launches = 0;
+  ~RbcBatch() {
+    if (stream) cudaStreamSynchronize(stream);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    for (RbcCase* c : cases) delete c;
+    for (auto e : events) cudaEventDestroy(e);
+    for (auto s : branch) cudaStreamDestroy(s);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+extern "C" {
+
+int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
+  API_BEGIN
+  require(params != nullptr && out != nullptr && ncases > 0, "rbc_batch_create: invalid argument");
+  *out = nullptr;
+  for (int i = 0; i < ncases; i++) validate_params(params[i]);
+  cuda_check(configure_prim_kernels(), "configure kernels");
+  std::unique_ptr<RbcBatch> b(new RbcBatch());
+  cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream create");
+  for (int i = 0; i < ncases; i++) {
+    std::unique_ptr<RbcCase> c(new RbcCase());
+    c->p = params[i];
+    c->periodic = params[i].kind == RBC_PERIODIC;
+    c->stream = b->stream;
+    c->own_stream = false;
+    c->in_batch = true;
+    build_case(c.get(), false);
+    b->cases.push_back(c.release());
+  }
+  // device table of all case descriptors
+  std::vector<CaseDev> hd;
+  for (RbcCase* c : b->cases) hd.push_back(c->hd);
+  b->d_cases = b->arena.upload(hd);
+  // buckets of equal (kind, nx, ny)
+  for (int i = 0; i < ncases; i++) {
+    const RbcParams& p = params[i];
+    int kind = p.kind == RBC_PERIODIC ? 2 : 0;  // both box kinds share kernels
+    int found = -1;
+    for (size_t k = 0; k < b->buckets.size(); k++)
+      if (b->buckets[k].kind == kind && b->buckets[k].nx == p.nx && b->buckets[k].ny == p.ny) found = (int)k;
+    if (found < 0) {
+      RbcBatch::Bucket bk;
+      bk.kind = kind;
+      bk.nx = p.nx;
+      bk.ny = p.ny;
+      b->buckets.push_back(bk);
+      found = (int)b->buckets.size() - 1;
+    }
+    b->buckets[found].members.push_back(i);
+  }
+  for (auto& bk : b->buckets) {
+    const RbcCase* first = b->cases[bk.members[0]];
+    bk.plan = first->plan;
+    for (auto& L : bk.plan.launches) {
+      std::vector<int4> items;
+      size_t lanes = L.items.size();
+      items.reserve(lanes * bk.members.size());
+      for (size_t li = 0; li < lanes; li++)
+        for (int m : bk.members) items.push_back(make_int4(m, L.items[li].y, L.items[li].z, L.items[li].w));
+      L.items = items;
+      bk.d_work.push_back(b->arena.upload(items));
+    }
+  }
+  cuda_check(cudaDeviceSynchronize(), "batch set-up");
+  // graph: one branch per bucket
+  size_t nb = b->buckets.size();
+  b->branch.resize(nb);
+  b->events.resize(nb + 1);
+  for (size_t k = 0; k < nb; k++) cuda_check(cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking), "stream");
+  for (auto& e : b->events) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+  cuda_check(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  cudaError_t le = cudaEventRecord(b->events[nb], b->stream);
+  for (size_t k = 0; k < nb && le == cudaSuccess; k++) {
+    auto& bk = b->buckets[k];
+    cudaStream_t s = b->branch[k];
+    le = cudaStreamWaitEvent(s, b->events[nb], 0);
+    for (size_t li = 0; li < bk.plan.launches.size() && le == cudaSuccess; li++) {
+      auto& L = bk.plan.launches[li];
+      le = launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, s, b->d_cases, bk.d_work[li]);
+      b->launches++;
+    }
+    if (le == cudaSuccess) le = cudaEventRecord(b->events[k], s);
+    if (le == cudaSuccess) le = cudaStreamWaitEvent(b->stream, b->events[k], 0);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  cuda_check(le, "batch capture");
+  cuda_check(ce, "end capture");
+  b->graph = g;
+  cuda_check(cudaGraphInstantiate(&b->gexec, g, 0), "graph instantiate");
+  *out = b.release();
+  API_END
+}
+
+int rbc_batch_destroy(RbcBatch* b) {
+  API_BEGIN
+  delete b;
+  API_END
+}
+int rbc_batch_size(const RbcBatch* b, int* n) {
+  API_BEGIN
+  require(b && n, "null argument");
+  *n = (int)b->cases.size();
+  API_END
+}
+int rbc_batch_case(RbcBatch* b, int i, RbcCase** c) {
+  API_BEGIN
+  require(b && c && i >= 0 && i < (int)b->cases.size(), "rbc_batch_case: invalid argument");
+  *c = b->cases[i];
+  API_END
+}
+int rbc_batch_step(RbcBatch* b, int nsteps) {
+  API_BEGIN
+  require(b && nsteps >= 0, "rbc_batch_step: invalid argument");
+  for (int s = 0; s < nsteps; s++) {
+    cuda_check(cudaGraphLaunch(b->gexec, b->stream), "graph launch");
+    for (RbcCase* c : b->cases) c->time += c->p.dt;
+  }
+  API_END
+}
+int rbc_batch_synchronize(RbcBatch* b) {
+  API_BEGIN
+  require(b != nullptr, "null batch");
+  cuda_check(cudaStreamSynchronize(b->stream), "stream synchronize");
+  API_END
+}
+int rbc_batch_layout(const RbcBatch* b, int* nbuckets, int* launches) {
+  API_BEGIN
+  require(b && nbuckets && launches, "null argument");
+  *nbuckets = (int)b->buckets.size();
+  *launches = b->launches;
+  API_END
+}
+int rbc_batch_get_stream(RbcBatch* b, void** stream) {
+  API_BEGIN
+  require(b && stream, "null argument");
+  *stream = (void*)b->stream;
+  API_END
+}
+
 int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, int* nstages) {
   API_BEGIN
   require(c && stage_ms && nstages && nsteps > 0, "rbc_profile_step: invalid argument");
+  require(!c->in_batch, "rbc_profile_step: the case belongs to a batch");
   int ns = (int)c->plan.launches.size();
   *nstages = ns;
   std::vector<cudaEvent_t> ev(ns + 1);
@@ -704,10 +877,11 @@ int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, i
 
 const char* rbc_stage_name(const RbcCase* c, int k) {
   static const char* names[] = {"y1_complex", "y1_real", "periodic_x", "periodic_y2", "box_x1", "box_y2",
-                                "box_x2", "box_y3", "box_x3", "box_y4", "box_x4", "box_y5"};
+                                "box_x2", "box_y3", "box_x3", "box_y4", "box_x4", "box_y5", "periodic_y2a",
+                                "periodic_y2b"};
   if (!c || k < 0 || k >= (int)c->plan.launches.size()) return "";
   int id = c->plan.launches[k].kernel;
-  return (id >= 0 && id < 12) ? names[id] : "";
+  return (id >= 0 && id < 14) ? names[id] : "";
 }
 
 // ---- device memory helpers

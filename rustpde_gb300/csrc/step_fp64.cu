@@ -295,6 +295,171 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
   if (bad) flag_nonfinite(c.status);
 }
 
+// ============================================================================
+// Periodic Y2 split in two launches for more CTAs per SM:
+//  Y2a (row i, field f): convection transform, right-hand side, pinv_y and the
+//       row's banded Helmholtz solve; writes ux*, uy* (into the state arrays,
+//       overwritten by Y2b) and the new temperature.
+//  Y2b (row i): divergence, Poisson row solve, projection, pressure update.
+// ============================================================================
+__global__ void __launch_bounds__(256) k_per_y2a(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y, f = w.w;
+  const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double dt = c.dt, inv_asp = 1.0 / c.aspect, ki = (double)i;
+  extern __shared__ double2 smem[];
+  double2* CV = smem;   // conv lane
+  double2* REG = CV + ld;
+  double2* F = REG;      // composite row of field f
+  double2* T2 = F + ld;  // composite temperature row (buoyancy of uy)
+  double2* O = T2 + ld;  // ortho of F
+  double2* OT = O + ld;  // ortho of T2
+  double2* R = OT + ld;  // rhs
+  double2* P = R + ld;   // p0 row
+  double2* G = P + ld;   // d/dy p0
+  const int wld = c.cy.use_fft ? c.cy.L : 1;
+  double2* WA = REG;
+  double2* WB = WA + wld;
+  const size_t reg_elems = max((size_t)7 * ld, (size_t)2 * wld);
+  double* FAC = reinterpret_cast<double*>(REG + reg_elems);
+  const FdmaDev fr = stage_fdma_row(f == 2 ? c.ht_y : c.hu_y, i, FAC, tid, nth);
+  void* f3[3] = {c.ux, c.uy, c.temp};
+  // convection
+  if (i < kx) {
+    const double2* q = static_cast<const double2*>(c.q[0]) + (size_t)f * kx * ny + (size_t)i * ny;
+    for (int k = tid; k < ny; k += nth) CV[k] = q[k];
+    __syncthreads();
+    if (c.cy.use_fft) dct1_fft_c(c.cy, true, CV, ld, CV, ld, 1, WA, WB, wld, tid, nth);
+    else {
+      dct1_dense<double2>(c.cy, true, CV, ld, REG, ld, 1, tid, nth);
+      for (int k = tid; k < ny; k += nth) CV[k] = REG[k];
+      __syncthreads();
+    }
+    for (int k = tid; k < ny; k += nth)
+      if (k >= ky) CV[k] = c2(0.0, 0.0);
+  } else {
+    for (int k = tid; k < ny; k += nth) CV[k] = c2(0.0, 0.0);
+  }
+  __syncthreads();
+  // right-hand side
+  const double2* st = static_cast<const double2*>(f3[f]) + (size_t)i * myc;
+  for (int k = tid; k < myc; k += nth) F[k] = st[k];
+  const double2* p0 = static_cast<const double2*>(c.p0) + (size_t)i * ny;
+  if (f < 2)
+    for (int k = tid; k < ny; k += nth) P[k] = p0[k];
+  if (f == 1) {
+    const double2* tt = static_cast<const double2*>(c.temp) + (size_t)i * myc;
+    for (int k = tid; k < myc; k += nth) T2[k] = tt[k];
+  }
+  __syncthreads();
+  to_ortho<double2>(c.ycd, F, ld, O, ld, f == 1 ? 2 : 1, tid, nth);  // O (and OT for uy)
+  if (f == 1) cheb_diff<double2>(P, ld, G, ld, ny, 1, 1, nullptr, ld, tid, nth);
+  const double2* bco = static_cast<const double2*>(c.bc_ortho) + (size_t)i * ny;
+  const double2* bcd = static_cast<const double2*>(c.bc_diff) + (size_t)i * ny;
+  for (int k = tid; k < ny; k += nth) {
+    double2 r;
+    if (f == 0) {
+      double2 gx = mul_ik(P[k], ki) * inv_asp;
+      r = fnms(fnms(O[k], gx, dt), CV[k], dt);
+    } else if (f == 1) {
+      double2 that = OT[k] + bco[k];
+      r = fnms(fmas(fnms(O[k], G[k], dt), that, dt), CV[k], dt);
+    } else {
+      r = fnms(O[k] + bcd[k], CV[k], dt);
+    }
+    R[k] = r;
+  }
+  __syncthreads();
+  matvec_pinv<double2>(c.pinv_y, R, ld, F, ld, 1, tid, nth);
+  fdma_solve<double2>(fr, F, ld, 1, 0, 0, tid, nth);
+  // ux*, uy* go to the state arrays (Y2b overwrites them with the projected
+  // fields); the new temperature goes to scratch yw[0] because the uy work of
+  // the same row still reads the old temperature for the buoyancy.
+  double2* out = (f == 2 ? static_cast<double2*>(c.yw[0]) : static_cast<double2*>(f3[f])) + (size_t)i * myc;
+  bool bad = false;
+  for (int k = tid; k < myc; k += nth) {
+    double2 v = F[k];
+    out[k] = v;
+    bad |= !finite_v(v);
+  }
+  if (bad) flag_nonfinite(c.status);
+}
+
+size_t smem_per_y2a(const CaseDev& c) {
+  size_t ld = c.ny + 1;
+  size_t wld = c.cy.use_fft ? c.cy.L : 1;
+  size_t reg = std::max((size_t)7 * ld, (size_t)2 * wld);
+  return (ld + reg) * 16 + (size_t)4 * c.myc * 8 + 64;
+}
+
+__global__ void __launch_bounds__(256) k_per_y2b(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int i = w.y;
+  const int ny = c.ny, myc = c.myc;
+  const int ld = ny + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double nu = c.nu, inv_asp = 1.0 / c.aspect, ki = (double)i;
+  extern __shared__ double2 smem[];
+  double2* F = smem;       // 2 lanes: ux*, uy*
+  double2* O = F + 2 * ld; // 3 lanes
+  double2* R = O + 3 * ld; // divergence
+  double2* G = R + ld;
+  double2* X1 = G + ld;    // 3 lanes
+  double* FAC = reinterpret_cast<double*>(X1 + 3 * ld);
+  const FdmaDev fp = stage_fdma_row(c.pois_y, i, FAC, tid, nth);
+  double2* ux = static_cast<double2*>(c.ux) + (size_t)i * myc;
+  double2* uy = static_cast<double2*>(c.uy) + (size_t)i * myc;
+  for (int k = tid; k < myc; k += nth) {
+    F[k] = ux[k];
+    F[ld + k] = uy[k];
+  }
+  __syncthreads();
+  to_ortho<double2>(c.ycd, F, ld, O, ld, 2, tid, nth);
+  cheb_diff<double2>(O + ld, ld, G, ld, ny, 1, 1, nullptr, ld, tid, nth);
+  for (int k = tid; k < ny; k += nth) R[k] = mul_ik(O[k], ki) * inv_asp + G[k];
+  __syncthreads();
+  matvec_pinv<double2>(c.pinv_y, R, ld, X1, ld, 1, tid, nth);
+  fdma_solve<double2>(fp, X1, ld, 1, 0, 0, tid, nth);
+  if (i == 0 && tid == 0) X1[0] = c2(0.0, 0.0);
+  __syncthreads();
+  double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
+  for (int k = tid; k < myc; k += nth) p1[k] = X1[k];
+  to_ortho<double2>(c.ycn, X1, ld, O, ld, 1, tid, nth);
+  cheb_diff<double2>(O, ld, G, ld, ny, 1, 1, nullptr, ld, tid, nth);
+  for (int k = tid; k < ny; k += nth) {
+    O[ld + k] = mul_ik(O[k], ki) * inv_asp;
+    O[2 * ld + k] = G[k];
+  }
+  __syncthreads();
+  from_ortho<double2>(c.ycd, O + ld, ld, X1 + ld, ld, 2, tid, nth);
+  double2* pw = static_cast<double2*>(c.p0) + (size_t)i * ny;
+  for (int k = tid; k < ny; k += nth) {
+    double2 v = fnms(pw[k], R[k], nu);
+    pw[k] = fmas(v, O[k], c.inv_dt);
+  }
+  const double2* tn = static_cast<const double2*>(c.yw[0]) + (size_t)i * myc;
+  double2* tt = static_cast<double2*>(c.temp) + (size_t)i * myc;
+  bool bad = false;
+  for (int k = tid; k < myc; k += nth) {
+    double2 a = F[k] - X1[ld + k];
+    double2 b = F[ld + k] - X1[2 * ld + k];
+    ux[k] = a;
+    uy[k] = b;
+    tt[k] = tn[k];
+    bad |= !(finite_v(a) && finite_v(b));
+  }
+  if (bad) flag_nonfinite(c.status);
+}
+
+size_t smem_per_y2b(const CaseDev& c) {
+  size_t ld = c.ny + 1;
+  return (size_t)10 * ld * 16 + (size_t)4 * c.myc * 8 + 64;
+}
+
 size_t smem_per_y2(const CaseDev& c) {
   size_t ld = c.ny + 1;
   size_t wld = c.cy.use_fft ? c.cy.L : 1;
@@ -723,6 +888,8 @@ cudaError_t configure_step_kernels() {
   SET_ATTR(dev::k_y1<double2>);
   SET_ATTR(dev::k_per_x);
   SET_ATTR(dev::k_per_y2);
+  SET_ATTR(dev::k_per_y2a);
+  SET_ATTR(dev::k_per_y2b);
   SET_ATTR(dev::k_box_x1);
   SET_ATTR(dev::k_box_y2);
   SET_ATTR(dev::k_box_x2);
@@ -749,6 +916,9 @@ StepPlan build_step_plan(const CaseDev& c) {
   if (per) {
     add(K_Y1_C, c.mxc, dev::smem_y1(c, 1, true));
     add(K_PER_X, c.ny, dev::smem_per_x(c));
+    // fused Y2 (one CTA per row): faster than the split Y2a/Y2b pair on this
+    // GPU because each FP64 warp instruction costs its warp ~64 cycles and the
+    // split leaves single-lane CTAs with long per-warp FP64 chains
     add(K_PER_Y2, c.mx, dev::smem_per_y2(c));
   } else {
     add(K_Y1_R, c.mxc, dev::smem_y1(c, 1, false));
@@ -772,6 +942,8 @@ cudaError_t launch_step_kernel(int kernel, int nblocks, size_t smem, cudaStream_
     case K_Y1_R: dev::k_y1<double><<<g, b, smem, s>>>(cases, work); break;
     case K_PER_X: dev::k_per_x<<<g, b, smem, s>>>(cases, work); break;
     case K_PER_Y2: dev::k_per_y2<<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_Y2A: dev::k_per_y2a<<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_Y2B: dev::k_per_y2b<<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X1: dev::k_box_x1<<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_Y2: dev::k_box_y2<<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X2: dev::k_box_x2<<<g, b, smem, s>>>(cases, work); break;

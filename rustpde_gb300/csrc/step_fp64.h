@@ -11,6 +11,7 @@ namespace rbc {
 enum StepKernel {
   K_Y1_C = 0, K_Y1_R, K_PER_X, K_PER_Y2,
   K_BOX_X1, K_BOX_Y2, K_BOX_X2, K_BOX_Y3, K_BOX_X3, K_BOX_Y4, K_BOX_X4, K_BOX_Y5,
+  K_PER_Y2A, K_PER_Y2B,
   K_NUM_STEP_KERNELS
 };
 
@@ -33,6 +34,8 @@ namespace dev {
 size_t smem_y1(const CaseDev& c, int nr, bool cplx);
 size_t smem_per_x(const CaseDev& c);
 size_t smem_per_y2(const CaseDev& c);
+size_t smem_per_y2a(const CaseDev& c);
+size_t smem_per_y2b(const CaseDev& c);
 size_t smem_box_x1(const CaseDev& c);
 size_t smem_box_y2(const CaseDev& c);
 size_t smem_box_x2(const CaseDev& c);
