@@ -191,6 +191,28 @@ int fs_from_ortho(FsSpace* s, const double* d_ortho, double* d_spec, void* strea
 int fs_gradient(FsSpace* s, const double* d_spec, double* d_ortho, int deriv0, int deriv1, const double* scale,
                 void* stream);
 
+/* fs_forward_noalloc: the transform of fs_forward, computed by the same
+ * kernels, for callers that must not allocate while they run -- a loop that
+ * has handed all device memory to a fixed budget, or that cannot afford the
+ * device-wide synchronisation cudaFree implies.  No counterpart in the
+ * reference (Field2::forward, src/field.rs:103-107, allocates freely).
+ *
+ * The call allocates nothing, on the device or the host: the intermediate
+ * array between the two axis passes (phys0 x spec1 doubles) lives in a fixed
+ * device buffer of FS_NOALLOC_SCRATCH_BYTES that the library owns, one per
+ * device.  A space whose intermediate needs more returns RBC_ERR_INVALID
+ * before anything is enqueued.  Nothing in the buffer has to start at zero:
+ * the first pass writes every element the second pass reads.
+ *
+ * The first call on a device looks the buffer's address up (this can load
+ * the library's device code); make it before any stream capture, with the
+ * space's device current.  All calls on one device share the buffer, so two
+ * calls that may run at the same time (on different streams, or from
+ * different threads without ordering) race on it; calls ordered on one
+ * stream do not. */
+#define FS_NOALLOC_SCRATCH_BYTES (4u * 1024u * 1024u)
+int fs_forward_noalloc(FsSpace* s, const double* d_phys, double* d_spec, void* stream);
+
 /* ---- solvers ----------------------------------------------------------------
  * Hholtz::new (src/solver/hholtz.rs:42-76), HholtzAdi::new (hholtz_adi.rs:44-63),
  * Poisson::new (poisson.rs:50-90); Solve::solve (src/solver.rs:56-64) maps an

@@ -109,6 +109,7 @@ _SIGNATURES = {
     "fs_space_destroy": (_I, [_P]),
     "fs_space_shape": (_I, [_P, _I, _IP, _IP, _IP]),
     "fs_forward": (_I, [_P, _P, _P, _P]),
+    "fs_forward_noalloc": (_I, [_P, _P, _P, _P]),
     "fs_backward": (_I, [_P, _P, _P, _P]),
     "fs_to_ortho": (_I, [_P, _P, _P, _P]),
     "fs_from_ortho": (_I, [_P, _P, _P, _P]),
@@ -261,6 +262,12 @@ class Space2:
     # device-buffer level (drop-in primitives)
     def forward_dev(self, d_phys, d_spec, stream=None):
         _check(lib().fs_forward(self._h, d_phys.ptr, d_spec.ptr, stream))
+
+    def forward_noalloc_dev(self, d_phys, d_spec, stream=None):
+        """forward_dev through fs_forward_noalloc: no allocation; the
+        intermediate uses the library's fixed device scratch, shared by all
+        calls on the device (calls that may overlap in time race on it)."""
+        _check(lib().fs_forward_noalloc(self._h, d_phys.ptr, d_spec.ptr, stream))
 
     def backward_dev(self, d_spec, d_phys, stream=None):
         _check(lib().fs_backward(self._h, d_spec.ptr, d_phys.ptr, stream))

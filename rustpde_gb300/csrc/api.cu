@@ -1,4 +1,5 @@
 // api.cu -- C ABI of the spectral RBC library (include/spectral_rbc.h).
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -986,6 +987,48 @@ int fs_gradient(FsSpace* s, const double* d_spec, double* d_ortho, int deriv0, i
   FS_CHECK(s); FS_CHECK(d_spec); FS_CHECK(d_ortho);
   require(deriv0 >= 0 && deriv0 <= 2 && deriv1 >= 0 && deriv1 <= 2, "fs_gradient: derivative order must be 0..2");
   space_gradient(s->s, d_spec, d_ortho, deriv0, deriv1, scale, s->tmp, (cudaStream_t)stream);
+  API_END
+}
+
+}  // extern "C"
+
+// ---- fs_forward_noalloc: fixed device scratch instead of the space's own.
+// The buffer is a file-scope device array, so it exists as soon as the
+// library's device code is loaded on a device; its address is looked up once
+// per device and cached.
+namespace {
+static __device__ __align__(256) double g_noalloc_scratch[FS_NOALLOC_SCRATCH_BYTES / sizeof(double)];
+constexpr int kNoallocMaxDevices = 64;
+std::atomic<void*> g_noalloc_addr[kNoallocMaxDevices];
+
+void* noalloc_scratch_for_current_device() {
+  int dev = -1;
+  cuda_check(cudaGetDevice(&dev), "fs_forward_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kNoallocMaxDevices)
+    throw ApiError(RBC_ERR_UNSUPPORTED, "fs_forward_noalloc: device ordinal beyond 63");
+  void* p = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (p) return p;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr)
+    throw ApiError(RBC_ERR_CUDA, std::string("fs_forward_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  g_noalloc_addr[dev].store(p, std::memory_order_release);
+  return p;
+}
+}  // namespace
+
+extern "C" {
+
+int fs_forward_noalloc(FsSpace* s, const double* d_phys, double* d_spec, void* stream) {
+  API_BEGIN
+  FS_CHECK(s); FS_CHECK(d_phys); FS_CHECK(d_spec);
+  // intermediate of space_forward: phys0 x spec1 real values after the axis-1 pass
+  const size_t need = (size_t)s->s.phys0 * (size_t)s->s.spec1 * sizeof(double);
+  if (need > (size_t)FS_NOALLOC_SCRATCH_BYTES)
+    throw ApiError(RBC_ERR_INVALID, "fs_forward_noalloc: the space needs " + std::to_string(need) +
+                                        " bytes of scratch, more than the fixed " +
+                                        std::to_string((size_t)FS_NOALLOC_SCRATCH_BYTES));
+  void* scratch = noalloc_scratch_for_current_device();
+  space_forward(s->s, d_phys, d_spec, scratch, (cudaStream_t)stream);
   API_END
 }
 
