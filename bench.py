@@ -1,24 +1,37 @@
 """Benchmark of the spectral Rayleigh-Benard time step on GB300.
 
-Workload (one "step" = one Integrate::update of the whole case):
-  Navier2D::new_periodic(nx=512, ny=257, Ra=1e7, Pr=1, dt=1e-3, aspect=2), FP64,
-  seeded initial fields (set_velocity(0.2,1,1) + 1e-3 interior temperature noise).
-Metric: grid-point-steps per second (nx*ny*steps / s), higher is better.
+Metric: grid-point-steps per second (sum over cases of nx*ny*steps / s),
+higher is better.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Workloads (--workload):
+  ensemble (default)  256 independent cases of uneven size (rustpde_gb300.ensemble,
+                      seed 2024): (nx, ny) in {64,128,256}^2, box or periodic
+                      50/50, Ra log-uniform [1e4, 1e8], Pr in {0.7,1,7}, aspect
+                      U[1,2], dt = min(0.02, 2/sqrt(Ra)).  `value` is the batched
+                      mixed-precision form (one CUDA graph per ensemble step,
+                      tensor-core 3xTF32 transforms, FP32 products, FP64 solves);
+                      `plain_fp64` times the plain FP64 path run case by case on
+                      the same ensemble, and `mixed_error` gives the Nu / KE
+                      deviation of every mixed case from its FP64 run.
+  periodic512         Navier2D::new_periodic(512, 257, Ra=1e7, Pr=1, dt=1e-3,
+                      aspect=2), plain FP64, one case.
 
-Timing: W untimed warm-up steps, then K steps, each bracketed by CUDA events
-on the case stream; L2 is flushed (256 MiB memset) between timed steps, outside
-the events.  `e2e` repeats the measurement through the public API with the
-step's state copied host->device from pinned memory and back every step.
-`--impl reference` times the CPU restatement of the reference algorithm
-(oracle/, the reference itself is Rust and cannot be built here) on all host
-cores.  With N > 1 (torchrun) every rank advances its own replica of the case;
-there is no collective on the data path (replicas only).
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
+
+Timing: W untimed warm-up steps, then K steps each bracketed by CUDA events on
+the stream that runs them; L2 is flushed (256 MiB memset, outside the events)
+between timed steps.  `e2e` is the same metric through the public API with the
+whole state copied host->device from pinned memory before, and device->host
+after, every step.  `--impl reference` times the CPU restatement of the
+reference algorithm (oracle/, the reference is Rust and cannot be built here)
+on all host cores over a bounded sample of the workload.  With N > 1
+(torchrun) every rank advances its own replica; there is no collective on the
+data path (replicas only).
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -29,17 +42,18 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-NX, NY, RA, PR, DT, ASPECT = 512, 257, 1e7, 1.0, 1e-3, 2.0
-GP = NX * NY
 METRIC = "grid-pt-steps/s"
-WORKLOAD = "Navier2D::new_periodic 512x257 Ra=1e7 Pr=1 dt=1e-3 aspect=2 (FourierR2c x ChebDirichlet), plain FP64"
+NX, NY, RA, PR, DT, ASPECT = 512, 257, 1e7, 1.0, 1e-3, 2.0
+WORKLOAD_512 = "Navier2D::new_periodic 512x257 Ra=1e7 Pr=1 dt=1e-3 aspect=2 (FourierR2c x ChebDirichlet), plain FP64"
+ENSEMBLE_N, ENSEMBLE_SEED = 256, 2024
+WORKLOAD_ENS = ("256-case RBC ensemble of uneven size (nx,ny in {64,128,256}^2, box/periodic 50/50, "
+                "Ra log-U[1e4,1e8], Pr {0.7,1,7}, aspect U[1,2], dt=min(0.02,2/sqrt(Ra)), seed 2024), "
+                "batched mixed precision")
 
 
 def dist_info():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
 
 
 class ClockSampler:
@@ -96,154 +110,271 @@ class ClockSampler:
         return {"sm_mhz": med, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def fp64_peak_tflops():
-    """Measured FP64 throughput of this GPU: cuBLAS DGEMM 4096^3 (best of 5)."""
-    try:
-        import torch
-        a = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-        b = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
-        for _ in range(2):
-            torch.matmul(a, b)
-        torch.cuda.synchronize()
-        best = 0.0
-        for _ in range(5):
-            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            s.record()
-            torch.matmul(a, b)
-            e.record()
-            e.synchronize()
-            best = max(best, 2 * 4096 ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
-        del a, b
-        torch.cuda.empty_cache()
-        return best, "torch.matmul float64 4096^3 (cuBLAS DGEMM), best of 5"
-    except Exception as exc:  # pragma: no cover - torch missing on the box
-        return 1.19, f"probe value 1.19 TFLOP/s (DFMA loop); torch unavailable: {exc}"
+class Cudart:
+    """CUDA events and memset through the runtime the library links."""
+
+    def __init__(self):
+        try:
+            self.lib = ctypes.CDLL("libcudart.so.13")
+        except OSError:
+            self.lib = ctypes.CDLL("libcudart.so")
+        L = self.lib
+        L.cudaEventCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
+        L.cudaEventRecord.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+        L.cudaEventSynchronize.argtypes = [ctypes.c_void_p]
+        L.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
+        L.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
+        L.cudaEventDestroy.argtypes = [ctypes.c_void_p]
+
+    def event(self):
+        e = ctypes.c_void_p()
+        assert self.lib.cudaEventCreate(ctypes.byref(e)) == 0
+        return e
+
+    def record(self, e, stream):
+        self.lib.cudaEventRecord(e, ctypes.c_void_p(stream))
+
+    def elapsed(self, a, b):
+        f = ctypes.c_float()
+        self.lib.cudaEventSynchronize(b)
+        self.lib.cudaEventElapsedTime(ctypes.byref(f), a, b)
+        return f.value
+
+    def memset(self, ptr, v, n, stream):
+        self.lib.cudaMemsetAsync(ptr, v, n, ctypes.c_void_p(stream))
+
+    def destroy(self, *evs):
+        for e in evs:
+            self.lib.cudaEventDestroy(e)
 
 
-def stage_model(name):
-    """Algorithmic HBM bytes and FP64 flops of one launch of a stage of the
-    periodic step.  Bytes: every array the stage must read or write, once.
-    Flops: conventional 5 N log2 N per complex FFT of length N plus the
-    element-wise work of the pass (stencils, derivatives, banded solves)."""
-    import math
-    mx, ny, nx, myc, kx = NX // 2 + 1, NY, NX, NY - 2, (NX // 2 + 1) * 2 // 3
-    c16 = 16
-    N = NY - 1  # DCT-I through a complex FFT of length ny-1
-    M = NX // 2  # r2c/c2r through a complex FFT of length nx/2
-    fft = lambda n: 5.0 * n * math.log2(n)  # noqa: E731
-    dct = fft(N) + 24.0 * N  # pre-twiddle, C_1, even/odd outputs (complex lane)
-    if name == "y1_complex":
-        b = 3 * mx * myc * c16 + 6 * mx * ny * c16
-        f = mx * 3 * (2 * dct + 30 * ny)
-    elif name == "periodic_x":
-        b = 6 * mx * ny * c16 + 2 * nx * ny * 8 + 3 * kx * ny * c16
-        f = ny * (11 * (fft(M) + 12 * M) + 3 * nx * 4)
-    elif name == "periodic_y2":
-        # q (3 fields) in; ux, uy, temp read and written; p1, p0 written;
-        # the boundary-field constants read; per-row solver factors read
-        b = (3 * kx * ny * c16 + 2 * 3 * mx * myc * c16 + mx * myc * c16 + mx * ny * c16
-             + 2 * mx * ny * c16 + 3 * 4 * mx * myc * 8)
-        f = kx * 3 * dct + mx * ny * 180
-    elif name == "periodic_y2a":
-        b = 3 * kx * ny * c16 + 2 * 3 * mx * myc * c16 + 4 * mx * ny * c16 + 3 * 4 * mx * myc * 8
-        f = kx * 3 * dct + mx * 3 * ny * 60
-    elif name == "periodic_y2b":
-        b = 2 * 2 * mx * myc * c16 + mx * myc * c16 + 2 * mx * ny * c16 + 4 * mx * myc * 8
-        f = mx * ny * 120
-    else:
-        b, f = 0, 0
-    return b, f
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback 6.8 TB/s"
 
 
-def run_ours(args, rank, world, local):
+def timed_steps(cu, stream, K, step, flush):
+    """K steps, each between CUDA events on `stream`, L2 flushed in between."""
+    starts = [cu.event() for _ in range(K)]
+    ends = [cu.event() for _ in range(K)]
+    for k in range(K):
+        cu.memset(flush.ptr, k & 0xFF, flush.nbytes, stream)
+        cu.record(starts[k], stream)
+        step()
+        cu.record(ends[k], stream)
+    total = sum(cu.elapsed(starts[k], ends[k]) for k in range(K))
+    cu.destroy(*starts, *ends)
+    return total
+
+
+def max_over_ranks(v, world):
+    if world <= 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# ensemble workload (default)
+# ---------------------------------------------------------------------------
+def run_ensemble(args, rank, world, local):
+    import numpy as np
+
+    import rustpde_gb300 as R
+    from rustpde_gb300 import build
+    from rustpde_gb300.ensemble import draw_ensemble
+    build.build()
+    cu = Cudart()
+    params = draw_ensemble(ENSEMBLE_N, ENSEMBLE_SEED)
+    gp = sum(p[0] * p[1] for p in params)
+    flush = R.DeviceArray((256 * 1024 * 1024 // 8,))
+    W, K = args.warmup, args.steps
+
+    # ---- batched mixed precision
+    t_setup = time.perf_counter()
+    B = R.Batch(params, precision=R.PREC_MIXED)
+    t_setup = time.perf_counter() - t_setup
+    for i, c in enumerate(B.cases):
+        R.standard_ic(c, seed=1000 + i)
+    stream = B.stream()
+    B.update(W)
+    B.synchronize()
+    barrier(world)
+    clocks = ClockSampler(local)
+    clocks.start()
+    t_wall = time.perf_counter()
+    total_ms = timed_steps(cu, stream, K, lambda: B.update(1), flush)
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    barrier(world)
+    total_ms = max_over_ranks(total_ms, world)
+    nb, launches = B.layout()
+    status = [c.status() for c in B.cases]
+    mixed_nu = [c.eval(R.NU) for c in B.cases]
+    mixed_ke = [c.eval(R.KE) for c in B.cases]
+    value = gp * K / (total_ms * 1e-3) * world
+
+    # ---- per-kernel profile of the batched step (each launch alone) and roofline
+    prof = B.profile_step(3)
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_bytes = prof[dom]
+    pk, pk_src = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+
+    # ---- end to end through the public API (whole ensemble state in and out every step)
+    nbytes = B.state_bytes()
+    host = R.PinnedArray((nbytes,), np.uint8)
+    B.get_state_all(host.array)
+    Ke = min(K, 20)
+    t0 = time.perf_counter()
+    for _ in range(Ke):
+        B.set_state_all(host.array)
+        B.update(1)
+        B.get_state_all(host.array)
+    e2e_s = time.perf_counter() - t0
+    del B
+
+    # ---- plain FP64, case by case, same ensemble and initial fields
+    plain_ms = 0.0
+    err_nu, err_ke = [], []
+    t_plain = time.perf_counter()
+    for i, p in enumerate(params):
+        nav = R.Navier2D(*p, precision=R.PREC_FP64, seed=None)
+        R.standard_ic(nav, seed=1000 + i)
+        nav.update(W)
+        st = nav.stream()
+        e0, e1 = cu.event(), cu.event()
+        cu.memset(flush.ptr, i & 0xFF, flush.nbytes, st)
+        cu.record(e0, st)
+        nav.update(K)
+        cu.record(e1, st)
+        plain_ms += cu.elapsed(e0, e1)
+        cu.destroy(e0, e1)
+        for lst, what, ref in ((err_nu, R.NU, mixed_nu[i]), (err_ke, R.KE, mixed_ke[i])):
+            v = nav.eval(what)
+            lst.append(abs(ref - v) / max(abs(v), 1e-300))
+        del nav
+    t_plain = time.perf_counter() - t_plain
+    plain_value = gp * K / (plain_ms * 1e-3) * world
+    err_nu, err_ke = np.array(err_nu), np.array(err_ke)
+
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "grid-pt-steps/s",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": total_ms / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64 state and solves, tf32x3 tensor-core transforms, f32 products",
+        "data": "synthetic: seeded ensemble draw; set_velocity(0.2,1,1) + splitmix64 temperature noise 1e-3 per case",
+        "config": {"workload": WORKLOAD_ENS, "cases": len(params), "grid_points": gp, "precision": "mixed",
+                   "buckets": nb, "launches_per_step": launches, "parallelism": f"replicas{world}",
+                   "l2": "flushed between timed steps (256 MiB memset outside the events); ensemble state > L2",
+                   "setup_s": t_setup, "wall_s_timed_region": t_wall},
+        "plain_fp64": {"value": plain_value, "unit": "grid-pt-steps/s", "ms_per_ensemble_step": plain_ms / K,
+                       "how": "each case alone through rbc_step (its own CUDA graph), K steps between CUDA events, "
+                              "cases one after another; L2 flushed before each case", "wall_s": t_plain},
+        "speedup_vs_plain_fp64": value / plain_value,
+        "mixed_error": {"steps": W + K, "nu_max_rel": float(err_nu.max()), "nu_median_rel": float(np.median(err_nu)),
+                        "ke_max_rel": float(err_ke.max()), "ke_median_rel": float(np.median(err_ke)),
+                        "against": "the plain FP64 GPU path (parity with the FP64 oracle <= 1e-9)"},
+        "e2e": {"value": gp * Ke / e2e_s * world, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "steps": Ke,
+                "how": "per step: rbc_batch_set_state_all (pinned h2d), rbc_batch_step(1), rbc_batch_get_state_all"},
+        "gpu_launches": K * launches,
+        "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_launch": dom_bytes,
+                     "peak_source": pk_src},
+        "clocks": clk,
+        "status_nonzero_cases": int(sum(1 for s in status if s)),
+    }
+    if rank == 0 and world == 1:
+        line["cpu_baseline"] = cpu_baseline_ensemble(params, budget_s=args.cpu_budget)
+    return line
+
+
+def cpu_baseline_ensemble(params, budget_s=15.0, steps_per_case=2):
+    """The oracle (CPU restatement of the reference algorithm, OpenMP over
+    lanes, all host threads) on the leading cases of the same ensemble."""
+    from oracle import oracle as O
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    done_gp, t_acc, ncase = 0, 0.0, 0
+    for p in params:
+        nx, ny, ra, pr, dt, asp, kind = p
+        o = O.Navier2D(nx, ny, ra, pr, dt, asp, kind)
+        O.standard_ic(o, 1)
+        o.update(1)
+        t0 = time.perf_counter()
+        o.update(steps_per_case)
+        t_acc += time.perf_counter() - t0
+        done_gp += nx * ny * steps_per_case
+        ncase += 1
+        if t_acc > budget_s:
+            break
+    return {"value": done_gp / t_acc, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"first {ncase} ensemble cases x {steps_per_case} steps after 1 warm-up step each "
+                      f"({t_acc:.1f} s timed)"}
+
+
+# ---------------------------------------------------------------------------
+# single periodic 512x257 case, plain FP64
+# ---------------------------------------------------------------------------
+def run_periodic512(args, rank, world, local):
     import numpy as np
 
     import rustpde_gb300 as R
     from rustpde_gb300 import build
     build.build()
-
+    cu = Cudart()
+    gp = NX * NY
     nav = R.Navier2D(NX, NY, RA, PR, DT, ASPECT, R.PERIODIC, seed=None)
     R.standard_ic(nav, seed=1 + rank)
     flush = R.DeviceArray((256 * 1024 * 1024 // 8,))
-    lib = R.lib()
     stream = nav.stream()
-
-    import ctypes
-    cudart = ctypes.CDLL("libcudart.so.13") if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else None
-    if cudart is None:
-        cudart = ctypes.CDLL("libcudart.so")
-    cudart.cudaEventCreate.argtypes = [ctypes.POINTER(ctypes.c_void_p)]
-    cudart.cudaEventRecord.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
-    cudart.cudaEventSynchronize.argtypes = [ctypes.c_void_p]
-    cudart.cudaEventElapsedTime.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_void_p, ctypes.c_void_p]
-    cudart.cudaMemsetAsync.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_void_p]
-
-    def ev():
-        e = ctypes.c_void_p()
-        assert cudart.cudaEventCreate(ctypes.byref(e)) == 0
-        return e
-
-    # warm-up
     nav.update(args.warmup)
     nav.synchronize()
-    if args.quick:
-        t0 = time.perf_counter()
-        nav.update(args.steps)
-        nav.synchronize()
-        dt = time.perf_counter() - t0
-        return {"metric": METRIC, "value": GP * args.steps / dt, "unit": "grid-pt-steps/s", "steps": args.steps,
-                "warmup": args.warmup, "mode": "quick (host wall clock, no L2 flush)", "status": nav.status()}
-
-    barrier = None
-    if world > 1:
-        import torch.distributed as dist
-        barrier = dist.barrier
-        barrier()
-
+    barrier(world)
     K = args.steps
-    starts = [ev() for _ in range(K)]
-    ends = [ev() for _ in range(K)]
     clocks = ClockSampler(local)
     clocks.start()
-    t_wall0 = time.perf_counter()
-    for k in range(K):
-        cudart.cudaMemsetAsync(flush.ptr, k & 0xFF, flush.nbytes, ctypes.c_void_p(stream))
-        cudart.cudaEventRecord(starts[k], ctypes.c_void_p(stream))
-        nav.update(1)
-        cudart.cudaEventRecord(ends[k], ctypes.c_void_p(stream))
-    nav.synchronize()
-    t_wall = time.perf_counter() - t_wall0
+    t_wall = time.perf_counter()
+    total_ms = timed_steps(cu, stream, K, lambda: nav.update(1), flush)
+    t_wall = time.perf_counter() - t_wall
     clk = clocks.stop()
-    total_ms = 0.0
-    f = ctypes.c_float()
-    for k in range(K):
-        cudart.cudaEventElapsedTime(ctypes.byref(f), starts[k], ends[k])
-        total_ms += f.value
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    status = nav.status()
-
-    # per-stage timing of the step kernels (dominant kernel roofline)
-    stages = nav.profile_step(20)
-    dom = max(stages, key=stages.get)
-    b_alg, f_alg = stage_model(dom)
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    dom_s = stages[dom] * 1e-3
-    fp64_peak, fp64_how = fp64_peak_tflops()
-
-    # end-to-end through the public API: state host->device, step, state device->host
+    barrier(world)
+    total_ms = max_over_ranks(total_ms, world)
+    stages = nav.profile_step(20, with_bytes=True)
+    dom = max(stages, key=lambda k: stages[k][0])
+    dom_ms, dom_bytes = stages[dom]
+    pk, pk_src = peaks()
+    hbm = pk.get("hbm_gbs", 6800.0)
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     fields = (R.TEMP, R.UX, R.UY, R.PRES, R.PSEUDO_PRES)
     pinned = {fid: R.PinnedArray(nav.shape(fid)[0], np.complex128) for fid in fields}
     for fid in fields:
         pinned[fid].array[...] = nav.get(fid)
     h2d = sum(p.array.nbytes for p in pinned.values())
     Ke = min(K, 50)
+    lib = R.lib()
     t0 = time.perf_counter()
     for _ in range(Ke):
         for fid in fields:
@@ -254,92 +385,99 @@ def run_ours(args, rank, world, local):
                               pinned[fid].array.size * 2)
     nav.synchronize()
     e2e_s = time.perf_counter() - t0
-
-    value = GP * K / (total_ms * 1e-3) * world
     line = {
-        "metric": METRIC,
-        "value": value,
-        "unit": "grid-pt-steps/s",
-        "n_gpus": world,
-        "steps": K,
-        "warmup": args.warmup,
-        "ms_per_step": total_ms / K,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f64",
+        "metric": METRIC, "value": gp * K / (total_ms * 1e-3) * world, "unit": "grid-pt-steps/s", "n_gpus": world,
+        "steps": K, "warmup": args.warmup, "ms_per_step": total_ms / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic seeded fields (set_velocity(0.2,1,1) + splitmix64 temperature noise 1e-3)",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "ra": RA, "pr": PR, "dt": DT, "aspect": ASPECT,
+        "config": {"workload": WORKLOAD_512, "nx": NX, "ny": NY, "ra": RA, "pr": PR, "dt": DT, "aspect": ASPECT,
                    "precision": "fp64", "parallelism": f"replicas{world}",
                    "l2": "flushed between timed steps (256 MiB memset outside the events)",
                    "wall_s_timed_region": t_wall},
-        "e2e": {"value": GP * Ke / e2e_s * world, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": gp * Ke / e2e_s * world, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": h2d, "steps": Ke,
                 "how": "per step: rbc_set_state x5 from pinned host memory, rbc_step(1), rbc_get_state x5"},
         "gpu_launches": K * len(stages),
-        "stages_ms": stages,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": b_alg / dom_s / 1e9, "peak": hbm_peak,
-                     "unit": "GB/s", "frac": b_alg / dom_s / 1e9 / hbm_peak, "traffic": None,
-                     "algorithmic_bytes_per_launch": b_alg,
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"},
-        "fp64_roofline": {"kernel": dom, "achieved_tflops": f_alg / dom_s / 1e12, "peak_tflops": fp64_peak,
-                          "frac": f_alg / dom_s / 1e12 / fp64_peak, "algorithmic_flops_per_launch": f_alg,
-                          "peak_source": fp64_how},
-        "clocks": clk,
-        "status": status,
+        "stages_ms": {k: v[0] for k, v in stages.items()},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_launch": dom_bytes,
+                     "peak_source": pk_src},
+        "clocks": clk, "status": nav.status(),
     }
     if rank == 0 and world == 1:
-        line["cpu_baseline"] = cpu_baseline(budget_s=args.cpu_budget)
+        line["cpu_baseline"] = cpu_baseline_512(budget_s=args.cpu_budget)
     return line
 
 
-def cpu_baseline(budget_s=15.0):
-    """The oracle (CPU restatement of the reference algorithm, OpenMP over
-    lanes) on a bounded sample of the same workload."""
+def cpu_baseline_512(budget_s=15.0):
     from oracle import oracle as O
     O.build()
-    threads = os.cpu_count() or 1
-    O.set_threads(threads)
+    O.set_threads(os.cpu_count() or 1)
     o = O.Navier2D(NX, NY, RA, PR, DT, ASPECT, O.PERIODIC)
     O.standard_ic(o, 1)
-    o.update(1)  # warm-up (plans, first touch)
+    o.update(1)
     n = 0
     t0 = time.perf_counter()
-    while n < 3 or time.perf_counter() - t0 < budget_s:
+    while n < 3 or (time.perf_counter() - t0 < budget_s and n < 400):
         o.update(1)
         n += 1
-        if n >= 400:
-            break
     dt = time.perf_counter() - t0
-    return {"value": GP * n / dt, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
+    return {"value": NX * NY * n / dt, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
             "sample": f"{n} steps of the same 512x257 periodic case after 1 warm-up step ({dt:.1f} s)"}
 
 
+# ---------------------------------------------------------------------------
+# reference arm: the oracle on the host cores
+# ---------------------------------------------------------------------------
 def run_reference(args, rank, world):
     if rank != 0:
         return None
     from oracle import oracle as O
     O.build()
     O.set_threads(os.cpu_count() or 1)
-    o = O.Navier2D(NX, NY, RA, PR, DT, ASPECT, O.PERIODIC)
-    O.standard_ic(o, 1)
+    budget = 90.0
+    if args.workload == "periodic512":
+        cases = [(NX, NY, RA, PR, DT, ASPECT, O.PERIODIC)]
+        config = {"workload": WORKLOAD_512, "nx": NX, "ny": NY}
+    else:
+        from rustpde_gb300.ensemble import draw_ensemble
+        cases = draw_ensemble(ENSEMBLE_N, ENSEMBLE_SEED)
+        config = {"workload": WORKLOAD_ENS.replace("batched mixed precision", "case by case, FP64"),
+                  "cases": len(cases)}
+    # one timed "step" advances every sampled case once; the sample is the
+    # leading cases of the workload that fit the time budget
+    objs, per_case = [], []
+    for p in cases:
+        nx, ny, ra, pr, dt, asp, kind = p
+        o = O.Navier2D(nx, ny, ra, pr, dt, asp, kind)
+        O.standard_ic(o, 1)
+        t0 = time.perf_counter()
+        o.update(1)
+        per_case.append(time.perf_counter() - t0)
+        objs.append((o, nx * ny))
+        if sum(per_case) * max(args.steps, 1) > budget:
+            break
+    warm = min(args.warmup, 2)
+    for o, _ in objs:
+        o.update(warm)
+    K = max(1, args.steps)
     t0 = time.perf_counter()
-    o.update(1)
-    per_step = time.perf_counter() - t0
-    warm = max(0, min(args.warmup, int(20.0 / max(per_step, 1e-6))))
-    o.update(warm)
-    K = max(1, min(args.steps, int(90.0 / max(per_step, 1e-6))))
-    t0 = time.perf_counter()
-    o.update(K)
-    dt = time.perf_counter() - t0
-    v = GP * K / dt
+    done = 0
+    for _ in range(K):
+        for o, _g in objs:
+            o.update(1)
+        done += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt_s = time.perf_counter() - t0
+    gp = sum(g for _, g in objs)
+    v = gp * done / dt_s
     return {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "grid-pt-steps/s", "n_gpus": world, "steps": K,
-        "warmup": warm, "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded fields",
-        "config": {"workload": WORKLOAD, "nx": NX, "ny": NY, "ra": RA, "pr": PR, "dt": DT, "aspect": ASPECT},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "grid-pt-steps/s", "n_gpus": world,
+        "steps": done, "warmup": warm, "ms_per_step": dt_s / done * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded fields", "config": config,
         "cpu_baseline": {"value": v, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
-                         "sample": f"{K} steps of the workload (bounded to ~90 s)"},
+                         "sample": f"{len(objs)} of {len(cases)} cases, {done} steps each (bounded to ~{budget:.0f} s)"},
         "e2e": {"value": v, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference is Rust (no toolchain here or on the box); timed: the C++ restatement in oracle/",
     }
@@ -348,13 +486,14 @@ def run_reference(args, rank, world):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "periodic512"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
-    ap.add_argument("--quick", action="store_true",
-                    help="only warm-up + timed steps (profiling target); prints a reduced line")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 50 if args.workload == "ensemble" else 200
     rank, world, local = dist_info()
     if world > 1 and args.impl == "ours":
         import torch
@@ -365,7 +504,7 @@ def main():
         line = run_reference(args, rank, world)
     else:
         args.warmup = max(args.warmup, 3)
-        line = run_ours(args, rank, world, local)
+        line = (run_ensemble if args.workload == "ensemble" else run_periodic512)(args, rank, world, local)
     if rank == 0 and line is not None:
         print(json.dumps(line))
 

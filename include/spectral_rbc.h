@@ -64,7 +64,9 @@ typedef struct RbcParams {
   double dt;        /* time step */
   double aspect;    /* aspect ratio L/H */
   int kind;         /* RBC_BOX_ADIABATIC / RBC_BOX_CONDUCTING / RBC_PERIODIC */
-  int precision;    /* RBC_PREC_FP64 (RBC_PREC_MIXED: see rbc_batch_*) */
+  int precision;    /* RBC_PREC_FP64, or RBC_PREC_MIXED: dense transforms on the tensor
+                       cores (3xTF32), convection products in FP32, banded solves,
+                       projection and state update in FP64 */
 } RbcParams;
 
 typedef struct RbcCase RbcCase;
@@ -133,6 +135,10 @@ int rbc_device_bytes(const RbcCase* c, size_t* bytes);
 int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, int* nstages);
 /* name of stage k of the step (static string) */
 const char* rbc_stage_name(const RbcCase* c, int k);
+/* algorithmic HBM bytes of stage k (every array it must read or write, once) */
+int rbc_stage_bytes(const RbcCase* c, int k, double* bytes);
+/* name of a kernel id returned by rbc_batch_profile_step */
+const char* rbc_kernel_name(int kernel);
 
 /* ---- batches --------------------------------------------------------------
  * Many independent cases advanced together (no reference counterpart: the
@@ -152,6 +158,20 @@ int rbc_batch_synchronize(RbcBatch* b);
 /* number of size buckets and of kernel launches per batch step */
 int rbc_batch_layout(const RbcBatch* b, int* nbuckets, int* launches_per_step);
 int rbc_batch_get_stream(RbcBatch* b, void** stream);
+/* The spectral state of every case of a batch lives in one device region:
+ * case after case, each as temp, ux, uy, pres[0], pres[1] (the rbc_get_state
+ * layouts), every array padded to a multiple of 256 bytes.  These copy the
+ * whole region in one transfer (host memory may be pinned for speed). */
+/* Per-kernel timing of the batch step: every launch of every bucket runs
+ * alone between two events; stage k aggregates one kernel (stage_kernel[k],
+ * see rbc_kernel_name) over all buckets: mean ms per step and algorithmic
+ * bytes per step (stage_bytes and stage_kernel may be NULL). */
+int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* stage_bytes, int* stage_kernel,
+                           int max_stages, int* nstages);
+int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes);
+int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
+int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes);
+int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes);
 
 /* ---- device memory helpers (callers that do not link the CUDA runtime) ---- */
 int rbc_host_alloc_pinned(void** ptr, size_t bytes);
@@ -212,6 +232,29 @@ int fs_gradient(FsSpace* s, const double* d_spec, double* d_ortho, int deriv0, i
  * stream do not. */
 #define FS_NOALLOC_SCRATCH_BYTES (4u * 1024u * 1024u)
 int fs_forward_noalloc(FsSpace* s, const double* d_phys, double* d_spec, void* stream);
+
+/* ---- batched 1-D transforms and solves (precision microbenchmark) ----------
+ * `lanes` contiguous lanes (row-major lanes x length) of one Chebyshev-family
+ * basis (FS_CHEBYSHEV, FS_CHEB_DIRICHLET, FS_CHEB_NEUMANN) of length n, the
+ * 1-D restriction of Space2's axis operations (funspace ortho.rs:235-312,
+ * composite.rs:156-238) and of HholtzAdi::solve along one axis
+ * (hholtz_adi.rs:92-131).  precision RBC_PREC_FP64 runs the FP64 lane
+ * kernels; RBC_PREC_MIXED applies each operator as one dense matrix on the
+ * tensor cores (3xTF32, FP32 accumulation) and keeps the banded Helmholtz
+ * sweep in FP64.  Inputs and outputs are FP64 in both forms. */
+#define FS_OP_FORWARD 0    /* physical (n) -> spectral (m) */
+#define FS_OP_BACKWARD 1   /* spectral (m) -> physical (n) */
+#define FS_OP_TO_ORTHO 2   /* spectral (m) -> ortho (n) */
+#define FS_OP_FROM_ORTHO 3 /* ortho (n) -> spectral (m) */
+#define FS_OP_HHOLTZ 4     /* ortho right-hand side (n) -> spectral solution (m) */
+typedef struct FsLanes FsLanes;
+int fs_lanes_create(int base, int n, int precision, FsLanes** out);
+int fs_lanes_destroy(FsLanes* p);
+/* n: physical / ortho length, m: spectral length */
+int fs_lanes_shape(const FsLanes* p, int* n, int* m);
+/* coefficient c of (I - c D2) for FS_OP_HHOLTZ (HholtzAdi::new(field, [c]) along this axis) */
+int fs_lanes_set_hholtz(FsLanes* p, double c);
+int fs_lanes_apply(FsLanes* p, int op, const double* d_in, double* d_out, int lanes, void* stream);
 
 /* ---- solvers ----------------------------------------------------------------
  * Hholtz::new (src/solver/hholtz.rs:42-76), HholtzAdi::new (hholtz_adi.rs:44-63),

@@ -98,6 +98,13 @@ _SIGNATURES = {
     "rbc_batch_synchronize": (_I, [_P]),
     "rbc_batch_layout": (_I, [_P, _IP, _IP]),
     "rbc_batch_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "rbc_batch_state_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
+    "rbc_batch_profile_step": (_I, [_P, _I, _DP, _DP, _IP, _I, _IP]),
+    "rbc_stage_bytes": (_I, [_P, _I, _DP]),
+    "rbc_kernel_name": (ctypes.c_char_p, [_I]),
+    "rbc_batch_state_offset": (_I, [_P, _I, ctypes.POINTER(_SZ)]),
+    "rbc_batch_get_state_all": (_I, [_P, _P, _SZ]),
+    "rbc_batch_set_state_all": (_I, [_P, _P, _SZ]),
     "rbc_host_alloc_pinned": (_I, [ctypes.POINTER(_P), _SZ]),
     "rbc_host_free_pinned": (_I, [_P]),
     "rbc_dev_alloc": (_I, [ctypes.POINTER(_P), _SZ]),
@@ -114,6 +121,11 @@ _SIGNATURES = {
     "fs_to_ortho": (_I, [_P, _P, _P, _P]),
     "fs_from_ortho": (_I, [_P, _P, _P, _P]),
     "fs_gradient": (_I, [_P, _P, _P, _I, _I, _DP, _P]),
+    "fs_lanes_create": (_I, [_I, _I, _I, ctypes.POINTER(_P)]),
+    "fs_lanes_destroy": (_I, [_P]),
+    "fs_lanes_shape": (_I, [_P, _IP, _IP]),
+    "fs_lanes_set_hholtz": (_I, [_P, _D]),
+    "fs_lanes_apply": (_I, [_P, _I, _P, _P, _I, _P]),
     "sv_create": (_I, [_P, _I, _DP, ctypes.POINTER(_P)]),
     "sv_destroy": (_I, [_P]),
     "sv_solve": (_I, [_P, _P, _P, _P]),
@@ -336,6 +348,50 @@ class Field2:
         return self.space.gradient(self.vhat, deriv, scale)
 
 
+OP_FORWARD, OP_BACKWARD, OP_TO_ORTHO, OP_FROM_ORTHO, OP_HHOLTZ = 0, 1, 2, 3, 4
+
+
+class Lanes:
+    """Batched 1-D operations of one Chebyshev-family basis on many lanes
+    (row-major lanes x length): forward / backward / to_ortho / from_ortho and
+    the 1-D HholtzAdi solve, in FP64 or mixed precision (tensor-core 3xTF32
+    dense products, FP64 banded sweep)."""
+
+    def __init__(self, base: Base, precision=PREC_FP64, hholtz_c=None):
+        h = _P()
+        _check(lib().fs_lanes_create(base.kind, base.n, int(precision), ctypes.byref(h)))
+        self._h = h
+        n, m = _I(), _I()
+        _check(lib().fs_lanes_shape(h, ctypes.byref(n), ctypes.byref(m)))
+        self.n, self.m = n.value, m.value
+        if hholtz_c is not None:
+            _check(lib().fs_lanes_set_hholtz(h, float(hholtz_c)))
+
+    def lengths(self, op):
+        return {OP_FORWARD: (self.n, self.m), OP_BACKWARD: (self.m, self.n), OP_TO_ORTHO: (self.m, self.n),
+                OP_FROM_ORTHO: (self.n, self.m), OP_HHOLTZ: (self.n, self.m)}[op]
+
+    def apply_dev(self, op, d_in, d_out, lanes, stream=None):
+        _check(lib().fs_lanes_apply(self._h, int(op), d_in.ptr, d_out.ptr, int(lanes), stream))
+
+    def apply(self, op, a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        il, ol = self.lengths(op)
+        assert a.shape[-1] == il
+        lanes = a.size // il
+        d_in = DeviceArray.from_host(a)
+        d_out = DeviceArray((lanes, ol))
+        self.apply_dev(op, d_in, d_out, lanes)
+        _check(lib().rbc_device_synchronize())
+        return d_out.to_host()
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.fs_lanes_destroy(h)
+            self._h = None
+
+
 class _Solver:
     kind = HHOLTZ
 
@@ -531,12 +587,21 @@ class Navier2D:
     def div_norm(self):
         return self.eval(DIV_NORM)
 
-    def profile_step(self, nsteps=10):
-        """Mean device time (ms) of each kernel of the step: {stage name: ms}."""
+    def profile_step(self, nsteps=10, with_bytes=False):
+        """Mean device time (ms) of each kernel of the step, summed over the
+        stages that run the same kernel: {kernel name: ms}, or {name: (ms,
+        algorithmic bytes)} with ``with_bytes``."""
         ms = np.zeros(64)
         n = _I()
         _check(lib().rbc_profile_step(self._h, int(nsteps), _dptr(ms), 64, ctypes.byref(n)))
-        return {lib().rbc_stage_name(self._h, k).decode(): float(ms[k]) for k in range(n.value)}
+        out = {}
+        for k in range(n.value):
+            name = lib().rbc_stage_name(self._h, k).decode()
+            b = _D()
+            _check(lib().rbc_stage_bytes(self._h, k, ctypes.byref(b)))
+            t, by = out.get(name, (0.0, 0.0))
+            out[name] = (t + float(ms[k]), by + b.value)
+        return out if with_bytes else {k: v[0] for k, v in out.items()}
 
     def stream(self):
         s = _P()
@@ -551,21 +616,24 @@ class Navier2D:
 
 class Batch:
     """Independent cases advanced together (rbc_batch_*).  ``params`` is a
-    list of (nx, ny, ra, pr, dt, aspect, kind) tuples; ``cases[i]`` is a
-    borrowed Navier2D handle of case i (initial conditions, state, diagnostics)."""
+    list of (nx, ny, ra, pr, dt, aspect, kind[, precision]) tuples;
+    ``precision`` (default for all) applies to tuples without one.
+    ``cases[i]`` is a borrowed Navier2D handle of case i (initial conditions,
+    state, diagnostics)."""
 
-    def __init__(self, params):
-        arr = (RbcParams * len(params))()
-        for i, (nx, ny, ra, pr, dt, asp, kind) in enumerate(params):
-            arr[i] = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(asp), int(kind), PREC_FP64)
+    def __init__(self, params, precision=PREC_FP64):
+        full = [tuple(p) if len(p) == 8 else tuple(p) + (precision,) for p in params]
+        arr = (RbcParams * len(full))()
+        for i, (nx, ny, ra, pr, dt, asp, kind, prec) in enumerate(full):
+            arr[i] = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(asp), int(kind), int(prec))
         h = _P()
-        _check(lib().rbc_batch_create(arr, len(params), ctypes.byref(h)))
+        _check(lib().rbc_batch_create(arr, len(full), ctypes.byref(h)))
         self._h = h
         self.cases = []
-        for i, (nx, ny, ra, pr, dt, asp, kind) in enumerate(params):
+        for i, (nx, ny, ra, pr, dt, asp, kind, prec) in enumerate(full):
             c = _P()
             _check(lib().rbc_batch_case(h, i, ctypes.byref(c)))
-            self.cases.append(Navier2D(nx, ny, ra, pr, dt, asp, kind, _borrowed=c.value))
+            self.cases.append(Navier2D(nx, ny, ra, pr, dt, asp, kind, prec, _borrowed=c.value))
 
     def update(self, nsteps=1):
         _check(lib().rbc_batch_step(self._h, int(nsteps)))
@@ -582,6 +650,30 @@ class Batch:
         s = _P()
         _check(lib().rbc_batch_get_stream(self._h, ctypes.byref(s)))
         return s.value
+
+    def profile_step(self, nsteps=5):
+        """{kernel name: (mean ms per step, algorithmic bytes per step)} with
+        every launch timed alone (advances the batch by nsteps steps)."""
+        cap = 64
+        ms = (ctypes.c_double * cap)()
+        by = (ctypes.c_double * cap)()
+        kd = (ctypes.c_int * cap)()
+        n = _I()
+        _check(lib().rbc_batch_profile_step(self._h, int(nsteps), ms, by, kd, cap, ctypes.byref(n)))
+        return {lib().rbc_kernel_name(kd[k]).decode(): (ms[k], by[k]) for k in range(n.value)}
+
+    def state_bytes(self):
+        n = _SZ()
+        _check(lib().rbc_batch_state_bytes(self._h, ctypes.byref(n)))
+        return n.value
+
+    def get_state_all(self, host):
+        """Copy every case's spectral state into ``host`` (a uint8 array of
+        state_bytes(), e.g. PinnedArray(...).array)."""
+        _check(lib().rbc_batch_get_state_all(self._h, host.ctypes.data_as(_P), host.nbytes))
+
+    def set_state_all(self, host):
+        _check(lib().rbc_batch_set_state_all(self._h, host.ctypes.data_as(_P), host.nbytes))
 
     def __del__(self):
         h = getattr(self, "_h", None)

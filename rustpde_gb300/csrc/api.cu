@@ -2,12 +2,16 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
+#include "dense_ops.h"
 #include "host_ops.h"
+#include "lane_gemm.h"
 #include "prims.h"
 #include "spectral_rbc.h"
 #include "step_fp64.h"
@@ -49,6 +53,93 @@ static double get_ka(double ra, double pr, double h) { return std::sqrt(1.0 / ((
 
 using namespace rbc;
 
+// Device copies of a step plan: work tables of the lane kernels, job and tile
+// tables of the tensor-core GEMM launches.
+struct DevPlan {
+  std::vector<int4*> work;
+  std::vector<GemmJobDev*> jobs;
+  std::vector<int4*> tiles;
+  std::vector<int> ntiles, max_nt;
+};
+
+static void upload_plan(Arena& A, const StepPlan& plan, DevPlan& dp) {
+  dp = DevPlan();
+  for (const StepLaunch& L : plan.launches) {
+    int4* w = nullptr;
+    GemmJobDev* j = nullptr;
+    int4* t = nullptr;
+    int nt = 0, mnt = 0;
+    if (L.kernel == K_GEMM) {
+      std::vector<int4> tiles;
+      gemm_tiles(L.jobs, tiles);
+      j = A.upload(L.jobs);
+      t = A.upload(tiles);
+      nt = (int)tiles.size();
+      for (const GemmJobDev& g : L.jobs) mnt = std::max(mnt, g.NT);
+    } else {
+      w = A.upload(L.items);
+    }
+    dp.work.push_back(w);
+    dp.jobs.push_back(j);
+    dp.tiles.push_back(t);
+    dp.ntiles.push_back(nt);
+    dp.max_nt.push_back(mnt);
+  }
+}
+
+static cudaError_t launch_entry(const StepLaunch& L, const DevPlan& dp, size_t k, cudaStream_t st,
+                                const CaseDev* cases) {
+  if (L.kernel == K_GEMM) return launch_lane_gemm(dp.jobs[k], dp.tiles[k], dp.ntiles[k], dp.max_nt[k], st);
+  return launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, st, cases, dp.work[k]);
+}
+
+// Dense operator compositions of the mixed step (long double, before the
+// split), shared by every case of a size.
+enum MixedOpKind {
+  MOP_BS_CD = 0,   // B S (Dirichlet composite -> physical)
+  MOP_BDS_CD = 1,  // B D S (first derivative, physical)
+  MOP_BS_CN = 2,   // the same for the Neumann composite basis
+  MOP_BDS_CN = 3,
+  MOP_FWD_23 = 4   // forward Chebyshev, rows < 2n/3 (one axis of the 2/3 truncation)
+};
+static std::mutex g_ops_mu;
+static std::map<std::pair<int, int>, LMat> g_ops_cache;
+
+static const LMat& mixed_operator(int which, int n) {
+  std::lock_guard<std::mutex> lk(g_ops_mu);
+  auto key = std::make_pair(which, n);
+  auto it = g_ops_cache.find(key);
+  if (it != g_ops_cache.end()) return it->second;
+  LMat M;
+  if (which == MOP_FWD_23) {
+    M = lm_rows(lm_cheb_forward(n), 0, n * 2 / 3);
+  } else {
+    HostBasis b = make_basis(which <= MOP_BDS_CD ? CD : CN, n);
+    LMat S = lm_stencil(b), Bk = lm_cheb_backward(n);
+    if (which == MOP_BS_CD || which == MOP_BS_CN) M = lm_mul(Bk, S);
+    else M = lm_mul(Bk, lm_mul(lm_cheb_diff(n), S));
+  }
+  return g_ops_cache.emplace(key, std::move(M)).first->second;
+}
+
+// Pack rows blocks [A0 * s0 ; A1 * s1 ; ...] (long double) as one split operand.
+static const float* upload_op(Arena& a, std::initializer_list<std::pair<const LMat*, long double>> blocks) {
+  int rows = 0, cols = -1;
+  for (auto& b : blocks) {
+    rows += b.first->rows;
+    if (cols < 0) cols = b.first->cols;
+    if (cols != b.first->cols) throw std::runtime_error("upload_op: column mismatch");
+  }
+  std::vector<double> W((size_t)rows * cols);
+  size_t o = 0;
+  for (auto& b : blocks)
+    for (long double v : b.first->a) W[o++] = (double)(v * b.second);
+  return a.upload(pack_gemm_w(W, rows, cols, gemm_tile_n(rows)));
+}
+static const float* upload_op(Arena& a, const std::vector<double>& W, int rows, int cols) {
+  return a.upload(pack_gemm_w(W, rows, cols, gemm_tile_n(rows)));
+}
+
 struct RbcCase {
   RbcParams p{};
   bool periodic = false;
@@ -67,7 +158,8 @@ struct RbcCase {
   double* d_red = nullptr;
   cudaStream_t stream = nullptr;
   StepPlan plan;
-  std::vector<int4*> d_work;
+  DevPlan dp;
+  MixedOps mops;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   double time = 0.0;
@@ -89,6 +181,15 @@ struct FsSpace {
   Arena arena;
   SpaceDev s;
   void* tmp = nullptr;
+};
+
+struct FsLanes {
+  Arena arena;
+  LanesDev L;
+  int precision = RBC_PREC_FP64;
+  // mixed form: packed split operators per FS_OP_* (device)
+  const float* w[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  unsigned int* d_status = nullptr;
 };
 
 struct SvSolver {
@@ -154,7 +255,24 @@ std::vector<double> get_dx(const std::vector<double>& x, bool periodic) {  // fi
   return dx;
 }
 
-void build_case(RbcCase* c, bool with_graph = true) {
+// Spectral state of a case: temp, ux, uy, pres[0], pres[1] (each rounded up
+// to 256 bytes).  sizes[k] receives the unpadded bytes of array k.
+static size_t state_layout(const RbcParams& p, size_t sizes[5]) {
+  const bool per = p.kind == RBC_PERIODIC;
+  const size_t es = per ? 16 : 8;
+  const size_t mx = per ? (size_t)p.nx / 2 + 1 : (size_t)p.nx;
+  const size_t mxc = per ? mx : (size_t)p.nx - 2;
+  const size_t nstate = mxc * (size_t)(p.ny - 2);
+  sizes[0] = sizes[1] = sizes[2] = sizes[4] = nstate * es;
+  sizes[3] = mx * (size_t)p.ny * es;
+  size_t t = 0;
+  for (int k = 0; k < 5; k++) t += (sizes[k] + 255) & ~size_t(255);
+  return t;
+}
+
+// state_region: optional device region of state_layout() bytes that holds the
+// case's spectral state (a batch keeps all its cases' state contiguous).
+void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr) {
   const RbcParams& p = c->p;
   Arena& A = c->arena;
   const int nx = p.nx, ny = p.ny;
@@ -221,18 +339,62 @@ void build_case(RbcCase* c, bool with_graph = true) {
     h.pois_y = upload_fdma(A, hholtz_rows(c->sp_p1.hb0, c->sp_p1.hb1, cp[0], cp[1], 0.0, true, nullptr, &fwd, &bwd, &err));
     h.pois_fwd = A.upload(fwd);
     h.pois_bwd = A.upload(bwd);
+    if (p.precision == RBC_PREC_MIXED) {
+      const int mxc = nx - 2;
+      c->mops.pf = upload_op(A, fwd, mxc, mxc);
+      c->mops.pb = upload_op(A, bwd, mxc, mxc);
+    }
   }
   const size_t es = c->spec_elem();
   const size_t nstate = (size_t)h.mxc * h.myc;
-  h.ux = A.alloc(nstate * es);
-  h.uy = A.alloc(nstate * es);
-  h.temp = A.alloc(nstate * es);
-  h.p0 = A.alloc((size_t)h.mx * ny * es);
-  h.p1 = A.alloc(nstate * es);
+  if (state_region) {
+    size_t sz[5];
+    state_layout(p, sz);
+    void* arr[5];
+    char* q = state_region;
+    for (int k = 0; k < 5; k++) {
+      arr[k] = q;
+      q += (sz[k] + 255) & ~size_t(255);
+    }
+    h.temp = arr[0]; h.ux = arr[1]; h.uy = arr[2]; h.p0 = arr[3]; h.p1 = arr[4];
+    cuda_check(cudaMemset(state_region, 0, (size_t)(q - state_region)), "clear state");
+  } else {
+    h.ux = A.alloc(nstate * es);
+    h.uy = A.alloc(nstate * es);
+    h.temp = A.alloc(nstate * es);
+    h.p0 = A.alloc((size_t)h.mx * ny * es);
+    h.p1 = A.alloc(nstate * es);
+  }
   for (int k = 0; k < 6; k++) h.yw[k] = A.alloc((size_t)h.mxc * ny * es);
   h.q[0] = A.alloc((size_t)3 * std::max(h.kx, 1) * ny * es);
   if (!per)
     for (int k = 0; k < 8; k++) h.s[k] = A.alloc((size_t)nx * ny * 8);
+  h.mixed = p.precision == RBC_PREC_MIXED;
+  if (h.mixed) {
+    for (int f = 0; f < 3; f++) h.m_y[f] = A.alloc((size_t)2 * ny * h.mx * 8);
+    h.m_q = A.alloc((size_t)3 * ny * std::max(h.kx, 1) * 8);
+    h.m_cv = A.alloc((size_t)3 * std::max(h.kx, 1) * h.ky * 16);
+    h.m_bcx = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
+    h.m_bcy = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
+    c->mops.y1 = upload_op(A, {{&mixed_operator(MOP_BS_CD, ny), 1.0L}, {&mixed_operator(MOP_BDS_CD, ny), 1.0L}});
+    c->mops.y2 = upload_op(A, {{&mixed_operator(MOP_FWD_23, ny), 1.0L}});
+    if (!per) {
+      for (int k = 0; k < 6; k++) h.m_ph[k] = A.alloc((size_t)2 * nx * ny * 4);
+      for (int k = 0; k < 3; k++) h.m_p[k] = A.alloc((size_t)nx * ny * 4);
+      h.m_z = A.alloc((size_t)nx * ny * 8);
+      const long double inv_asp = 1.0L / (long double)p.aspect;
+      const bool tn = p.kind == RBC_BOX_ADIABATIC;  // temperature: Neumann in x
+      const LMat& bsu = mixed_operator(MOP_BS_CD, nx);
+      const LMat& bdsu = mixed_operator(MOP_BDS_CD, nx);
+      const LMat& bst = mixed_operator(tn ? MOP_BS_CN : MOP_BS_CD, nx);
+      const LMat& bdst = mixed_operator(tn ? MOP_BDS_CN : MOP_BDS_CD, nx);
+      c->mops.xa = upload_op(A, {{&bsu, 1.0L}, {&bdsu, inv_asp}});
+      c->mops.xb = upload_op(A, {{&bsu, 1.0L}});
+      c->mops.xc = upload_op(A, {{&bdst, inv_asp}});
+      c->mops.xd = upload_op(A, {{&bst, 1.0L}});
+      c->mops.x2 = upload_op(A, {{&mixed_operator(MOP_FWD_23, nx), 1.0L}});
+    }
+  }
   void* bco = A.alloc((size_t)h.mx * ny * es);
   void* bcd = A.alloc((size_t)h.mx * ny * es);
   double* bdx = static_cast<double*>(A.alloc((size_t)nx * ny * 8));
@@ -291,21 +453,35 @@ void build_case(RbcCase* c, bool with_graph = true) {
     space_gradient(c->sp_bc, c->bc_vhat, gxx, 0, 1, c->scale, c->tmp, st);
     space_backward(c->sp_field, gxx, bdy, c->tmp, st);
     c->sync();
+    if (h.mixed) {
+      // FP32 copies of the boundary-field derivatives, transposed (ny x nx)
+      std::vector<double> hx((size_t)nx * ny), hy((size_t)nx * ny);
+      cuda_check(cudaMemcpy(hx.data(), bdx, hx.size() * 8, cudaMemcpyDeviceToHost), "copy bc dx");
+      cuda_check(cudaMemcpy(hy.data(), bdy, hy.size() * 8, cudaMemcpyDeviceToHost), "copy bc dy");
+      std::vector<float> tx((size_t)nx * ny), ty((size_t)nx * ny);
+      for (int i = 0; i < nx; i++)
+        for (int j = 0; j < ny; j++) {
+          tx[(size_t)j * nx + i] = (float)hx[(size_t)i * ny + j];
+          ty[(size_t)j * nx + i] = (float)hy[(size_t)i * ny + j];
+        }
+      cuda_check(cudaMemcpy(const_cast<float*>(h.m_bcx), tx.data(), tx.size() * 4, cudaMemcpyHostToDevice), "bc dx");
+      cuda_check(cudaMemcpy(const_cast<float*>(h.m_bcy), ty.data(), ty.size() * 4, cudaMemcpyHostToDevice), "bc dy");
+    }
   }
   // ---- step plan, work tables and the CUDA graph of one update()
   cuda_check(configure_step_kernels(), "configure step kernels");
-  c->plan = build_step_plan(h);
-  if (!with_graph) return;
-  for (auto& L : c->plan.launches) {
-    int4* w = static_cast<int4*>(A.alloc(L.items.size() * sizeof(int4)));
-    cuda_check(cudaMemcpy(w, L.items.data(), L.items.size() * sizeof(int4), cudaMemcpyHostToDevice), "work table");
-    c->d_work.push_back(w);
+  if (h.mixed) {
+    cuda_check(configure_mixed_kernels(), "configure mixed kernels");
+    c->plan = build_mixed_plan(h, c->mops);
+  } else {
+    c->plan = build_step_plan(h);
   }
+  if (!with_graph) return;
+  upload_plan(A, c->plan, c->dp);
   cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t le = cudaSuccess;
   for (size_t k = 0; k < c->plan.launches.size(); k++) {
-    auto& L = c->plan.launches[k];
-    cudaError_t e = launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, st, c->d_case, c->d_work[k]);
+    cudaError_t e = launch_entry(c->plan.launches[k], c->dp, k, st, c->d_case);
     if (e != cudaSuccess && le == cudaSuccess) le = e;
   }
   cudaGraph_t g = nullptr;
@@ -428,8 +604,8 @@ static void validate_params(const RbcParams& p) {
   if (p.kind == RBC_PERIODIC)
     require(p.nx >= 8 && p.nx <= 8192 && is_pow2(p.nx), "rbc_create: periodic nx must be a power of two in [8, 8192]");
   else require(p.nx >= 8 && p.nx <= 4097, "rbc_create: nx must be in [8, 4097]");
-  if (p.precision != RBC_PREC_FP64)
-    throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_create: single cases run in FP64; mixed precision is a batch form");
+  require(p.precision == RBC_PREC_FP64 || p.precision == RBC_PREC_MIXED, "rbc_create: unknown precision");
+
 }
 
 int rbc_create(const RbcParams* params, RbcCase** out) {
@@ -698,9 +874,12 @@ struct RbcBatch {
     int kind, nx, ny;
     std::vector<int> members;
     StepPlan plan;
-    std::vector<int4*> d_work;
+    DevPlan dp;
   };
   std::vector<Bucket> buckets;
+  char* d_state = nullptr;            // every case's spectral state, contiguous
+  size_t state_bytes = 0;
+  std::vector<size_t> state_offset;   // byte offset of case i in d_state
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   int launches = 0;
@@ -725,6 +904,12 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   cuda_check(configure_prim_kernels(), "configure kernels");
   std::unique_ptr<RbcBatch> b(new RbcBatch());
   cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream create");
+  size_t sz[5];
+  for (int i = 0; i < ncases; i++) {
+    b->state_offset.push_back(b->state_bytes);
+    b->state_bytes += state_layout(params[i], sz);
+  }
+  b->d_state = static_cast<char*>(b->arena.alloc(b->state_bytes));
   for (int i = 0; i < ncases; i++) {
     std::unique_ptr<RbcCase> c(new RbcCase());
     c->p = params[i];
@@ -732,7 +917,7 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     c->stream = b->stream;
     c->own_stream = false;
     c->in_batch = true;
-    build_case(c.get(), false);
+    build_case(c.get(), false, b->d_state + b->state_offset[i]);
     b->cases.push_back(c.release());
   }
   // device table of all case descriptors
@@ -742,7 +927,8 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   // buckets of equal (kind, nx, ny)
   for (int i = 0; i < ncases; i++) {
     const RbcParams& p = params[i];
-    int kind = p.kind == RBC_PERIODIC ? 2 : 0;  // both box kinds share kernels
+    // both box kinds share kernels; the precision selects the plan
+    int kind = (p.kind == RBC_PERIODIC ? 2 : 0) + 4 * p.precision;
     int found = -1;
     for (size_t k = 0; k < b->buckets.size(); k++)
       if (b->buckets[k].kind == kind && b->buckets[k].nx == p.nx && b->buckets[k].ny == p.ny) found = (int)k;
@@ -759,15 +945,23 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   for (auto& bk : b->buckets) {
     const RbcCase* first = b->cases[bk.members[0]];
     bk.plan = first->plan;
-    for (auto& L : bk.plan.launches) {
+    for (size_t li = 0; li < bk.plan.launches.size(); li++) {
+      StepLaunch& L = bk.plan.launches[li];
+      if (L.kernel == K_GEMM) {
+        // every member's jobs (each job addresses that case's arrays)
+        L.jobs.clear();
+        for (int m : bk.members)
+          for (const GemmJobDev& j : b->cases[m]->plan.launches[li].jobs) L.jobs.push_back(j);
+        continue;
+      }
       std::vector<int4> items;
       size_t lanes = L.items.size();
       items.reserve(lanes * bk.members.size());
-      for (size_t li = 0; li < lanes; li++)
-        for (int m : bk.members) items.push_back(make_int4(m, L.items[li].y, L.items[li].z, L.items[li].w));
+      for (size_t li2 = 0; li2 < lanes; li2++)
+        for (int m : bk.members) items.push_back(make_int4(m, L.items[li2].y, L.items[li2].z, L.items[li2].w));
       L.items = items;
-      bk.d_work.push_back(b->arena.upload(items));
     }
+    upload_plan(b->arena, bk.plan, bk.dp);
   }
   cuda_check(cudaDeviceSynchronize(), "batch set-up");
   // graph: one branch per bucket
@@ -783,8 +977,7 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     cudaStream_t s = b->branch[k];
     le = cudaStreamWaitEvent(s, b->events[nb], 0);
     for (size_t li = 0; li < bk.plan.launches.size() && le == cudaSuccess; li++) {
-      auto& L = bk.plan.launches[li];
-      le = launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, s, b->d_cases, bk.d_work[li]);
+      le = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
       b->launches++;
     }
     if (le == cudaSuccess) le = cudaEventRecord(b->events[k], s);
@@ -839,6 +1032,35 @@ int rbc_batch_layout(const RbcBatch* b, int* nbuckets, int* launches) {
   *launches = b->launches;
   API_END
 }
+int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes) {
+  API_BEGIN
+  require(b && bytes, "null argument");
+  *bytes = b->state_bytes;
+  API_END
+}
+int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes) {
+  API_BEGIN
+  require(b && host, "null argument");
+  require(bytes == b->state_bytes, "rbc_batch_get_state_all: size mismatch (see rbc_batch_state_bytes)");
+  cuda_check(cudaMemcpyAsync(host, b->d_state, bytes, cudaMemcpyDeviceToHost, b->stream), "state copy d2h");
+  cuda_check(cudaStreamSynchronize(b->stream), "stream synchronize");
+  API_END
+}
+int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes) {
+  API_BEGIN
+  require(b && host, "null argument");
+  require(bytes == b->state_bytes, "rbc_batch_set_state_all: size mismatch (see rbc_batch_state_bytes)");
+  cuda_check(cudaMemcpyAsync(b->d_state, host, bytes, cudaMemcpyHostToDevice, b->stream), "state copy h2d");
+  cuda_check(cudaStreamSynchronize(b->stream), "stream synchronize");
+  API_END
+}
+int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset) {
+  API_BEGIN
+  require(b && offset && i >= 0 && i < (int)b->cases.size(), "rbc_batch_state_offset: invalid argument");
+  *offset = b->state_offset[i];
+  API_END
+}
+
 int rbc_batch_get_stream(RbcBatch* b, void** stream) {
   API_BEGIN
   require(b && stream, "null argument");
@@ -858,8 +1080,7 @@ int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, i
   for (int s = 0; s < nsteps; s++) {
     cuda_check(cudaEventRecord(ev[0], c->stream), "event record");
     for (int k = 0; k < ns; k++) {
-      auto& L = c->plan.launches[k];
-      cuda_check(launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, c->stream, c->d_case, c->d_work[k]),
+      cuda_check(launch_entry(c->plan.launches[k], c->dp, k, c->stream, c->d_case),
                  "stage launch");
       cuda_check(cudaEventRecord(ev[k + 1], c->stream), "event record");
     }
@@ -876,13 +1097,65 @@ int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, i
   API_END
 }
 
+int rbc_stage_bytes(const RbcCase* c, int k, double* bytes) {
+  API_BEGIN
+  require(c && bytes && k >= 0 && k < (int)c->plan.launches.size(), "rbc_stage_bytes: invalid argument");
+  *bytes = launch_algorithmic_bytes(c->plan.launches[k], &c->hd);
+  API_END
+}
+
+int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* stage_bytes, int* stage_kernel,
+                           int max_stages, int* nstages) {
+  API_BEGIN
+  require(b && stage_ms && nstages && nsteps > 0, "rbc_batch_profile_step: invalid argument");
+  // stages = distinct kernels of the batch step, in order of first appearance;
+  // each launch of every bucket runs alone between two events
+  std::vector<int> kid;
+  std::vector<double> ms_acc, bytes;
+  std::vector<CaseDev> hd;
+  for (RbcCase* c : b->cases) hd.push_back(c->hd);
+  auto slot = [&](int kernel) {
+    for (size_t i = 0; i < kid.size(); i++)
+      if (kid[i] == kernel) return (int)i;
+    kid.push_back(kernel);
+    ms_acc.push_back(0.0);
+    bytes.push_back(0.0);
+    return (int)kid.size() - 1;
+  };
+  for (auto& bk : b->buckets)
+    for (auto& L : bk.plan.launches) bytes[slot(L.kernel)] += launch_algorithmic_bytes(L, hd.data());
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "event create");
+  cuda_check(cudaEventCreate(&e1), "event create");
+  for (int s = 0; s < nsteps; s++) {
+    for (auto& bk : b->buckets)
+      for (size_t li = 0; li < bk.plan.launches.size(); li++) {
+        cuda_check(cudaEventRecord(e0, b->stream), "event record");
+        cuda_check(launch_entry(bk.plan.launches[li], bk.dp, li, b->stream, b->d_cases), "stage launch");
+        cuda_check(cudaEventRecord(e1, b->stream), "event record");
+        cuda_check(cudaEventSynchronize(e1), "event sync");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+        ms_acc[slot(bk.plan.launches[li].kernel)] += ms;
+      }
+    for (RbcCase* c : b->cases) c->time += c->p.dt;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *nstages = (int)kid.size();
+  for (int k = 0; k < (int)kid.size() && k < max_stages; k++) {
+    stage_ms[k] = ms_acc[k] / nsteps;
+    if (stage_bytes) stage_bytes[k] = bytes[k];
+    if (stage_kernel) stage_kernel[k] = kid[k];
+  }
+  API_END
+}
+
+const char* rbc_kernel_name(int kernel) { return step_kernel_name(kernel); }
+
 const char* rbc_stage_name(const RbcCase* c, int k) {
-  static const char* names[] = {"y1_complex", "y1_real", "periodic_x", "periodic_y2", "box_x1", "box_y2",
-                                "box_x2", "box_y3", "box_x3", "box_y4", "box_x4", "box_y5", "periodic_y2a",
-                                "periodic_y2b"};
   if (!c || k < 0 || k >= (int)c->plan.launches.size()) return "";
-  int id = c->plan.launches[k].kernel;
-  return (id >= 0 && id < 14) ? names[id] : "";
+  return step_kernel_name(c->plan.launches[k].kernel);
 }
 
 // ---- device memory helpers
@@ -1029,6 +1302,80 @@ int fs_forward_noalloc(FsSpace* s, const double* d_phys, double* d_spec, void* s
                                         std::to_string((size_t)FS_NOALLOC_SCRATCH_BYTES));
   void* scratch = noalloc_scratch_for_current_device();
   space_forward(s->s, d_phys, d_spec, scratch, (cudaStream_t)stream);
+  API_END
+}
+
+// ---- batched 1-D lanes
+static const float* upload_split(Arena& a, const LMat& M) {
+  std::vector<float> pk = pack_gemm_w(lm_to_double(M), M.rows, M.cols, gemm_tile_n(M.rows));
+  return a.upload(pk);
+}
+
+int fs_lanes_create(int base, int n, int precision, FsLanes** out) {
+  API_BEGIN
+  require(out != nullptr, "null argument");
+  *out = nullptr;
+  require(base == FS_CHEBYSHEV || base == FS_CHEB_DIRICHLET || base == FS_CHEB_NEUMANN,
+          "fs_lanes_create: Chebyshev-family bases only");
+  require(n >= 8 && n <= 2048, "fs_lanes_create: n must be in [8, 2048]");
+  require(precision == RBC_PREC_FP64 || precision == RBC_PREC_MIXED, "fs_lanes_create: unknown precision");
+  cuda_check(configure_prim_kernels(), "configure kernels");
+  cuda_check(configure_gemm_kernels(), "configure gemm kernels");
+  std::unique_ptr<FsLanes> p(new FsLanes());
+  p->precision = precision;
+  build_lanes(p->arena, p->L, base, n);
+  p->d_status = static_cast<unsigned int*>(p->arena.alloc(16));
+  if (precision == RBC_PREC_MIXED) {
+    const HostBasis& hb = p->L.hb;
+    LMat S = lm_stencil(hb), P = lm_from_ortho(hb);
+    p->w[FS_OP_FORWARD] = upload_split(p->arena, lm_mul(P, lm_cheb_forward(n)));
+    p->w[FS_OP_BACKWARD] = upload_split(p->arena, lm_mul(lm_cheb_backward(n), S));
+    p->w[FS_OP_TO_ORTHO] = upload_split(p->arena, S);
+    p->w[FS_OP_FROM_ORTHO] = upload_split(p->arena, P);
+    if (hb.composite()) p->w[FS_OP_HHOLTZ] = upload_split(p->arena, lm_pinv(n));
+  }
+  *out = p.release();
+  API_END
+}
+int fs_lanes_destroy(FsLanes* p) {
+  API_BEGIN
+  delete p;
+  API_END
+}
+int fs_lanes_shape(const FsLanes* p, int* n, int* m) {
+  API_BEGIN
+  require(p && n && m, "null argument");
+  *n = p->L.hb.n;
+  *m = p->L.hb.m;
+  API_END
+}
+int fs_lanes_set_hholtz(FsLanes* p, double c) {
+  API_BEGIN
+  require(p != nullptr, "null argument");
+  require(std::isfinite(c), "fs_lanes_set_hholtz: coefficient must be finite");
+  lanes_set_hholtz(p->arena, p->L, c);
+  API_END
+}
+int fs_lanes_apply(FsLanes* p, int op, const double* d_in, double* d_out, int lanes, void* stream) {
+  API_BEGIN
+  require(p && d_in && d_out, "null argument");
+  require(op >= FS_OP_FORWARD && op <= FS_OP_HHOLTZ, "fs_lanes_apply: unknown operation");
+  require(lanes >= 0, "fs_lanes_apply: negative lane count");
+  if (lanes == 0) return RBC_OK;
+  if (op == FS_OP_HHOLTZ) require(p->L.has_solver, "fs_lanes_apply: call fs_lanes_set_hholtz first");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (p->precision == RBC_PREC_FP64) {
+    lanes_apply(p->L, op, d_in, d_out, lanes, st);
+  } else {
+    int il, ol;
+    lane_op_lengths(p->L, op, &il, &ol);
+    void* ip[1] = {const_cast<double*>(d_in)};
+    void* opp[1] = {d_out};
+    GemmJobDev j = make_gemm_job(lane_rows(ip, 1, lanes, il, il, LT_F64, false),
+                                 lane_rows(opp, 1, lanes, ol, ol, LT_F64, false), p->w[op], il, ol, 1.0, p->d_status);
+    cuda_check(launch_lane_gemm_one(j, st), "lane gemm launch");
+    if (op == FS_OP_HHOLTZ) lanes_fdma(p->L, d_out, lanes, st);
+  }
   API_END
 }
 

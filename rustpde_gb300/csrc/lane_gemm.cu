@@ -1,0 +1,397 @@
+// lane_gemm.cu -- tcgen05 3xTF32 lane GEMM (see lane_gemm.h).
+//
+// One CTA (4 warps) computes a tile of 128 lanes x NT outputs of one job:
+//   * the threads stage a 128 x 32 chunk of the input lanes into shared memory,
+//     converting each value v to TF32 hi = rna(v) and lo = rna(v - hi), written
+//     straight into the K-major core-matrix layout the tensor core reads
+//     (8 rows x 16 bytes per core matrix, no swizzle);
+//   * the matching chunk of the pre-split operator W is copied as-is;
+//   * one thread issues 4 k-steps x 3 tcgen05.mma (lo*hi, hi*lo, hi*hi) into
+//     an FP32 accumulator in tensor memory and commits to an mbarrier;
+//   * after the last chunk each warp reads its 32 accumulator lanes back with
+//     tcgen05.ld, stages them through shared memory and stores them coalesced.
+// Every wait is bounded: on time-out the kernel sets kStatusGemmTimeout, skips
+// the stores, frees its tensor memory and returns.
+#include "lane_gemm.h"
+
+#include <algorithm>
+#include <cstring>
+
+namespace rbc {
+namespace dev {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// tcgen05 shared-memory matrix descriptor, no swizzle: start address, leading
+// (K-direction) and stride (M/N-direction) byte offsets between core matrices.
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFF) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of this architecture
+  return d;
+}
+
+// byte offset of element (row r, k) of an R-row, 32-wide K-major chunk
+__device__ __forceinline__ int cm_off(int r, int k, int R) {
+  return ((k >> 2) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 3) * 4;
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ const char* lane_addr(const LaneSideDev& s, int l) {
+  const int per_f = s.rows * s.parts;
+  const int f = l / per_f;
+  const int rem = l - f * per_f;
+  const int r = rem / s.parts;
+  const int p = rem - r * s.parts;
+  const long long es = s.type == LT_F64 ? 8 : 4;
+  return static_cast<const char*>(s.ptr[f]) + ((long long)r * s.lane_stride + (long long)p * s.part_stride) * es;
+}
+
+__device__ __forceinline__ float load_elem(const char* base, long long idx, int type) {
+  if (type == LT_F64) return (float)__ldg(reinterpret_cast<const double*>(base) + idx);
+  return __ldg(reinterpret_cast<const float*>(base) + idx);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* m, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
+}
+__device__ __forceinline__ bool mbar_try(uint64_t* m, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(m)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+constexpr long kWaitLimit = 1L << 22;  // try_wait polls before a completion wait is declared lost
+
+__device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, const int tile_n) {
+  const int NT = J.NT;
+  const int tid = threadIdx.x, warp = tid >> 5, wl = tid & 31;
+  extern __shared__ __align__(128) unsigned char sm[];
+  unsigned char* Ahi = sm;
+  unsigned char* Alo = sm + 16384;
+  unsigned char* Whi = sm + 32768;
+  unsigned char* Wlo = Whi + NT * 128;
+  unsigned char* tail = Wlo + NT * 128;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(tail);
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 8);
+  const char** ib = reinterpret_cast<const char**>(tail + 16);
+  char** ob = reinterpret_cast<char**>(tail + 16 + kGemmLanes * 8);
+  float* stage = reinterpret_cast<float*>(sm);  // [128][33], reuses the A chunk after the last MMA
+
+  {
+    const int l = lane0 + tid;
+    const char* ip = nullptr;
+    char* op = nullptr;
+    if (l < J.lanes) {
+      ip = lane_addr(J.in, l);
+      op = const_cast<char*>(lane_addr(J.out, l));
+    }
+    ib[tid] = ip;
+    ob[tid] = op;
+  }
+  const uint32_t ncols = NT <= 32 ? 32u : NT <= 64 ? 64u : NT <= 128 ? 128u : 256u;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) mbar_init(mbar, 1);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  // instruction descriptor: D f32, A/B tf32, K-major both, N = NT, M = 128
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NT >> 3) << 17) | ((128u >> 4) << 24);
+  const uint32_t a_lbo = (kGemmLanes / 8) * 128, w_lbo = (uint32_t)(NT / 8) * 128;
+  const float* wsrc = J.w + (size_t)tile_n * J.kchunks * 2 * NT * kGemmKC;
+  const long long ies = J.in.elem_stride;
+  const int itype = J.in.type;
+  bool ok = true;
+
+  for (int c = 0; c < J.kchunks; c++) {
+    const int k0 = c * kGemmKC;
+    // --- A chunk: item (lane l, quad kq) -> 4 consecutive k of one lane
+#pragma unroll 2
+    for (int it = 0; it < 8; it++) {
+      const int q = tid + 128 * it;
+      const int llo = q & 7, r = q >> 3;
+      int l, kq;
+      if (J.in.lane_fast) { l = (r & 15) * 8 + llo; kq = r >> 4; }
+      else { l = (r >> 3) * 8 + llo; kq = r & 7; }
+      const char* base = ib[l];
+      float v[4];
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int k = k0 + kq * 4 + e;
+        v[e] = (base != nullptr && k < J.K) ? load_elem(base, (long long)k * ies, itype) : 0.0f;
+      }
+      float4 hi, lo;
+      // lo is rounded to TF32 here: left to the tensor core it would be
+      // truncated, a bias that accumulates along K
+      hi.x = tf32_rna(v[0]); lo.x = tf32_rna(v[0] - hi.x);
+      hi.y = tf32_rna(v[1]); lo.y = tf32_rna(v[1] - hi.y);
+      hi.z = tf32_rna(v[2]); lo.z = tf32_rna(v[2] - hi.z);
+      hi.w = tf32_rna(v[3]); lo.w = tf32_rna(v[3] - hi.w);
+      const int off = cm_off(l, kq * 4, kGemmLanes);
+      *reinterpret_cast<float4*>(Ahi + off) = hi;
+      *reinterpret_cast<float4*>(Alo + off) = lo;
+    }
+    // --- W chunk (hi block then lo block, already in operand order)
+    {
+      const uint4* ws = reinterpret_cast<const uint4*>(wsrc + (size_t)c * 2 * NT * kGemmKC);
+      uint4* wd = reinterpret_cast<uint4*>(Whi);
+      for (int i = tid; i < NT * 16; i += 128) wd[i] = __ldg(ws + i);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (tid == 0) {
+#pragma unroll
+      for (int s = 0; s < kGemmKC / 8; s++) {
+        const uint64_t ah = umma_desc(smem_u32(Ahi) + s * 2 * a_lbo, a_lbo, 128);
+        const uint64_t al = umma_desc(smem_u32(Alo) + s * 2 * a_lbo, a_lbo, 128);
+        const uint64_t wh = umma_desc(smem_u32(Whi) + s * 2 * w_lbo, w_lbo, 128);
+        const uint64_t wlo = umma_desc(smem_u32(Wlo) + s * 2 * w_lbo, w_lbo, 128);
+        mma_tf32(tmem, al, wh, idesc, (c > 0 || s > 0) ? 1u : 0u);
+        mma_tf32(tmem, ah, wlo, idesc, 1u);
+        mma_tf32(tmem, ah, wh, idesc, 1u);
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_u32(mbar))
+                   : "memory");
+    }
+    bool done = false;
+    for (long i = 0; i < kWaitLimit && !done; i++) done = mbar_try(mbar, (uint32_t)(c & 1));
+    ok = __syncthreads_and(done) != 0;
+    tc_fence_after();
+    if (!ok) break;
+  }
+
+  if (ok) {
+    const int P = J.out.parts;
+    const long long oes = J.out.elem_stride;
+    const int otype = J.out.type;
+    const double scale = J.scale;
+    const int nbase = tile_n * NT;
+    for (int cc = 0; cc < NT; cc += 32) {
+      uint32_t r[32];
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, r);
+#pragma unroll
+      for (int j = 0; j < 32; j++) stage[(warp * 32 + wl) * 33 + j] = __uint_as_float(r[j]);
+      __syncthreads();
+#pragma unroll 4
+      for (int it = 0; it < 32; it++) {
+        const int q = tid + 128 * it;
+        int l, n;
+        if (J.out.lane_fast) { l = q & 127; n = q >> 7; }
+        else {
+          const int p = q % P;
+          n = (q / P) & 31;
+          l = (q / (32 * P)) * P + p;
+        }
+        char* base = ob[l];
+        const int nl = cc + n, ng = nbase + nl;
+        if (base != nullptr && nl < NT && ng < J.N) {
+          const double v = (double)stage[l * 33 + n] * scale;
+          if (otype == LT_F64) reinterpret_cast<double*>(base)[(long long)ng * oes] = v;
+          else reinterpret_cast<float*>(base)[(long long)ng * oes] = (float)v;
+        }
+      }
+      __syncthreads();
+    }
+  } else if (tid == 0 && J.status != nullptr) {
+    atomicOr(J.status, kStatusGemmTimeout);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+// grouped form: tile table entries (job, first lane, output tile, 0)
+__global__ void __launch_bounds__(128) k_lane_gemm(const GemmJobDev* __restrict__ jobs, const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  gemm_tile(jobs[tl.x], tl.y, tl.z);
+}
+
+// single job passed by value: block b -> lanes (b / ntiles) * 128, output tile b % ntiles
+__global__ void __launch_bounds__(128) k_lane_gemm_one(const __grid_constant__ GemmJobDev J) {
+  const int b = blockIdx.x;
+  gemm_tile(J, (b / J.ntiles) * kGemmLanes, b % J.ntiles);
+}
+
+}  // namespace dev
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int gemm_tile_n(int N) {
+  auto r16 = [](int v) { return (v + 15) & ~15; };
+  if (N <= 256) return r16(N);
+  int t = (N + 255) / 256;
+  return r16((N + t - 1) / t);
+}
+
+static float tf32_rna_host(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  u = (u + 0x1000u) & 0xFFFFE000u;  // round to nearest (ties away) at the 10-bit mantissa
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+static int cm_off_host(int r, int k, int R) {
+  return ((k >> 2) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 3) * 4;
+}
+
+std::vector<float> pack_gemm_w(const std::vector<double>& W, int N, int K, int NT) {
+  const int ntiles = (N + NT - 1) / NT, kch = (K + kGemmKC - 1) / kGemmKC;
+  const size_t blk = (size_t)2 * NT * kGemmKC;
+  std::vector<float> out((size_t)ntiles * kch * blk, 0.0f);
+  for (int t = 0; t < ntiles; t++)
+    for (int c = 0; c < kch; c++) {
+      float* b = out.data() + ((size_t)t * kch + c) * blk;
+      for (int nl = 0; nl < NT; nl++) {
+        const int n = t * NT + nl;
+        if (n >= N) break;
+        for (int kl = 0; kl < kGemmKC; kl++) {
+          const int k = c * kGemmKC + kl;
+          if (k >= K) break;
+          const double w = W[(size_t)n * K + k];
+          const float hi = tf32_rna_host((float)w);
+          const float lo = tf32_rna_host((float)(w - (double)hi));
+          const int off = cm_off_host(nl, kl, NT) / 4;
+          b[off] = hi;
+          b[(size_t)NT * kGemmKC + off] = lo;
+        }
+      }
+    }
+  return out;
+}
+
+void gemm_tiles(const std::vector<GemmJobDev>& jobs, std::vector<int4>& tiles) {
+  tiles.clear();
+  for (size_t j = 0; j < jobs.size(); j++)
+    for (int l0 = 0; l0 < jobs[j].lanes; l0 += kGemmLanes)
+      for (int t = 0; t < jobs[j].ntiles; t++) tiles.push_back(make_int4((int)j, l0, t, 0));
+}
+
+size_t gemm_smem_bytes(int NT) {
+  const size_t base = 32768 + (size_t)2 * NT * 128 + 16 + 2 * kGemmLanes * 8;
+  const int ncols = NT <= 32 ? 32 : NT <= 64 ? 64 : NT <= 128 ? 128 : 256;
+  // keep (resident CTAs per SM) x (tensor-memory columns) within the 512 columns
+  size_t floor_b = ncols == 256 ? 77 * 1024 : ncols == 128 ? 58 * 1024 : 0;
+  return std::max(base, floor_b);
+}
+
+cudaError_t configure_gemm_kernels() {
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(dev::k_lane_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)gemm_smem_bytes(256));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(dev::k_lane_gemm_one, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)gemm_smem_bytes(256));
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+cudaError_t launch_lane_gemm_one(const GemmJobDev& job, cudaStream_t st) {
+  const int blocks = ((job.lanes + kGemmLanes - 1) / kGemmLanes) * job.ntiles;
+  if (blocks <= 0) return cudaSuccess;
+  dev::k_lane_gemm_one<<<blocks, 128, gemm_smem_bytes(job.NT), st>>>(job);
+  return cudaGetLastError();
+}
+
+GemmJobDev make_gemm_job(const LaneSideDev& in, const LaneSideDev& out, const float* w, int K, int N, double scale,
+                         unsigned int* status) {
+  GemmJobDev j;
+  std::memset(&j, 0, sizeof j);
+  j.in = in;
+  j.out = out;
+  j.w = w;
+  j.K = K;
+  j.N = N;
+  j.NT = gemm_tile_n(N);
+  j.kchunks = (K + kGemmKC - 1) / kGemmKC;
+  j.ntiles = (N + j.NT - 1) / j.NT;
+  j.lanes = in.nf * in.rows * in.parts;
+  j.scale = scale;
+  j.status = status;
+  return j;
+}
+
+LaneSideDev lane_rows(void* const* ptrs, int nf, int rows, int len, int row_len, int type, bool complex_) {
+  LaneSideDev s;
+  std::memset(&s, 0, sizeof s);
+  for (int f = 0; f < nf; f++) s.ptr[f] = ptrs[f];
+  s.nf = nf;
+  s.rows = rows;
+  s.parts = complex_ ? 2 : 1;
+  s.type = type;
+  s.lane_stride = (long long)row_len * s.parts;
+  s.elem_stride = s.parts;
+  s.part_stride = complex_ ? 1 : 0;
+  s.len = len;
+  s.lane_fast = 0;
+  return s;
+}
+
+LaneSideDev lane_cols(void* const* ptrs, int nf, int cols, int len, int row_len, int type, int col0) {
+  LaneSideDev s;
+  std::memset(&s, 0, sizeof s);
+  const size_t es = type == LT_F64 ? 8 : 4;
+  for (int f = 0; f < nf; f++) s.ptr[f] = static_cast<char*>(ptrs[f]) + (size_t)col0 * es;
+  s.nf = nf;
+  s.rows = cols;
+  s.parts = 1;
+  s.type = type;
+  s.lane_stride = 1;
+  s.elem_stride = row_len;
+  s.part_stride = 0;
+  s.len = len;
+  s.lane_fast = 1;
+  return s;
+}
+
+cudaError_t launch_lane_gemm(const GemmJobDev* jobs, const int4* tiles, int ntiles_total, int max_nt,
+                             cudaStream_t st) {
+  if (ntiles_total <= 0) return cudaSuccess;
+  dev::k_lane_gemm<<<ntiles_total, 128, gemm_smem_bytes(max_nt), st>>>(jobs, tiles);
+  return cudaGetLastError();
+}
+
+}  // namespace rbc

@@ -84,7 +84,11 @@ FourierXformDev upload_fourier(Arena& a, int n) {
   d.n = n;
   d.M = n / 2;
   d.log2M = ilog2(d.M);
-  d.tw = reinterpret_cast<const double2*>(a.upload(twiddles(n)));
+  std::vector<double> tw = twiddles(n);
+  d.tw = reinterpret_cast<const double2*>(a.upload(tw));
+  std::vector<float> twf(tw.size());
+  for (size_t i = 0; i < tw.size(); i++) twf[i] = (float)tw[i];
+  d.twf = reinterpret_cast<const float2*>(a.upload(twf));
   return d;
 }
 
@@ -647,6 +651,72 @@ void solver_solve(const SolverDev& sv, const SpaceDev& s, const void* in_ortho, 
     add_op(f, P_DENSE);
     run_pass(f, st);
   }
+}
+
+void build_lanes(Arena& a, LanesDev& L, int kind, int n) {
+  if (kind != CHEB && kind != CD && kind != CN) throw std::runtime_error("lanes: Chebyshev-family bases only");
+  L.hb = make_basis(kind, n);
+  L.b = upload_basis(a, L.hb);
+  L.cx = upload_cheb(a, n);
+  L.has_solver = false;
+}
+
+void lanes_set_hholtz(Arena& a, LanesDev& L, double c) {
+  if (!L.hb.composite()) throw std::runtime_error("lanes: the Helmholtz solve needs a composite basis");
+  L.pinv = upload_pinv(a, L.hb.n);
+  L.adi = upload_fdma(a, {adi_factor(L.hb, c)});
+  L.has_solver = true;
+}
+
+void lane_op_lengths(const LanesDev& L, int op, int* in_len, int* out_len) {
+  const int n = L.hb.n, m = L.hb.m;
+  switch (op) {
+    case LOP_FORWARD: *in_len = n; *out_len = m; break;
+    case LOP_BACKWARD: *in_len = m; *out_len = n; break;
+    case LOP_TO_ORTHO: *in_len = m; *out_len = n; break;
+    case LOP_FROM_ORTHO: *in_len = n; *out_len = m; break;
+    case LOP_HHOLTZ: *in_len = n; *out_len = m; break;
+    default: throw std::runtime_error("lanes: unknown operation");
+  }
+}
+
+static PassDesc lanes_desc(const LanesDev& L) {
+  PassDesc d;
+  std::memset(&d, 0, sizeof d);
+  d.lmax = L.hb.n + 2;
+  d.wl = L.cx.use_fft ? std::max(2, L.cx.L) : 2;
+  d.basis = L.b;
+  d.cx = L.cx;
+  return d;
+}
+
+void lanes_apply(const LanesDev& L, int op, const double* in, double* out, int lanes, cudaStream_t st) {
+  int il, ol;
+  lane_op_lengths(L, op, &il, &ol);
+  PassDesc d = lanes_desc(L);
+  set_axis1(d, in, 0, out, 0, lanes, il, ol);
+  const bool comp = L.hb.composite();
+  switch (op) {
+    case LOP_FORWARD: add_op(d, P_DCT_FWD); if (comp) add_op(d, P_FROM_ORTHO); break;
+    case LOP_BACKWARD: if (comp) add_op(d, P_TO_ORTHO); add_op(d, P_DCT_BWD); break;
+    case LOP_TO_ORTHO: add_op(d, P_TO_ORTHO); break;
+    case LOP_FROM_ORTHO: add_op(d, P_FROM_ORTHO); break;
+    case LOP_HHOLTZ:
+      if (!L.has_solver) throw std::runtime_error("lanes: Helmholtz coefficient not set");
+      d.pinv = L.pinv; add_op(d, P_MATVEC);
+      d.fdma = L.adi; add_op(d, P_FDMA);
+      break;
+  }
+  run_pass(d, st);
+}
+
+void lanes_fdma(const LanesDev& L, double* x, int lanes, cudaStream_t st) {
+  if (!L.has_solver) throw std::runtime_error("lanes: Helmholtz coefficient not set");
+  PassDesc d = lanes_desc(L);
+  set_axis1(d, x, 0, x, 0, lanes, L.hb.m, L.hb.m);
+  d.fdma = L.adi;
+  add_op(d, P_FDMA);
+  run_pass(d, st);
 }
 
 void axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st) {

@@ -97,6 +97,26 @@ void solver_solve(const SolverDev& sv, const SpaceDev& s, const void* in_ortho, 
                   cudaStream_t st);
 size_t tmp_elems(const SpaceDev& s);
 
+// Batched 1-D operations (FP64) on `lanes` contiguous lanes of one
+// Chebyshev-family basis: forward, backward, to_ortho, from_ortho and the 1-D
+// HholtzAdi solve (hholtz_adi.rs:92-131 along one axis).
+enum LaneOp { LOP_FORWARD = 0, LOP_BACKWARD = 1, LOP_TO_ORTHO = 2, LOP_FROM_ORTHO = 3, LOP_HHOLTZ = 4 };
+struct LanesDev {
+  HostBasis hb;
+  BasisDev b;
+  ChebXformDev cx;
+  PinvDev pinv;
+  FdmaDev adi;
+  bool has_solver = false;
+};
+void build_lanes(Arena& a, LanesDev& L, int kind, int n);
+void lanes_set_hholtz(Arena& a, LanesDev& L, double c);
+// input / output lengths of an operation
+void lane_op_lengths(const LanesDev& L, int op, int* in_len, int* out_len);
+void lanes_apply(const LanesDev& L, int op, const double* in, double* out, int lanes, cudaStream_t st);
+// the banded part of the HholtzAdi solve alone: x (m per lane) solved in place
+void lanes_fdma(const LanesDev& L, double* x, int lanes, cudaStream_t st);
+
 // Elementwise helpers on device arrays of n doubles
 void axpby(double* y, const double* x, double a, double b, size_t n, cudaStream_t st);  // y = a*y + b*x
 void set_value(double* y, double v, size_t n, cudaStream_t st);

@@ -64,6 +64,7 @@ struct FourierXformDev {
   int log2M;
   int pad_;
   const double2* tw;  // exp(-2 pi i t / n), t < n
+  const float2* twf;  // the same table rounded to FP32 (mixed-precision form)
 };
 
 enum CaseKind { KIND_BOX_ADIABATIC = 0, KIND_BOX_CONDUCTING = 1, KIND_PERIODIC = 2 };
@@ -116,6 +117,19 @@ struct CaseDev {
   void* s[8];    // further scratch for the box pass sequence
   unsigned int* status;  // bit 0: non-finite value seen
   double* accum;         // reductions
+
+  // mixed-precision form (precision RBC_PREC_MIXED): the dense transforms run
+  // as tensor-core lane GEMMs, the convection products in FP32
+  int mixed;
+  int pad_m;
+  void* m_y[3];   // FP32 y-pass outputs [Y0 | Y1] per field, stored transposed: (2 ny) x mx
+  void* m_q;      // FP32 x-transformed products, transposed: 3 x (ny x kx)
+  void* m_cv;     // FP64 convection term, spectral: 3 x (kx x ky)
+  void* m_ph[8];  // box: FP32 physical fields (nx x ny)
+  void* m_p[3];   // box: FP32 products, then their x transforms
+  void* m_z;      // box: FP64 pinv_x of the divergence (mxc x ny)
+  const float* m_bcx;  // FP32 d(fieldbc)/dx, transposed: ny x nx
+  const float* m_bcy;  // FP32 d(fieldbc)/dy, transposed: ny x nx
 };
 
 }  // namespace rbc

@@ -173,6 +173,9 @@ __device__ FdmaDev stage_fdma_row(const FdmaDev& f, int row, double* dst, int ti
   return r;
 }
 
+// PRE: the convection term arrives already transformed along y (m_cv, FP64,
+// from the mixed-precision form's tensor-core GEMM) instead of q.
+template <bool PRE>
 __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
@@ -202,7 +205,13 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
   const FdmaDev fp = stage_fdma_row(c.pois_y, i, FAC + 8 * myc, tid, nth);
 
   // 1. convection: forward Chebyshev transform of Q_f[i], dealiased
-  if (i < kx) {
+  if (PRE) {
+    const double2* cv = static_cast<const double2*>(c.m_cv);
+    for (int idx = tid; idx < 3 * ny; idx += nth) {
+      int f = idx / ny, k = idx - f * ny;
+      CV[f * ld + k] = (i < kx && k < ky) ? cv[((size_t)f * kx + i) * ky + k] : c2(0.0, 0.0);
+    }
+  } else if (i < kx) {
     const double2* q = static_cast<const double2*>(c.q[0]);
     for (int idx = tid; idx < 3 * ny; idx += nth) {
       int f = idx / ny, k = idx - f * ny;
@@ -537,6 +546,29 @@ __global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ case
   for (int k = tid; k < nx; k += nth) gp[(size_t)k * ny + j] = TMP[k] * inv_asp;
 }
 
+// d/dx p0 / aspect for column j -> s[0] (nx x ny): the pressure-gradient part
+// of X1, run on its own in the mixed-precision step (FP64)
+__global__ void __launch_bounds__(256) k_box_gpx(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  const int j = w.y;
+  const int nx = c.nx, ny = c.ny;
+  const int ld = nx + 1;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const double inv_asp = 1.0 / c.aspect;
+  extern __shared__ double2 smem[];
+  double* IN = reinterpret_cast<double*>(smem);
+  double* TMP = IN + ld;
+  const double* p0 = static_cast<const double*>(c.p0);
+  for (int k = tid; k < nx; k += nth) IN[k] = p0[(size_t)k * ny + j];
+  __syncthreads();
+  cheb_diff<double>(IN, ld, TMP, ld, nx, 1, 1, TMP + ld, ld, tid, nth);
+  double* gp = static_cast<double*>(c.s[0]);
+  for (int k = tid; k < nx; k += nth) gp[(size_t)k * ny + j] = TMP[k] * inv_asp;
+}
+
+size_t smem_box_gpx(const CaseDev& c) { return 3 * (size_t)(c.nx + 1) * 8 + 64; }
+
 size_t smem_box_x1(const CaseDev& c) {
   size_t ld = c.nx + 1;
   size_t wld = c.cx.use_fft ? c.cx.L : 1;
@@ -544,6 +576,8 @@ size_t smem_box_x1(const CaseDev& c) {
 }
 
 // Y2: rows i < nx (ortho x).  conv (y forward, dealiased), rhs, pinv_y -> s[1..3]
+// PRE: the convection term arrives transformed (m_cv, from the tensor-core GEMMs).
+template <bool PRE>
 __global__ void __launch_bounds__(256) k_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
@@ -565,7 +599,13 @@ __global__ void __launch_bounds__(256) k_box_y2(const CaseDev* __restrict__ case
   const int wld = c.cy.use_fft ? c.cy.L : 1;
   double2* WB = WA + 2 * wld;
   (void)nx;
-  if (i < kx) {
+  if (PRE) {
+    const double* cv = static_cast<const double*>(c.m_cv);
+    for (int idx = tid; idx < 3 * ny; idx += nth) {
+      int f = idx / ny, k = idx - f * ny;
+      CV[f * ld + k] = (i < kx && k < ky) ? cv[((size_t)f * kx + i) * ky + k] : 0.0;
+    }
+  } else if (i < kx) {
     const double* q = static_cast<const double*>(c.q[0]);
     for (int idx = tid; idx < 3 * ny; idx += nth) {
       int f = idx / ny, k = idx - f * ny;
@@ -697,6 +737,8 @@ size_t smem_box_y3(const CaseDev& c) { return 8 * (size_t)(c.ny + 1) * 8 + 64; }
 
 // X3: columns j < ny.  div = Dx Sx A / s + Sx B  (-> s[3], nx x ny);
 // Zf = fwd * pinv_x div  (-> s[1] reused? no: s[6], mxc x ny)
+// MIX: stop after pinv_x and store it (m_z); the eigenbasis product runs as a GEMM.
+template <bool MIX>
 __global__ void __launch_bounds__(256) k_box_x3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
@@ -728,6 +770,11 @@ __global__ void __launch_bounds__(256) k_box_x3(const CaseDev* __restrict__ case
   }
   __syncthreads();
   matvec_pinv<double>(c.pinv_x, DV, ld, Z, ld, 1, tid, nth);
+  if (MIX) {
+    double* mz = static_cast<double*>(c.m_z);
+    for (int r = tid; r < mxc; r += nth) mz[(size_t)r * ny + j] = Z[r];
+    return;
+  }
   // dense eigenbasis forward along x
   double* zf = static_cast<double*>(c.s[6]);
   for (int r = tid; r < mxc; r += nth) {
@@ -764,6 +811,8 @@ size_t smem_box_y4(const CaseDev& c) { return 2 * (size_t)(c.ny + 1) * 8 + 64; }
 
 // X4: columns j < myc.  p1 = bwd * W (p1[0][0] = 0).  E = Sx+ Dx Sx^N p1 / s,
 // Fv = Sx+ Sx^N p1 (-> s[1], s[2] as mxc x myc), Gp = Sx^N p1 (-> s[0], nx x myc)
+// MIX: p1 = bwd * W was computed by a GEMM; read it (and set p1[0][0] = 0).
+template <bool MIX>
 __global__ void __launch_bounds__(256) k_box_x4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
@@ -779,17 +828,28 @@ __global__ void __launch_bounds__(256) k_box_x4(const CaseDev* __restrict__ case
   double* D = OR + ld;        // 2 lanes: Dx OR / s, OR copy
   double* FO = D + 2 * ld;    // 2 lanes from_ortho
   double* TMP = FO + 2 * ld;  // 2 lanes
-  const double* wv = static_cast<const double*>(c.s[7]);
-  for (int k = tid; k < mxc; k += nth) W[k] = wv[(size_t)k * myc + j];
-  __syncthreads();
   double* p1 = static_cast<double*>(c.p1);
-  for (int r = tid; r < mxc; r += nth) {
-    const double* row = c.pois_bwd + (size_t)r * mxc;
-    double acc = 0.0;
-    for (int k = 0; k < mxc; k++) acc = fma(__ldg(row + k), W[k], acc);
-    if (j == 0 && r == 0) acc = 0.0;
-    PV[r] = acc;
-    p1[(size_t)r * myc + j] = acc;
+  if (MIX) {
+    for (int r = tid; r < mxc; r += nth) {
+      double v = p1[(size_t)r * myc + j];
+      if (j == 0 && r == 0) {
+        v = 0.0;
+        p1[0] = 0.0;
+      }
+      PV[r] = v;
+    }
+  } else {
+    const double* wv = static_cast<const double*>(c.s[7]);
+    for (int k = tid; k < mxc; k += nth) W[k] = wv[(size_t)k * myc + j];
+    __syncthreads();
+    for (int r = tid; r < mxc; r += nth) {
+      const double* row = c.pois_bwd + (size_t)r * mxc;
+      double acc = 0.0;
+      for (int k = 0; k < mxc; k++) acc = fma(__ldg(row + k), W[k], acc);
+      if (j == 0 && r == 0) acc = 0.0;
+      PV[r] = acc;
+      p1[(size_t)r * myc + j] = acc;
+    }
   }
   __syncthreads();
   to_ortho<double>(c.xp, PV, ld, OR, ld, 1, tid, nth);
@@ -887,16 +947,21 @@ cudaError_t configure_step_kernels() {
   SET_ATTR(dev::k_y1<double>);
   SET_ATTR(dev::k_y1<double2>);
   SET_ATTR(dev::k_per_x);
-  SET_ATTR(dev::k_per_y2);
+  SET_ATTR(dev::k_per_y2<false>);
+  SET_ATTR(dev::k_per_y2<true>);
   SET_ATTR(dev::k_per_y2a);
   SET_ATTR(dev::k_per_y2b);
   SET_ATTR(dev::k_box_x1);
-  SET_ATTR(dev::k_box_y2);
+  SET_ATTR(dev::k_box_y2<false>);
+  SET_ATTR(dev::k_box_y2<true>);
   SET_ATTR(dev::k_box_x2);
+  SET_ATTR(dev::k_box_gpx);
   SET_ATTR(dev::k_box_y3);
-  SET_ATTR(dev::k_box_x3);
+  SET_ATTR(dev::k_box_x3<false>);
+  SET_ATTR(dev::k_box_x3<true>);
   SET_ATTR(dev::k_box_y4);
-  SET_ATTR(dev::k_box_x4);
+  SET_ATTR(dev::k_box_x4<false>);
+  SET_ATTR(dev::k_box_x4<true>);
   SET_ATTR(dev::k_box_y5);
 #undef SET_ATTR
   done = true;
@@ -941,18 +1006,23 @@ cudaError_t launch_step_kernel(int kernel, int nblocks, size_t smem, cudaStream_
     case K_Y1_C: dev::k_y1<double2><<<g, b, smem, s>>>(cases, work); break;
     case K_Y1_R: dev::k_y1<double><<<g, b, smem, s>>>(cases, work); break;
     case K_PER_X: dev::k_per_x<<<g, b, smem, s>>>(cases, work); break;
-    case K_PER_Y2: dev::k_per_y2<<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_Y2: dev::k_per_y2<false><<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_Y2_PRE: dev::k_per_y2<true><<<g, b, smem, s>>>(cases, work); break;
     case K_PER_Y2A: dev::k_per_y2a<<<g, b, smem, s>>>(cases, work); break;
     case K_PER_Y2B: dev::k_per_y2b<<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X1: dev::k_box_x1<<<g, b, smem, s>>>(cases, work); break;
-    case K_BOX_Y2: dev::k_box_y2<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y2: dev::k_box_y2<false><<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y2_PRE: dev::k_box_y2<true><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X2: dev::k_box_x2<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_GPX: dev::k_box_gpx<<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_Y3: dev::k_box_y3<<<g, b, smem, s>>>(cases, work); break;
-    case K_BOX_X3: dev::k_box_x3<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X3: dev::k_box_x3<false><<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X3_MIX: dev::k_box_x3<true><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_Y4: dev::k_box_y4<<<g, b, smem, s>>>(cases, work); break;
-    case K_BOX_X4: dev::k_box_x4<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X4: dev::k_box_x4<false><<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_X4_MIX: dev::k_box_x4<true><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_Y5: dev::k_box_y5<<<g, b, smem, s>>>(cases, work); break;
-    default: return cudaErrorInvalidValue;
+    default: return launch_mixed_kernel(kernel, nblocks, smem, s, cases, work);
   }
   return cudaGetLastError();
 }

@@ -4,6 +4,7 @@
 
 #include <vector>
 
+#include "lane_gemm.h"
 #include "rbc_dev.h"
 
 namespace rbc {
@@ -12,13 +13,17 @@ enum StepKernel {
   K_Y1_C = 0, K_Y1_R, K_PER_X, K_PER_Y2,
   K_BOX_X1, K_BOX_Y2, K_BOX_X2, K_BOX_Y3, K_BOX_X3, K_BOX_Y4, K_BOX_X4, K_BOX_Y5,
   K_PER_Y2A, K_PER_Y2B,
-  K_NUM_STEP_KERNELS
+  // mixed-precision form
+  K_PER_Y2_PRE, K_PER_X_MIXED, K_BOX_PROD_MIXED, K_BOX_Y2_PRE, K_BOX_X3_MIX, K_BOX_X4_MIX, K_BOX_GPX,
+  K_NUM_STEP_KERNELS,
+  K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };
 
 struct StepLaunch {
   int kernel;
   size_t smem;
-  std::vector<int4> items;  // (case index, first lane, lane count, 0)
+  std::vector<int4> items;       // (case index, first lane, lane count, 0)
+  std::vector<GemmJobDev> jobs;  // K_GEMM only
 };
 
 struct StepPlan {
@@ -27,6 +32,27 @@ struct StepPlan {
 
 cudaError_t configure_step_kernels();
 StepPlan build_step_plan(const CaseDev& c);
+
+// Operators of the mixed-precision step (packed tensor-core operands, device).
+struct MixedOps {
+  const float* y1 = nullptr;  // [B S ; B D S] along y: (2 ny) x (ny - 2)
+  const float* y2 = nullptr;  // forward Chebyshev along y, rows < ky: ky x ny
+  // box only, along x (aspect ratio folded into the derivative rows)
+  const float* xa = nullptr;  // [B S_u ; B D S_u / s] : (2 nx) x (nx - 2)
+  const float* xb = nullptr;  // B S_u : nx x (nx - 2)
+  const float* xc = nullptr;  // B D S_t / s : nx x (nx - 2)
+  const float* xd = nullptr;  // B S_t : nx x (nx - 2)
+  const float* x2 = nullptr;  // forward Chebyshev along x, rows < kx: kx x nx
+  const float* pf = nullptr;  // Poisson eigenbasis forward: (nx - 2) x (nx - 2)
+  const float* pb = nullptr;  // Poisson eigenbasis backward: (nx - 2) x (nx - 2)
+};
+StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops);
+const char* step_kernel_name(int kernel);
+// algorithmic HBM bytes of one launch (cases: host copies indexed by item case)
+double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases);
+cudaError_t configure_mixed_kernels();
+cudaError_t launch_mixed_kernel(int kernel, int nblocks, size_t smem, cudaStream_t s, const CaseDev* cases,
+                                const int4* work);
 cudaError_t launch_step_kernel(int kernel, int nblocks, size_t smem, cudaStream_t s, const CaseDev* cases,
                                const int4* work);
 
@@ -36,7 +62,9 @@ size_t smem_per_x(const CaseDev& c);
 size_t smem_per_y2(const CaseDev& c);
 size_t smem_per_y2a(const CaseDev& c);
 size_t smem_per_y2b(const CaseDev& c);
+size_t smem_per_x_mixed(const CaseDev& c);
 size_t smem_box_x1(const CaseDev& c);
+size_t smem_box_gpx(const CaseDev& c);
 size_t smem_box_y2(const CaseDev& c);
 size_t smem_box_x2(const CaseDev& c);
 size_t smem_box_y3(const CaseDev& c);
