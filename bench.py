@@ -197,7 +197,7 @@ def run_ensemble(args, rank, world, local):
     from rustpde_gb300.ensemble import draw_ensemble
     build.build()
     cu = Cudart()
-    params = draw_ensemble(ENSEMBLE_N, ENSEMBLE_SEED)
+    params = draw_ensemble(args.cases, ENSEMBLE_SEED)
     gp = sum(p[0] * p[1] for p in params)
     flush = R.DeviceArray((256 * 1024 * 1024 // 8,))
     W, K = args.warmup, args.steps
@@ -246,6 +246,10 @@ def run_ensemble(args, rank, world, local):
         B.get_state_all(host.array)
     e2e_s = time.perf_counter() - t0
     del B
+
+    if args.skip_plain:  # profiling runs: the batched mixed step only
+        return {"metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "steps": K, "warmup": W,
+                "cases": len(params), "mode": "batched mixed only", "kernels_ms_per_step": {k: v[0] for k, v in prof.items()}}
 
     # ---- plain FP64, case by case, same ensemble and initial fields
     plain_ms = 0.0
@@ -307,6 +311,7 @@ def run_ensemble(args, rank, world, local):
         "status_nonzero_cases": int(sum(1 for s in status if s)),
     }
     if rank == 0 and world == 1:
+        line["serving"] = run_serving(args, args.requests, args.horizon_scale)
         line["cpu_baseline"] = cpu_baseline_ensemble(params, budget_s=args.cpu_budget)
     return line
 
@@ -333,6 +338,65 @@ def cpu_baseline_ensemble(params, budget_s=15.0, steps_per_case=2):
     return {"value": done_gp / t_acc, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
             "sample": f"first {ncase} ensemble cases x {steps_per_case} steps after 1 warm-up step each "
                       f"({t_acc:.1f} s timed)"}
+
+
+# ---------------------------------------------------------------------------
+# serving: Poisson arrivals of solve requests, continuous batching
+# ---------------------------------------------------------------------------
+def run_serving(args, n_requests, horizon_scale, n_check=12):
+    """Requests of rustpde_gb300.ensemble.draw_requests (50/s, seed 7, 5 %
+    512x257) with horizons scaled by `horizon_scale`, submitted at their
+    arrival times to the serving loop (mixed precision, 150 GB budget).
+    Returns p50/p99 completion latency, aggregate throughput, and the Nu/KE
+    deviation of the first `n_check` results from the same cases run alone in
+    FP64."""
+    import numpy as np
+
+    import rustpde_gb300 as R
+    from rustpde_gb300.ensemble import draw_requests
+    reqs = draw_requests(n_requests, rate=50.0, seed=7)
+    srv = R.Server(hbm_budget_bytes=150 * 10**9, max_active=256, chunk_steps=8,
+                   setup_threads=max(1, min(8, (os.cpu_count() or 2) // 2)))
+    t0 = time.perf_counter()
+    ids = {}
+    for rq in reqs:
+        wait = rq.arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        rid = srv.submit(rq.params + (R.PREC_MIXED,), rq.horizon * horizon_scale, rq.seed)
+        ids[rid] = rq
+    ok = srv.wait_idle(1800.0)
+    res = srv.poll(len(reqs) + 8)
+    st = srv.stats()
+    srv.close()
+    lat = np.array([r["t_done"] - r["t_submit"] for r in res])
+    setup = np.array([r["t_admit"] - r["t_submit"] for r in res])
+    gp_steps = sum(r["grid_points"] * r["steps"] for r in res)
+    span = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
+    errs_nu, errs_ke = [], []
+    for r in sorted(res, key=lambda r: r["id"])[:n_check]:
+        rq = ids[r["id"]]
+        c = R.Navier2D(*rq.params, precision=R.PREC_FP64, seed=None)
+        c.set_velocity(0.2, 1.0, 1.0)
+        c.set_temperature_noise(1e-3, rq.seed)
+        c.update(r["steps"])
+        for lst, what, v in ((errs_nu, R.NU, r["nu"]), (errs_ke, R.KE, r["ke"])):
+            ref = c.eval(what)
+            lst.append(abs(v - ref) / max(abs(ref), 1e-300))
+        del c
+    return {
+        "requests": len(reqs), "completed": len(res), "idle": ok,
+        "failed": int(sum(1 for r in res if r["status"] != 0)),
+        "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
+        "p50_queue_and_setup_s": float(np.percentile(setup, 50)),
+        "aggregate_grid_pt_steps_per_s": gp_steps / span, "span_s": span,
+        "steps_launched": st["steps_launched"], "graph_rebuilds": st["rebuilds"],
+        "nu_max_rel_vs_fp64": float(max(errs_nu)), "ke_max_rel_vs_fp64": float(max(errs_ke)),
+        "checked": len(errs_nu),
+        "workload": (f"{n_requests} requests, Poisson 50/s (seed 7), sizes as the ensemble + 512x257 at 5 %, "
+                     f"horizon U[1,20] time units x {horizon_scale} (scaled so the run fits in minutes), "
+                     "mixed precision, 150 GB budget, max 256 active, 8 steps per round"),
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -441,7 +505,7 @@ def run_reference(args, rank, world):
         config = {"workload": WORKLOAD_512, "nx": NX, "ny": NY}
     else:
         from rustpde_gb300.ensemble import draw_ensemble
-        cases = draw_ensemble(ENSEMBLE_N, ENSEMBLE_SEED)
+        cases = draw_ensemble(args.cases, ENSEMBLE_SEED)
         config = {"workload": WORKLOAD_ENS.replace("batched mixed precision", "case by case, FP64"),
                   "cases": len(cases)}
     # one timed "step" advances every sampled case once; the sample is the
@@ -489,8 +553,13 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "periodic512"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "periodic512", "serving"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
+    ap.add_argument("--skip-plain", action="store_true",
+                    help="time the batched mixed step only (profiling runs; prints a reduced line)")
+    ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
+    ap.add_argument("--horizon-scale", type=float, default=0.01, help="serving: horizon multiplier")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 50 if args.workload == "ensemble" else 200
@@ -502,6 +571,10 @@ def main():
         dist.init_process_group("gloo")
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.workload == "serving":
+        from rustpde_gb300 import build
+        build.build()
+        line = {"metric": METRIC, "workload": "serving", **run_serving(args, args.requests, args.horizon_scale)}
     else:
         args.warmup = max(args.warmup, 3)
         line = (run_ensemble if args.workload == "ensemble" else run_periodic512)(args, rank, world, local)

@@ -173,6 +173,55 @@ int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
 int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes);
 int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes);
 
+/* ---- serving loop ------------------------------------------------------------
+ * No reference counterpart (the reference runs one Navier2D per process).  A
+ * request is one RBC solve: the case of `params` from the standard initial
+ * fields (set_velocity(0.2, 1, 1) and seeded temperature noise 1e-3, see
+ * rbc_set_temperature_noise) to `horizon` time units, i.e. round(horizon/dt)
+ * steps.  Set-up threads build requested cases (operators, factorisations,
+ * boundary field, initial fields) while memory is reserved within the budget;
+ * a scheduler thread admits built cases while slots (max_active) allow, keeps
+ * every admitted case's state and
+ * factorised operators on the device, and advances all of them together in
+ * batched steps (continuous batching: requests that arrive while others run
+ * join at the next chunk of chunk_steps steps).  Each finished request yields
+ * a result (Nu, KE at its horizon, timestamps on the server clock).  A case
+ * computes exactly the same numbers alone or in any mix. */
+typedef struct RbcServer RbcServer;
+typedef struct RbcServerConfig {
+  size_t hbm_budget_bytes; /* admission budget for the cases' device memory */
+  int max_active;          /* cases advanced together at most */
+  int chunk_steps;         /* steps launched per scheduling round */
+  int setup_threads;       /* host threads building admitted cases */
+} RbcServerConfig;
+typedef struct RbcRequestResult {
+  long long id;
+  int status;      /* RBC_OK, RBC_ERR_NUMERIC (non-finite state) or RBC_ERR_NOMEM (never fits) */
+  int steps;       /* steps advanced */
+  double sim_time; /* simulated time reached */
+  double t_submit, t_admit, t_done; /* server clock, seconds */
+  double nu, ke;   /* eval_nu and kinetic energy at the horizon */
+  long long grid_points;
+} RbcRequestResult;
+typedef struct RbcServerStats {
+  double now;      /* server clock, seconds */
+  int pending, active;
+  long long completed;
+  size_t bytes_in_use;
+  double grid_point_steps; /* advanced so far */
+  long long steps_launched, rebuilds;
+} RbcServerStats;
+int rbc_server_create(const RbcServerConfig* cfg, RbcServer** out);
+/* params->precision selects the form of the case (RBC_PREC_FP64 / RBC_PREC_MIXED) */
+int rbc_server_submit(RbcServer* s, const RbcParams* params, double horizon, uint64_t seed, long long* id);
+/* completed results (at most max_results, *n of them; non-blocking) */
+int rbc_server_poll(RbcServer* s, RbcRequestResult* out, int max_results, int* n);
+/* wait until nothing is pending or running (or timeout); *idle = 1 when idle */
+int rbc_server_wait_idle(RbcServer* s, double timeout_s, int* idle);
+int rbc_server_stats(RbcServer* s, RbcServerStats* stats);
+/* stops the scheduler; unfinished requests are dropped */
+int rbc_server_destroy(RbcServer* s);
+
 /* ---- device memory helpers (callers that do not link the CUDA runtime) ---- */
 int rbc_host_alloc_pinned(void** ptr, size_t bytes);
 int rbc_host_free_pinned(void* ptr);

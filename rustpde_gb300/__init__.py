@@ -62,6 +62,25 @@ _IP = ctypes.POINTER(ctypes.c_int)
 _SZ = ctypes.c_size_t
 CALLBACK = ctypes.CFUNCTYPE(ctypes.c_int, _P, _D, _P)
 
+class RbcServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int), ("chunk_steps", ctypes.c_int),
+                ("setup_threads", ctypes.c_int)]
+
+
+class RbcRequestResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_longlong), ("status", ctypes.c_int), ("steps", ctypes.c_int),
+                ("sim_time", ctypes.c_double), ("t_submit", ctypes.c_double), ("t_admit", ctypes.c_double),
+                ("t_done", ctypes.c_double), ("nu", ctypes.c_double), ("ke", ctypes.c_double),
+                ("grid_points", ctypes.c_longlong)]
+
+
+class RbcServerStats(ctypes.Structure):
+    _fields_ = [("now", ctypes.c_double), ("pending", ctypes.c_int), ("active", ctypes.c_int),
+                ("completed", ctypes.c_longlong), ("bytes_in_use", ctypes.c_size_t),
+                ("grid_point_steps", ctypes.c_double), ("steps_launched", ctypes.c_longlong),
+                ("rebuilds", ctypes.c_longlong)]
+
+
 _SIGNATURES = {
     "rbc_last_error": (ctypes.c_char_p, []),
     "rbc_version": (ctypes.c_char_p, []),
@@ -99,6 +118,12 @@ _SIGNATURES = {
     "rbc_batch_layout": (_I, [_P, _IP, _IP]),
     "rbc_batch_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "rbc_batch_state_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
+    "rbc_server_create": (_I, [ctypes.POINTER(RbcServerConfig), ctypes.POINTER(_P)]),
+    "rbc_server_submit": (_I, [_P, ctypes.POINTER(RbcParams), _D, ctypes.c_uint64, ctypes.POINTER(ctypes.c_longlong)]),
+    "rbc_server_poll": (_I, [_P, ctypes.POINTER(RbcRequestResult), _I, _IP]),
+    "rbc_server_wait_idle": (_I, [_P, _D, _IP]),
+    "rbc_server_stats": (_I, [_P, ctypes.POINTER(RbcServerStats)]),
+    "rbc_server_destroy": (_I, [_P]),
     "rbc_batch_profile_step": (_I, [_P, _I, _DP, _DP, _IP, _I, _IP]),
     "rbc_stage_bytes": (_I, [_P, _I, _DP]),
     "rbc_kernel_name": (ctypes.c_char_p, [_I]),
@@ -682,6 +707,58 @@ class Batch:
                 c._h = None
             _lib.rbc_batch_destroy(h)
             self._h = None
+
+
+class Server:
+    """Serving loop (rbc_server_*): requests are RBC solves (params, horizon
+    in time units, initial-condition seed) admitted against a device-memory
+    budget and advanced together with continuous batching."""
+
+    def __init__(self, hbm_budget_bytes=150 * 10**9, max_active=256, chunk_steps=8, setup_threads=4):
+        cfg = RbcServerConfig(int(hbm_budget_bytes), int(max_active), int(chunk_steps), int(setup_threads))
+        h = _P()
+        _check(lib().rbc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    def submit(self, params, horizon, seed, precision=PREC_FP64):
+        nx, ny, ra, pr, dt, asp, kind = params[:7]
+        prec = params[7] if len(params) > 7 else precision
+        p = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(asp), int(kind), int(prec))
+        rid = ctypes.c_longlong()
+        _check(lib().rbc_server_submit(self._h, ctypes.byref(p), float(horizon), int(seed), ctypes.byref(rid)))
+        return rid.value
+
+    def poll(self, max_results=1024):
+        buf = (RbcRequestResult * max_results)()
+        n = _I()
+        _check(lib().rbc_server_poll(self._h, buf, max_results, ctypes.byref(n)))
+        out = []
+        for k in range(n.value):
+            r = buf[k]
+            out.append({f: getattr(r, f) for f, _ in RbcRequestResult._fields_})
+        return out
+
+    def wait_idle(self, timeout=60.0):
+        idle = _I()
+        _check(lib().rbc_server_wait_idle(self._h, float(timeout), ctypes.byref(idle)))
+        return bool(idle.value)
+
+    def stats(self):
+        st = RbcServerStats()
+        _check(lib().rbc_server_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in RbcServerStats._fields_}
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _check(_lib.rbc_server_destroy(h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def integrate(pde: Navier2D, max_time: float, save_intervall=None, callback=None):

@@ -165,6 +165,7 @@ struct RbcCase {
   double time = 0.0;
   bool own_stream = true;
   bool in_batch = false;
+  int* gate_mem = nullptr;  // device int[2] used by the serving loop (CaseDev::gate)
   ~RbcCase() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
@@ -404,6 +405,7 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   h.bc_dx = bdx;
   h.bc_dy = bdy;
   h.status = static_cast<unsigned int*>(A.alloc(16));
+  c->gate_mem = static_cast<int*>(A.alloc(16));
   h.accum = static_cast<double*>(A.alloc(64));
   // generic scratch
   size_t te = 0;
@@ -426,7 +428,9 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     c->d_wx = A.upload(wx);
     c->d_wy = A.upload(wy);
   }
-  cuda_check(cudaDeviceSynchronize(), "allocation");
+  // the arena's zero fills ran on the legacy stream (or were synchronised by a
+  // stream-ordered arena); wait for them without waiting for other streams
+  cuda_check(cudaStreamSynchronize(cudaStreamLegacy), "allocation");
   c->d_case = static_cast<CaseDev*>(A.alloc(sizeof(CaseDev)));
   cuda_check(cudaMemcpy(c->d_case, &h, sizeof(CaseDev), cudaMemcpyHostToDevice), "copy case descriptor");
 
@@ -515,6 +519,21 @@ void apply_mode(RbcCase* c, int field, double amp, double m, double n, bool sin_
       v[i * y.size() + j] = sin_cos ? amp * std::sin(ax * xs[i]) * std::cos(ay * ys[j])
                                     : amp * std::cos(ax * xs[i]) * std::sin(ay * ys[j]);
   set_phys(c, field, v);
+}
+
+// temperature = amp*(2u-1) at interior collocation points, 0 on the walls,
+// u from splitmix64(seed) drawn in row-major order
+void set_temperature_noise(RbcCase* c, double amp, uint64_t seed) {
+  int nx = c->p.nx, ny = c->p.ny;
+  std::vector<double> v((size_t)nx * ny);
+  uint64_t s = seed;
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      double u = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
+      bool wall = (j == 0 || j == ny - 1) || (!c->periodic && (i == 0 || i == nx - 1));
+      v[(size_t)i * ny + j] = wall ? 0.0 : amp * (2.0 * u - 1.0);
+    }
+  set_phys(c, RBC_TEMP, v);
 }
 
 double eval_case(RbcCase* c, int what) {
@@ -657,16 +676,7 @@ int rbc_set_temperature(RbcCase* c, double amp, double m, double n) {
 int rbc_set_temperature_noise(RbcCase* c, double amp, uint64_t seed) {
   API_BEGIN
   require(c != nullptr, "null case");
-  int nx = c->p.nx, ny = c->p.ny;
-  std::vector<double> v((size_t)nx * ny);
-  uint64_t s = seed;
-  for (int i = 0; i < nx; i++)
-    for (int j = 0; j < ny; j++) {
-      double u = (double)(splitmix64(s) >> 11) * (1.0 / 9007199254740992.0);
-      bool wall = (j == 0 || j == ny - 1) || (!c->periodic && (i == 0 || i == nx - 1));
-      v[(size_t)i * ny + j] = wall ? 0.0 : amp * (2.0 * u - 1.0);
-    }
-  set_phys(c, RBC_TEMP, v);
+  set_temperature_noise(c, amp, seed);
   API_END
 }
 
@@ -1400,6 +1410,459 @@ int sv_solve(SvSolver* sv, const double* d_in, double* d_out, void* stream) {
   API_BEGIN
   require(sv && d_in && d_out, "null argument");
   solver_solve(sv->sv, sv->space->s, d_in, d_out, sv->space->tmp, (cudaStream_t)stream);
+  API_END
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Serving loop (rbc_server_*): continuous batching of RBC solve requests.
+//
+// A scheduler thread owns the GPU work.  Each round it (1) admits pending
+// requests whose case fits the HBM budget (host set-up on a separate stream,
+// so it overlaps the steps in flight), (2) when the set of active cases has
+// changed, rebuilds the batched step -- buckets of equal (kind, nx, ny,
+// precision), a gate kernel per bucket, the bucket's launches, all captured
+// into one CUDA graph -- and (3) launches `chunk_steps` graph steps.  The gate
+// kernel counts each case's remaining steps down on the device and idles the
+// case once it has reached its horizon, so cases of different horizons share
+// a chunk and every case stops exactly at its own step count.  Finished cases
+// are evaluated (Nu, KE), their memory returned to the pool and their results
+// queued for rbc_server_poll.  A case computes the same numbers alone or in
+// any mix: no kernel or tile combines data of two cases.
+// ============================================================================
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+
+struct RbcServer {
+  RbcServerConfig cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;  // steps
+  std::vector<cudaStream_t> branch;
+  std::vector<cudaEvent_t> bev;
+  cudaEvent_t fork = nullptr, chunk_done = nullptr;
+  std::thread th;
+  std::vector<std::thread> workers;
+  std::mutex mu;
+  std::condition_variable cv;
+  bool stop = false;
+  bool failed = false;
+  std::string error;
+  struct Req {
+    long long id;
+    RbcParams p;
+    double horizon;
+    uint64_t seed;
+    double t_submit;
+    long steps;
+  };
+  struct Slot {
+    Req r;
+    RbcCase* c;
+    long left;
+    double t_admit;
+    size_t bytes;
+  };
+  std::deque<Req> pending;      // submitted, not yet taken by a set-up worker
+  std::deque<Slot> ready;       // built, initial fields set, waiting for a slot
+  std::vector<Slot> active;     // advancing
+  std::deque<RbcRequestResult> done;
+  int building = 0;
+  long long next_id = 0;
+  size_t bytes_in_use = 0;      // building (reserved), ready and active cases
+  double gp_steps = 0;
+  long long steps_launched = 0, rebuilds = 0, completed = 0;
+  std::chrono::steady_clock::time_point t0;
+  // batched step of the current active set
+  std::unique_ptr<Arena> plan_arena;
+  struct Bucket {
+    std::vector<int> members;
+    StepPlan plan;
+    DevPlan dp;
+    int* d_members = nullptr;
+  };
+  std::vector<Bucket> buckets;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  bool dirty = true;
+  double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+};
+
+// Upper bound of a case's device bytes (reserved against the budget while the
+// case is built; the actual arena size replaces it afterwards).
+static size_t case_bytes_bound(const RbcParams& p) {
+  const size_t n = (size_t)(p.nx + 2) * (size_t)(p.ny + 2);
+  size_t b = n * 8 * 160;                       // fields, scratch and tables
+  if (p.kind != RBC_PERIODIC) b += (size_t)p.nx * p.nx * 8 * 16;  // eigenbases and dense x operators
+  if (p.precision == RBC_PREC_MIXED) b += ((size_t)p.nx * p.nx + (size_t)p.ny * p.ny) * 4 * 24;
+  return b + (4u << 20);
+}
+
+static void server_free_graph(RbcServer* S) {
+  if (S->gexec) cudaGraphExecDestroy(S->gexec);
+  if (S->graph) cudaGraphDestroy(S->graph);
+  S->gexec = nullptr;
+  S->graph = nullptr;
+}
+
+// Set-up worker: builds the case of the next pending request on its own
+// stream (host arithmetic, allocations from the stream-ordered pool, boundary
+// field, initial fields) while the scheduler keeps stepping.
+static void server_worker(RbcServer* S) {
+  cudaStream_t st = nullptr;
+  try {
+    cuda_check(cudaSetDevice(S->device), "set device");
+    cuda_check(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream");
+    for (;;) {
+      RbcServer::Req r;
+      size_t reserve = 0;
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        for (;;) {
+          if (S->stop || S->failed) {
+            cudaStreamDestroy(st);
+            return;
+          }
+          if (!S->pending.empty()) {
+            reserve = case_bytes_bound(S->pending.front().p);
+            const bool alone = S->bytes_in_use == 0;
+            if (alone || S->bytes_in_use + reserve <= S->cfg.hbm_budget_bytes) break;
+          }
+          S->cv.wait_for(lk, std::chrono::milliseconds(2));
+        }
+        r = S->pending.front();
+        S->pending.pop_front();
+        S->bytes_in_use += reserve;
+        S->building++;
+      }
+      std::unique_ptr<RbcCase> c(new RbcCase());
+      c->p = r.p;
+      c->periodic = r.p.kind == RBC_PERIODIC;
+      c->stream = st;
+      c->own_stream = false;
+      c->in_batch = true;  // stepped by the server only
+      c->arena.set_stream_ordered(true);
+      bool fits = true;
+      try {
+        build_case(c.get(), false);
+        fits = c->arena.bytes() <= S->cfg.hbm_budget_bytes;
+        if (fits) {
+          // initial fields: set_velocity(0.2, 1, 1) and seeded temperature noise 1e-3
+          apply_mode(c.get(), RBC_UX, 0.2, 1.0, 1.0, true);
+          apply_mode(c.get(), RBC_UY, -0.2, 1.0, 1.0, false);
+          set_temperature_noise(c.get(), 1e-3, r.seed);
+          const int g[2] = {(int)r.steps, 0};
+          cuda_check(cudaMemcpyAsync(c->gate_mem, g, sizeof g, cudaMemcpyHostToDevice, st), "gate");
+          cuda_check(cudaStreamSynchronize(st), "setup synchronize");
+        }
+      } catch (std::exception& e) {
+        // an allocation that fails is an answer for this request, not for the loop
+        if (std::string(e.what()).find("cudaMalloc") == std::string::npos) throw;
+        fits = false;
+      }
+      const size_t bytes = c->arena.bytes();
+      std::lock_guard<std::mutex> lk(S->mu);
+      S->building--;
+      S->bytes_in_use -= reserve;
+      if (!fits) {
+        RbcRequestResult res{};
+        res.id = r.id;
+        res.status = RBC_ERR_NOMEM;
+        res.t_submit = r.t_submit;
+        res.t_admit = res.t_done = S->now();
+        res.grid_points = (long long)r.p.nx * r.p.ny;
+        S->done.push_back(res);
+        S->completed++;
+        c.reset();
+      } else {
+        S->bytes_in_use += bytes;
+        c->stream = S->stream;
+        S->ready.push_back(RbcServer::Slot{r, c.release(), r.steps, 0.0, bytes});
+      }
+      S->cv.notify_all();
+    }
+  } catch (std::exception& e) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->failed = true;
+    S->error = e.what();
+    S->cv.notify_all();
+  }
+  if (st) cudaStreamDestroy(st);
+}
+
+// Move built cases into free slots.
+static void server_admit(RbcServer* S) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  while (!S->ready.empty() && (int)S->active.size() < S->cfg.max_active) {
+    RbcServer::Slot sl = S->ready.front();
+    S->ready.pop_front();
+    sl.t_admit = S->now();
+    S->active.push_back(sl);
+    S->dirty = true;
+  }
+}
+
+// Batched step of the active set: buckets, gate kernels, one CUDA graph.
+static void server_rebuild(RbcServer* S) {
+  server_free_graph(S);
+  S->buckets.clear();
+  S->plan_arena.reset(new Arena());
+  S->plan_arena->set_stream_ordered(true);
+  Arena& A = *S->plan_arena;
+  std::vector<CaseDev> hd;
+  for (auto& sl : S->active) {
+    CaseDev d = sl.c->hd;
+    d.gate = sl.c->gate_mem;
+    hd.push_back(d);
+  }
+  CaseDev* d_cases = A.upload(hd);
+  for (int i = 0; i < (int)S->active.size(); i++) {
+    const RbcParams& p = S->active[i].r.p;
+    int found = -1;
+    for (size_t k = 0; k < S->buckets.size(); k++) {
+      const RbcParams& q = S->active[S->buckets[k].members[0]].r.p;
+      if ((q.kind == RBC_PERIODIC) == (p.kind == RBC_PERIODIC) && q.nx == p.nx && q.ny == p.ny &&
+          q.precision == p.precision)
+        found = (int)k;
+    }
+    if (found < 0) {
+      S->buckets.emplace_back();
+      found = (int)S->buckets.size() - 1;
+    }
+    S->buckets[found].members.push_back(i);
+  }
+  for (auto& bk : S->buckets) {
+    bk.plan = S->active[bk.members[0]].c->plan;
+    for (size_t li = 0; li < bk.plan.launches.size(); li++) {
+      StepLaunch& L = bk.plan.launches[li];
+      if (L.kernel == K_GEMM) {
+        L.jobs.clear();
+        for (int m : bk.members)
+          for (GemmJobDev j : S->active[m].c->plan.launches[li].jobs) {
+            j.active = S->active[m].c->gate_mem + 1;
+            L.jobs.push_back(j);
+          }
+        continue;
+      }
+      std::vector<int4> items;
+      const std::vector<int4>& proto = S->active[bk.members[0]].c->plan.launches[li].items;
+      for (const int4& it : proto)
+        for (int m : bk.members) items.push_back(make_int4(m, it.y, it.z, it.w));
+      L.items = items;
+    }
+    upload_plan(A, bk.plan, bk.dp);
+    bk.d_members = A.upload(bk.members);
+  }
+  const size_t nb = S->buckets.size();
+  while (S->branch.size() < nb) {
+    cudaStream_t s;
+    cudaEvent_t e;
+    cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+    cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+    S->branch.push_back(s);
+    S->bev.push_back(e);
+  }
+  cuda_check(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  cudaError_t le = cudaEventRecord(S->fork, S->stream);
+  for (size_t k = 0; k < nb && le == cudaSuccess; k++) {
+    auto& bk = S->buckets[k];
+    cudaStream_t s = S->branch[k];
+    le = cudaStreamWaitEvent(s, S->fork, 0);
+    if (le == cudaSuccess) le = launch_gate(d_cases, bk.d_members, (int)bk.members.size(), s);
+    for (size_t li = 0; li < bk.plan.launches.size() && le == cudaSuccess; li++)
+      le = launch_entry(bk.plan.launches[li], bk.dp, li, s, d_cases);
+    if (le == cudaSuccess) le = cudaEventRecord(S->bev[k], s);
+    if (le == cudaSuccess) le = cudaStreamWaitEvent(S->stream, S->bev[k], 0);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(S->stream, &g);
+  cuda_check(le, "server capture");
+  cuda_check(ce, "end capture");
+  S->graph = g;
+  cuda_check(cudaGraphInstantiate(&S->gexec, g, 0), "graph instantiate");
+  S->rebuilds++;
+  S->dirty = false;
+}
+
+static void server_finish(RbcServer* S) {
+  for (int i = (int)S->active.size() - 1; i >= 0; i--) {
+    RbcServer::Slot& sl = S->active[i];
+    if (sl.left > 0) continue;
+    RbcRequestResult res{};
+    res.id = sl.r.id;
+    res.steps = (int)sl.r.steps;
+    res.sim_time = sl.c->time;
+    res.t_submit = sl.r.t_submit;
+    res.t_admit = sl.t_admit;
+    unsigned int st = 0;
+    cuda_check(cudaMemcpy(&st, sl.c->hd.status, sizeof st, cudaMemcpyDeviceToHost), "status");
+    res.status = st == 0 ? RBC_OK : ((st & 1u) ? RBC_ERR_NUMERIC : RBC_ERR_CUDA);
+    res.nu = eval_case(sl.c, RBC_NU);
+    res.ke = eval_case(sl.c, RBC_KE);
+    res.t_done = S->now();
+    res.grid_points = sl.r.p.nx * sl.r.p.ny;
+    delete sl.c;
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->bytes_in_use -= sl.bytes;
+    S->active.erase(S->active.begin() + i);
+    S->dirty = true;
+    S->done.push_back(res);
+    S->completed++;
+  }
+  S->cv.notify_all();
+}
+
+static void server_main(RbcServer* S) {
+  try {
+    cuda_check(cudaSetDevice(S->device), "set device");
+    for (;;) {
+      server_admit(S);
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        if (S->stop || S->failed) break;
+        if (S->active.empty()) {
+          S->cv.notify_all();
+          S->cv.wait_for(lk, std::chrono::milliseconds(1), [&] { return S->stop || !S->ready.empty(); });
+          continue;
+        }
+      }
+      if (S->dirty) server_rebuild(S);
+      const int n = S->cfg.chunk_steps;
+      for (int k = 0; k < n; k++) cuda_check(cudaGraphLaunch(S->gexec, S->stream), "graph launch");
+      cuda_check(cudaEventRecord(S->chunk_done, S->stream), "event record");
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        for (auto& sl : S->active) {
+          const long applied = std::min<long>(n, sl.left);
+          sl.left -= applied;
+          sl.c->time += applied * sl.r.p.dt;
+          S->gp_steps += (double)applied * sl.r.p.nx * sl.r.p.ny;
+        }
+        S->steps_launched += n;
+      }
+      cuda_check(cudaEventSynchronize(S->chunk_done), "chunk");
+      server_finish(S);
+    }
+  } catch (std::exception& e) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->failed = true;
+    S->error = e.what();
+  }
+  S->cv.notify_all();
+}
+
+extern "C" {
+
+int rbc_server_create(const RbcServerConfig* cfg, RbcServer** out) {
+  API_BEGIN
+  require(cfg && out, "null argument");
+  *out = nullptr;
+  require(cfg->max_active > 0 && cfg->chunk_steps > 0 && cfg->hbm_budget_bytes > 0,
+          "rbc_server_create: max_active, chunk_steps and hbm_budget_bytes must be positive");
+  require(cfg->setup_threads > 0 && cfg->setup_threads <= 64, "rbc_server_create: setup_threads must be in [1, 64]");
+  cuda_check(configure_prim_kernels(), "configure kernels");
+  cuda_check(configure_step_kernels(), "configure step kernels");
+  cuda_check(configure_mixed_kernels(), "configure mixed kernels");
+  std::unique_ptr<RbcServer> S(new RbcServer());
+  S->cfg = *cfg;
+  cuda_check(cudaGetDevice(&S->device), "get device");
+  cuda_check(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking), "stream");
+  cuda_check(cudaEventCreateWithFlags(&S->fork, cudaEventDisableTiming), "event");
+  cuda_check(cudaEventCreateWithFlags(&S->chunk_done, cudaEventDisableTiming), "event");
+  S->t0 = std::chrono::steady_clock::now();
+  RbcServer* raw = S.get();
+  S->th = std::thread([raw] { server_main(raw); });
+  for (int k = 0; k < cfg->setup_threads; k++) S->workers.emplace_back([raw] { server_worker(raw); });
+  *out = S.release();
+  API_END
+}
+
+int rbc_server_submit(RbcServer* S, const RbcParams* p, double horizon, uint64_t seed, long long* id) {
+  API_BEGIN
+  require(S && p && id, "null argument");
+  validate_params(*p);
+  require(std::isfinite(horizon) && horizon > 0, "rbc_server_submit: horizon must be positive");
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (S->failed) throw ApiError(RBC_ERR_CUDA, "server stopped: " + S->error);
+  RbcServer::Req r;
+  r.id = S->next_id++;
+  r.p = *p;
+  r.horizon = horizon;
+  r.seed = seed;
+  r.t_submit = S->now();
+  r.steps = std::max<long>(1, std::lround(horizon / p->dt));
+  S->pending.push_back(r);
+  *id = r.id;
+  S->cv.notify_all();
+  API_END
+}
+
+int rbc_server_poll(RbcServer* S, RbcRequestResult* out, int max_results, int* n) {
+  API_BEGIN
+  require(S && n && (out || max_results == 0), "null argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  int k = 0;
+  while (k < max_results && !S->done.empty()) {
+    out[k++] = S->done.front();
+    S->done.pop_front();
+  }
+  *n = k;
+  if (S->failed && k == 0) throw ApiError(RBC_ERR_CUDA, "server stopped: " + S->error);
+  API_END
+}
+
+int rbc_server_wait_idle(RbcServer* S, double timeout_s, int* idle) {
+  API_BEGIN
+  require(S && idle, "null argument");
+  std::unique_lock<std::mutex> lk(S->mu);
+  auto quiet = [&] { return S->pending.empty() && S->ready.empty() && S->active.empty() && S->building == 0; };
+  S->cv.wait_for(lk, std::chrono::duration<double>(std::max(0.0, timeout_s)), [&] { return S->failed || quiet(); });
+  if (S->failed) throw ApiError(RBC_ERR_CUDA, "server stopped: " + S->error);
+  *idle = quiet() ? 1 : 0;
+  API_END
+}
+
+int rbc_server_stats(RbcServer* S, RbcServerStats* st) {
+  API_BEGIN
+  require(S && st, "null argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  st->now = S->now();
+  st->pending = (int)(S->pending.size() + S->ready.size()) + S->building;
+  st->active = (int)S->active.size();
+  st->completed = S->completed;
+  st->bytes_in_use = S->bytes_in_use;
+  st->grid_point_steps = S->gp_steps;
+  st->steps_launched = S->steps_launched;
+  st->rebuilds = S->rebuilds;
+  API_END
+}
+
+int rbc_server_destroy(RbcServer* S) {
+  API_BEGIN
+  if (!S) return RBC_OK;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cv.notify_all();
+  if (S->th.joinable()) S->th.join();
+  for (auto& w : S->workers)
+    if (w.joinable()) w.join();
+  cudaStreamSynchronize(S->stream);
+  server_free_graph(S);
+  for (auto& sl : S->active) delete sl.c;
+  for (auto& sl : S->ready) delete sl.c;
+  S->active.clear();
+  S->ready.clear();
+  S->plan_arena.reset();
+  for (auto s : S->branch) cudaStreamDestroy(s);
+  for (auto e : S->bev) cudaEventDestroy(e);
+  cudaEventDestroy(S->fork);
+  cudaEventDestroy(S->chunk_done);
+  cudaStreamDestroy(S->stream);
+  delete S;
   API_END
 }
 

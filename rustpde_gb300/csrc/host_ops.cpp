@@ -3,6 +3,9 @@
 // roundings as the reference's (non-fused) products.
 #include "host_ops.h"
 
+#include <map>
+#include <mutex>
+
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -427,7 +430,23 @@ static double cospi_frac(long jk, int N) {
   return (double)cosl(PI_L * (long double)t / (long double)N);
 }
 
-std::vector<double> cheb_dense_forward(int n) {
+static std::vector<double> cheb_dense_forward_impl(int n);
+static std::vector<double> cheb_dense_backward_impl(int n);
+
+// The dense transform matrices depend on n only: computed once per size.
+static std::vector<double> cheb_dense_cached(int n, bool fwd) {
+  static std::mutex mu;
+  static std::map<std::pair<int, bool>, std::vector<double>> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  auto key = std::make_pair(n, fwd);
+  auto it = cache.find(key);
+  if (it == cache.end()) it = cache.emplace(key, fwd ? cheb_dense_forward_impl(n) : cheb_dense_backward_impl(n)).first;
+  return it->second;
+}
+std::vector<double> cheb_dense_forward(int n) { return cheb_dense_cached(n, true); }
+std::vector<double> cheb_dense_backward(int n) { return cheb_dense_cached(n, false); }
+
+static std::vector<double> cheb_dense_forward_impl(int n) {
   int N = n - 1;
   std::vector<double> M((size_t)n * n);
   for (int k = 0; k < n; k++) {
@@ -441,7 +460,7 @@ std::vector<double> cheb_dense_forward(int n) {
   return M;
 }
 
-std::vector<double> cheb_dense_backward(int n) {
+static std::vector<double> cheb_dense_backward_impl(int n) {
   int N = n - 1;
   std::vector<double> M((size_t)n * n);
   for (int j = 0; j < n; j++)

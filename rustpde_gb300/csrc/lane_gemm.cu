@@ -95,15 +95,85 @@ __device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
 
 constexpr long kWaitLimit = 1L << 22;  // try_wait polls before a completion wait is declared lost
 
-__device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, const int tile_n) {
+__device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// bounded wait for completion phase `parity` of the MMA barrier; true when
+// every thread of the CTA saw it complete
+__device__ __forceinline__ bool mma_wait(uint64_t* mbar, uint32_t parity) {
+  bool done = false;
+  for (long i = 0; i < kWaitLimit && !done; i++) done = mbar_try(mbar, parity);
+  return __syncthreads_and(done) != 0;
+}
+
+// Input chunk of a tile held in registers between its global loads and its
+// conversion: item (lane l, quad kq) -> 4 consecutive k of one lane.
+template <class T>
+struct AChunk {
+  T v[8][4];
+};
+
+template <class T>
+__device__ __forceinline__ void a_load(AChunk<T>& a, const GemmJobDev& J, const char* const* ib, int k0, int tid) {
+  const long long es = J.in.elem_stride;
+#pragma unroll
+  for (int it = 0; it < 8; it++) {
+    const int q = tid + 128 * it;
+    const int llo = q & 7, r = q >> 3;
+    const int l = J.in.lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
+    const int kq = J.in.lane_fast ? r >> 4 : r & 7;
+    const T* base = reinterpret_cast<const T*>(ib[l]);
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+      const int k = k0 + kq * 4 + e;
+      a.v[it][e] = (base != nullptr && k < J.K) ? __ldg(base + (long long)k * es) : T(0);
+    }
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void a_store(const AChunk<T>& a, const GemmJobDev& J, unsigned char* Ahi,
+                                        unsigned char* Alo, int tid) {
+#pragma unroll
+  for (int it = 0; it < 8; it++) {
+    const int q = tid + 128 * it;
+    const int llo = q & 7, r = q >> 3;
+    const int l = J.in.lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
+    const int kq = J.in.lane_fast ? r >> 4 : r & 7;
+    float4 hi, lo;
+    float x;
+    // lo is rounded to TF32 here: left to the tensor core it would be
+    // truncated, a bias that accumulates along K
+    x = (float)a.v[it][0]; hi.x = tf32_rna(x); lo.x = tf32_rna(x - hi.x);
+    x = (float)a.v[it][1]; hi.y = tf32_rna(x); lo.y = tf32_rna(x - hi.y);
+    x = (float)a.v[it][2]; hi.z = tf32_rna(x); lo.z = tf32_rna(x - hi.z);
+    x = (float)a.v[it][3]; hi.w = tf32_rna(x); lo.w = tf32_rna(x - hi.w);
+    const int off = cm_off(l, kq * 4, kGemmLanes);
+    *reinterpret_cast<float4*>(Ahi + off) = hi;
+    *reinterpret_cast<float4*>(Alo + off) = lo;
+  }
+}
+
+// issue the asynchronous copy of operator chunk c (hi block then lo block)
+__device__ __forceinline__ void w_issue(const float* wsrc, int c, int NT, unsigned char* wbuf, int tid) {
+  const char* g = reinterpret_cast<const char*>(wsrc + (size_t)c * 2 * NT * kGemmKC);
+  const uint32_t sb = smem_u32(wbuf);
+  for (int i = tid; i < NT * 16; i += 128) cp_async16(sb + i * 16, g + (size_t)i * 16);
+}
+
+template <class T>
+__device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0, const int tile_n) {
   const int NT = J.NT;
   const int tid = threadIdx.x, warp = tid >> 5, wl = tid & 31;
   extern __shared__ __align__(128) unsigned char sm[];
+  // A chunk (hi, lo) | operator chunk buffers 0 and 1 (hi, lo each) | tail
   unsigned char* Ahi = sm;
   unsigned char* Alo = sm + 16384;
-  unsigned char* Whi = sm + 32768;
-  unsigned char* Wlo = Whi + NT * 128;
-  unsigned char* tail = Wlo + NT * 128;
+  unsigned char* Wb[2] = {sm + 32768, sm + 32768 + 2 * NT * 128};
+  unsigned char* tail = sm + 32768 + 4 * NT * 128;
   uint64_t* mbar = reinterpret_cast<uint64_t*>(tail);
   uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 8);
   const char** ib = reinterpret_cast<const char**>(tail + 16);
@@ -121,6 +191,9 @@ __device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, 
     ib[tid] = ip;
     ob[tid] = op;
   }
+  const float* wsrc = J.w + (size_t)tile_n * J.kchunks * 2 * NT * kGemmKC;
+  w_issue(wsrc, 0, NT, Wb[0], tid);  // operator chunk 0 in flight during the set-up
+  cp_async_commit();
   const uint32_t ncols = NT <= 32 ? 32u : NT <= 64 ? 64u : NT <= 128 ? 128u : 256u;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
@@ -135,50 +208,28 @@ __device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, 
   // instruction descriptor: D f32, A/B tf32, K-major both, N = NT, M = 128
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NT >> 3) << 17) | ((128u >> 4) << 24);
   const uint32_t a_lbo = (kGemmLanes / 8) * 128, w_lbo = (uint32_t)(NT / 8) * 128;
-  const float* wsrc = J.w + (size_t)tile_n * J.kchunks * 2 * NT * kGemmKC;
-  const long long ies = J.in.elem_stride;
-  const int itype = J.in.type;
   bool ok = true;
+  AChunk<T> a;
+  a_load<T>(a, J, ib, 0, tid);
 
   for (int c = 0; c < J.kchunks; c++) {
-    const int k0 = c * kGemmKC;
-    // --- A chunk: item (lane l, quad kq) -> 4 consecutive k of one lane
-#pragma unroll 2
-    for (int it = 0; it < 8; it++) {
-      const int q = tid + 128 * it;
-      const int llo = q & 7, r = q >> 3;
-      int l, kq;
-      if (J.in.lane_fast) { l = (r & 15) * 8 + llo; kq = r >> 4; }
-      else { l = (r >> 3) * 8 + llo; kq = r & 7; }
-      const char* base = ib[l];
-      float v[4];
-#pragma unroll
-      for (int e = 0; e < 4; e++) {
-        const int k = k0 + kq * 4 + e;
-        v[e] = (base != nullptr && k < J.K) ? load_elem(base, (long long)k * ies, itype) : 0.0f;
-      }
-      float4 hi, lo;
-      // lo is rounded to TF32 here: left to the tensor core it would be
-      // truncated, a bias that accumulates along K
-      hi.x = tf32_rna(v[0]); lo.x = tf32_rna(v[0] - hi.x);
-      hi.y = tf32_rna(v[1]); lo.y = tf32_rna(v[1] - hi.y);
-      hi.z = tf32_rna(v[2]); lo.z = tf32_rna(v[2] - hi.z);
-      hi.w = tf32_rna(v[3]); lo.w = tf32_rna(v[3] - hi.w);
-      const int off = cm_off(l, kq * 4, kGemmLanes);
-      *reinterpret_cast<float4*>(Ahi + off) = hi;
-      *reinterpret_cast<float4*>(Alo + off) = lo;
+    // the A buffer and operator buffer (c+1)&1 were read by MMA c-1
+    if (c > 0) {
+      ok = mma_wait(mbar, (uint32_t)((c - 1) & 1));
+      tc_fence_after();
+      if (!ok) break;
     }
-    // --- W chunk (hi block then lo block, already in operand order)
-    {
-      const uint4* ws = reinterpret_cast<const uint4*>(wsrc + (size_t)c * 2 * NT * kGemmKC);
-      uint4* wd = reinterpret_cast<uint4*>(Whi);
-      for (int i = tid; i < NT * 16; i += 128) wd[i] = __ldg(ws + i);
-    }
+    a_store<T>(a, J, Ahi, Alo, tid);
+    if (c + 1 < J.kchunks) w_issue(wsrc, c + 1, NT, Wb[(c + 1) & 1], tid);
+    cp_async_commit();
+    cp_async_wait1();  // operator chunk c has landed (this thread's copies)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     if (tid == 0) {
+      unsigned char* Whi = Wb[c & 1];
+      unsigned char* Wlo = Whi + NT * 128;
 #pragma unroll
       for (int s = 0; s < kGemmKC / 8; s++) {
         const uint64_t ah = umma_desc(smem_u32(Ahi) + s * 2 * a_lbo, a_lbo, 128);
@@ -193,12 +244,14 @@ __device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, 
                        smem_u32(mbar))
                    : "memory");
     }
-    bool done = false;
-    for (long i = 0; i < kWaitLimit && !done; i++) done = mbar_try(mbar, (uint32_t)(c & 1));
-    ok = __syncthreads_and(done) != 0;
-    tc_fence_after();
-    if (!ok) break;
+    // next input chunk in flight while the tensor core works
+    if (c + 1 < J.kchunks) a_load<T>(a, J, ib, (c + 1) * kGemmKC, tid);
   }
+  if (ok) {
+    ok = mma_wait(mbar, (uint32_t)((J.kchunks - 1) & 1));
+    tc_fence_after();
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
 
   if (ok) {
     const int P = J.out.parts;
@@ -240,6 +293,12 @@ __device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, 
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
+__device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, const int tile_n) {
+  if (J.active != nullptr && *J.active == 0) return;
+  if (J.in.type == LT_F64) gemm_tile_t<double>(J, lane0, tile_n);
+  else gemm_tile_t<float>(J, lane0, tile_n);
+}
+
 // grouped form: tile table entries (job, first lane, output tile, 0)
 __global__ void __launch_bounds__(128) k_lane_gemm(const GemmJobDev* __restrict__ jobs, const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
@@ -258,9 +317,11 @@ __global__ void __launch_bounds__(128) k_lane_gemm_one(const __grid_constant__ G
 // host side
 // ---------------------------------------------------------------------------
 int gemm_tile_n(int N) {
+  // at most 128 outputs per tile: two operator buffers of 32 KB and two CTAs
+  // per SM; wider outputs are split into equal tiles
   auto r16 = [](int v) { return (v + 15) & ~15; };
-  if (N <= 256) return r16(N);
-  int t = (N + 255) / 256;
+  if (N <= 128) return r16(N);
+  int t = (N + 127) / 128;
   return r16((N + t - 1) / t);
 }
 
@@ -310,10 +371,14 @@ void gemm_tiles(const std::vector<GemmJobDev>& jobs, std::vector<int4>& tiles) {
 }
 
 size_t gemm_smem_bytes(int NT) {
-  const size_t base = 32768 + (size_t)2 * NT * 128 + 16 + 2 * kGemmLanes * 8;
-  const int ncols = NT <= 32 ? 32 : NT <= 64 ? 64 : NT <= 128 ? 128 : 256;
-  // keep (resident CTAs per SM) x (tensor-memory columns) within the 512 columns
-  size_t floor_b = ncols == 256 ? 77 * 1024 : ncols == 128 ? 58 * 1024 : 0;
+  // A chunk (hi, lo) + two operator chunks (hi, lo) + barrier, tmem slot, lane bases
+  const size_t base = 32768 + (size_t)4 * NT * 128 + 16 + 2 * kGemmLanes * 8;
+  const size_t ncols = NT <= 32 ? 32 : NT <= 64 ? 64 : NT <= 128 ? 128 : 256;
+  // keep (resident CTAs per SM) x (tensor-memory columns) within the 512
+  // columns: at most 512 / ncols CTAs fit, so ask for enough shared memory
+  // (of the 228 KB per SM, 1 KB reserved per CTA) that no more become resident
+  const size_t max_ctas = 512 / ncols;
+  const size_t floor_b = (228 * 1024) / (max_ctas + 1) - 1024 + 1;
   return std::max(base, floor_b);
 }
 

@@ -37,6 +37,7 @@ struct GemmJobDev {
   LaneSideDev in, out;
   const float* w;  // split operand packed by pack_gemm_w
   unsigned int* status;  // receives kStatusGemmTimeout
+  const int* active;     // when set and 0, the job's tiles do nothing (serving gate)
   double scale;
   int K, N;
   int NT;       // output columns per tile (multiple of 16, <= 256)

@@ -6,21 +6,64 @@
 #include "lane_ops.cuh"
 #include "prims.h"
 
+#include <map>
+#include <mutex>
+#include <tuple>
+
 namespace rbc {
 
 // ---------------------------------------------------------------- arena
+// library-owned stream of the stream-ordered arenas, one per device
+static cudaStream_t pool_stream() {
+  static std::mutex mu;
+  static std::map<int, cudaStream_t> streams;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = streams.find(dev);
+  if (it != streams.end()) return it->second;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+    throw std::runtime_error("cudaStreamCreate failed");
+  // keep freed blocks in the pool for the next cases instead of returning them
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  streams[dev] = s;
+  return s;
+}
+
 Arena::~Arena() {
-  for (void* p : ptrs_) cudaFree(p);
+  if (ordered_) {
+    cudaStream_t s = pool_stream();
+    for (void* p : ptrs_) cudaFreeAsync(p, s);
+  } else {
+    for (void* p : ptrs_) cudaFree(p);
+  }
 }
 void* Arena::alloc(size_t bytes) {
   if (bytes == 0) bytes = 16;
   void* p = nullptr;
-  cudaError_t e = cudaMalloc(&p, bytes);
-  if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
-  e = cudaMemset(p, 0, bytes);
-  if (e != cudaSuccess) {
-    cudaFree(p);
-    throw std::runtime_error(std::string("cudaMemset failed: ") + cudaGetErrorString(e));
+  if (ordered_) {
+    cudaStream_t s = pool_stream();
+    cudaError_t e = cudaMallocAsync(&p, bytes, s);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    e = cudaMemsetAsync(p, 0, bytes, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);  // usable from any stream once this returns
+    if (e != cudaSuccess) {
+      cudaFreeAsync(p, s);
+      throw std::runtime_error(std::string("cudaMemset failed: ") + cudaGetErrorString(e));
+    }
+  } else {
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    e = cudaMemset(p, 0, bytes);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      throw std::runtime_error(std::string("cudaMemset failed: ") + cudaGetErrorString(e));
+    }
   }
   ptrs_.push_back(p);
   bytes_ += bytes;
@@ -195,24 +238,48 @@ std::vector<Band4> hholtz_rows(const HostBasis& bx, const HostBasis& by, double 
     }
   } else {
     if (!bx.composite() || bx.bc()) throw std::runtime_error("tensor solver: axis 0 must be composite or Fourier");
-    Band4 Ax, Bx;
-    hholtz_ingredients(bx, Ax, Bx);
-    int m = bx.m;
-    std::vector<double> a0 = band_dense(Bx), c0 = band_dense(Ax);
-    for (double& e : a0) e = poisson ? e * cx : (-1.0 * e) * cx;
-    std::vector<double> cinv;
-    if (!invert(m, c0, cinv)) throw std::runtime_error("tensor solver: singular mass matrix");
-    std::vector<double> xmat = matmul(m, m, m, cinv, a0);
-    std::vector<double> Q;
-    std::string e2;
-    if (!eig_real(m, xmat, lam, Q, &e2)) {
-      if (err) *err = e2;
-      throw std::runtime_error(e2);
+    // The eigen-decomposition of inv(C) (s B) with s = +1 (Poisson) or -1
+    // (Hholtz) depends on the basis and size only; the scale cx > 0 of the
+    // reference's matrix multiplies the eigenvalues and leaves the
+    // eigenvectors unchanged, so it is applied afterwards and the O(n^3)
+    // decomposition is computed once per (basis, size, sign) and shared.
+    struct Eig {
+      std::vector<double> lam, fwd, bwd;
+    };
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, bool>, Eig> cache;
+    const auto key = std::make_tuple(bx.kind, bx.n, poisson);
+    const Eig* E = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      auto it = cache.find(key);
+      if (it != cache.end()) E = &it->second;
     }
-    std::vector<double> P;
-    if (!invert(m, Q, P)) throw std::runtime_error("tensor solver: eigenvector matrix is singular");
-    if (fwd) *fwd = matmul(m, m, m, P, cinv);
-    if (bwd) *bwd = Q;
+    if (E == nullptr) {
+      Band4 Ax, Bx;
+      hholtz_ingredients(bx, Ax, Bx);
+      int m = bx.m;
+      std::vector<double> a0 = band_dense(Bx), c0 = band_dense(Ax);
+      for (double& e : a0) e = poisson ? e : (-1.0 * e);
+      std::vector<double> cinv;
+      if (!invert(m, c0, cinv)) throw std::runtime_error("tensor solver: singular mass matrix");
+      std::vector<double> xmat = matmul(m, m, m, cinv, a0);
+      Eig ne;
+      std::string e2;
+      if (!eig_real(m, xmat, ne.lam, ne.bwd, &e2)) {
+        if (err) *err = e2;
+        throw std::runtime_error(e2);
+      }
+      std::vector<double> P;
+      if (!invert(m, ne.bwd, P)) throw std::runtime_error("tensor solver: eigenvector matrix is singular");
+      ne.fwd = matmul(m, m, m, P, cinv);
+      std::lock_guard<std::mutex> lk(mu);
+      E = &cache.emplace(key, std::move(ne)).first->second;
+    }
+    lam = E->lam;
+    for (double& l : lam) l *= cx;
+    if (fwd) *fwd = E->fwd;
+    if (bwd) *bwd = E->bwd;
   }
   if (poisson && std::fabs(lam[0]) < 1e-10) {  // poisson.rs:80-83
     for (double& l : lam) l -= 1e-10;

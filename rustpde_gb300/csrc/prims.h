@@ -16,13 +16,19 @@
 
 namespace rbc {
 
-// Owner of device allocations (freed on destruction).
+// Owner of device allocations (freed on destruction).  By default blocks come
+// from cudaMalloc (whose free waits for the device).  A stream-ordered arena
+// takes them from the device's memory pool (cudaMallocAsync / cudaFreeAsync on
+// a library-owned stream): allocating and freeing never waits for other
+// streams, so a serving loop can build and retire cases while steps run.  Its
+// owner must make sure no work still uses the memory when it is destroyed.
 class Arena {
  public:
   Arena() = default;
   Arena(const Arena&) = delete;
   Arena& operator=(const Arena&) = delete;
   ~Arena();
+  void set_stream_ordered(bool on) { ordered_ = on; }
   void* alloc(size_t bytes);  // zero-initialised; throws std::runtime_error on failure
   template <class T> T* upload(const std::vector<T>& v) {
     if (v.empty()) return nullptr;
@@ -36,6 +42,7 @@ class Arena {
   void copy_h2d(void* d, const void* h, size_t n);
   std::vector<void*> ptrs_;
   size_t bytes_ = 0;
+  bool ordered_ = false;
 };
 
 void cuda_check(cudaError_t e, const char* what);  // throws std::runtime_error

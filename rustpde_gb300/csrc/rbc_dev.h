@@ -117,6 +117,11 @@ struct CaseDev {
   void* s[8];    // further scratch for the box pass sequence
   unsigned int* status;  // bit 0: non-finite value seen
   double* accum;         // reductions
+  // serving: gate[0] = steps left, gate[1] = 1 when the case advances in the
+  // current step (set by the gate kernel at the start of each step); null
+  // outside the serving loop (always advance)
+  int* gate;
+  int pad_g;
 
   // mixed-precision form (precision RBC_PREC_MIXED): the dense transforms run
   // as tensor-core lane GEMMs, the convection products in FP32

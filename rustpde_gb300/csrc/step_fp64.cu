@@ -39,6 +39,7 @@ template <class T>
 __global__ void __launch_bounds__(256) k_y1(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int r0 = w.y, nr = w.z;
   const int ny = c.ny, myc = c.myc, ld = c.ny + 1;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -103,6 +104,7 @@ size_t smem_y1(const CaseDev& c, int nr, bool cplx) {
 __global__ void __launch_bounds__(256) k_per_x(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int mx = c.mx, nx = c.nx, ny = c.ny, M = c.fx.M;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -179,6 +181,7 @@ template <bool PRE>
 __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y;
   const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
   const int ld = ny + 1;
@@ -314,6 +317,7 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
 __global__ void __launch_bounds__(256) k_per_y2a(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y, f = w.w;
   const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
   const int ld = ny + 1;
@@ -407,6 +411,7 @@ size_t smem_per_y2a(const CaseDev& c) {
 __global__ void __launch_bounds__(256) k_per_y2b(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y;
   const int ny = c.ny, myc = c.myc;
   const int ld = ny + 1;
@@ -484,6 +489,7 @@ size_t smem_per_y2(const CaseDev& c) {
 __global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int nx = c.nx, ny = c.ny, mxc = c.mxc, kx = c.kx;
   const int ld = nx + 1;
@@ -551,6 +557,7 @@ __global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ case
 __global__ void __launch_bounds__(256) k_box_gpx(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int nx = c.nx, ny = c.ny;
   const int ld = nx + 1;
@@ -581,6 +588,7 @@ template <bool PRE>
 __global__ void __launch_bounds__(256) k_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y;
   const int nx = c.nx, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, mxc = c.mxc;
   const int ld = ny + 1;
@@ -669,6 +677,7 @@ size_t smem_box_y2(const CaseDev& c) {
 __global__ void __launch_bounds__(256) k_box_x2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int nx = c.nx, myc = c.myc, mxc = c.mxc;
   const int ld = nx + 1;
@@ -696,6 +705,7 @@ size_t smem_box_x2(const CaseDev& c) { return 6 * (size_t)(c.nx + 1) * 8 + 64; }
 __global__ void __launch_bounds__(256) k_box_y3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y;
   const int ny = c.ny, myc = c.myc;
   const int ld = ny + 1;
@@ -742,6 +752,7 @@ template <bool MIX>
 __global__ void __launch_bounds__(256) k_box_x3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int nx = c.nx, ny = c.ny, mxc = c.mxc;
   const int ld = nx + 1;
@@ -791,6 +802,7 @@ size_t smem_box_x3(const CaseDev& c) { return 8 * (size_t)(c.nx + 1) * 8 + 64; }
 __global__ void __launch_bounds__(256) k_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y;
   const int ny = c.ny, myc = c.myc;
   const int ld = ny + 1;
@@ -816,6 +828,7 @@ template <bool MIX>
 __global__ void __launch_bounds__(256) k_box_x4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int nx = c.nx, myc = c.myc, mxc = c.mxc;
   const int ld = nx + 1;
@@ -877,6 +890,7 @@ size_t smem_box_x4(const CaseDev& c) { return 9 * (size_t)(c.nx + 1) * 8 + 64; }
 __global__ void __launch_bounds__(256) k_box_y5(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int i = w.y;
   const int ny = c.ny, myc = c.myc, mxc = c.mxc;
   const int ld = ny + 1;

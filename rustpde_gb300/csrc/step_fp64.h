@@ -48,6 +48,8 @@ struct MixedOps {
 };
 StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops);
 const char* step_kernel_name(int kernel);
+// serving gate of the cases members[0..n) of `cases` (see CaseDev::gate)
+cudaError_t launch_gate(const CaseDev* cases, const int* members, int n, cudaStream_t s);
 // algorithmic HBM bytes of one launch (cases: host copies indexed by item case)
 double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases);
 cudaError_t configure_mixed_kernels();

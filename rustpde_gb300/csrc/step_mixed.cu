@@ -31,6 +31,7 @@ namespace dev {
 __global__ void __launch_bounds__(256) k_per_x_mixed(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   const int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int j = w.y;
   const int mx = c.mx, nx = c.nx, ny = c.ny, M = c.fx.M, kx = c.kx;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -82,6 +83,7 @@ __global__ void __launch_bounds__(256) k_box_prod_mixed(const CaseDev* __restric
                                                         const int4* __restrict__ work) {
   const int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // case idle this step (serving)
   const int n = w.y, nx = c.nx;
   const float* pu = static_cast<const float*>(c.m_ph[0]) + (size_t)n * 2 * nx;
   const float* pv = static_cast<const float*>(c.m_ph[1]) + (size_t)n * 2 * nx;
@@ -101,6 +103,18 @@ __global__ void __launch_bounds__(256) k_box_prod_mixed(const CaseDev* __restric
     p1[x] = u * dxv + v * dyv[x];
     p2[x] = u * dxt[x] + v * dyt[x] + u * bx[x] + v * by[x];
   }
+}
+
+// Serving gate: for each member case decide whether it advances in this step
+// (steps left > 0) and count the step down.
+__global__ void k_gate(const CaseDev* __restrict__ cases, const int* __restrict__ members, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int* g = cases[members[i]].gate;
+  if (g == nullptr) return;
+  const int run = g[0] > 0 ? 1 : 0;
+  g[1] = run;
+  g[0] -= run;
 }
 
 size_t smem_per_x_mixed(const CaseDev& c) {
@@ -312,6 +326,12 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
     b += v * lanes;
   }
   return b;
+}
+
+cudaError_t launch_gate(const CaseDev* cases, const int* members, int n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  dev::k_gate<<<(n + 127) / 128, 128, 0, s>>>(cases, members, n);
+  return cudaGetLastError();
 }
 
 const char* step_kernel_name(int kernel) {

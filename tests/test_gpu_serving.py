@@ -1,0 +1,80 @@
+"""Serving loop (rbc_server_*): continuous batching of RBC solve requests.
+
+* every request's result (Nu and KE at its horizon) is the same when it is
+  served alone and when it shares the device with other requests that arrive
+  while it runs (tolerance 0: no kernel combines data of two cases);
+* the results equal the same case stepped on its own through rbc_step;
+* requests that can never fit the memory budget fail with RBC_ERR_NOMEM
+  without stopping the loop.
+"""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 0.0
+
+
+@pytest.fixture(scope="module")
+def R():
+    from rustpde_gb300 import build
+    build.build()
+    import rustpde_gb300
+    return rustpde_gb300
+
+
+REQS = [  # (params, horizon, seed)
+    ((64, 64, 1e5, 1.0, 0.02, 1.0, 0), 0.3, 11),
+    ((64, 33, 1e5, 1.0, 0.005, 1.0, 2), 0.06, 12),
+    ((128, 64, 1e6, 0.7, 2e-3, 1.5, 2), 0.05, 13),
+    ((48, 40, 1e6, 7.0, 5e-3, 1.2, 1), 0.11, 14),
+    ((64, 64, 1e5, 1.0, 0.02, 1.0, 0, 1), 0.3, 15),      # mixed precision
+    ((128, 65, 1e6, 1.0, 4e-3, 2.0, 2, 1), 0.07, 16),     # mixed precision
+]
+
+
+def serve(R, reqs, stagger=0.0):
+    srv = R.Server(hbm_budget_bytes=8 * 10**9, max_active=8, chunk_steps=4)
+    ids = []
+    for p, h, seed in reqs:
+        ids.append(srv.submit(p, h, seed))
+        if stagger:
+            time.sleep(stagger)
+    assert srv.wait_idle(120.0)
+    res = {r["id"]: r for r in srv.poll()}
+    st = srv.stats()
+    srv.close()
+    return [res[i] for i in ids], st
+
+
+def test_alone_equals_in_mix(R):
+    mixed, st = serve(R, REQS, stagger=0.01)
+    assert st["rebuilds"] >= 2  # the active set changed while cases were running
+    for k, req in enumerate(REQS):
+        alone, _ = serve(R, [req])
+        a, b = alone[0], mixed[k]
+        assert a["status"] == 0 and b["status"] == 0
+        assert a["steps"] == b["steps"] == max(1, round(req[1] / req[0][4]))
+        for key in ("nu", "ke", "sim_time"):
+            assert abs(a[key] - b[key]) <= TOL * abs(a[key]), (k, key, a[key], b[key])
+
+
+def test_served_equals_single_case(R):
+    res, _ = serve(R, REQS[:4])
+    for (p, h, seed), r in zip(REQS[:4], res):
+        c = R.Navier2D(*p[:7], precision=p[7] if len(p) > 7 else R.PREC_FP64, seed=None)
+        c.set_velocity(0.2, 1.0, 1.0)
+        c.set_temperature_noise(1e-3, seed)
+        c.update(r["steps"])
+        assert c.eval(R.NU) == r["nu"] and c.eval(R.KE) == r["ke"]
+
+
+def test_budget_rejection(R):
+    srv = R.Server(hbm_budget_bytes=1 << 20, max_active=4, chunk_steps=2)
+    rid = srv.submit((64, 64, 1e5, 1.0, 0.02, 1.0, 0), 0.1, 1)
+    assert srv.wait_idle(60.0)
+    out = srv.poll()
+    srv.close()
+    assert len(out) == 1 and out[0]["id"] == rid and out[0]["status"] == -5
