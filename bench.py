@@ -298,6 +298,8 @@ def run_ensemble(args, rank, world, local):
         "speedup_vs_plain_fp64": value / plain_value,
         "mixed_error": {"steps": W + K, "nu_max_rel": float(err_nu.max()), "nu_median_rel": float(np.median(err_nu)),
                         "ke_max_rel": float(err_ke.max()), "ke_median_rel": float(np.median(err_ke)),
+                        "worst_ke_cases": [{"case": int(i), "params": list(params[i]), "ke_rel": float(err_ke[i])}
+                                           for i in np.argsort(err_ke)[::-1][:3]],
                         "against": "the plain FP64 GPU path (parity with the FP64 oracle <= 1e-9)"},
         "e2e": {"value": gp * Ke / e2e_s * world, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes, "steps": Ke,

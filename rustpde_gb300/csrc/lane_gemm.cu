@@ -93,6 +93,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// tensor-memory columns of a tile: a power of two >= 2 NT (main sum and corrections)
+__host__ __device__ inline uint32_t gemm_tmem_cols(int NT) {
+  uint32_t c = 32;
+  while (c < 2u * (uint32_t)NT) c <<= 1;
+  return c;
+}
+
 constexpr long kWaitLimit = 1L << 22;  // try_wait polls before a completion wait is declared lost
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
@@ -194,7 +201,12 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   const float* wsrc = J.w + (size_t)tile_n * J.kchunks * 2 * NT * kGemmKC;
   w_issue(wsrc, 0, NT, Wb[0], tid);  // operator chunk 0 in flight during the set-up
   cp_async_commit();
-  const uint32_t ncols = NT <= 32 ? 32u : NT <= 64 ? 64u : NT <= 128 ? 128u : 256u;
+  // two accumulators of NT columns: the hi*hi products and, apart, the small
+  // lo*hi + hi*lo corrections (added to the main sum with round-to-nearest at
+  // the end; accumulated into the main sum they would lose bits to the tensor
+  // core's truncating accumulation)
+  const uint32_t ncols = gemm_tmem_cols(NT);
+  const uint32_t corr = ncols / 2;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
                  "r"(ncols));
@@ -236,9 +248,10 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
         const uint64_t al = umma_desc(smem_u32(Alo) + s * 2 * a_lbo, a_lbo, 128);
         const uint64_t wh = umma_desc(smem_u32(Whi) + s * 2 * w_lbo, w_lbo, 128);
         const uint64_t wlo = umma_desc(smem_u32(Wlo) + s * 2 * w_lbo, w_lbo, 128);
-        mma_tf32(tmem, al, wh, idesc, (c > 0 || s > 0) ? 1u : 0u);
-        mma_tf32(tmem, ah, wlo, idesc, 1u);
-        mma_tf32(tmem, ah, wh, idesc, 1u);
+        const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
+        mma_tf32(tmem + corr, al, wh, idesc, acc);
+        mma_tf32(tmem + corr, ah, wlo, idesc, 1u);
+        mma_tf32(tmem, ah, wh, idesc, acc);
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                        smem_u32(mbar))
@@ -260,10 +273,12 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     const double scale = J.scale;
     const int nbase = tile_n * NT;
     for (int cc = 0; cc < NT; cc += 32) {
-      uint32_t r[32];
+      uint32_t r[32], q[32];
       tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, r);
+      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
 #pragma unroll
-      for (int j = 0; j < 32; j++) stage[(warp * 32 + wl) * 33 + j] = __uint_as_float(r[j]);
+      for (int j = 0; j < 32; j++)
+        stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
       __syncthreads();
 #pragma unroll 4
       for (int it = 0; it < 32; it++) {
@@ -373,7 +388,7 @@ void gemm_tiles(const std::vector<GemmJobDev>& jobs, std::vector<int4>& tiles) {
 size_t gemm_smem_bytes(int NT) {
   // A chunk (hi, lo) + two operator chunks (hi, lo) + barrier, tmem slot, lane bases
   const size_t base = 32768 + (size_t)4 * NT * 128 + 16 + 2 * kGemmLanes * 8;
-  const size_t ncols = NT <= 32 ? 32 : NT <= 64 ? 64 : NT <= 128 ? 128 : 256;
+  const size_t ncols = dev::gemm_tmem_cols(NT);
   // keep (resident CTAs per SM) x (tensor-memory columns) within the 512
   // columns: at most 512 / ncols CTAs fit, so ask for enough shared memory
   // (of the 228 KB per SM, 1 KB reserved per CTA) that no more become resident
