@@ -142,10 +142,11 @@ const char* rbc_kernel_name(int kernel);
 
 /* ---- batches --------------------------------------------------------------
  * Many independent cases advanced together (no reference counterpart: the
- * reference advances one Navier2D at a time).  Cases are grouped in buckets of
- * equal (kind, nx, ny); each pass of the step is one launch per bucket whose
- * work table covers the lanes of every case in the bucket, buckets run as
- * parallel branches, and the whole batch step is one CUDA graph.  Case handles
+ * reference advances one Navier2D at a time).  Cases are grouped by kind (box /
+ * periodic) and precision, whatever their sizes; each pass of the step is one
+ * launch per group whose work table covers the lanes of every case in the
+ * group, groups run as parallel branches, and the whole batch step is one
+ * CUDA graph.  Case handles
  * from rbc_batch_case are borrowed (do not destroy them); they share the batch
  * stream, so their state/diagnostic calls are ordered after rbc_batch_step. */
 typedef struct RbcBatch RbcBatch;

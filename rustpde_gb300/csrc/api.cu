@@ -93,6 +93,32 @@ static cudaError_t launch_entry(const StepLaunch& L, const DevPlan& dp, size_t k
   return launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, st, cases, dp.work[k]);
 }
 
+// One plan for a group of cases of the same kind and precision (any sizes):
+// each launch carries every member's work items (case index = the member's
+// position in the case table) or GEMM jobs; its shared memory is the largest
+// any member needs.  gates (optional): per member, the device flag that
+// idles the member's GEMM jobs.
+static StepPlan merge_plans(const std::vector<const StepPlan*>& plans, const std::vector<int>& case_index,
+                            const std::vector<const int*>& gates) {
+  StepPlan P = *plans[0];
+  for (size_t li = 0; li < P.launches.size(); li++) {
+    StepLaunch& L = P.launches[li];
+    L.items.clear();
+    L.jobs.clear();
+    for (size_t m = 0; m < plans.size(); m++) {
+      const StepLaunch& S = plans[m]->launches.at(li);
+      if (S.kernel != L.kernel) throw std::runtime_error("merge_plans: plans of different structure");
+      L.smem = std::max(L.smem, S.smem);
+      for (const int4& it : S.items) L.items.push_back(make_int4(case_index[m], it.y, it.z, it.w));
+      for (GemmJobDev j : S.jobs) {
+        if (!gates.empty()) j.active = gates[m];
+        L.jobs.push_back(j);
+      }
+    }
+  }
+  return P;
+}
+
 // Dense operator compositions of the mixed step (long double, before the
 // split), shared by every case of a size.
 enum MixedOpKind {
@@ -934,14 +960,14 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   std::vector<CaseDev> hd;
   for (RbcCase* c : b->cases) hd.push_back(c->hd);
   b->d_cases = b->arena.upload(hd);
-  // buckets of equal (kind, nx, ny)
+  // groups of equal kind (box / periodic) and precision, any size: one launch
+  // per pass covers every case of the group
   for (int i = 0; i < ncases; i++) {
     const RbcParams& p = params[i];
-    // both box kinds share kernels; the precision selects the plan
     int kind = (p.kind == RBC_PERIODIC ? 2 : 0) + 4 * p.precision;
     int found = -1;
     for (size_t k = 0; k < b->buckets.size(); k++)
-      if (b->buckets[k].kind == kind && b->buckets[k].nx == p.nx && b->buckets[k].ny == p.ny) found = (int)k;
+      if (b->buckets[k].kind == kind) found = (int)k;
     if (found < 0) {
       RbcBatch::Bucket bk;
       bk.kind = kind;
@@ -953,24 +979,9 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     b->buckets[found].members.push_back(i);
   }
   for (auto& bk : b->buckets) {
-    const RbcCase* first = b->cases[bk.members[0]];
-    bk.plan = first->plan;
-    for (size_t li = 0; li < bk.plan.launches.size(); li++) {
-      StepLaunch& L = bk.plan.launches[li];
-      if (L.kernel == K_GEMM) {
-        // every member's jobs (each job addresses that case's arrays)
-        L.jobs.clear();
-        for (int m : bk.members)
-          for (const GemmJobDev& j : b->cases[m]->plan.launches[li].jobs) L.jobs.push_back(j);
-        continue;
-      }
-      std::vector<int4> items;
-      size_t lanes = L.items.size();
-      items.reserve(lanes * bk.members.size());
-      for (size_t li2 = 0; li2 < lanes; li2++)
-        for (int m : bk.members) items.push_back(make_int4(m, L.items[li2].y, L.items[li2].z, L.items[li2].w));
-      L.items = items;
-    }
+    std::vector<const StepPlan*> plans;
+    for (int m : bk.members) plans.push_back(&b->cases[m]->plan);
+    bk.plan = merge_plans(plans, bk.members, {});
     upload_plan(b->arena, bk.plan, bk.dp);
   }
   cuda_check(cudaDeviceSynchronize(), "batch set-up");
@@ -1421,9 +1432,9 @@ int sv_solve(SvSolver* sv, const double* d_in, double* d_out, void* stream) {
 // A scheduler thread owns the GPU work.  Each round it (1) admits pending
 // requests whose case fits the HBM budget (host set-up on a separate stream,
 // so it overlaps the steps in flight), (2) when the set of active cases has
-// changed, rebuilds the batched step -- buckets of equal (kind, nx, ny,
-// precision), a gate kernel per bucket, the bucket's launches, all captured
-// into one CUDA graph -- and (3) launches `chunk_steps` graph steps.  The gate
+// changed, rebuilds the batched step -- groups of equal kind and precision,
+// a gate kernel per group, the group's launches, all captured into one CUDA
+// graph -- and (3) launches `chunk_steps` graph steps.  The gate
 // kernel counts each case's remaining steps down on the device and idles the
 // case once it has reached its horizon, so cases of different horizons share
 // a chunk and every case stops exactly at its own step count.  Finished cases
@@ -1623,9 +1634,7 @@ static void server_rebuild(RbcServer* S) {
     int found = -1;
     for (size_t k = 0; k < S->buckets.size(); k++) {
       const RbcParams& q = S->active[S->buckets[k].members[0]].r.p;
-      if ((q.kind == RBC_PERIODIC) == (p.kind == RBC_PERIODIC) && q.nx == p.nx && q.ny == p.ny &&
-          q.precision == p.precision)
-        found = (int)k;
+      if ((q.kind == RBC_PERIODIC) == (p.kind == RBC_PERIODIC) && q.precision == p.precision) found = (int)k;
     }
     if (found < 0) {
       S->buckets.emplace_back();
@@ -1634,24 +1643,13 @@ static void server_rebuild(RbcServer* S) {
     S->buckets[found].members.push_back(i);
   }
   for (auto& bk : S->buckets) {
-    bk.plan = S->active[bk.members[0]].c->plan;
-    for (size_t li = 0; li < bk.plan.launches.size(); li++) {
-      StepLaunch& L = bk.plan.launches[li];
-      if (L.kernel == K_GEMM) {
-        L.jobs.clear();
-        for (int m : bk.members)
-          for (GemmJobDev j : S->active[m].c->plan.launches[li].jobs) {
-            j.active = S->active[m].c->gate_mem + 1;
-            L.jobs.push_back(j);
-          }
-        continue;
-      }
-      std::vector<int4> items;
-      const std::vector<int4>& proto = S->active[bk.members[0]].c->plan.launches[li].items;
-      for (const int4& it : proto)
-        for (int m : bk.members) items.push_back(make_int4(m, it.y, it.z, it.w));
-      L.items = items;
+    std::vector<const StepPlan*> plans;
+    std::vector<const int*> gates;
+    for (int m : bk.members) {
+      plans.push_back(&S->active[m].c->plan);
+      gates.push_back(S->active[m].c->gate_mem + 1);
     }
+    bk.plan = merge_plans(plans, bk.members, gates);
     upload_plan(A, bk.plan, bk.dp);
     bk.d_members = A.upload(bk.members);
   }

@@ -28,7 +28,7 @@ def R():
 def test_batch_equals_single_cases(R):
     b = R.Batch(PARAMS)
     nb, nl = b.layout()
-    assert nb == 4  # (box,64,64), (per,32,17), (box,33,33), (per,64,33)
+    assert nb == 2  # box cases of every size in one group, periodic cases in the other
     singles = []
     for i, p in enumerate(PARAMS):
         R.standard_ic(b.cases[i], seed=10 + i)
