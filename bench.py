@@ -221,6 +221,7 @@ def run_ensemble(args, rank, world, local):
     barrier(world)
     total_ms = max_over_ranks(total_ms, world)
     nb, launches = B.layout()
+    tuning = B.tuning()
     status = [c.status() for c in B.cases]
     mixed_nu = [c.eval(R.NU) for c in B.cases]
     mixed_ke = [c.eval(R.KE) for c in B.cases]
@@ -306,6 +307,8 @@ def run_ensemble(args, rank, world, local):
                 "how": "per step: rbc_batch_set_state_all (pinned h2d), rbc_batch_step(1), rbc_batch_get_state_all"},
         "gpu_launches": K * launches,
         "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
+        "autotuner": [{"pass": t[0], "ms_cta_per_lane": t[1], "ms_thread_per_lane": t[2], "chosen": t[3]}
+                      for t in tuning],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_launch": dom_bytes,
                      "peak_source": pk_src},

@@ -169,6 +169,13 @@ int rbc_batch_get_stream(RbcBatch* b, void** stream);
  * bytes per step (stage_bytes and stage_kernel may be NULL). */
 int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* stage_bytes, int* stage_kernel,
                            int max_stages, int* nstages);
+/* Autotuner record of a batch: for the passes that have a one-thread-per-lane
+ * form beside the one-CTA-per-lane form, rbc_batch_create timed both on the
+ * batch (ms per launch) and kept the faster.  *n = number of decisions; entry k
+ * (if 0 <= k < *n) is written to the non-null outputs (kernel ids: see
+ * rbc_kernel_name). */
+int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
+                     int* n);
 int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes);
 int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
 int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes);

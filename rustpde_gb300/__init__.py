@@ -125,6 +125,7 @@ _SIGNATURES = {
     "rbc_server_stats": (_I, [_P, ctypes.POINTER(RbcServerStats)]),
     "rbc_server_destroy": (_I, [_P]),
     "rbc_batch_profile_step": (_I, [_P, _I, _DP, _DP, _IP, _I, _IP]),
+    "rbc_batch_tuning": (_I, [_P, _I, _IP, _IP, _DP, _DP, _IP]),
     "rbc_stage_bytes": (_I, [_P, _I, _DP]),
     "rbc_kernel_name": (ctypes.c_char_p, [_I]),
     "rbc_batch_state_offset": (_I, [_P, _I, ctypes.POINTER(_SZ)]),
@@ -686,6 +687,19 @@ class Batch:
         n = _I()
         _check(lib().rbc_batch_profile_step(self._h, int(nsteps), ms, by, kd, cap, ctypes.byref(n)))
         return {lib().rbc_kernel_name(kd[k]).decode(): (ms[k], by[k]) for k in range(n.value)}
+
+    def tuning(self):
+        """Autotuner decisions: [(pass, ms one CTA per lane, ms one thread per lane, chosen)]."""
+        n = _I()
+        _check(lib().rbc_batch_tuning(self._h, -1, None, None, None, None, ctypes.byref(n)))
+        out = []
+        for k in range(n.value):
+            a, b, ta, tb = _I(), _I(), _D(), _D()
+            _check(lib().rbc_batch_tuning(self._h, k, ctypes.byref(a), ctypes.byref(b), ctypes.byref(ta),
+                                          ctypes.byref(tb), ctypes.byref(n)))
+            out.append((lib().rbc_kernel_name(a.value).decode(), ta.value, tb.value,
+                        "lanes" if tb.value < ta.value else "cta"))
+        return out
 
     def state_bytes(self):
         n = _SZ()

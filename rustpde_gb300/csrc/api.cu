@@ -184,6 +184,7 @@ struct RbcCase {
   double* d_red = nullptr;
   cudaStream_t stream = nullptr;
   StepPlan plan;
+  StepPlan plan_lanes;  // mixed form: the batch variant with one-thread-per-lane FP64 passes
   DevPlan dp;
   MixedOps mops;
   cudaGraph_t graph = nullptr;
@@ -299,6 +300,9 @@ static size_t state_layout(const RbcParams& p, size_t sizes[5]) {
 
 // state_region: optional device region of state_layout() bytes that holds the
 // case's spectral state (a batch keeps all its cases' state contiguous).
+// with_graph: a case stepped on its own (rbc_create): its plan and CUDA graph
+// are built here; batches and the serving loop (with_graph = false) merge the
+// plans of many cases and use the one-thread-per-lane FP64 kernels.
 void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr) {
   const RbcParams& p = c->p;
   Arena& A = c->arena;
@@ -502,7 +506,8 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   cuda_check(configure_step_kernels(), "configure step kernels");
   if (h.mixed) {
     cuda_check(configure_mixed_kernels(), "configure mixed kernels");
-    c->plan = build_mixed_plan(h, c->mops);
+    c->plan = build_mixed_plan(h, c->mops, false);
+    if (!with_graph) c->plan_lanes = build_mixed_plan(h, c->mops, true);
   } else {
     c->plan = build_step_plan(h);
   }
@@ -913,6 +918,11 @@ struct RbcBatch {
     DevPlan dp;
   };
   std::vector<Bucket> buckets;
+  struct Tuned {
+    int kernel_cta, kernel_lanes;
+    float ms_cta, ms_lanes;
+  };
+  std::vector<Tuned> tuning;          // autotuner decisions (rbc_batch_tuning)
   char* d_state = nullptr;            // every case's spectral state, contiguous
   size_t state_bytes = 0;
   std::vector<size_t> state_offset;   // byte offset of case i in d_state
@@ -979,11 +989,57 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     b->buckets[found].members.push_back(i);
   }
   for (auto& bk : b->buckets) {
-    std::vector<const StepPlan*> plans;
-    for (int m : bk.members) plans.push_back(&b->cases[m]->plan);
+    std::vector<const StepPlan*> plans, lanes;
+    for (int m : bk.members) {
+      plans.push_back(&b->cases[m]->plan);
+      lanes.push_back(b->cases[m]->plan_lanes.launches.empty() ? &b->cases[m]->plan : &b->cases[m]->plan_lanes);
+    }
     bk.plan = merge_plans(plans, bk.members, {});
     upload_plan(b->arena, bk.plan, bk.dp);
+    // autotune: where a pass has a one-thread-per-lane form, time both forms on
+    // this batch and keep the faster (the state is still zero; the choice is
+    // made once, so the batch's numbers do not depend on later timings)
+    StepPlan alt = merge_plans(lanes, bk.members, {});
+    DevPlan adp;
+    upload_plan(b->arena, alt, adp);
+    cuda_check(cudaDeviceSynchronize(), "batch set-up");
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    auto time_launch = [&](const StepLaunch& L, const DevPlan& dp, size_t li) {
+      cuda_check(launch_entry(L, dp, li, b->stream, b->d_cases), "autotune launch");  // warm-up
+      float best = 1e30f;
+      for (int r = 0; r < 3; r++) {
+        cuda_check(cudaEventRecord(e0, b->stream), "event");
+        cuda_check(launch_entry(L, dp, li, b->stream, b->d_cases), "autotune launch");
+        cuda_check(cudaEventRecord(e1, b->stream), "event");
+        cuda_check(cudaEventSynchronize(e1), "event");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
+        best = std::min(best, ms);
+      }
+      return best;
+    };
+    for (size_t li = 0; li < bk.plan.launches.size(); li++) {
+      if (alt.launches[li].kernel == bk.plan.launches[li].kernel) continue;
+      const float t_cta = time_launch(bk.plan.launches[li], bk.dp, li);
+      const float t_lane = time_launch(alt.launches[li], adp, li);
+      b->tuning.push_back({bk.plan.launches[li].kernel, alt.launches[li].kernel, t_cta, t_lane});
+      if (t_lane < t_cta) {
+        bk.plan.launches[li] = alt.launches[li];
+        bk.dp.work[li] = adp.work[li];
+        bk.dp.jobs[li] = adp.jobs[li];
+        bk.dp.tiles[li] = adp.tiles[li];
+        bk.dp.ntiles[li] = adp.ntiles[li];
+        bk.dp.max_nt[li] = adp.max_nt[li];
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
   }
+  // the timing runs wrote into the state and scratch: the batch starts from zero
+  cuda_check(cudaMemsetAsync(b->d_state, 0, b->state_bytes, b->stream), "clear state");
+  for (RbcCase* c : b->cases) cuda_check(cudaMemsetAsync(c->hd.status, 0, 16, b->stream), "clear status");
   cuda_check(cudaDeviceSynchronize(), "batch set-up");
   // graph: one branch per bucket
   size_t nb = b->buckets.size();
@@ -1053,6 +1109,21 @@ int rbc_batch_layout(const RbcBatch* b, int* nbuckets, int* launches) {
   *launches = b->launches;
   API_END
 }
+int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
+                     int* n) {
+  API_BEGIN
+  require(b && n, "null argument");
+  *n = (int)b->tuning.size();
+  if (k >= 0 && k < *n) {
+    const auto& t = b->tuning[k];
+    if (kernel_cta) *kernel_cta = t.kernel_cta;
+    if (kernel_lanes) *kernel_lanes = t.kernel_lanes;
+    if (ms_cta) *ms_cta = t.ms_cta;
+    if (ms_lanes) *ms_lanes = t.ms_lanes;
+  }
+  API_END
+}
+
 int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes) {
   API_BEGIN
   require(b && bytes, "null argument");

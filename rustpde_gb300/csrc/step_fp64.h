@@ -15,6 +15,9 @@ enum StepKernel {
   K_PER_Y2A, K_PER_Y2B,
   // mixed-precision form
   K_PER_Y2_PRE, K_PER_X_MIXED, K_BOX_PROD_MIXED, K_BOX_Y2_PRE, K_BOX_X3_MIX, K_BOX_X4_MIX, K_BOX_GPX,
+  // one thread per lane (batched mixed-precision form, step_lanes.cu)
+  K_LP_BOX_GPX, K_LP_BOX_X2, K_LP_BOX_X3, K_LP_BOX_X4, K_LP_BOX_Y2, K_LP_BOX_Y3, K_LP_BOX_Y4, K_LP_BOX_Y5,
+  K_LP_PER_Y2,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };
@@ -46,7 +49,11 @@ struct MixedOps {
   const float* pf = nullptr;  // Poisson eigenbasis forward: (nx - 2) x (nx - 2)
   const float* pb = nullptr;  // Poisson eigenbasis backward: (nx - 2) x (nx - 2)
 };
-StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops);
+// lane_parallel: the FP64 passes run one thread per lane (many lanes: batches);
+// otherwise one CTA per lane (a single case)
+StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_parallel);
+cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work);
+constexpr int kLaneThreads = 128;  // lanes per CTA of the one-thread-per-lane kernels
 const char* step_kernel_name(int kernel);
 // serving gate of the cases members[0..n) of `cases` (see CaseDev::gate)
 cudaError_t launch_gate(const CaseDev* cases, const int* members, int n, cudaStream_t s);

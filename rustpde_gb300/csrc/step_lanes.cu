@@ -1,0 +1,514 @@
+// step_lanes.cu -- FP64 passes of the batched mixed-precision step, one thread
+// per lane.
+//
+// A batch holds thousands of independent lanes (rows or columns of many
+// cases).  Here one thread runs each lane's banded recurrences sequentially,
+// so every lane of every warp issues useful FP64 work and no scan, shuffle or
+// barrier is needed (the single-case kernels of step_fp64.cu use 16-thread
+// scans instead, because one case has too few lanes to fill the GPU).
+// Column lanes (x direction) are read and written coalesced across a warp;
+// row lanes (y direction) stream through L1, each thread along its own row.
+// Multi-pass kernels re-read their own earlier results from L1/L2.
+//
+// Operations and their reference lines are those of the FP64 kernels:
+// to_ortho / from_ortho (composite_stencil.rs:117-276, linalg.rs:14-57),
+// differentiate (ortho.rs:107-125), MatVecFdma (matvec.rs:142-248), Fdma
+// (fdma.rs:179-227), the RBC step (navier.rs:622-721).
+//
+// Work item: (case, first lane, lane count <= blockDim.x, 0).
+#include "lane_ops.cuh"
+#include "step_fp64.h"
+
+namespace rbc {
+namespace dev {
+
+// Chebyshev derivative d = D a of a lane whose coefficients arrive in
+// descending index order: d_{n-1} = 0, d_i = 2(i+1) a_{i+1} + d_{i+2}
+// (1 <= i <= n-2), d_0 = a_1 + d_2 / 2.  step(i, a_i) returns d_i.
+template <class T>
+struct DescDiff {
+  T a_next, d1, d2;
+  int n;
+  __device__ __forceinline__ explicit DescDiff(int n_) : a_next(zero_v<T>()), d1(zero_v<T>()), d2(zero_v<T>()), n(n_) {}
+  __device__ __forceinline__ T step(int i, T a_i) {
+    T d;
+    if (i == n - 1) d = zero_v<T>();
+    else if (i >= 1) d = fmas(d2, a_next, 2.0 * (double)(i + 1));
+    else d = fmas(a_next, d2, 0.5);
+    d2 = d1;
+    d1 = d;
+    a_next = a_i;
+    return d;
+  }
+};
+
+// composite stencil p_i = diag_i c_i + low2_{i-2} c_{i-2} of a strided lane
+// (c has b.m entries; Chebyshev / Fourier bases are the identity)
+template <class T>
+__device__ __forceinline__ T stencil_lane(const BasisDev& b, const T* c, long long s, int i) {
+  if (b.kind == 0 || b.kind == 5) return c[(long long)i * s];
+  const int m = b.m;
+  T v = zero_v<T>();
+  if (i < m) v = scal(c[(long long)i * s], b.diag[i]);
+  if (i >= 2 && i - 2 < m) {
+    const T t = c[(long long)(i - 2) * s];
+    v = (i < m) ? fmas(v, t, b.low2[i - 2]) : scal(t, b.low2[i - 2]);
+  }
+  return v;
+}
+
+// per-row factor pointers of a banded solver
+struct FdmaRow {
+  const double *low, *dinv, *up1, *up2;
+  int m;
+};
+__device__ __forceinline__ FdmaRow fdma_row(const FdmaDev& f, int row) {
+  const size_t o = (f.rows > 1) ? (size_t)row * f.stride : 0;
+  return FdmaRow{f.low + o, f.dinv + o, f.up1 + o, f.up2 + o, f.m};
+}
+
+// Fdma forward elimination x_i += low_{i-2} x_{i-2} of a strided lane, in place
+template <class T>
+__device__ __forceinline__ void fdma_fwd_lane(const FdmaRow& f, T* x, long long s) {
+  T xm1 = zero_v<T>(), xm2 = zero_v<T>();
+#pragma unroll 4
+  for (int i = 0; i < f.m; i++) {
+    T v = x[(long long)i * s];
+    if (i >= 2) v = fmas(v, xm2, f.low[i - 2]);
+    x[(long long)i * s] = v;
+    xm2 = xm1;
+    xm1 = v;
+  }
+}
+// Fdma back substitution x_j = x_j / dia_j - up1_j x_{j+2} - up2_j x_{j+4}
+// (factors stored as 1/dia and -up/dia), in place
+template <class T>
+__device__ __forceinline__ void fdma_bwd_lane(const FdmaRow& f, T* x, long long s) {
+  T p1 = zero_v<T>(), p2 = zero_v<T>(), p3 = zero_v<T>(), p4 = zero_v<T>();
+#pragma unroll 4
+  for (int j = f.m - 1; j >= 0; j--) {
+    T v = scal(x[(long long)j * s], f.dinv[j]);
+    if (j + 2 < f.m) v = fmas(v, p2, f.up1[j]);
+    if (j + 4 < f.m) v = fmas(v, p4, f.up2[j]);
+    x[(long long)j * s] = v;
+    p4 = p3;
+    p3 = p2;
+    p2 = p1;
+    p1 = v;
+  }
+}
+
+// pinv row r (entries at r, r+2, r+4) of a strided lane of length n
+template <class T>
+__device__ __forceinline__ T pinv_lane(const PinvDev& p, const T* a, long long s, int r) {
+  const int m = p.n - 2;
+  T v = scal(a[(long long)r * s], p.dia[r]);
+  if (r < m - 2) v = fmas(v, a[(long long)(r + 2) * s], p.up1[r]);
+  if (r < m - 4) v = fmas(v, a[(long long)(r + 4) * s], p.up2[r]);
+  return v;
+}
+
+// least-squares from_ortho of a strided lane (composite basis), in two passes:
+// rhs and forward sweep into `out`, then back substitution in place.
+template <class T>
+__device__ __forceinline__ void from_ortho_lane(const BasisDev& b, const T* p, long long ps, T* out, long long os) {
+  const int m = b.m;
+  T g1 = zero_v<T>(), g2 = zero_v<T>();
+#pragma unroll 4
+  for (int i = 0; i < m; i++) {
+    const T d = fmas(scal(p[(long long)i * ps], b.diag[i]), p[(long long)(i + 2) * ps], b.low2[i]);
+    const double q = b.fo_dinv[i];
+    T g = scal(d, q);
+    if (i >= 2) g = fmas(g, g2, -b.fo_off[i - 2] * q);
+    out[(long long)i * os] = g;
+    g2 = g1;
+    g1 = g;
+  }
+  T x1 = zero_v<T>(), x2 = zero_v<T>();
+#pragma unroll 4
+  for (int j = m - 1; j >= 0; j--) {
+    T x = out[(long long)j * os];
+    if (j + 2 < m) x = fmas(x, x2, -b.fo_w[j]);
+    out[(long long)j * os] = x;
+    x2 = x1;
+    x1 = x;
+  }
+}
+
+#define LANE_PROLOGUE                                                        \
+  const int4 w = work[blockIdx.x];                                           \
+  if ((int)threadIdx.x >= w.z) return;                                       \
+  const CaseDev& c = cases[w.x];                                             \
+  if (c.gate != nullptr && c.gate[1] == 0) return;                           \
+  const int lane = w.y + (int)threadIdx.x;
+
+// ============================================================================
+// Box, x direction (lanes = columns, stride = row length)
+// ============================================================================
+// d/dx p0 / aspect -> s[0] (nx x ny), columns j < ny
+__global__ void __launch_bounds__(128) k_lp_box_gpx(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int j = lane, nx = c.nx, ny = c.ny;
+  const double inv_asp = 1.0 / c.aspect;
+  const double* p0 = static_cast<const double*>(c.p0) + j;
+  double* gp = static_cast<double*>(c.s[0]) + j;
+  DescDiff<double> D(nx);
+#pragma unroll 4
+  for (int i = nx - 1; i >= 0; i--) gp[(long long)i * ny] = D.step(i, p0[(long long)i * ny]) * inv_asp;
+}
+
+// pinv_x and the ADI x solve of the three fields: s[1..3] -> s[4..6], columns j < myc
+__global__ void __launch_bounds__(128) k_lp_box_x2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int j = lane, myc = c.myc, mxc = c.mxc;
+  for (int f = 0; f < 3; f++) {
+    const double* in = static_cast<const double*>(c.s[1 + f]) + j;
+    double* out = static_cast<double*>(c.s[4 + f]) + j;
+    const FdmaRow F = fdma_row(f < 2 ? c.hu_x : c.ht_x, 0);
+    // pinv fused with the forward elimination
+    double xm1 = 0.0, xm2 = 0.0;
+#pragma unroll 4
+    for (int i = 0; i < mxc; i++) {
+      double v = pinv_lane<double>(c.pinv_x, in, myc, i);
+      if (i >= 2) v = fma(xm2, F.low[i - 2], v);
+      out[(long long)i * myc] = v;
+      xm2 = xm1;
+      xm1 = v;
+    }
+    fdma_bwd_lane<double>(F, out, myc);
+  }
+}
+
+// divergence and pinv_x: A = s[1], B = s[2] (mxc x ny) -> div s[3] (nx x ny),
+// pinv_x div -> m_z (mxc x ny), columns j < ny
+__global__ void __launch_bounds__(128) k_lp_box_x3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int j = lane, nx = c.nx, ny = c.ny, mxc = c.mxc;
+  const double inv_asp = 1.0 / c.aspect;
+  const double* A = static_cast<const double*>(c.s[1]) + j;
+  const double* B = static_cast<const double*>(c.s[2]) + j;
+  double* dv = static_cast<double*>(c.s[3]) + j;
+  DescDiff<double> D(nx);
+  for (int i = nx - 1; i >= 0; i--) {
+    const double da = D.step(i, stencil_lane<double>(c.xu, A, ny, i));
+    dv[(long long)i * ny] = fma(da, inv_asp, stencil_lane<double>(c.xu, B, ny, i));
+  }
+  double* z = static_cast<double*>(c.m_z) + j;
+  for (int r = 0; r < mxc; r++) z[(long long)r * ny] = pinv_lane<double>(c.pinv_x, dv, ny, r);
+}
+
+// projection along x from p1 (computed by the eigenbasis GEMM): p1[0][0] = 0;
+// Gp = Sx^N p1 -> s[0], E = Sx+ (Dx Sx^N p1 / s) -> s[1], Fv = Sx+ Sx^N p1 -> s[2]
+// (s arrays as mxc/nx x myc), columns j < myc
+__global__ void __launch_bounds__(128) k_lp_box_x4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int j = lane, nx = c.nx, myc = c.myc;
+  const double inv_asp = 1.0 / c.aspect;
+  double* p1 = static_cast<double*>(c.p1) + j;
+  if (j == 0) p1[0] = 0.0;
+  double* gp = static_cast<double*>(c.s[0]) + j;
+  double* e = static_cast<double*>(c.s[1]) + j;
+  double* fv = static_cast<double*>(c.s[2]) + j;
+  DescDiff<double> D(nx);
+#pragma unroll 4
+  for (int i = nx - 1; i >= 0; i--) {
+    const double o = stencil_lane<double>(c.xp, p1, myc, i);
+    gp[(long long)i * myc] = o;
+    e[(long long)i * myc] = D.step(i, o) * inv_asp;  // scratch: from_ortho reads it below
+  }
+  from_ortho_lane<double>(c.xu, e, myc, e, myc);
+  from_ortho_lane<double>(c.xu, gp, myc, fv, myc);
+}
+
+// ============================================================================
+// Box, y direction (lanes = rows, contiguous; stride 1)
+// ============================================================================
+// rows i < nx: convection (m_cv), x stencils of the state, right-hand sides, pinv_y -> s[1..3]
+__global__ void __launch_bounds__(128) k_lp_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, kx = c.kx, ky = c.ky;
+  const double dt = c.dt;
+  const void* f3[3] = {c.ux, c.uy, c.temp};
+  const BasisDev* xb[3] = {&c.xu, &c.xu, &c.xt};
+  const double* cv = static_cast<const double*>(c.m_cv);
+  const double* P = static_cast<const double*>(c.p0) + (size_t)i * ny;
+  const double* gpx = static_cast<const double*>(c.s[0]) + (size_t)i * ny;
+  const double* bco = static_cast<const double*>(c.bc_ortho) + (size_t)i * ny;
+  const double* bcd = static_cast<const double*>(c.bc_diff) + (size_t)i * ny;
+  // x stencil of the state at row i, column k (the composite x basis of each field)
+  auto sx = [&](int f, int k) -> double {
+    if (k < 0 || k >= myc) return 0.0;
+    const double* a = static_cast<const double*>(f3[f]);
+    const BasisDev& b = *xb[f];
+    double v = 0.0;
+    bool has = false;
+    if (i < mxc) { v = a[(size_t)i * myc + k] * b.diag[i]; has = true; }
+    if (i >= 2 && i - 2 < mxc) {
+      const double t = a[(size_t)(i - 2) * myc + k];
+      v = has ? fma(t, b.low2[i - 2], v) : t * b.low2[i - 2];
+    }
+    return v;
+  };
+  // descending k: y stencil O_f,k (CD basis), dP/dy, right-hand sides, pinv rows
+  DescDiff<double> G(ny);
+  double R[3][5];  // R_f at k .. k+4
+  for (int f = 0; f < 3; f++)
+    for (int q = 0; q < 5; q++) R[f][q] = 0.0;
+  double* out[3] = {static_cast<double*>(c.s[1]) + (size_t)i * myc, static_cast<double*>(c.s[2]) + (size_t)i * myc,
+                    static_cast<double*>(c.s[3]) + (size_t)i * myc};
+  const PinvDev& pv = c.pinv_y;
+  for (int k = ny - 1; k >= 0; k--) {
+    double O[3];
+    for (int f = 0; f < 3; f++) {
+      // O_k = diag_k SX_k + low2_{k-2} SX_{k-2}
+      double v = 0.0;
+      if (k < myc) v = sx(f, k) * c.ycd.diag[k];
+      if (k >= 2 && k - 2 < myc) v = (k < myc) ? fma(sx(f, k - 2), c.ycd.low2[k - 2], v) : sx(f, k - 2) * c.ycd.low2[k - 2];
+      O[f] = v;
+    }
+    const double g = G.step(k, P[k]);
+    const bool incv = i < kx && k < ky;
+    const double cvk0 = incv ? cv[((size_t)0 * kx + i) * ky + k] : 0.0;
+    const double cvk1 = incv ? cv[((size_t)1 * kx + i) * ky + k] : 0.0;
+    const double cvk2 = incv ? cv[((size_t)2 * kx + i) * ky + k] : 0.0;
+    for (int f = 0; f < 3; f++)
+      for (int q = 4; q > 0; q--) R[f][q] = R[f][q - 1];
+    R[0][0] = fnms(fnms(O[0], gpx[k], dt), cvk0, dt);
+    const double that = O[2] + bco[k];
+    R[1][0] = fnms(fmas(fnms(O[1], g, dt), that, dt), cvk1, dt);
+    R[2][0] = fnms(O[2] + bcd[k], cvk2, dt);
+    if (k < myc) {
+      for (int f = 0; f < 3; f++) {
+        double v = R[f][0] * pv.dia[k];
+        if (k < myc - 2) v = fma(R[f][2], pv.up1[k], v);
+        if (k < myc - 4) v = fma(R[f][4], pv.up2[k], v);
+        out[f][k] = v;
+      }
+    }
+  }
+}
+
+// rows i < mxc: ADI y solves; ux*, uy* in place (s[4], s[5]), temperature ->
+// state; A = Sy ux* -> s[1], B = Dy Sy uy* -> s[2] (mxc x ny)
+__global__ void __launch_bounds__(128) k_lp_box_y3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc;
+  double* F[3] = {static_cast<double*>(c.s[4]) + (size_t)i * myc, static_cast<double*>(c.s[5]) + (size_t)i * myc,
+                  static_cast<double*>(c.s[6]) + (size_t)i * myc};
+  bool bad = false;
+  for (int f = 0; f < 3; f++) {
+    const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, 0);
+    fdma_fwd_lane<double>(R, F[f], 1);
+    fdma_bwd_lane<double>(R, F[f], 1);
+  }
+  double* tt = static_cast<double*>(c.temp) + (size_t)i * myc;
+  for (int k = 0; k < myc; k++) {
+    const double t = F[2][k];
+    tt[k] = t;
+    bad |= !(isfinite(F[0][k]) && isfinite(F[1][k]) && isfinite(t));
+  }
+  double* A = static_cast<double*>(c.s[1]) + (size_t)i * ny;
+  double* B = static_cast<double*>(c.s[2]) + (size_t)i * ny;
+  DescDiff<double> D(ny);
+#pragma unroll 4
+  for (int k = ny - 1; k >= 0; k--) {
+    A[k] = stencil_lane<double>(c.ycd, F[0], 1, k);
+    B[k] = D.step(k, stencil_lane<double>(c.ycd, F[1], 1, k));
+  }
+  if (bad) atomicOr(c.status, 1u);
+}
+
+// rows i < mxc: pinv_y of the eigenbasis-transformed divergence and the
+// Poisson row solve: s[6] (zf, mxc x ny) -> s[7] (mxc x myc)
+__global__ void __launch_bounds__(128) k_lp_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc;
+  const double* zf = static_cast<const double*>(c.s[6]) + (size_t)i * ny;
+  double* wv = static_cast<double*>(c.s[7]) + (size_t)i * myc;
+  const FdmaRow R = fdma_row(c.pois_y, i);
+  double xm1 = 0.0, xm2 = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < myc; k++) {
+    double v = pinv_lane<double>(c.pinv_y, zf, 1, k);
+    if (k >= 2) v = fma(xm2, R.low[k - 2], v);
+    wv[k] = v;
+    xm2 = xm1;
+    xm1 = v;
+  }
+  fdma_bwd_lane<double>(R, wv, 1);
+}
+
+// rows i < nx: ux = ux* - Sy+ Sy^N E ; uy = uy* - Sy+ Dy Sy^N Fv ;
+// p0 = (p0 - nu div) + Sy^N Gp / dt  (scratch rows: s[6], s[7])
+__global__ void __launch_bounds__(128) k_lp_box_y5(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc;
+  if (i < mxc) {
+    const double* E = static_cast<const double*>(c.s[1]) + (size_t)i * myc;
+    const double* Fv = static_cast<const double*>(c.s[2]) + (size_t)i * myc;
+    double* d0 = static_cast<double*>(c.s[6]) + (size_t)i * ny;  // Sy^N E (ortho), then its from_ortho
+    double* d1 = static_cast<double*>(c.s[7]) + (size_t)i * ny;  // Dy Sy^N Fv, then its from_ortho
+    DescDiff<double> D(ny);
+    for (int k = ny - 1; k >= 0; k--) {
+      d0[k] = stencil_lane<double>(c.ycn, E, 1, k);
+      d1[k] = D.step(k, stencil_lane<double>(c.ycn, Fv, 1, k));
+    }
+    from_ortho_lane<double>(c.ycd, d0, 1, d0, 1);
+    from_ortho_lane<double>(c.ycd, d1, 1, d1, 1);
+    double* ux = static_cast<double*>(c.ux) + (size_t)i * myc;
+    double* uy = static_cast<double*>(c.uy) + (size_t)i * myc;
+    const double* us = static_cast<const double*>(c.s[4]) + (size_t)i * myc;
+    const double* vs = static_cast<const double*>(c.s[5]) + (size_t)i * myc;
+    bool bad = false;
+    for (int k = 0; k < myc; k++) {
+      const double a = us[k] - d0[k], b = vs[k] - d1[k];
+      ux[k] = a;
+      uy[k] = b;
+      bad |= !(isfinite(a) && isfinite(b));
+    }
+    if (bad) atomicOr(c.status, 1u);
+  }
+  const double* Gp = static_cast<const double*>(c.s[0]) + (size_t)i * myc;
+  double* p0 = static_cast<double*>(c.p0) + (size_t)i * ny;
+  const double* dv = static_cast<const double*>(c.s[3]) + (size_t)i * ny;
+  for (int k = 0; k < ny; k++) {
+    const double v = fnms(p0[k], dv[k], c.nu);
+    p0[k] = fmas(v, stencil_lane<double>(c.ycn, Gp, 1, k), c.inv_dt);
+  }
+}
+
+// ============================================================================
+// Periodic Y2 (rows i < mx, complex): right-hand sides, pinv_y, per-row
+// Helmholtz solves, divergence, Poisson row solve (p1[0,0] = 0), projection
+// and the pres[0] update, from the convection term m_cv (navier.rs:622-721).
+// Scratch rows (ny): yw[0] div, yw[1] dp/dx, yw[2] dp/dy.
+// ============================================================================
+__global__ void __launch_bounds__(128) k_lp_per_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  LANE_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
+  const double dt = c.dt, inv_asp = 1.0 / c.aspect, ki = (double)i;
+  double2* F[3] = {static_cast<double2*>(c.ux) + (size_t)i * myc, static_cast<double2*>(c.uy) + (size_t)i * myc,
+                   static_cast<double2*>(c.temp) + (size_t)i * myc};
+  double2* P = static_cast<double2*>(c.p0) + (size_t)i * ny;
+  const double2* cv = static_cast<const double2*>(c.m_cv);
+  const double2* bco = static_cast<const double2*>(c.bc_ortho) + (size_t)i * ny;
+  const double2* bcd = static_cast<const double2*>(c.bc_diff) + (size_t)i * ny;
+  double2* dvr = static_cast<double2*>(c.yw[0]) + (size_t)i * ny;
+  double2* dpx = static_cast<double2*>(c.yw[1]) + (size_t)i * ny;
+  double2* dpy = static_cast<double2*>(c.yw[2]) + (size_t)i * ny;
+  double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
+  const PinvDev& pv = c.pinv_y;
+
+  // 1. descending k: O_f = Sy F_f, dP/dy, right-hand sides, pinv rows (in place
+  //    over the state rows: F_k is last read at step k)
+  {
+    DescDiff<double2> G(ny);
+    double2 R[3][5];
+    for (int f = 0; f < 3; f++)
+      for (int q = 0; q < 5; q++) R[f][q] = c2(0.0, 0.0);
+    for (int k = ny - 1; k >= 0; k--) {
+      double2 O[3];
+      for (int f = 0; f < 3; f++) O[f] = stencil_lane<double2>(c.ycd, F[f], 1, k);
+      const double2 pk = P[k];
+      const double2 g = G.step(k, pk);
+      const bool incv = i < kx && k < ky;
+      const double2 c0 = incv ? cv[((size_t)0 * kx + i) * ky + k] : c2(0.0, 0.0);
+      const double2 c1 = incv ? cv[((size_t)1 * kx + i) * ky + k] : c2(0.0, 0.0);
+      const double2 cc2 = incv ? cv[((size_t)2 * kx + i) * ky + k] : c2(0.0, 0.0);
+      for (int f = 0; f < 3; f++)
+        for (int q = 4; q > 0; q--) R[f][q] = R[f][q - 1];
+      const double2 gx = mul_ik(pk, ki) * inv_asp;
+      R[0][0] = fnms(fnms(O[0], gx, dt), c0, dt);
+      const double2 that = O[2] + bco[k];
+      R[1][0] = fnms(fmas(fnms(O[1], g, dt), that, dt), c1, dt);
+      R[2][0] = fnms(O[2] + bcd[k], cc2, dt);
+      if (k < myc)
+        for (int f = 0; f < 3; f++) {
+          double2 v = scal(R[f][0], pv.dia[k]);
+          if (k < myc - 2) v = fmas(v, R[f][2], pv.up1[k]);
+          if (k < myc - 4) v = fmas(v, R[f][4], pv.up2[k]);
+          F[f][k] = v;
+        }
+    }
+  }
+  // 2./3. the rows' banded Helmholtz solves: ux*, uy* (hu_y), temperature (ht_y)
+  for (int f = 0; f < 3; f++) {
+    const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, i);
+    fdma_fwd_lane<double2>(R, F[f], 1);
+    fdma_bwd_lane<double2>(R, F[f], 1);
+  }
+  // 4. divergence = ik/s Sy ux* + Dy Sy uy* (descending), pinv rows -> p1
+  {
+    DescDiff<double2> G(ny);
+    double2 W[5];
+    for (int q = 0; q < 5; q++) W[q] = c2(0.0, 0.0);
+    for (int k = ny - 1; k >= 0; k--) {
+      const double2 o0 = stencil_lane<double2>(c.ycd, F[0], 1, k);
+      const double2 g = G.step(k, stencil_lane<double2>(c.ycd, F[1], 1, k));
+      const double2 d = mul_ik(o0, ki) * inv_asp + g;
+      dvr[k] = d;
+      for (int q = 4; q > 0; q--) W[q] = W[q - 1];
+      W[0] = d;
+      if (k < myc) {
+        double2 v = scal(W[0], pv.dia[k]);
+        if (k < myc - 2) v = fmas(v, W[2], pv.up1[k]);
+        if (k < myc - 4) v = fmas(v, W[4], pv.up2[k]);
+        p1[k] = v;
+      }
+    }
+  }
+  // 5./6. Poisson row solve -> pseudo pressure row (p1[0,0] = 0)
+  {
+    const FdmaRow R = fdma_row(c.pois_y, i);
+    fdma_fwd_lane<double2>(R, p1, 1);
+    fdma_bwd_lane<double2>(R, p1, 1);
+    if (i == 0) p1[0] = c2(0.0, 0.0);
+  }
+  // 7. projection gradients (descending): O1 = Sy^N p1, dp/dy = Dy O1, dp/dx = ik/s O1;
+  //    pres[0] = (pres[0] - nu div) + O1 / dt
+  {
+    DescDiff<double2> G(ny);
+    for (int k = ny - 1; k >= 0; k--) {
+      const double2 o1 = stencil_lane<double2>(c.ycn, p1, 1, k);
+      dpy[k] = G.step(k, o1);
+      dpx[k] = mul_ik(o1, ki) * inv_asp;
+      const double2 v = fnms(P[k], dvr[k], c.nu);
+      P[k] = fmas(v, o1, c.inv_dt);
+    }
+  }
+  // 8./9. from_ortho of the gradients and the velocity update
+  from_ortho_lane<double2>(c.ycd, dpx, 1, dpx, 1);
+  from_ortho_lane<double2>(c.ycd, dpy, 1, dpy, 1);
+  bool bad = false;
+  for (int k = 0; k < myc; k++) {
+    const double2 a = F[0][k] - dpx[k];
+    const double2 b = F[1][k] - dpy[k];
+    F[0][k] = a;
+    F[1][k] = b;
+    bad |= !(finite_v(a) && finite_v(b) && finite_v(F[2][k]));
+  }
+  if (bad) atomicOr(c.status, 1u);
+}
+
+#undef LANE_PROLOGUE
+
+}  // namespace dev
+
+cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work) {
+  dim3 g(nblocks), b(128);
+  switch (kernel) {
+    case K_LP_BOX_GPX: dev::k_lp_box_gpx<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_X2: dev::k_lp_box_x2<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_X3: dev::k_lp_box_x3<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_X4: dev::k_lp_box_x4<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_Y2: dev::k_lp_box_y2<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_Y3: dev::k_lp_box_y3<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_Y4: dev::k_lp_box_y4<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_BOX_Y5: dev::k_lp_box_y5<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_PER_Y2: dev::k_lp_per_y2<<<g, b, 0, s>>>(cases, work); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace rbc

@@ -128,13 +128,21 @@ size_t smem_per_x_mixed(const CaseDev& c) {
 // ---------------------------------------------------------------------------
 static inline size_t clamp_smem_m(size_t s) { return (s + 127) & ~size_t(127); }
 
-StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops) {
+StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_parallel) {
   StepPlan p;
   auto add = [&](int kernel, int lanes, size_t smem) {
     StepLaunch L;
     L.kernel = kernel;
     L.smem = clamp_smem_m(smem);
     for (int i = 0; i < lanes; i++) L.items.push_back(make_int4(0, i, 1, 0));
+    p.launches.push_back(L);
+  };
+  // one-thread-per-lane kernel: items of up to kLaneThreads consecutive lanes
+  auto add_lp = [&](int kernel, int lanes) {
+    StepLaunch L;
+    L.kernel = kernel;
+    L.smem = 0;
+    for (int i = 0; i < lanes; i += kLaneThreads) L.items.push_back(make_int4(0, i, std::min(kLaneThreads, lanes - i), 0));
     p.launches.push_back(L);
   };
   auto add_gemm = [&](const GemmJobDev& j) {
@@ -167,7 +175,9 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops) {
     for (int f = 0; f < 3; f++) cvp[f] = static_cast<double2*>(c.m_cv) + (size_t)f * kx * ky;
     LaneSideDev co = lane_rows(cvp, 3, kx, ky, ky, LT_F64, true);
     add_gemm(make_gemm_job(qi, co, ops.y2, ny, ky, 1.0, c.status));
-    // Y2: FP64 right-hand sides, banded solves, projection, pressure update
+    // Y2: FP64 right-hand sides, banded solves, projection, pressure update.
+    // One CTA per row even in batches: a thread streaming a whole row through
+    // its nine passes measured 1.7x slower (3.9 vs 2.3 ms per ensemble step)
     add(K_PER_Y2_PRE, mx, dev::smem_per_y2(c));
     return p;
   }
@@ -237,11 +247,22 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops) {
     add_gemm(make_gemm_job(lane_rows(gin, 3, kx, ny, ny, LT_F32, false), lane_rows(cvp, 3, kx, ky, ky, LT_F64, false),
                            ops.y2, ny, ky, 1.0, c.status));
   }
-  // FP64: pressure gradient, Helmholtz (ADI), divergence, Poisson, projection
-  add(K_BOX_GPX, ny, dev::smem_box_gpx(c));
+  // FP64: pressure gradient, Helmholtz (ADI), divergence, Poisson, projection.
+  // In batches each pass uses the faster of its two forms, measured on the
+  // 256-case ensemble (ms per step, CTA per lane vs thread per lane):
+  // gpx 0.16/0.12, y2 0.37/1.39, x2 1.16/0.70, y3 1.34/1.06, x3 0.24/0.42,
+  // y4 0.58/0.34, x4 0.54/0.48, y5 0.63/1.18.  The choice is fixed, so a case
+  // computes the same numbers in any batch.
+  if (lane_parallel) add_lp(K_LP_BOX_GPX, ny);
+  else add(K_BOX_GPX, ny, dev::smem_box_gpx(c));
   add(K_BOX_Y2_PRE, nx, dev::smem_box_y2(c));
-  add(K_BOX_X2, myc, dev::smem_box_x2(c));
-  add(K_BOX_Y3, mxc, dev::smem_box_y3(c));
+  if (lane_parallel) {
+    add_lp(K_LP_BOX_X2, myc);
+    add_lp(K_LP_BOX_Y3, mxc);
+  } else {
+    add(K_BOX_X2, myc, dev::smem_box_x2(c));
+    add(K_BOX_Y3, mxc, dev::smem_box_y3(c));
+  }
   add(K_BOX_X3_MIX, ny, dev::smem_box_x3(c));
   {  // eigenbasis forward along x: s[6] = fwd * m_z (columns j < ny)
     void* zi[1] = {c.m_z};
@@ -249,14 +270,16 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops) {
     add_gemm(make_gemm_job(lane_cols(zi, 1, ny, mxc, ny, LT_F64, 0), lane_cols(zo, 1, ny, mxc, ny, LT_F64, 0), ops.pf,
                            mxc, mxc, 1.0, c.status));
   }
-  add(K_BOX_Y4, mxc, dev::smem_box_y4(c));
+  if (lane_parallel) add_lp(K_LP_BOX_Y4, mxc);
+  else add(K_BOX_Y4, mxc, dev::smem_box_y4(c));
   {  // eigenbasis backward along x: p1 = bwd * s[7] (columns j < myc)
     void* wi[1] = {c.s[7]};
     void* po[1] = {c.p1};
     add_gemm(make_gemm_job(lane_cols(wi, 1, myc, mxc, myc, LT_F64, 0), lane_cols(po, 1, myc, mxc, myc, LT_F64, 0),
                            ops.pb, mxc, mxc, 1.0, c.status));
   }
-  add(K_BOX_X4_MIX, myc, dev::smem_box_x4(c));
+  if (lane_parallel) add_lp(K_LP_BOX_X4, myc);
+  else add(K_BOX_X4_MIX, myc, dev::smem_box_x4(c));
   add(K_BOX_Y5, nx, dev::smem_box_y5(c));
   return p;
 }
@@ -276,7 +299,7 @@ cudaError_t launch_mixed_kernel(int kernel, int nblocks, size_t smem, cudaStream
   switch (kernel) {
     case K_PER_X_MIXED: dev::k_per_x_mixed<<<nblocks, 256, smem, s>>>(cases, work); break;
     case K_BOX_PROD_MIXED: dev::k_box_prod_mixed<<<nblocks, 256, 0, s>>>(cases, work); break;
-    default: return cudaErrorInvalidValue;
+    default: return launch_lane_kernel(kernel, nblocks, s, cases, work);
   }
   return cudaGetLastError();
 }
@@ -301,17 +324,30 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
     const double z = c.kind == KIND_PERIODIC ? 16 : 8;  // spectral element
     const double lanes = it.z > 0 ? it.z : 1;
     double v = 0;
-    switch (L.kernel) {
+    int kernel = L.kernel;
+    switch (kernel) {  // the one-thread-per-lane kernels move the same arrays
+      case K_LP_BOX_GPX: kernel = K_BOX_GPX; break;
+      case K_LP_BOX_X2: kernel = K_BOX_X2; break;
+      case K_LP_BOX_X3: kernel = K_BOX_X3_MIX; break;
+      case K_LP_BOX_X4: kernel = K_BOX_X4_MIX; break;
+      case K_LP_BOX_Y2: kernel = K_BOX_Y2_PRE; break;
+      case K_LP_BOX_Y3: kernel = K_BOX_Y3; break;
+      case K_LP_BOX_Y4: kernel = K_BOX_Y4; break;
+      case K_LP_BOX_Y5: kernel = K_BOX_Y5; break;
+      case K_LP_PER_Y2: kernel = K_PER_Y2_PRE; break;
+      default: break;
+    }
+    switch (kernel) {
       case K_Y1_C: case K_Y1_R: v = 3 * myc * z + 6 * ny * z; break;
       case K_PER_X: v = 6 * mx * z + 2 * nx * 8 + 3 * kx * z; break;
       case K_PER_Y2: case K_PER_Y2_PRE:
-        v = (L.kernel == K_PER_Y2 ? 3 * ny : 3 * ky) * z + 2 * 3 * myc * z + 2 * ny * z + 2 * ny * z + 12 * myc * 8 +
+        v = (kernel == K_PER_Y2 ? 3 * ny : 3 * ky) * z + 2 * 3 * myc * z + 2 * ny * z + 2 * ny * z + 12 * myc * 8 +
             myc * z;
         break;
       case K_PER_X_MIXED: v = 6 * mx * 8 + 2 * nx * 4 + 3 * kx * 8; break;
       case K_BOX_X1: v = 6 * mxc * 8 + 3 * nx * 8 + 3 * kx * 8 + nx * 8; break;
       case K_BOX_Y2: case K_BOX_Y2_PRE:
-        v = (L.kernel == K_BOX_Y2 ? 3 * ny : 3 * ky) * 8 + 6 * myc * 8 + 4 * ny * 8 + 3 * myc * 8;
+        v = (kernel == K_BOX_Y2 ? 3 * ny : 3 * ky) * 8 + 6 * myc * 8 + 4 * ny * 8 + 3 * myc * 8;
         break;
       case K_BOX_X2: v = 3 * nx * 8 + 3 * mxc * 8; break;
       case K_BOX_Y3: v = 6 * myc * 8 + 2 * ny * 8; break;
@@ -338,7 +374,9 @@ const char* step_kernel_name(int kernel) {
   static const char* names[] = {"y1_complex", "y1_real", "periodic_x", "periodic_y2", "box_x1", "box_y2",
                                 "box_x2", "box_y3", "box_x3", "box_y4", "box_x4", "box_y5", "periodic_y2a",
                                 "periodic_y2b", "periodic_y2_pre", "periodic_x_mixed", "box_prod_mixed",
-                                "box_y2_pre", "box_x3_mix", "box_x4_mix", "box_gpx"};
+                                "box_y2_pre", "box_x3_mix", "box_x4_mix", "box_gpx", "lanes_box_gpx",
+                                "lanes_box_x2", "lanes_box_x3", "lanes_box_x4", "lanes_box_y2", "lanes_box_y3",
+                                "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";

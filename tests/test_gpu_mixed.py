@@ -78,13 +78,39 @@ def test_mixed_100_steps_nu_ke(R, name):
         assert abs(a - b) <= NU_KE_TOL[name] * abs(b), (name, what, a, b)
 
 
-def test_mixed_batch_equals_single(R):
-    params = [(64, 33, 1e5, 1.0, 0.005, 1.0, O.PERIODIC), (128, 64, 1e6, 0.7, 2e-3, 1.5, O.PERIODIC),
+MIX_PARAMS = [(64, 33, 1e5, 1.0, 0.005, 1.0, O.PERIODIC), (128, 64, 1e6, 0.7, 2e-3, 1.5, O.PERIODIC),
               (64, 33, 1e6, 7.0, 4e-3, 2.0, O.PERIODIC), (48, 40, 1e6, 0.7, 5e-3, 1.5, O.BOX_CONDUCTING),
               (64, 64, 1e5, 1.0, 0.02, 1.0, O.BOX_ADIABATIC)]
-    b = R.Batch(params, precision=R.PREC_MIXED)
+
+
+def test_mixed_batch_matches_batch_of_one(R):
+    # batches choose per pass between the one-CTA-per-lane and one-thread-per-
+    # lane forms of the FP64 passes (autotuned on the batch), so a case's
+    # numbers match its batch of one up to the roundings of the two forms;
+    # bitwise identity alone vs in a mix is the serving loop's guarantee
+    # (test_gpu_serving.py)
+    b = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
+    print("autotuner:", b.tuning())
+    for i in range(len(MIX_PARAMS)):
+        R.standard_ic(b.cases[i], seed=20 + i)
+    b.update(5)
+    b.synchronize()
+    for i, p in enumerate(MIX_PARAMS):
+        one = R.Batch([p], precision=R.PREC_MIXED)
+        R.standard_ic(one.cases[0], seed=20 + i)
+        one.update(5)
+        one.synchronize()
+        for f in FIELDS:
+            e = rel(b.cases[i].get(f), one.cases[0].get(f))
+            assert e < 1e-10, (i, f, e)
+
+
+def test_mixed_batch_matches_single_case(R):
+    # a single case runs the FP64 passes one CTA per lane (scans): same
+    # arithmetic up to the order of the recurrences' roundings
+    b = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     singles = []
-    for i, p in enumerate(params):
+    for i, p in enumerate(MIX_PARAMS):
         R.standard_ic(b.cases[i], seed=20 + i)
         s = R.Navier2D(*p, precision=R.PREC_MIXED, seed=None)
         R.standard_ic(s, seed=20 + i)
@@ -95,4 +121,5 @@ def test_mixed_batch_equals_single(R):
     b.synchronize()
     for i, s in enumerate(singles):
         for f in FIELDS:
-            assert np.array_equal(b.cases[i].get(f), s.get(f)), (i, f)
+            e = rel(b.cases[i].get(f), s.get(f))
+            assert e < 1e-10, (i, f, e)
