@@ -1036,6 +1036,10 @@ cudaError_t launch_step_kernel(int kernel, int nblocks, size_t smem, cudaStream_
     case K_BOX_X4: dev::k_box_x4<false><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X4_MIX: dev::k_box_x4<true><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_Y5: dev::k_box_y5<<<g, b, smem, s>>>(cases, work); break;
+    case K_PER_Y2_PRE_T128: dev::k_per_y2<true><<<g, dim3(128), smem, s>>>(cases, work); break;
+    case K_BOX_Y2_PRE_T128: dev::k_box_y2<true><<<g, dim3(128), smem, s>>>(cases, work); break;
+    case K_BOX_X3_MIX_T128: dev::k_box_x3<true><<<g, dim3(128), smem, s>>>(cases, work); break;
+    case K_BOX_Y5_T128: dev::k_box_y5<<<g, dim3(128), smem, s>>>(cases, work); break;
     default: return launch_mixed_kernel(kernel, nblocks, smem, s, cases, work);
   }
   return cudaGetLastError();

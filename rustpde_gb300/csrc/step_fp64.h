@@ -18,6 +18,8 @@ enum StepKernel {
   // one thread per lane (batched mixed-precision form, step_lanes.cu)
   K_LP_BOX_GPX, K_LP_BOX_X2, K_LP_BOX_X3, K_LP_BOX_X4, K_LP_BOX_Y2, K_LP_BOX_Y3, K_LP_BOX_Y4, K_LP_BOX_Y5,
   K_LP_PER_Y2,
+  // the same CTA-per-lane kernels launched with 128 threads (more CTAs per SM)
+  K_PER_Y2_PRE_T128, K_BOX_Y2_PRE_T128, K_BOX_X3_MIX_T128, K_BOX_Y5_T128,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };

@@ -176,9 +176,10 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
     LaneSideDev co = lane_rows(cvp, 3, kx, ky, ky, LT_F64, true);
     add_gemm(make_gemm_job(qi, co, ops.y2, ny, ky, 1.0, c.status));
     // Y2: FP64 right-hand sides, banded solves, projection, pressure update.
-    // One CTA per row even in batches: a thread streaming a whole row through
-    // its nine passes measured 1.7x slower (3.9 vs 2.3 ms per ensemble step)
-    add(K_PER_Y2_PRE, mx, dev::smem_per_y2(c));
+    // One CTA per row even in batches (a thread streaming a whole row through
+    // its nine passes measured 1.7x slower: 3.9 vs 2.3 ms per ensemble step);
+    // the batch variant launches it with 128 threads per row instead of 256
+    add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2(c));
     return p;
   }
   // ---- box
@@ -248,14 +249,16 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
                            ops.y2, ny, ky, 1.0, c.status));
   }
   // FP64: pressure gradient, Helmholtz (ADI), divergence, Poisson, projection.
-  // In batches each pass uses the faster of its two forms, measured on the
-  // 256-case ensemble (ms per step, CTA per lane vs thread per lane):
-  // gpx 0.16/0.12, y2 0.37/1.39, x2 1.16/0.70, y3 1.34/1.06, x3 0.24/0.42,
-  // y4 0.58/0.34, x4 0.54/0.48, y5 0.63/1.18.  The choice is fixed, so a case
-  // computes the same numbers in any batch.
+  // The batch variant (lane_parallel) offers each pass in a second form: one
+  // thread per lane where that measured faster on the 256-case ensemble (ms per
+  // step, CTA per lane vs thread per lane: gpx 0.16/0.12, x2 1.16/0.70, y3
+  // 1.34/1.06, y4 0.58/0.34, x4 0.54/0.48), and otherwise the same CTA kernel
+  // with 128 threads (y2 0.37/1.39, x3 0.24/0.42, y5 0.63/1.18 with threads per
+  // lane); rbc_batch_create times both variants of every pass on the batch and
+  // keeps the faster.
   if (lane_parallel) add_lp(K_LP_BOX_GPX, ny);
   else add(K_BOX_GPX, ny, dev::smem_box_gpx(c));
-  add(K_BOX_Y2_PRE, nx, dev::smem_box_y2(c));
+  add(lane_parallel ? K_BOX_Y2_PRE_T128 : K_BOX_Y2_PRE, nx, dev::smem_box_y2(c));
   if (lane_parallel) {
     add_lp(K_LP_BOX_X2, myc);
     add_lp(K_LP_BOX_Y3, mxc);
@@ -263,7 +266,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
     add(K_BOX_X2, myc, dev::smem_box_x2(c));
     add(K_BOX_Y3, mxc, dev::smem_box_y3(c));
   }
-  add(K_BOX_X3_MIX, ny, dev::smem_box_x3(c));
+  add(lane_parallel ? K_BOX_X3_MIX_T128 : K_BOX_X3_MIX, ny, dev::smem_box_x3(c));
   {  // eigenbasis forward along x: s[6] = fwd * m_z (columns j < ny)
     void* zi[1] = {c.m_z};
     void* zo[1] = {c.s[6]};
@@ -280,7 +283,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
   }
   if (lane_parallel) add_lp(K_LP_BOX_X4, myc);
   else add(K_BOX_X4_MIX, myc, dev::smem_box_x4(c));
-  add(K_BOX_Y5, nx, dev::smem_box_y5(c));
+  add(lane_parallel ? K_BOX_Y5_T128 : K_BOX_Y5, nx, dev::smem_box_y5(c));
   return p;
 }
 
@@ -335,6 +338,10 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
       case K_LP_BOX_Y4: kernel = K_BOX_Y4; break;
       case K_LP_BOX_Y5: kernel = K_BOX_Y5; break;
       case K_LP_PER_Y2: kernel = K_PER_Y2_PRE; break;
+      case K_PER_Y2_PRE_T128: kernel = K_PER_Y2_PRE; break;
+      case K_BOX_Y2_PRE_T128: kernel = K_BOX_Y2_PRE; break;
+      case K_BOX_X3_MIX_T128: kernel = K_BOX_X3_MIX; break;
+      case K_BOX_Y5_T128: kernel = K_BOX_Y5; break;
       default: break;
     }
     switch (kernel) {
@@ -376,7 +383,8 @@ const char* step_kernel_name(int kernel) {
                                 "periodic_y2b", "periodic_y2_pre", "periodic_x_mixed", "box_prod_mixed",
                                 "box_y2_pre", "box_x3_mix", "box_x4_mix", "box_gpx", "lanes_box_gpx",
                                 "lanes_box_x2", "lanes_box_x3", "lanes_box_x4", "lanes_box_y2", "lanes_box_y3",
-                                "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2"};
+                                "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2", "periodic_y2_pre_t128",
+                                "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";
