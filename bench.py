@@ -15,6 +15,8 @@ Workloads (--workload):
                       deviation of every mixed case from its FP64 run.
   periodic512         Navier2D::new_periodic(512, 257, Ra=1e7, Pr=1, dt=1e-3,
                       aspect=2), plain FP64, one case.
+  serving             the serving loop alone (see run_serving).
+  precision           batched 1-D stages, FP64 vs mixed (see run_precision).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
@@ -405,6 +407,61 @@ def run_serving(args, n_requests, horizon_scale, n_check=12):
 
 
 # ---------------------------------------------------------------------------
+# precision microbenchmark: batched 1-D stages, FP64 vs mixed
+# ---------------------------------------------------------------------------
+def run_precision(args):
+    """4096 lanes of length N in {128, 256, 512}, Chebyshev-Dirichlet basis:
+    forward, backward, to_ortho, from_ortho and the 1-D Helmholtz solve
+    (c = dt/2, dt = 1e-3), each in FP64 and in the mixed form (tensor-core
+    3xTF32 products, FP64 banded sweep).  Inputs: spectral coefficients
+    g_k exp(-k/20), g ~ N(0, 1) (seed 11).  Per stage: relative L2 error of
+    the mixed result against FP64, and the device time of both forms."""
+    import numpy as np
+
+    import rustpde_gb300 as R
+    from rustpde_gb300 import build
+    build.build()
+    cu = Cudart()
+    lanes = 4096
+    names = {R.OP_FORWARD: "forward", R.OP_BACKWARD: "backward", R.OP_TO_ORTHO: "to_ortho",
+             R.OP_FROM_ORTHO: "from_ortho", R.OP_HHOLTZ: "hholtz"}
+    rng = np.random.default_rng(11)
+    out = {}
+    for n in (128, 256, 512):
+        f64 = R.Lanes(R.Base(1, n), R.PREC_FP64, hholtz_c=5e-4)
+        mix = R.Lanes(R.Base(1, n), R.PREC_MIXED, hholtz_c=5e-4)
+        spec = rng.standard_normal((lanes, f64.m)) * np.exp(-np.arange(f64.m) / 20.0)
+        phys = f64.apply(R.OP_BACKWARD, spec)
+        ortho = f64.apply(R.OP_TO_ORTHO, spec)
+        inputs = {R.OP_FORWARD: phys, R.OP_BACKWARD: spec, R.OP_TO_ORTHO: spec, R.OP_FROM_ORTHO: ortho,
+                  R.OP_HHOLTZ: ortho}
+        row = {}
+        for op, x in inputs.items():
+            il, ol = f64.lengths(op)
+            d_in = R.DeviceArray.from_host(x)
+            d_a, d_b = R.DeviceArray((lanes, ol)), R.DeviceArray((lanes, ol))
+            times = {}
+            for tag, L, d_out in (("fp64", f64, d_a), ("mixed", mix, d_b)):
+                for _ in range(3):
+                    L.apply_dev(op, d_in, d_out, lanes)
+                e0, e1 = cu.event(), cu.event()
+                cu.record(e0, 0)
+                for _ in range(20):
+                    L.apply_dev(op, d_in, d_out, lanes)
+                cu.record(e1, 0)
+                times[tag] = cu.elapsed(e0, e1) / 20
+                cu.destroy(e0, e1)
+            a, b = d_a.to_host(), d_b.to_host()
+            row[names[op]] = {"rel_l2_mixed_vs_fp64": float(np.linalg.norm(b - a) / np.linalg.norm(a)),
+                              "ms_fp64": times["fp64"], "ms_mixed": times["mixed"]}
+        out[f"N={n}"] = row
+    return {"metric": "relative L2 error of the mixed form per stage", "workload": "precision microbenchmark",
+            "config": {"lanes": lanes, "basis": "ChebDirichlet", "N": [128, 256, 512], "hholtz_c": 5e-4,
+                       "inputs": "g_k exp(-k/20), g ~ N(0,1), seed 11"},
+            "stages": out}
+
+
+# ---------------------------------------------------------------------------
 # single periodic 512x257 case, plain FP64
 # ---------------------------------------------------------------------------
 def run_periodic512(args, rank, world, local):
@@ -558,7 +615,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "periodic512", "serving"])
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "periodic512", "serving", "precision"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
     ap.add_argument("--skip-plain", action="store_true",
@@ -576,6 +633,8 @@ def main():
         dist.init_process_group("gloo")
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.workload == "precision":
+        line = run_precision(args)
     elif args.workload == "serving":
         from rustpde_gb300 import build
         build.build()

@@ -181,6 +181,17 @@ int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
 int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes);
 int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes);
 
+/* ---- snapshots -----------------------------------------------------------------
+ * Navier2D::write (navier.rs:975-1013) and Navier2D::read (navier.rs:961-972)
+ * with the reference's dataset layout (groups temp, ux, uy, pres with v and
+ * vhat / vhat_re / vhat_im; x, dx, y, dy; time, ra, pr, nu, kappa) in a
+ * self-describing little-endian binary file ("RBCSNAP1") plus a JSON sidecar
+ * (path + ".json").  Reading restores the spectral fields and the time; a
+ * snapshot of another resolution is broadcast (overlapping low modes copied,
+ * the rest zero), as field/read.rs:116-125. */
+int rbc_write_snapshot(RbcCase* c, const char* path);
+int rbc_read_snapshot(RbcCase* c, const char* path);
+
 /* ---- serving loop ------------------------------------------------------------
  * No reference counterpart (the reference runs one Navier2D per process).  A
  * request is one RBC solve: the case of `params` from the standard initial

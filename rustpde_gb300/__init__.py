@@ -118,6 +118,8 @@ _SIGNATURES = {
     "rbc_batch_layout": (_I, [_P, _IP, _IP]),
     "rbc_batch_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "rbc_batch_state_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
+    "rbc_write_snapshot": (_I, [_P, ctypes.c_char_p]),
+    "rbc_read_snapshot": (_I, [_P, ctypes.c_char_p]),
     "rbc_server_create": (_I, [ctypes.POINTER(RbcServerConfig), ctypes.POINTER(_P)]),
     "rbc_server_submit": (_I, [_P, ctypes.POINTER(RbcParams), _D, ctypes.c_uint64, ctypes.POINTER(ctypes.c_longlong)]),
     "rbc_server_poll": (_I, [_P, ctypes.POINTER(RbcRequestResult), _I, _IP]),
@@ -612,6 +614,15 @@ class Navier2D:
 
     def div_norm(self):
         return self.eval(DIV_NORM)
+
+    def write(self, filename):
+        """Navier2D::write (navier.rs:975-1013): snapshot file + JSON sidecar."""
+        _check(lib().rbc_write_snapshot(self._h, os.fsencode(filename)))
+
+    def read(self, filename):
+        """Navier2D::read (navier.rs:961-972): restore fields and time
+        (broadcast from another resolution)."""
+        _check(lib().rbc_read_snapshot(self._h, os.fsencode(filename)))
 
     def profile_step(self, nsteps=10, with_bytes=False):
         """Mean device time (ms) of each kernel of the step, summed over the

@@ -1936,3 +1936,199 @@ int rbc_server_destroy(RbcServer* S) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Snapshots: Navier2D::write / Navier2D::read (navier.rs:961-1013) in a
+// self-describing binary file (no HDF5 library here) with a JSON sidecar.
+// Datasets follow the reference's HDF5 layout: groups temp, ux, uy, pres with
+// "v" (physical; temp includes the boundary field) and "vhat" (spectral;
+// complex arrays as "vhat_re" / "vhat_im"), the grid "x", "dx", "y", "dy" at
+// the root, and the scalars time, ra, pr, nu, kappa.  Reading restores vhat
+// of each group, broadcasting (copying the overlapping low modes, read.rs:
+// 116-125) when the resolution differs, and the time.
+//
+// File layout (little-endian):
+//   "RBCSNAP1" | u32 version | u32 ndatasets | i32 nx, ny, kind, precision |
+//   f64 dt, aspect | f64 time, ra, pr, nu, kappa |
+//   ndatasets x { char name[32] | i64 rows, cols | u64 offset, bytes } | data
+// ============================================================================
+#include <cstdio>
+#include <fstream>
+
+namespace {
+
+struct SnapEntry {
+  char name[32];
+  int64_t rows, cols;
+  uint64_t offset, bytes;
+};
+
+constexpr char kSnapMagic[8] = {'R', 'B', 'C', 'S', 'N', 'A', 'P', '1'};
+
+void put_dataset(std::vector<SnapEntry>& table, std::vector<std::vector<double>>& blobs, const std::string& name,
+                 int64_t rows, int64_t cols, std::vector<double> data) {
+  SnapEntry e{};
+  std::snprintf(e.name, sizeof e.name, "%s", name.c_str());
+  e.rows = rows;
+  e.cols = cols;
+  e.bytes = data.size() * 8;
+  table.push_back(e);
+  blobs.push_back(std::move(data));
+}
+
+}  // namespace
+
+extern "C" {
+
+int rbc_write_snapshot(RbcCase* c, const char* path) {
+  API_BEGIN
+  require(c && path, "null argument");
+  c->sync();
+  const int nx = c->p.nx, ny = c->p.ny;
+  std::vector<SnapEntry> table;
+  std::vector<std::vector<double>> blobs;
+  const struct { const char* group; int field; } groups[4] = {
+      {"temp", RBC_TEMP}, {"ux", RBC_UX}, {"uy", RBC_UY}, {"pres", RBC_PRES}};
+  std::vector<double> bc((size_t)nx * ny);
+  cuda_check(cudaMemcpy(bc.data(), c->bc_phys, bc.size() * 8, cudaMemcpyDeviceToHost), "d2h");
+  for (const auto& g : groups) {
+    const SpaceDev& s = field_space(c, g.field);
+    // physical values (Field2::backward; the temperature with the boundary field added)
+    space_backward(s, field_ptr(c, g.field), c->phys[0], c->tmp, c->stream);
+    std::vector<double> v((size_t)nx * ny);
+    cuda_check(cudaMemcpyAsync(v.data(), c->phys[0], v.size() * 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    c->sync();
+    if (g.field == RBC_TEMP)
+      for (size_t k = 0; k < v.size(); k++) v[k] += bc[k];
+    put_dataset(table, blobs, std::string(g.group) + "/v", nx, ny, std::move(v));
+    const size_t n = spec_doubles(c, g.field);
+    std::vector<double> vh(n);
+    cuda_check(cudaMemcpy(vh.data(), field_ptr(c, g.field), n * 8, cudaMemcpyDeviceToHost), "d2h");
+    if (s.cplx) {
+      std::vector<double> re(n / 2), im(n / 2);
+      for (size_t k = 0; k < n / 2; k++) {
+        re[k] = vh[2 * k];
+        im[k] = vh[2 * k + 1];
+      }
+      put_dataset(table, blobs, std::string(g.group) + "/vhat_re", s.spec0, s.spec1, std::move(re));
+      put_dataset(table, blobs, std::string(g.group) + "/vhat_im", s.spec0, s.spec1, std::move(im));
+    } else {
+      put_dataset(table, blobs, std::string(g.group) + "/vhat", s.spec0, s.spec1, std::move(vh));
+    }
+  }
+  std::vector<double> x, y;
+  coords(c, RBC_TEMP, x, y);
+  put_dataset(table, blobs, "x", (int64_t)x.size(), 1, x);
+  put_dataset(table, blobs, "dx", (int64_t)x.size(), 1, get_dx(x, c->periodic));
+  put_dataset(table, blobs, "y", (int64_t)y.size(), 1, y);
+  put_dataset(table, blobs, "dy", (int64_t)y.size(), 1, get_dx(y, false));
+  // offsets
+  const uint64_t head = 8 + 4 + 4 + 4 * 4 + 8 * 2 + 8 * 5 + table.size() * sizeof(SnapEntry);
+  uint64_t off = head;
+  for (auto& e : table) {
+    e.offset = off;
+    off += e.bytes;
+  }
+  const std::string tmp_path = std::string(path) + ".partial";
+  {
+    std::ofstream f(tmp_path, std::ios::binary | std::ios::trunc);
+    if (!f) throw ApiError(RBC_ERR_INVALID, std::string("rbc_write_snapshot: cannot open ") + tmp_path);
+    const uint32_t version = 1, nd = (uint32_t)table.size();
+    const int32_t ip[4] = {c->p.nx, c->p.ny, c->p.kind, c->p.precision};
+    const double dp[2] = {c->p.dt, c->p.aspect};
+    const double sc[5] = {c->time, c->p.ra, c->p.pr, c->nu, c->ka};
+    f.write(kSnapMagic, 8);
+    f.write(reinterpret_cast<const char*>(&version), 4);
+    f.write(reinterpret_cast<const char*>(&nd), 4);
+    f.write(reinterpret_cast<const char*>(ip), sizeof ip);
+    f.write(reinterpret_cast<const char*>(dp), sizeof dp);
+    f.write(reinterpret_cast<const char*>(sc), sizeof sc);
+    f.write(reinterpret_cast<const char*>(table.data()), table.size() * sizeof(SnapEntry));
+    for (const auto& b : blobs) f.write(reinterpret_cast<const char*>(b.data()), b.size() * 8);
+    if (!f) throw ApiError(RBC_ERR_INVALID, "rbc_write_snapshot: write failed");
+  }
+  if (std::rename(tmp_path.c_str(), path) != 0)
+    throw ApiError(RBC_ERR_INVALID, std::string("rbc_write_snapshot: cannot create ") + path);
+  // human-readable sidecar
+  std::ofstream js(std::string(path) + ".json", std::ios::trunc);
+  js.precision(17);
+  js << "{\"format\": \"RBCSNAP1\", \"version\": 1, \"binary\": \"" << path << "\",\n"
+     << " \"params\": {\"nx\": " << c->p.nx << ", \"ny\": " << c->p.ny << ", \"kind\": " << c->p.kind
+     << ", \"precision\": " << c->p.precision << ", \"ra\": " << c->p.ra << ", \"pr\": " << c->p.pr
+     << ", \"dt\": " << c->p.dt << ", \"aspect\": " << c->p.aspect << "},\n"
+     << " \"scalars\": {\"time\": " << c->time << ", \"ra\": " << c->p.ra << ", \"pr\": " << c->p.pr
+     << ", \"nu\": " << c->nu << ", \"kappa\": " << c->ka << "},\n \"datasets\": [";
+  for (size_t k = 0; k < table.size(); k++)
+    js << (k ? ",\n  " : "\n  ") << "{\"name\": \"" << table[k].name << "\", \"shape\": [" << table[k].rows << ", "
+       << table[k].cols << "], \"dtype\": \"<f8\", \"offset\": " << table[k].offset << "}";
+  js << "\n ]}\n";
+  API_END
+}
+
+int rbc_read_snapshot(RbcCase* c, const char* path) {
+  API_BEGIN
+  require(c && path, "null argument");
+  std::ifstream f(path, std::ios::binary);
+  if (!f) throw ApiError(RBC_ERR_INVALID, std::string("rbc_read_snapshot: cannot open ") + path);
+  char magic[8];
+  uint32_t version = 0, nd = 0;
+  int32_t ip[4];
+  double dp[2], sc[5];
+  f.read(magic, 8);
+  f.read(reinterpret_cast<char*>(&version), 4);
+  f.read(reinterpret_cast<char*>(&nd), 4);
+  f.read(reinterpret_cast<char*>(ip), sizeof ip);
+  f.read(reinterpret_cast<char*>(dp), sizeof dp);
+  f.read(reinterpret_cast<char*>(sc), sizeof sc);
+  if (!f || std::memcmp(magic, kSnapMagic, 8) != 0 || version != 1 || nd > 4096)
+    throw ApiError(RBC_ERR_INVALID, "rbc_read_snapshot: not a snapshot file of this library");
+  std::vector<SnapEntry> table(nd);
+  f.read(reinterpret_cast<char*>(table.data()), nd * sizeof(SnapEntry));
+  if (!f) throw ApiError(RBC_ERR_INVALID, "rbc_read_snapshot: truncated header");
+  auto find = [&](const std::string& name) -> const SnapEntry* {
+    for (const auto& e : table)
+      if (name == std::string(e.name, strnlen(e.name, sizeof e.name))) return &e;
+    return nullptr;
+  };
+  auto load = [&](const SnapEntry& e) {
+    if (e.rows < 0 || e.cols < 0 || e.bytes != (uint64_t)(e.rows * e.cols) * 8)
+      throw ApiError(RBC_ERR_INVALID, "rbc_read_snapshot: inconsistent dataset entry");
+    std::vector<double> v((size_t)(e.rows * e.cols));
+    f.seekg((std::streamoff)e.offset);
+    f.read(reinterpret_cast<char*>(v.data()), e.bytes);
+    if (!f) throw ApiError(RBC_ERR_INVALID, "rbc_read_snapshot: truncated data");
+    return v;
+  };
+  const struct { const char* group; int field; } groups[4] = {
+      {"temp", RBC_TEMP}, {"ux", RBC_UX}, {"uy", RBC_UY}, {"pres", RBC_PRES}};
+  for (const auto& g : groups) {
+    const SpaceDev& s = field_space(c, g.field);
+    const std::string base = std::string(g.group) + "/vhat";
+    std::vector<double> cur(spec_doubles(c, g.field), 0.0);
+    if (s.cplx) {
+      const SnapEntry* re = find(base + "_re");
+      const SnapEntry* im = find(base + "_im");
+      if (!re || !im) throw ApiError(RBC_ERR_INVALID, "rbc_read_snapshot: missing complex dataset " + base);
+      std::vector<double> vr = load(*re), vi = load(*im);
+      const int64_t r = std::min<int64_t>(re->rows, s.spec0), q = std::min<int64_t>(re->cols, s.spec1);
+      for (int64_t i = 0; i < r; i++)
+        for (int64_t j = 0; j < q; j++) {
+          cur[2 * ((size_t)i * s.spec1 + j)] = vr[(size_t)i * re->cols + j];
+          cur[2 * ((size_t)i * s.spec1 + j) + 1] = vi[(size_t)i * re->cols + j];
+        }
+    } else {
+      const SnapEntry* e = find(base);
+      if (!e) throw ApiError(RBC_ERR_INVALID, "rbc_read_snapshot: missing dataset " + base);
+      std::vector<double> v = load(*e);
+      const int64_t r = std::min<int64_t>(e->rows, s.spec0), q = std::min<int64_t>(e->cols, s.spec1);
+      for (int64_t i = 0; i < r; i++)
+        for (int64_t j = 0; j < q; j++) cur[(size_t)i * s.spec1 + j] = v[(size_t)i * e->cols + j];
+    }
+    c->sync();
+    cuda_check(cudaMemcpy(field_ptr(c, g.field), cur.data(), cur.size() * 8, cudaMemcpyHostToDevice), "h2d");
+  }
+  c->time = sc[0];
+  API_END
+}
+
+}  // extern "C"
