@@ -192,6 +192,27 @@ int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes);
 int rbc_write_snapshot(RbcCase* c, const char* path);
 int rbc_read_snapshot(RbcCase* c, const char* path);
 
+/* ---- statistics and diagnostics series ------------------------------------------
+ * Statistics (src/navier/statistics.rs) on the device, in the `field` space
+ * (ortho x ortho): rbc_stats_reset = Statistics::new (tot_time = current
+ * time); rbc_stats_update = Statistics::update with the case's current state
+ * (running mean of the temperature with the boundary field, the latest ux and
+ * uy, and the Nusselt field (dT/dz / -s + uy T / kappa) 2 s); rbc_stats_write
+ * = Statistics::write (groups temp, ux, uy, nusselt; scalars tot_time,
+ * avg_time, num_save, ka) in the snapshot format.  which: 0 temp, 1 ux, 2 uy,
+ * 3 nusselt. */
+int rbc_stats_reset(RbcCase* c);
+int rbc_stats_update(RbcCase* c);
+int rbc_stats_info(const RbcCase* c, double* tot_time, double* avg_time, long* num_save);
+int rbc_stats_get(RbcCase* c, int which, double* host, size_t n_doubles);
+int rbc_stats_write(RbcCase* c, const char* path);
+/* the diagnostics of Navier2D::callback (navier.rs:819-838): rbc_diag_record
+ * appends (time, Nu, Nuvol, Re) evaluated on the device; rbc_diag_series
+ * copies up to max_entries of them (*n = entries recorded; NULL outputs are
+ * skipped). */
+int rbc_diag_record(RbcCase* c);
+int rbc_diag_series(const RbcCase* c, double* time, double* nu, double* nuvol, double* re, int max_entries, int* n);
+
 /* ---- serving loop ------------------------------------------------------------
  * No reference counterpart (the reference runs one Navier2D per process).  A
  * request is one RBC solve: the case of `params` from the standard initial

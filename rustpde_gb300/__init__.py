@@ -118,6 +118,13 @@ _SIGNATURES = {
     "rbc_batch_layout": (_I, [_P, _IP, _IP]),
     "rbc_batch_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "rbc_batch_state_bytes": (_I, [_P, ctypes.POINTER(_SZ)]),
+    "rbc_stats_reset": (_I, [_P]),
+    "rbc_stats_update": (_I, [_P]),
+    "rbc_stats_info": (_I, [_P, _DP, _DP, ctypes.POINTER(ctypes.c_long)]),
+    "rbc_stats_get": (_I, [_P, _I, _DP, _SZ]),
+    "rbc_stats_write": (_I, [_P, ctypes.c_char_p]),
+    "rbc_diag_record": (_I, [_P]),
+    "rbc_diag_series": (_I, [_P, _DP, _DP, _DP, _DP, _I, _IP]),
     "rbc_write_snapshot": (_I, [_P, ctypes.c_char_p]),
     "rbc_read_snapshot": (_I, [_P, ctypes.c_char_p]),
     "rbc_server_create": (_I, [ctypes.POINTER(RbcServerConfig), ctypes.POINTER(_P)]),
@@ -614,6 +621,39 @@ class Navier2D:
 
     def div_norm(self):
         return self.eval(DIV_NORM)
+
+    # --- statistics (statistics.rs) and the callback's diagnostics series
+    def stats_reset(self):
+        _check(lib().rbc_stats_reset(self._h))
+
+    def stats_update(self):
+        _check(lib().rbc_stats_update(self._h))
+
+    def stats_info(self):
+        t, a, n = _D(), _D(), ctypes.c_long()
+        _check(lib().rbc_stats_info(self._h, ctypes.byref(t), ctypes.byref(a), ctypes.byref(n)))
+        return {"tot_time": t.value, "avg_time": a.value, "num_save": n.value}
+
+    def stats_get(self, which):
+        """which: 0 temperature average, 1 ux, 2 uy, 3 Nusselt field (spectral, field space)."""
+        sh, cx = self.shape(FIELDBC)
+        shape = (sh[0], self.ny)
+        out = np.empty(shape, dtype=np.complex128 if cx else np.float64)
+        _check(lib().rbc_stats_get(self._h, int(which), out.ctypes.data_as(_DP), out.size * (2 if cx else 1)))
+        return out
+
+    def stats_write(self, filename):
+        _check(lib().rbc_stats_write(self._h, os.fsencode(filename)))
+
+    def diag_record(self):
+        _check(lib().rbc_diag_record(self._h))
+
+    def diag_series(self):
+        n = _I()
+        _check(lib().rbc_diag_series(self._h, None, None, None, None, 0, ctypes.byref(n)))
+        arrs = [np.zeros(n.value) for _ in range(4)]
+        _check(lib().rbc_diag_series(self._h, *[_dptr(a) for a in arrs], n.value, ctypes.byref(n)))
+        return dict(zip(("time", "nu", "nuvol", "re"), arrs))
 
     def write(self, filename):
         """Navier2D::write (navier.rs:975-1013): snapshot file + JSON sidecar."""

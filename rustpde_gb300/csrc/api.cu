@@ -193,6 +193,12 @@ struct RbcCase {
   bool own_stream = true;
   bool in_batch = false;
   int* gate_mem = nullptr;  // device int[2] used by the serving loop (CaseDev::gate)
+  // Statistics (statistics.rs): averages in the `field` space, allocated on first use
+  void* st_field[4] = {nullptr, nullptr, nullptr, nullptr};  // temp, ux, uy, nusselt (spectral)
+  double st_tot_time = 0.0, st_avg_time = 0.0;
+  long st_num_save = 0;
+  // diagnostics series recorded by rbc_diag_record (navier.rs:826-838)
+  std::vector<double> dg_time, dg_nu, dg_nuvol, dg_re;
   ~RbcCase() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
@@ -2128,6 +2134,183 @@ int rbc_read_snapshot(RbcCase* c, const char* path) {
     cuda_check(cudaMemcpy(field_ptr(c, g.field), cur.data(), cur.size() * 8, cudaMemcpyHostToDevice), "h2d");
   }
   c->time = sc[0];
+  API_END
+}
+
+}  // extern "C"
+
+// ============================================================================
+// Statistics (src/navier/statistics.rs) and the diagnostics series of
+// Navier2D::callback (navier.rs:826-838), computed on the device.
+// ============================================================================
+namespace {
+
+void stats_alloc(RbcCase* c) {
+  if (c->st_field[0]) return;
+  const size_t bytes = (size_t)c->sp_field.spec0 * c->sp_field.spec1 * (c->periodic ? 16 : 8);
+  for (auto& f : c->st_field) f = c->arena.alloc(bytes);
+}
+
+size_t field_doubles(const RbcCase* c) {
+  return (size_t)c->sp_field.spec0 * c->sp_field.spec1 * (c->periodic ? 2 : 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+int rbc_stats_reset(RbcCase* c) {
+  // Statistics::new (statistics.rs:55-87)
+  API_BEGIN
+  require(c != nullptr, "null case");
+  stats_alloc(c);
+  c->sync();
+  for (auto f : c->st_field) cuda_check(cudaMemset(f, 0, field_doubles(c) * 8), "clear statistics");
+  c->st_tot_time = c->time;
+  c->st_avg_time = 0.0;
+  c->st_num_save = 0;
+  API_END
+}
+
+int rbc_stats_update(RbcCase* c) {
+  // Statistics::update (statistics.rs:127-153) with that = to_ortho(temp) +
+  // to_ortho(fieldbc), uxhat / uyhat = to_ortho of the velocities
+  // (navier.rs:795-800); the Nusselt field as statistics.rs:206-234
+  API_BEGIN
+  require(c != nullptr, "null case");
+  stats_alloc(c);
+  if (c->time < c->st_tot_time) throw ApiError(RBC_ERR_INVALID, "rbc_stats_update: time precedes the statistics");
+  cudaStream_t st = c->stream;
+  const int nx = c->p.nx, ny = c->p.ny;
+  const size_t nd = field_doubles(c), nphys = (size_t)nx * ny;
+  const CaseDev& h = c->hd;
+  void* that = c->spec_tmp[0];
+  space_to_ortho(c->sp_t, h.temp, that, c->tmp, st);
+  phys_combine(3, (const double*)that, (const double*)h.bc_ortho, nullptr, 0, 0, (double*)that, nd, st);
+  const double w = (double)c->st_num_save;
+  phys_combine(7, (const double*)c->st_field[0], (const double*)that, nullptr, w, w + 1.0,
+               (double*)c->st_field[0], nd, st);
+  space_to_ortho(c->sp_u, h.ux, c->st_field[1], c->tmp, st);
+  space_to_ortho(c->sp_u, h.uy, c->st_field[2], c->tmp, st);
+  // nusselt: ((dT/dz / -s_y) + uy T / kappa) * 2 s_y, forward
+  space_backward(c->sp_field, c->st_field[2], c->phys[1], c->tmp, st);  // uy
+  space_backward(c->sp_field, that, c->phys[0], c->tmp, st);            // T
+  void* g = c->spec_tmp[1];
+  space_gradient(c->sp_field, that, g, 0, 1, nullptr, c->tmp, st);
+  phys_combine(6, (const double*)g, nullptr, nullptr, c->scale[1] * -1.0, 0, (double*)g, nd, st);
+  space_backward(c->sp_field, g, c->phys[2], c->tmp, st);  // dT/dz
+  phys_combine(0, c->phys[2], c->phys[0], c->phys[1], c->ka, c->scale[1], c->phys[3], nphys, st);
+  space_forward(c->sp_field, c->phys[3], c->st_field[3], c->tmp, st);
+  c->sync();
+  c->st_num_save += 1;
+  c->st_avg_time += c->time - c->st_tot_time;
+  c->st_tot_time = c->time;
+  API_END
+}
+
+int rbc_stats_info(const RbcCase* c, double* tot_time, double* avg_time, long* num_save) {
+  API_BEGIN
+  require(c && tot_time && avg_time && num_save, "null argument");
+  *tot_time = c->st_tot_time;
+  *avg_time = c->st_avg_time;
+  *num_save = c->st_num_save;
+  API_END
+}
+
+// which: 0 temperature average, 1 ux, 2 uy, 3 Nusselt field (spectral, `field` space)
+int rbc_stats_get(RbcCase* c, int which, double* host, size_t n_doubles) {
+  API_BEGIN
+  require(c && host && which >= 0 && which < 4, "rbc_stats_get: invalid argument");
+  stats_alloc(c);
+  require(n_doubles == field_doubles(c), "rbc_stats_get: size mismatch, expected " + std::to_string(field_doubles(c)));
+  c->sync();
+  cuda_check(cudaMemcpy(host, c->st_field[which], n_doubles * 8, cudaMemcpyDeviceToHost), "d2h");
+  API_END
+}
+
+int rbc_stats_write(RbcCase* c, const char* path) {
+  // Statistics::write (statistics.rs:165-191): groups temp, ux, uy, nusselt
+  // (v and vhat) and the scalars, in the snapshot file format
+  API_BEGIN
+  require(c && path, "null argument");
+  stats_alloc(c);
+  c->sync();
+  const int nx = c->p.nx, ny = c->p.ny;
+  const SpaceDev& s = c->sp_field;
+  std::vector<SnapEntry> table;
+  std::vector<std::vector<double>> blobs;
+  const char* groups[4] = {"temp", "ux", "uy", "nusselt"};
+  for (int k = 0; k < 4; k++) {
+    space_backward(s, c->st_field[k], c->phys[0], c->tmp, c->stream);
+    std::vector<double> v((size_t)nx * ny);
+    cuda_check(cudaMemcpyAsync(v.data(), c->phys[0], v.size() * 8, cudaMemcpyDeviceToHost, c->stream), "d2h");
+    c->sync();
+    put_dataset(table, blobs, std::string(groups[k]) + "/v", nx, ny, std::move(v));
+    std::vector<double> vh(field_doubles(c));
+    cuda_check(cudaMemcpy(vh.data(), c->st_field[k], vh.size() * 8, cudaMemcpyDeviceToHost), "d2h");
+    if (s.cplx) {
+      std::vector<double> re(vh.size() / 2), im(vh.size() / 2);
+      for (size_t q = 0; q < re.size(); q++) { re[q] = vh[2 * q]; im[q] = vh[2 * q + 1]; }
+      put_dataset(table, blobs, std::string(groups[k]) + "/vhat_re", s.spec0, s.spec1, std::move(re));
+      put_dataset(table, blobs, std::string(groups[k]) + "/vhat_im", s.spec0, s.spec1, std::move(im));
+    } else {
+      put_dataset(table, blobs, std::string(groups[k]) + "/vhat", s.spec0, s.spec1, std::move(vh));
+    }
+  }
+  put_dataset(table, blobs, "tot_time", 1, 1, {c->st_tot_time});
+  put_dataset(table, blobs, "avg_time", 1, 1, {c->st_avg_time});
+  put_dataset(table, blobs, "num_save", 1, 1, {(double)c->st_num_save});
+  put_dataset(table, blobs, "ka", 1, 1, {c->ka});
+  std::vector<double> x, y;
+  coords(c, RBC_TEMP, x, y);
+  put_dataset(table, blobs, "x", (int64_t)x.size(), 1, x);
+  put_dataset(table, blobs, "dx", (int64_t)x.size(), 1, get_dx(x, c->periodic));
+  put_dataset(table, blobs, "y", (int64_t)y.size(), 1, y);
+  put_dataset(table, blobs, "dy", (int64_t)y.size(), 1, get_dx(y, false));
+  const uint64_t head = 8 + 4 + 4 + 4 * 4 + 8 * 2 + 8 * 5 + table.size() * sizeof(SnapEntry);
+  uint64_t off = head;
+  for (auto& e : table) { e.offset = off; off += e.bytes; }
+  std::ofstream f(path, std::ios::binary | std::ios::trunc);
+  if (!f) throw ApiError(RBC_ERR_INVALID, std::string("rbc_stats_write: cannot open ") + path);
+  const uint32_t version = 1, nd = (uint32_t)table.size();
+  const int32_t ip[4] = {c->p.nx, c->p.ny, c->p.kind, c->p.precision};
+  const double dp[2] = {c->p.dt, c->p.aspect};
+  const double sc[5] = {c->st_tot_time, c->p.ra, c->p.pr, c->nu, c->ka};
+  f.write(kSnapMagic, 8);
+  f.write(reinterpret_cast<const char*>(&version), 4);
+  f.write(reinterpret_cast<const char*>(&nd), 4);
+  f.write(reinterpret_cast<const char*>(ip), sizeof ip);
+  f.write(reinterpret_cast<const char*>(dp), sizeof dp);
+  f.write(reinterpret_cast<const char*>(sc), sizeof sc);
+  f.write(reinterpret_cast<const char*>(table.data()), table.size() * sizeof(SnapEntry));
+  for (const auto& b : blobs) f.write(reinterpret_cast<const char*>(b.data()), b.size() * 8);
+  if (!f) throw ApiError(RBC_ERR_INVALID, "rbc_stats_write: write failed");
+  API_END
+}
+
+int rbc_diag_record(RbcCase* c) {
+  // Navier2D::callback diagnostics (navier.rs:819-838): time, Nu, Nuvol, Re
+  API_BEGIN
+  require(c != nullptr, "null case");
+  const double nu = eval_case(c, RBC_NU), nuv = eval_case(c, RBC_NUVOL), re = eval_case(c, RBC_RE);
+  c->dg_time.push_back(c->time);
+  c->dg_nu.push_back(nu);
+  c->dg_nuvol.push_back(nuv);
+  c->dg_re.push_back(re);
+  API_END
+}
+
+int rbc_diag_series(const RbcCase* c, double* time, double* nu, double* nuvol, double* re, int max_entries, int* n) {
+  API_BEGIN
+  require(c && n, "null argument");
+  *n = (int)c->dg_time.size();
+  const int k = std::min(*n, std::max(max_entries, 0));
+  for (int i = 0; i < k; i++) {
+    if (time) time[i] = c->dg_time[i];
+    if (nu) nu[i] = c->dg_nu[i];
+    if (nuvol) nuvol[i] = c->dg_nuvol[i];
+    if (re) re[i] = c->dg_re[i];
+  }
   API_END
 }
 

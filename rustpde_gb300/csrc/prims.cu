@@ -475,6 +475,7 @@ __global__ void k_combine(int op, const double* a, const double* b, const double
       case 3: r = a[i] + b[i]; break;
       case 5: r = (a[i] * s0) * s1 + (b[i] * s0) * s1; break;     // (g_xx dt) ka + (g_yy dt) ka
       case 6: r = a[i] / s0; break;
+      case 7: r = (a[i] * s0 + b[i]) / s1; break;                  // running mean (statistics.rs:142-144)
       default: r = a[i] * s0; break;
     }
     out[i] = r;
