@@ -1,6 +1,6 @@
 // lane_gemm.cu -- tcgen05 3xTF32 lane GEMM (see lane_gemm.h).
 //
-// One CTA (4 warps) computes a tile of 128 lanes x NT outputs of one job:
+// One CTA (8 warps) computes a tile of 128 lanes x NT outputs of one job:
 //   * the threads stage a 128 x 32 chunk of the input lanes into shared memory,
 //     converting each value v to TF32 hi = rna(v) and lo = rna(v - hi), written
 //     straight into the K-major core-matrix layout the tensor core reads
@@ -118,17 +118,19 @@ __device__ __forceinline__ bool mma_wait(uint64_t* mbar, uint32_t parity) {
 
 // Input chunk of a tile held in registers between its global loads and its
 // conversion: item (lane l, quad kq) -> 4 consecutive k of one lane.
+constexpr int kItems = 1024 / kGemmThreads;  // (lane, 4-k quad) items per thread per chunk
+
 template <class T>
 struct AChunk {
-  T v[8][4];
+  T v[kItems][4];
 };
 
 template <class T>
 __device__ __forceinline__ void a_load(AChunk<T>& a, const GemmJobDev& J, const char* const* ib, int k0, int tid) {
   const long long es = J.in.elem_stride;
 #pragma unroll
-  for (int it = 0; it < 8; it++) {
-    const int q = tid + 128 * it;
+  for (int it = 0; it < kItems; it++) {
+    const int q = tid + kGemmThreads * it;
     const int llo = q & 7, r = q >> 3;
     const int l = J.in.lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
     const int kq = J.in.lane_fast ? r >> 4 : r & 7;
@@ -145,8 +147,8 @@ template <class T>
 __device__ __forceinline__ void a_store(const AChunk<T>& a, const GemmJobDev& J, unsigned char* Ahi,
                                         unsigned char* Alo, int tid) {
 #pragma unroll
-  for (int it = 0; it < 8; it++) {
-    const int q = tid + 128 * it;
+  for (int it = 0; it < kItems; it++) {
+    const int q = tid + kGemmThreads * it;
     const int llo = q & 7, r = q >> 3;
     const int l = J.in.lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
     const int kq = J.in.lane_fast ? r >> 4 : r & 7;
@@ -168,7 +170,7 @@ __device__ __forceinline__ void a_store(const AChunk<T>& a, const GemmJobDev& J,
 __device__ __forceinline__ void w_issue(const float* wsrc, int c, int NT, unsigned char* wbuf, int tid) {
   const char* g = reinterpret_cast<const char*>(wsrc + (size_t)c * 2 * NT * kGemmKC);
   const uint32_t sb = smem_u32(wbuf);
-  for (int i = tid; i < NT * 16; i += 128) cp_async16(sb + i * 16, g + (size_t)i * 16);
+  for (int i = tid; i < NT * 16; i += kGemmThreads) cp_async16(sb + i * 16, g + (size_t)i * 16);
 }
 
 template <class T>
@@ -187,7 +189,7 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   char** ob = reinterpret_cast<char**>(tail + 16 + kGemmLanes * 8);
   float* stage = reinterpret_cast<float*>(sm);  // [128][33], reuses the A chunk after the last MMA
 
-  {
+  if (tid < kGemmLanes) {
     const int l = lane0 + tid;
     const char* ip = nullptr;
     char* op = nullptr;
@@ -273,16 +275,18 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     const double scale = J.scale;
     const int nbase = tile_n * NT;
     for (int cc = 0; cc < NT; cc += 32) {
-      uint32_t r[32], q[32];
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, r);
-      tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
+      if (warp < 4) {  // warp w reads accumulator lanes 32w .. 32w+31
+        uint32_t r[32], q[32];
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, r);
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
 #pragma unroll
-      for (int j = 0; j < 32; j++)
-        stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
+        for (int j = 0; j < 32; j++)
+          stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
+      }
       __syncthreads();
 #pragma unroll 4
-      for (int it = 0; it < 32; it++) {
-        const int q = tid + 128 * it;
+      for (int it = 0; it < 4096 / kGemmThreads; it++) {
+        const int q = tid + kGemmThreads * it;
         int l, n;
         if (J.out.lane_fast) { l = q & 127; n = q >> 7; }
         else {
@@ -315,13 +319,14 @@ __device__ __forceinline__ void gemm_tile(const GemmJobDev& J, const int lane0, 
 }
 
 // grouped form: tile table entries (job, first lane, output tile, 0)
-__global__ void __launch_bounds__(128) k_lane_gemm(const GemmJobDev* __restrict__ jobs, const int4* __restrict__ tiles) {
+__global__ void __launch_bounds__(kGemmThreads, 2) k_lane_gemm(const GemmJobDev* __restrict__ jobs,
+                                                                const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   gemm_tile(jobs[tl.x], tl.y, tl.z);
 }
 
 // single job passed by value: block b -> lanes (b / ntiles) * 128, output tile b % ntiles
-__global__ void __launch_bounds__(128) k_lane_gemm_one(const __grid_constant__ GemmJobDev J) {
+__global__ void __launch_bounds__(kGemmThreads, 2) k_lane_gemm_one(const __grid_constant__ GemmJobDev J) {
   const int b = blockIdx.x;
   gemm_tile(J, (b / J.ntiles) * kGemmLanes, b % J.ntiles);
 }
@@ -412,7 +417,7 @@ cudaError_t configure_gemm_kernels() {
 cudaError_t launch_lane_gemm_one(const GemmJobDev& job, cudaStream_t st) {
   const int blocks = ((job.lanes + kGemmLanes - 1) / kGemmLanes) * job.ntiles;
   if (blocks <= 0) return cudaSuccess;
-  dev::k_lane_gemm_one<<<blocks, 128, gemm_smem_bytes(job.NT), st>>>(job);
+  dev::k_lane_gemm_one<<<blocks, kGemmThreads, gemm_smem_bytes(job.NT), st>>>(job);
   return cudaGetLastError();
 }
 
@@ -470,7 +475,7 @@ LaneSideDev lane_cols(void* const* ptrs, int nf, int cols, int len, int row_len,
 cudaError_t launch_lane_gemm(const GemmJobDev* jobs, const int4* tiles, int ntiles_total, int max_nt,
                              cudaStream_t st) {
   if (ntiles_total <= 0) return cudaSuccess;
-  dev::k_lane_gemm<<<ntiles_total, 128, gemm_smem_bytes(max_nt), st>>>(jobs, tiles);
+  dev::k_lane_gemm<<<ntiles_total, kGemmThreads, gemm_smem_bytes(max_nt), st>>>(jobs, tiles);
   return cudaGetLastError();
 }
 

@@ -46,7 +46,8 @@ struct GemmJobDev {
   int ntiles;   // ceil(N / NT)
 };
 
-constexpr int kGemmLanes = 128;  // lanes per tile (tcgen05 M)
+constexpr int kGemmLanes = 128;    // lanes per tile (tcgen05 M)
+constexpr int kGemmThreads = 256;  // threads per CTA (warps 0-3 also read the accumulators)
 constexpr int kGemmKC = 32;      // K elements per staged chunk
 
 // Output tile width for N outputs.
