@@ -193,14 +193,16 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
   // during the convection transform REG holds the FFT work lanes; afterwards:
   double2* F = REG;          // 3 lanes composite state (old, then new)
   double2* O = F + 3 * ld;   // 3 lanes
-  double2* R = O + 3 * ld;   // 3 lanes rhs (lane 0 later: divergence)
-  double2* P = R + 3 * ld;   // p0 row
+  // rhs lanes (lane 0 later: divergence); with the convection term given (PRE)
+  // they overwrite the convection lanes, which are dead once the rhs is formed
+  double2* R = PRE ? CV : O + 3 * ld;
+  double2* P = PRE ? O + 3 * ld : R + 3 * ld;  // p0 row
   double2* G = P + ld;       // d/dy
   double2* X1 = G + ld;      // 3 lanes
   const int wld = c.cy.use_fft ? c.cy.L : 1;
   double2* WA = REG;
   double2* WB = WA + 3 * wld;
-  const size_t reg_elems = max((size_t)14 * ld, (size_t)6 * wld);
+  const size_t reg_elems = PRE ? (size_t)11 * ld : max((size_t)14 * ld, (size_t)6 * wld);
   double* FAC = reinterpret_cast<double*>(REG + reg_elems);
   // per-row factors of the three banded solves
   const FdmaDev fu = stage_fdma_row(c.hu_y, i, FAC, tid, nth);
@@ -479,6 +481,11 @@ size_t smem_per_y2(const CaseDev& c) {
   size_t wld = c.cy.use_fft ? c.cy.L : 1;
   size_t reg = std::max((size_t)14 * ld, (size_t)6 * wld);
   return (3 * ld + reg) * 16 + (size_t)12 * c.myc * 8 + 64;
+}
+// k_per_y2<true>: the rhs lanes reuse the convection lanes
+size_t smem_per_y2_pre(const CaseDev& c) {
+  size_t ld = c.ny + 1;
+  return (3 * ld + 11 * ld) * 16 + (size_t)12 * c.myc * 8 + 64;
 }
 
 // ============================================================================

@@ -71,6 +71,7 @@ namespace dev {
 size_t smem_y1(const CaseDev& c, int nr, bool cplx);
 size_t smem_per_x(const CaseDev& c);
 size_t smem_per_y2(const CaseDev& c);
+size_t smem_per_y2_pre(const CaseDev& c);
 size_t smem_per_y2a(const CaseDev& c);
 size_t smem_per_y2b(const CaseDev& c);
 size_t smem_per_x_mixed(const CaseDev& c);

@@ -179,7 +179,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
     // One CTA per row even in batches (a thread streaming a whole row through
     // its nine passes measured 1.7x slower: 3.9 vs 2.3 ms per ensemble step);
     // the batch variant launches it with 128 threads per row instead of 256
-    add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2(c));
+    add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
     return p;
   }
   // ---- box
