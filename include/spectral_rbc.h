@@ -93,6 +93,32 @@ int rbc_random_disturbance(RbcCase* c, double amp, uint64_t seed);
 /* temperature = amp*(2u-1) at interior points (0 on walls), u ~ splitmix64(seed) */
 int rbc_set_temperature_noise(RbcCase* c, double amp, uint64_t seed);
 
+/* ---- solid obstacles (penalisation) ---------------------------------------
+ * rbc_set_solid replaces `navier.solid = Some([mask, value])` (navier.rs:
+ * 189-190): conv_ux, conv_uy and conv_temp subtract (-1/eta) mask w with
+ * eta = 1e-2 and w = ux, uy, T + T_bc - value (navier.rs:551-560, 579-584,
+ * 603-608).  mask, value: physical nx*ny arrays on the temperature grid
+ * (value NULL = 0); mask NULL removes the solid.  FP64 cases stepped on their
+ * own only (RBC_ERR_UNSUPPORTED for batch members and RBC_PREC_MIXED). */
+int rbc_set_solid(RbcCase* c, const double* mask, const double* value, size_t n_doubles);
+/* present = 1 with the mask and value (either may be NULL) when a solid is set */
+int rbc_get_solid(const RbcCase* c, int* present, double* mask, double* value, size_t n_doubles);
+/* Mask generators (src/navier/solid_masks.rs), host only: x (nx), y (ny) are
+ * grid coordinates (e.g. rbc_get_coords of RBC_TEMP); mask, value: nx*ny.
+ *   solid_cylinder_inner      solid_masks.rs:32-55
+ *   solid_roughness_sinusoid  solid_masks.rs:58-98
+ *   solid_porosity            solid_masks.rs:101-140 */
+int rbc_solid_cylinder_inner(const double* x, int nx, const double* y, int ny, double x0, double y0, double radius,
+                             double* mask, double* value);
+int rbc_solid_roughness_sinusoid(const double* x, int nx, const double* y, int ny, double height, double wavenumber,
+                                 double* mask, double* value);
+int rbc_solid_porosity(const double* x, int nx, const double* y, int ny, double diameter, double porosity,
+                       double* mask, double* value);
+/* solid_porosity_interpolate (solid_masks.rs:144-174): the porosity mask on
+ * the 513 x 513 Chebyshev grid, truncated in spectral space to (nx, ny) on
+ * the GPU. */
+int rbc_solid_porosity_interpolate(int nx, int ny, double diameter, double porosity, double* mask, double* value);
+
 /* ---- stepping -------------------------------------------------------------
  * rbc_step: Integrate::update (src/lib.rs:137, navier.rs:737-765), nsteps
  * times, enqueued on the case stream (asynchronous). */
@@ -356,6 +382,35 @@ typedef struct SvSolver SvSolver;
 int sv_create(FsSpace* s, int kind, const double c[2], SvSolver** out);
 int sv_destroy(SvSolver* sv);
 int sv_solve(SvSolver* sv, const double* d_in, double* d_out, void* stream);
+
+/* ---- Diffusion2D (src/navier/diffusion.rs:113-238) ------------------------
+ * df_create replaces Diffusion2D::new(field, kappa, dt) (diffusion.rs:140-153)
+ * for a field on the space (base0, n0) x (base1, n1): composite or Fourier
+ * bases (Fourier along axis 0 only), Hholtz solver with c = dt*kappa on both
+ * axes.  df_step is Integrate::update (diffusion.rs:186-207): rhs =
+ * to_ortho(vhat) + dt force + dt kappa (d2/dx2 + d2/dy2) fieldbc, vhat =
+ * Hholtz.solve(rhs); one CUDA graph per update on the case stream.
+ * df_impulse: diffusion.rs:156-163; df_add_force: :168-171 (real spaces:
+ * the force has field.v's shape and is added in ortho space); df_add_fieldbc:
+ * :176-179 with the boundary field's spectral coefficients on (base0, base1);
+ * df_get_physical: field.backward() (+ fieldbc.v when with_bc, as callback
+ * writes it, :214-225).  State arrays: spectral (spec0 x spec1), interleaved
+ * re/im for a Fourier axis. */
+typedef struct DfCase DfCase;
+int df_create(int base0, int n0, int base1, int n1, double kappa, double dt, DfCase** out);
+int df_destroy(DfCase* d);
+int df_shape(const DfCase* d, int which, int* n0, int* n1, int* is_complex);
+int df_get_state(DfCase* d, double* host, size_t n_doubles);
+int df_set_state(DfCase* d, const double* host, size_t n_doubles);
+int df_impulse(DfCase* d);
+int df_add_force(DfCase* d, const double* force, size_t n_doubles);
+int df_add_fieldbc(DfCase* d, int base0, int base1, const double* vhat, size_t n_doubles);
+int df_step(DfCase* d, int nsteps);
+int df_synchronize(DfCase* d);
+int df_get_time(const DfCase* d, double* t);
+int df_get_dt(const DfCase* d, double* dt);
+int df_get_physical(DfCase* d, int with_bc, double* host, size_t n_doubles);
+int df_get_stream(DfCase* d, void** stream);
 
 #ifdef __cplusplus
 }

@@ -75,6 +75,7 @@ def lib():
                 "or_navier_set_temperature": (None, [P, D, D, D]),
                 "or_navier_set_temperature_noise": (None, [P, D, ctypes.c_uint64]),
                 "or_navier_zero_pressure": (None, [P]),
+                "or_navier_set_solid": (None, [P, DP, DP]),
                 "or_navier_update": (I, [P, I]),
                 "or_navier_time": (D, [P]),
                 "or_navier_set_time": (None, [P, D]),
@@ -239,6 +240,16 @@ class Navier2D:
 
     def zero_pressure(self):
         lib().or_navier_zero_pressure(self._h)
+
+    def set_solid(self, mask, value=None):
+        """``navier.solid = Some([mask, value])`` (navier.rs:189-190); None clears it."""
+        if mask is None:
+            lib().or_navier_set_solid(self._h, None, None)
+            return
+        _, ph, _ = self.shape(TEMP)
+        m = np.ascontiguousarray(mask, dtype=np.float64).reshape(ph)
+        v = np.zeros(ph) if value is None else np.ascontiguousarray(value, dtype=np.float64).reshape(ph)
+        lib().or_navier_set_solid(self._h, _dp(m), _dp(v))
 
     def update(self, nsteps: int = 1):
         if lib().or_navier_update(self._h, int(nsteps)) != 0:
@@ -502,3 +513,80 @@ class Tensor2:
         if h:
             lib().or_tensor_free(h)
             self._h = None
+
+
+# ---------------------------------------------------------------------------
+# Solid masks (src/navier/solid_masks.rs), restated with numpy (elementwise,
+# the same arithmetic per grid point as the reference's loops)
+# ---------------------------------------------------------------------------
+def solid_cylinder_inner(x, y, x0, y0, radius):
+    """solid_masks.rs:32-55: mask 1 inside r < radius - radius/10, tanh layer
+    0.5 (1 - tanh(2 (r - radius) / layer)) up to radius + radius/10; value 0."""
+    x = np.asarray(x, dtype=np.float64)[:, None]
+    y = np.asarray(y, dtype=np.float64)[None, :]
+    layer = radius / 10.0
+    r = np.sqrt((x0 - x) ** 2 + (y0 - y) ** 2)
+    smooth = 0.5 * (1.0 - np.tanh(2.0 * (r - radius) / layer))
+    mask = np.where(r < radius - layer, 1.0, np.where(r < radius + layer, smooth, 0.0))
+    return mask, np.zeros_like(mask)
+
+
+def solid_roughness_sinusoid(x, y, height, wavenumber):
+    """solid_masks.rs:58-98: sinusoidal roughness at both plates, value +0.5
+    (bottom) and -0.5 (top); the top assignment wins where both apply."""
+    x = np.asarray(x, dtype=np.float64)[:, None]
+    y = np.asarray(y, dtype=np.float64)[None, :]
+    bottom, top = y[0, 0], y[0, -1]
+    layer = height / 10.0
+    y_rough = height * (top - bottom) / 2.0 * (np.sin(wavenumber * x) + 0.5)
+    shape = (x.shape[0], y.shape[1])
+    mask = np.zeros(shape)
+    value = np.zeros(shape)
+    for y_dist, val in ((y - bottom, 0.5), (top - y, -0.5)):
+        y_dist = np.broadcast_to(y_dist, shape)
+        yr = np.broadcast_to(y_rough, shape)
+        inside = y_dist <= yr
+        edge = ~inside & (y_dist <= yr + layer)
+        mask = np.where(inside, 1.0, mask)
+        mask = np.where(edge, 0.5 * (1.0 - np.tanh(2.0 * (y_dist - yr) / layer)), mask)
+        value = np.where(inside | edge, val, value)
+    return mask, value
+
+
+def solid_porosity(x, y, diameter, porosity):
+    """solid_masks.rs:101-140: a regular lattice of cylinders whose count per
+    axis is round(sqrt((1 - porosity) 4 L^2 / (pi d^2))); masks are summed."""
+    x = np.asarray(x, dtype=np.float64)
+    y = np.asarray(y, dtype=np.float64)
+    mask = np.zeros((x.size, y.size))
+    radius = diameter / 2.0
+    length = x[-1] - x[0]
+    height = y[-1] - y[0]
+    ncx = np.round(np.sqrt((1.0 - porosity) * 4.0 * length ** 2 / (np.pi * diameter ** 2)))
+    ncy = np.round(np.sqrt((1.0 - porosity) * 4.0 * height ** 2 / (np.pi * diameter ** 2)))
+    dxs = (length - ncx * diameter) / (ncx + 1.0)
+    dys = (height - ncy * diameter) / (ncy + 1.0)
+    ox = x[0] + dxs + radius
+    for _ in range(int(ncx)):
+        oy = y[0] + dys + radius
+        for _ in range(int(ncy)):
+            mask += solid_cylinder_inner(x, y, ox, oy, radius)[0]
+            oy += dys + diameter
+        ox += dxs + diameter
+    return mask, np.zeros_like(mask)
+
+
+def solid_porosity_interpolate(nx, ny, diameter, porosity, n_fine=513):
+    """solid_masks.rs:144-174: porosity mask on the 513 x 513 Chebyshev grid,
+    forward transform, truncation of the coefficients to (nx, ny), backward."""
+    fine = Space2(CHEB, n_fine, CHEB, n_fine)
+    coarse = Space2(CHEB, nx, CHEB, ny)
+    (xf, yf), _ = fine.coords()
+    out = []
+    for arr in solid_porosity(xf, yf, diameter, porosity):
+        vh = fine.forward(arr)
+        vc = np.zeros((nx, ny))
+        a, b = min(nx, n_fine), min(ny, n_fine)
+        vc[:a, :b] = vh[:a, :b]
+        out.append(coarse.backward(vc))
+    return out[0], out[1]

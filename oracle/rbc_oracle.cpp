@@ -866,6 +866,11 @@ template <class T> struct Navier2D {
   double scale[2];
   bool dealias_on = true;
   bool periodic = false;
+  // solid-mask penalisation (navier.rs:189-190, 551-560, 579-584, 603-608):
+  // solid[0] = mask, solid[1] = target temperature, both physical (nx x ny)
+  bool has_solid = false;
+  Arr2<double> solid[2];
+  static constexpr double solid_eta = 1e-2;
 
   void scale_coords() {  // navier.rs:500-512
     Field2<T>* fs[4] = {&temp, &ux, &uy, &pres[0]};
@@ -899,14 +904,20 @@ template <class T> struct Navier2D {
     if (dealias_on) dealias(field.vhat);
     return field.vhat;
   }
+  // conv -= damp with damp = (-1/eta) * mask * w  (navier.rs:579-584)
+  void solid_damp(Arr2<double>& c, const Arr2<double>& w) const {
+    for (size_t i = 0; i < c.v.size(); i++) c.v[i] -= ((-1.0 / solid_eta) * solid[0].v[i]) * w.v[i];
+  }
   Arr2<T> conv_ux(const Arr2<double>& u, const Arr2<double>& v) {
     Arr2<double> c = conv_term(ux, u, 1, 0);
     add(c, conv_term(ux, v, 0, 1));
+    if (has_solid) solid_damp(c, u);
     return conv_finish(c);
   }
   Arr2<T> conv_uy(const Arr2<double>& u, const Arr2<double>& v) {
     Arr2<double> c = conv_term(uy, u, 1, 0);
     add(c, conv_term(uy, v, 0, 1));
+    if (has_solid) solid_damp(c, v);
     return conv_finish(c);
   }
   Arr2<T> conv_temp(const Arr2<double>& u, const Arr2<double>& v) {
@@ -914,6 +925,12 @@ template <class T> struct Navier2D {
     add(c, conv_term(temp, v, 0, 1));
     add(c, conv_term(fieldbc, u, 1, 0));
     add(c, conv_term(fieldbc, v, 0, 1));
+    if (has_solid) {  // navier.rs:551-560: damp = (-1/eta) * mask * (T + T_bc - value)
+      temp.backward();
+      Arr2<double> w(c.n0, c.n1);
+      for (size_t i = 0; i < w.v.size(); i++) w.v[i] = (temp.v.v[i] + fieldbc.v.v[i]) - solid[1].v[i];
+      solid_damp(c, w);
+    }
     return conv_finish(c);
   }
   static void axpy(Arr2<T>& r, const Arr2<T>& x, double a) {  // r += x * a (or r -= via a<0 handled by caller)
@@ -1325,6 +1342,20 @@ int or_navier_update(void* p, int nsteps) {
     g_err = e.what();
     return -1;
   }
+}
+// Navier2D::solid = Some([mask, value]) (navier.rs:189-190); mask == NULL clears it.
+// mask, value: physical nx x ny arrays (value NULL = zeros)
+void or_navier_set_solid(void* p, const double* mask, const double* value) {
+  auto* h = (OrNavier*)p;
+  auto set = [&](auto& n) {
+    if (!mask) { n.has_solid = false; return; }
+    int n0 = n.temp.v.n0, n1 = n.temp.v.n1;
+    n.solid[0] = mk<double>(mask, n0, n1);
+    n.solid[1] = Arr2<double>(n0, n1);
+    if (value) n.solid[1] = mk<double>(value, n0, n1);
+    n.has_solid = true;
+  };
+  if (h->periodic) set(h->per); else set(h->box);
 }
 double or_navier_time(void* p) {
   auto* h = (OrNavier*)p;

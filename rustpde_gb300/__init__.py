@@ -91,6 +91,12 @@ _SIGNATURES = {
     "rbc_set_temperature": (_I, [_P, _D, _D, _D]),
     "rbc_random_disturbance": (_I, [_P, _D, ctypes.c_uint64]),
     "rbc_set_temperature_noise": (_I, [_P, _D, ctypes.c_uint64]),
+    "rbc_set_solid": (_I, [_P, _DP, _DP, _SZ]),
+    "rbc_get_solid": (_I, [_P, _IP, _DP, _DP, _SZ]),
+    "rbc_solid_cylinder_inner": (_I, [_DP, _I, _DP, _I, _D, _D, _D, _DP, _DP]),
+    "rbc_solid_roughness_sinusoid": (_I, [_DP, _I, _DP, _I, _D, _D, _DP, _DP]),
+    "rbc_solid_porosity": (_I, [_DP, _I, _DP, _I, _D, _D, _DP, _DP]),
+    "rbc_solid_porosity_interpolate": (_I, [_I, _I, _D, _D, _DP, _DP]),
     "rbc_step": (_I, [_P, _I]),
     "rbc_synchronize": (_I, [_P]),
     "rbc_get_time": (_I, [_P, _DP]),
@@ -570,6 +576,29 @@ class Navier2D:
     def zero_pressure(self):
         for f in (PRES, PSEUDO_PRES):
             self.set(f, np.zeros_like(self.get(f)))
+
+    # --- solid obstacles (navier.rs:189-190 `pub solid: Option<[Array2<f64>; 2]>`)
+    @property
+    def solid(self):
+        """None, or [mask, value] (physical nx x ny arrays)."""
+        present = _I()
+        _check(lib().rbc_get_solid(self._h, ctypes.byref(present), None, None, 0))
+        if not present.value:
+            return None
+        m, v = np.empty((self.nx, self.ny)), np.empty((self.nx, self.ny))
+        _check(lib().rbc_get_solid(self._h, ctypes.byref(present), _dptr(m), _dptr(v), m.size))
+        return [m, v]
+
+    @solid.setter
+    def solid(self, mv):
+        if mv is None:
+            _check(lib().rbc_set_solid(self._h, None, None, 0))
+            return
+        m = np.ascontiguousarray(mv[0], dtype=np.float64)
+        v = np.ascontiguousarray(mv[1], dtype=np.float64)
+        if m.shape != (self.nx, self.ny) or v.shape != m.shape:
+            raise ValueError(f"solid mask and value must have shape {(self.nx, self.ny)}")
+        _check(lib().rbc_set_solid(self._h, _dptr(m), _dptr(v), m.size))
 
     # --- state
     def shape(self, field):

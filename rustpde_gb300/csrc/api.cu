@@ -13,6 +13,7 @@
 #include "host_ops.h"
 #include "lane_gemm.h"
 #include "prims.h"
+#include "solid_masks.h"
 #include "spectral_rbc.h"
 #include "step_fp64.h"
 
@@ -199,6 +200,10 @@ struct RbcCase {
   long st_num_save = 0;
   // diagnostics series recorded by rbc_diag_record (navier.rs:826-838)
   std::vector<double> dg_time, dg_nu, dg_nuvol, dg_re;
+  // solid mask (navier.rs:189-190): host copies of [mask, value] and the
+  // device arrays [(-1/eta) mask | value] the x pass reads
+  std::vector<double> solid_host[2];
+  double* solid_mem = nullptr;
   ~RbcCase() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
@@ -206,6 +211,7 @@ struct RbcCase {
       cudaStreamSynchronize(stream);
       if (own_stream) cudaStreamDestroy(stream);
     }
+    if (solid_mem) cudaFree(solid_mem);
   }
   size_t spec_elem() const { return periodic ? 16 : 8; }
   void sync() { cuda_check(cudaStreamSynchronize(stream), "stream synchronize"); }
@@ -303,6 +309,8 @@ static size_t state_layout(const RbcParams& p, size_t sizes[5]) {
   for (int k = 0; k < 5; k++) t += (sizes[k] + 255) & ~size_t(255);
   return t;
 }
+
+void capture_graph(RbcCase* c);
 
 // state_region: optional device region of state_layout() bytes that holds the
 // case's spectral state (a batch keeps all its cases' state contiguous).
@@ -452,6 +460,7 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   for (int k = 0; k < 3; k++) c->spec_tmp[k] = A.alloc((size_t)std::max(h.mx, nx) * ny * 16);
   c->bc_vhat = A.alloc((size_t)h.mx * 2 * es);
   c->bc_phys = static_cast<double*>(A.alloc((size_t)nx * ny * 8));
+  h.bc_v = c->bc_phys;
   c->d_red = static_cast<double*>(A.alloc(64));
   // averaging weights on the unscaled coordinates of `field` (average.rs)
   {
@@ -518,7 +527,18 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     c->plan = build_step_plan(h);
   }
   if (!with_graph) return;
-  upload_plan(A, c->plan, c->dp);
+  capture_graph(c);
+}
+
+// Upload the case's plan and capture one update() as a CUDA graph (replacing
+// a previous graph).
+void capture_graph(RbcCase* c) {
+  cudaStream_t st = c->stream;
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+  upload_plan(c->arena, c->plan, c->dp);
   cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t le = cudaSuccess;
   for (size_t k = 0; k < c->plan.launches.size(); k++) {
@@ -748,6 +768,122 @@ int rbc_step(RbcCase* c, int nsteps) {
   for (int s = 0; s < nsteps; s++) {
     cuda_check(cudaGraphLaunch(c->gexec, c->stream), "graph launch");
     c->time += c->p.dt;
+  }
+  API_END
+}
+
+// navier.rs:189-190 (`navier.solid = Some([mask, value])`) with the damping of
+// conv_ux / conv_uy / conv_temp (navier.rs:551-560, 579-584, 603-608).
+int rbc_set_solid(RbcCase* c, const double* mask, const double* value, size_t n_doubles) {
+  API_BEGIN
+  require(c != nullptr, "rbc_set_solid: null case");
+  if (c->in_batch) throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_set_solid: set solid masks on cases stepped on their own");
+  if (c->hd.mixed) throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_set_solid: solid masks need RBC_PREC_FP64");
+  const size_t np = (size_t)c->p.nx * c->p.ny;
+  c->sync();
+  if (mask == nullptr) {
+    c->hd.solid_cm = nullptr;
+    c->hd.solid_val = nullptr;
+    c->solid_host[0].clear();
+    c->solid_host[1].clear();
+  } else {
+    require(n_doubles == np, "rbc_set_solid: mask and value hold nx*ny doubles");
+    const double eta = 1e-2;  // navier.rs:553, 581, 605
+    std::vector<double> dev(2 * np);
+    c->solid_host[0].assign(mask, mask + np);
+    c->solid_host[1].assign(np, 0.0);
+    if (value) c->solid_host[1].assign(value, value + np);
+    for (size_t i = 0; i < np; i++) {
+      dev[i] = (-1.0 / eta) * mask[i];
+      dev[np + i] = c->solid_host[1][i];
+    }
+    if (!c->solid_mem) cuda_check(cudaMalloc(&c->solid_mem, 2 * np * 8), "cudaMalloc solid mask");
+    cuda_check(cudaMemcpy(c->solid_mem, dev.data(), 2 * np * 8, cudaMemcpyHostToDevice), "upload solid mask");
+    c->hd.solid_cm = c->solid_mem;
+    c->hd.solid_val = c->solid_mem + np;
+  }
+  cuda_check(cudaMemcpy(c->d_case, &c->hd, sizeof(CaseDev), cudaMemcpyHostToDevice), "copy case descriptor");
+  // the x pass's lane count (and shared memory) depends on the solid
+  c->plan = build_step_plan(c->hd);
+  capture_graph(c);
+  API_END
+}
+
+int rbc_get_solid(const RbcCase* c, int* present, double* mask, double* value, size_t n_doubles) {
+  API_BEGIN
+  require(c != nullptr && present != nullptr, "rbc_get_solid: null argument");
+  *present = c->solid_host[0].empty() ? 0 : 1;
+  if (*present && (mask || value)) {
+    const size_t np = c->solid_host[0].size();
+    require(n_doubles == np, "rbc_get_solid: mask and value hold nx*ny doubles");
+    if (mask) std::memcpy(mask, c->solid_host[0].data(), np * 8);
+    if (value) std::memcpy(value, c->solid_host[1].data(), np * 8);
+  }
+  API_END
+}
+
+// ---- solid mask generators (src/navier/solid_masks.rs) ----------------------
+int rbc_solid_cylinder_inner(const double* x, int nx, const double* y, int ny, double x0, double y0, double radius,
+                             double* mask, double* value) {
+  API_BEGIN
+  require(x && y && mask && value && nx > 0 && ny > 0, "rbc_solid_cylinder_inner: invalid argument");
+  require(radius > 0, "rbc_solid_cylinder_inner: radius must be positive");
+  solid_cylinder_inner(x, nx, y, ny, x0, y0, radius, mask, value);
+  API_END
+}
+
+int rbc_solid_roughness_sinusoid(const double* x, int nx, const double* y, int ny, double height, double wavenumber,
+                                 double* mask, double* value) {
+  API_BEGIN
+  require(x && y && mask && value && nx > 0 && ny > 1, "rbc_solid_roughness_sinusoid: invalid argument");
+  require(height > 0, "rbc_solid_roughness_sinusoid: height must be positive");
+  solid_roughness_sinusoid(x, nx, y, ny, height, wavenumber, mask, value);
+  API_END
+}
+
+int rbc_solid_porosity(const double* x, int nx, const double* y, int ny, double diameter, double porosity,
+                       double* mask, double* value) {
+  API_BEGIN
+  require(x && y && mask && value && nx > 1 && ny > 1, "rbc_solid_porosity: invalid argument");
+  require(diameter > 0 && porosity >= 0 && porosity <= 1, "rbc_solid_porosity: diameter > 0, porosity in [0, 1]");
+  solid_porosity(x, nx, y, ny, diameter, porosity, mask, value);
+  API_END
+}
+
+// solid_masks.rs:144-174: the porosity mask on a 513 x 513 Chebyshev grid,
+// forward transform, the first (nx, ny) coefficients (broadcast_2d), backward
+// transform on the (nx, ny) Chebyshev grid.  The transforms run on the GPU.
+int rbc_solid_porosity_interpolate(int nx, int ny, double diameter, double porosity, double* mask, double* value) {
+  API_BEGIN
+  require(mask && value && nx >= 4 && ny >= 4 && nx <= 8192 && ny <= 8192,
+          "rbc_solid_porosity_interpolate: invalid argument");
+  require(diameter > 0 && porosity >= 0 && porosity <= 1, "rbc_solid_porosity_interpolate: diameter > 0, porosity in [0, 1]");
+  cuda_check(configure_prim_kernels(), "configure kernels");
+  const int nf = 513;
+  Arena A;
+  SpaceDev fine, coarse;
+  build_space(A, fine, CHEB, nf, CHEB, nf);
+  build_space(A, coarse, CHEB, nx, CHEB, ny);
+  const size_t nff = (size_t)nf * nf, nc = (size_t)nx * ny;
+  std::vector<double> hm(nff), hv(nff);
+  solid_porosity(fine.hb0.x.data(), nf, fine.hb1.x.data(), nf, diameter, porosity, hm.data(), hv.data());
+  double* d_phys = static_cast<double*>(A.alloc(nff * 8));
+  double* d_spec = static_cast<double*>(A.alloc(nff * 8));
+  double* d_cs = static_cast<double*>(A.alloc(nc * 8));
+  double* d_out = static_cast<double*>(A.alloc(nc * 8));
+  void* tmp = A.alloc(std::max(tmp_elems(fine), tmp_elems(coarse)) * 16);
+  cuda_check(cudaDeviceSynchronize(), "allocation");
+  const int r = std::min(nx, nf), q = std::min(ny, nf);
+  double* outs[2] = {mask, value};
+  const std::vector<double>* ins[2] = {&hm, &hv};
+  for (int k = 0; k < 2; k++) {
+    cuda_check(cudaMemcpy(d_phys, ins[k]->data(), nff * 8, cudaMemcpyHostToDevice), "upload mask");
+    space_forward(fine, d_phys, d_spec, tmp, nullptr);
+    cuda_check(cudaMemset(d_cs, 0, nc * 8), "clear");
+    cuda_check(cudaMemcpy2D(d_cs, (size_t)ny * 8, d_spec, (size_t)nf * 8, (size_t)q * 8, r, cudaMemcpyDeviceToDevice),
+               "truncate coefficients");
+    space_backward(coarse, d_cs, d_out, tmp, nullptr);
+    cuda_check(cudaMemcpy(outs[k], d_out, nc * 8, cudaMemcpyDeviceToHost), "download mask");
   }
   API_END
 }
@@ -1501,6 +1637,247 @@ int sv_solve(SvSolver* sv, const double* d_in, double* d_out, void* stream) {
   API_END
 }
 
+// ---- Diffusion2D (src/navier/diffusion.rs:113-238) -------------------------
+}  // extern "C"
+
+struct DfCase {
+  Arena arena;
+  SpaceDev s;
+  SpaceDev sbc;  // space of the boundary field (add_fieldbc)
+  SolverDev sv;
+  double kappa = 0.0, dt = 0.0, time = 0.0;
+  void* vhat = nullptr;   // composite state (spec0 x spec1)
+  void* k = nullptr;      // F pinv_x pinv_y C (spec0 x spec1)
+  void* c_ortho = nullptr;
+  void* bc_vhat = nullptr;
+  double* bc_v = nullptr;  // physical boundary field
+  double* phys = nullptr;
+  void* tmp = nullptr;
+  void* tmp2 = nullptr;
+  std::vector<double> force;  // dt-free force (ortho0 x ortho1, real spaces)
+  bool has_bc = false;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  ~DfCase() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    if (stream) {
+      cudaStreamSynchronize(stream);
+      cudaStreamDestroy(stream);
+    }
+  }
+  size_t es() const { return s.cplx ? 16 : 8; }
+  size_t spec_doubles() const { return (size_t)s.spec0 * s.spec1 * (s.cplx ? 2 : 1); }
+  size_t ortho_doubles() const { return (size_t)s.ortho0 * s.ortho1 * (s.cplx ? 2 : 1); }
+  void sync() { cuda_check(cudaStreamSynchronize(stream), "stream synchronize"); }
+};
+
+namespace {
+// C = dt force + (dt kappa) d2/dx2 fieldbc + (dt kappa) d2/dy2 fieldbc in ortho
+// space (diffusion.rs:192-201), then K = F pinv_x pinv_y C on the device.
+void df_refresh_constant(DfCase* d) {
+  const size_t n = d->ortho_doubles();
+  std::vector<double> c(n, 0.0);
+  if (!d->force.empty())
+    for (size_t i = 0; i < n; i++) c[i] = d->dt * d->force[i];
+  if (d->has_bc) {
+    std::vector<double> gxx(n), gyy(n);
+    space_gradient(d->sbc, d->bc_vhat, d->c_ortho, 2, 0, nullptr, d->tmp, d->stream);
+    cuda_check(cudaMemcpyAsync(gxx.data(), d->c_ortho, n * 8, cudaMemcpyDeviceToHost, d->stream), "d2h");
+    d->sync();
+    space_gradient(d->sbc, d->bc_vhat, d->c_ortho, 0, 2, nullptr, d->tmp, d->stream);
+    cuda_check(cudaMemcpyAsync(gyy.data(), d->c_ortho, n * 8, cudaMemcpyDeviceToHost, d->stream), "d2h");
+    d->sync();
+    const double dk = d->dt * d->kappa;
+    for (size_t i = 0; i < n; i++) c[i] = (c[i] + dk * gxx[i]) + dk * gyy[i];
+  }
+  cuda_check(cudaMemcpyAsync(d->c_ortho, c.data(), n * 8, cudaMemcpyHostToDevice, d->stream), "h2d");
+  diffusion_constant(d->sv, d->s, d->c_ortho, d->k, d->tmp, d->stream);
+  d->sync();
+}
+}  // namespace
+
+extern "C" {
+
+int df_create(int base0, int n0, int base1, int n1, double kappa, double dt, DfCase** out) {
+  API_BEGIN
+  require(out != nullptr, "df_create: null argument");
+  *out = nullptr;
+  require(base0 >= 0 && base0 <= 5 && base1 >= 0 && base1 <= 4, "df_create: unknown base (Fourier along axis 0 only)");
+  require(n0 >= 6 && n1 >= 6 && n0 <= 8192 && n1 <= 8192, "df_create: sizes must be in [6, 8192]");
+  if (base0 == FS_FOURIER_R2C) require(is_pow2(n0), "df_create: Fourier length must be a power of two");
+  require(kappa > 0 && dt > 0, "df_create: kappa and dt must be positive");
+  cuda_check(configure_prim_kernels(), "configure kernels");
+  std::unique_ptr<DfCase> d(new DfCase());
+  d->kappa = kappa;
+  d->dt = dt;
+  build_space(d->arena, d->s, base0, n0, base1, n1);
+  // Hholtz::new(&field, [dt * kappa, dt * kappa]) (diffusion.rs:142)
+  const double c[2] = {dt * kappa, dt * kappa};
+  std::string err;
+  if (!build_solver(d->arena, d->s, SV_KIND_HHOLTZ, c, d->sv, &err))
+    throw ApiError(RBC_ERR_UNSUPPORTED, "df_create: " + err);
+  const size_t es = d->es();
+  d->vhat = d->arena.alloc((size_t)d->s.spec0 * d->s.spec1 * es);
+  d->k = d->arena.alloc((size_t)d->s.spec0 * d->s.spec1 * es);
+  d->c_ortho = d->arena.alloc((size_t)d->s.ortho0 * d->s.ortho1 * es);
+  d->tmp = d->arena.alloc(tmp_elems(d->s) * 16);
+  d->tmp2 = d->arena.alloc(tmp_elems(d->s) * 16);
+  d->phys = static_cast<double*>(d->arena.alloc((size_t)n0 * n1 * 8));
+  cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "stream create");
+  cuda_check(cudaStreamSynchronize(cudaStreamLegacy), "allocation");
+  // one update as a CUDA graph (the constant K stays at its address)
+  cuda_check(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  try {
+    diffusion_step(d->sv, d->s, d->vhat, d->k, d->tmp2, d->stream);
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(d->stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  cuda_check(cudaStreamEndCapture(d->stream, &d->graph), "end capture");
+  cuda_check(cudaGraphInstantiate(&d->gexec, d->graph, 0), "graph instantiate");
+  *out = d.release();
+  API_END
+}
+
+int df_destroy(DfCase* d) {
+  API_BEGIN
+  delete d;
+  API_END
+}
+
+int df_shape(const DfCase* d, int which, int* n0, int* n1, int* is_complex) {
+  API_BEGIN
+  require(d && n0 && n1 && is_complex, "df_shape: null argument");
+  switch (which) {
+    case FS_PHYSICAL: *n0 = d->s.phys0; *n1 = d->s.phys1; *is_complex = 0; break;
+    case FS_SPECTRAL: *n0 = d->s.spec0; *n1 = d->s.spec1; *is_complex = d->s.cplx; break;
+    case FS_ORTHO: *n0 = d->s.ortho0; *n1 = d->s.ortho1; *is_complex = d->s.cplx; break;
+    default: throw ApiError(RBC_ERR_INVALID, "df_shape: unknown array kind");
+  }
+  API_END
+}
+
+int df_get_state(DfCase* d, double* host, size_t n_doubles) {
+  API_BEGIN
+  require(d && host && n_doubles == d->spec_doubles(), "df_get_state: invalid argument");
+  cuda_check(cudaMemcpyAsync(host, d->vhat, n_doubles * 8, cudaMemcpyDeviceToHost, d->stream), "d2h");
+  d->sync();
+  API_END
+}
+
+int df_set_state(DfCase* d, const double* host, size_t n_doubles) {
+  API_BEGIN
+  require(d && host && n_doubles == d->spec_doubles(), "df_set_state: invalid argument");
+  cuda_check(cudaMemcpyAsync(d->vhat, host, n_doubles * 8, cudaMemcpyHostToDevice, d->stream), "h2d");
+  d->sync();
+  API_END
+}
+
+// diffusion.rs:156-163: v = 0 except v[n/2, m/2] = 1, then forward
+int df_impulse(DfCase* d) {
+  API_BEGIN
+  require(d != nullptr, "df_impulse: null argument");
+  const int n0 = d->s.phys0, n1 = d->s.phys1;
+  std::vector<double> v((size_t)n0 * n1, 0.0);
+  v[(size_t)(n0 / 2) * n1 + n1 / 2] = 1.0;
+  cuda_check(cudaMemcpyAsync(d->phys, v.data(), v.size() * 8, cudaMemcpyHostToDevice, d->stream), "h2d");
+  space_forward(d->s, d->phys, d->vhat, d->tmp, d->stream);
+  d->sync();
+  API_END
+}
+
+// diffusion.rs:168-171: the force has the shape of field.v and is added to the
+// ortho-space right-hand side, so real (Chebyshev x Chebyshev) spaces only
+int df_add_force(DfCase* d, const double* force, size_t n_doubles) {
+  API_BEGIN
+  require(d && force, "df_add_force: null argument");
+  require(!d->s.cplx && d->s.ortho0 == d->s.phys0 && d->s.ortho1 == d->s.phys1,
+          "df_add_force: shape mismatch (the force has the physical shape, the right-hand side the ortho shape)");
+  require(n_doubles == (size_t)d->s.phys0 * d->s.phys1, "df_add_force: the force holds n0*n1 doubles");
+  d->force.assign(force, force + n_doubles);
+  df_refresh_constant(d);
+  API_END
+}
+
+// diffusion.rs:176-179: boundary field on the space (base0, base1) of the same
+// sizes; its Laplacian enters the right-hand side (diffusion.rs:197-201)
+int df_add_fieldbc(DfCase* d, int base0, int base1, const double* vhat, size_t n_doubles) {
+  API_BEGIN
+  require(d && vhat, "df_add_fieldbc: null argument");
+  require(base0 >= 0 && base0 <= 5 && base1 >= 0 && base1 <= 4, "df_add_fieldbc: unknown base");
+  require((base0 == FS_FOURIER_R2C) == (d->s.cplx != 0), "df_add_fieldbc: the boundary field's space type differs");
+  SpaceDev sb;
+  build_space(d->arena, sb, base0, d->s.phys0, base1, d->s.phys1);
+  require(sb.ortho0 == d->s.ortho0 && sb.ortho1 == d->s.ortho1, "df_add_fieldbc: shape mismatch");
+  require(n_doubles == (size_t)sb.spec0 * sb.spec1 * (sb.cplx ? 2 : 1), "df_add_fieldbc: vhat size mismatch");
+  d->sbc = sb;
+  d->bc_vhat = d->arena.alloc(n_doubles * 8);
+  d->bc_v = static_cast<double*>(d->arena.alloc((size_t)d->s.phys0 * d->s.phys1 * 8));
+  cuda_check(cudaStreamSynchronize(cudaStreamLegacy), "allocation");
+  cuda_check(cudaMemcpyAsync(d->bc_vhat, vhat, n_doubles * 8, cudaMemcpyHostToDevice, d->stream), "h2d");
+  space_backward(d->sbc, d->bc_vhat, d->bc_v, d->tmp, d->stream);
+  d->has_bc = true;
+  df_refresh_constant(d);
+  API_END
+}
+
+int df_step(DfCase* d, int nsteps) {
+  API_BEGIN
+  require(d != nullptr && nsteps >= 0, "df_step: invalid argument");
+  for (int i = 0; i < nsteps; i++) {
+    cuda_check(cudaGraphLaunch(d->gexec, d->stream), "graph launch");
+    d->time += d->dt;
+  }
+  API_END
+}
+
+int df_synchronize(DfCase* d) {
+  API_BEGIN
+  require(d != nullptr, "df_synchronize: null argument");
+  d->sync();
+  API_END
+}
+
+int df_get_time(const DfCase* d, double* t) {
+  API_BEGIN
+  require(d && t, "df_get_time: null argument");
+  *t = d->time;
+  API_END
+}
+
+int df_get_dt(const DfCase* d, double* dt) {
+  API_BEGIN
+  require(d && dt, "df_get_dt: null argument");
+  *dt = d->dt;
+  API_END
+}
+
+// field.backward() (diffusion.rs:217), plus fieldbc.v when with_bc (diffusion.rs:219-221)
+int df_get_physical(DfCase* d, int with_bc, double* host, size_t n_doubles) {
+  API_BEGIN
+  require(d && host && n_doubles == (size_t)d->s.phys0 * d->s.phys1, "df_get_physical: invalid argument");
+  space_backward(d->s, d->vhat, d->phys, d->tmp, d->stream);
+  cuda_check(cudaMemcpyAsync(host, d->phys, n_doubles * 8, cudaMemcpyDeviceToHost, d->stream), "d2h");
+  d->sync();
+  if (with_bc && d->has_bc) {
+    std::vector<double> bc(n_doubles);
+    cuda_check(cudaMemcpy(bc.data(), d->bc_v, n_doubles * 8, cudaMemcpyDeviceToHost), "d2h");
+    for (size_t i = 0; i < n_doubles; i++) host[i] = host[i] + bc[i];
+  }
+  API_END
+}
+
+int df_get_stream(DfCase* d, void** stream) {
+  API_BEGIN
+  require(d && stream, "df_get_stream: null argument");
+  *stream = d->stream;
+  API_END
+}
+
 }  // extern "C"
 
 // ============================================================================
@@ -2022,6 +2399,8 @@ int rbc_write_snapshot(RbcCase* c, const char* path) {
       put_dataset(table, blobs, std::string(g.group) + "/vhat", s.spec0, s.spec1, std::move(vh));
     }
   }
+  // solid mask (navier.rs:998-1001)
+  if (!c->solid_host[0].empty()) put_dataset(table, blobs, "solid/mask", nx, ny, c->solid_host[0]);
   std::vector<double> x, y;
   coords(c, RBC_TEMP, x, y);
   put_dataset(table, blobs, "x", (int64_t)x.size(), 1, x);

@@ -332,7 +332,7 @@ bool build_solver(Arena& a, const SpaceDev& s, int kind, const double c[2], Solv
 // ---------------------------------------------------------------- generic pass
 enum PassOpCode {
   P_TO_ORTHO = 1, P_FROM_ORTHO, P_DIFF, P_FDIFF, P_DCT_FWD, P_DCT_BWD, P_R2C, P_C2R, P_SCALE, P_MATVEC, P_FDMA,
-  P_DENSE
+  P_DENSE, P_ADD
 };
 struct PassOp {
   int code;
@@ -355,6 +355,8 @@ struct PassDesc {
   int dense_rows, dense_cols;
   double scale;
   int lmax, wl;
+  const void* add;  // P_ADD: A[k] += add[lane*add_ls + k] (complex when in_cplx)
+  long long add_ls;
 };
 
 namespace dev {
@@ -434,6 +436,13 @@ __global__ void __launch_bounds__(128) k_pass(const __grid_constant__ PassDesc d
         break;
       case P_FDMA:
         fdma_solve<double2>(d.fdma, A, 0, 1, lane, 0, tid, nth);
+        break;
+      case P_ADD:
+        for (int k = tid; k < len; k += nth) {
+          long long off = lane * d.add_ls + k;
+          A[k] = A[k] + (d.in_cplx ? static_cast<const double2*>(d.add)[off] : c2(static_cast<const double*>(d.add)[off], 0.0));
+        }
+        __syncthreads();
         break;
       case P_DENSE:
         for (int r = tid; r < d.dense_rows; r += nth) {
@@ -715,6 +724,65 @@ void solver_solve(const SolverDev& sv, const SpaceDev& s, const void* in_ortho, 
   if (sv.dense) {
     PassDesc f = base_desc(s);
     set_axis0(f, t1, cx, out_spec, cx, s.spec1, s.spec0);
+    f.dense = sv.bwd; f.dense_rows = sv.m0; f.dense_cols = sv.m0;
+    add_op(f, P_DENSE);
+    run_pass(f, st);
+  }
+}
+
+// ---------------------------------------------------------------- Diffusion2D
+// Diffusion2D::update (src/navier/diffusion.rs:186-207): rhs = to_ortho(vhat) + C,
+// vhat = Hholtz.solve(rhs).  Operators acting on different axes commute, so
+// the update runs as lane passes over the composite state:
+//   X1 (columns): Sx, pinv_x, eigenbasis forward           vhat -> t0
+//   Y  (rows):    Sy, pinv_y, + K (row i), row i banded solve  t0 -> t1
+//   X2 (columns): eigenbasis backward                       t1 -> vhat
+// with K = F pinv_x pinv_y C.  With a Fourier axis 0 (no x operator) only the
+// Y pass runs, in place on vhat.
+void diffusion_constant(const SolverDev& sv, const SpaceDev& s, const void* c_ortho, void* k_out, void* tmp,
+                        cudaStream_t st) {
+  const int cx = s.cplx;
+  const bool xpass = sv.has_pinv[0] || sv.dense;
+  if (xpass) {
+    PassDesc d = base_desc(s);
+    set_axis0(d, c_ortho, cx, tmp, cx, s.ortho1, s.ortho0);
+    if (sv.has_pinv[0]) { d.pinv = sv.pinv[0]; add_op(d, P_MATVEC); }
+    if (sv.dense) { d.dense = sv.fwd; d.dense_rows = sv.m0; d.dense_cols = sv.m0; add_op(d, P_DENSE); }
+    run_pass(d, st);
+  }
+  PassDesc e = base_desc(s);
+  set_axis1(e, xpass ? tmp : c_ortho, cx, k_out, cx, s.spec0, s.ortho1, s.spec1);
+  if (sv.has_pinv[1]) { e.pinv = sv.pinv[1]; add_op(e, P_MATVEC); }
+  run_pass(e, st);
+}
+
+void diffusion_step(const SolverDev& sv, const SpaceDev& s, void* vhat, const void* k, void* tmp, cudaStream_t st) {
+  const int cx = s.cplx;
+  const bool xpass = s.hb0.composite() || sv.has_pinv[0] || sv.dense;
+  size_t half = tmp_elems(s) / 2;
+  void* t0 = tmp;
+  void* t1 = static_cast<char*>(tmp) + half * 16;
+  if (xpass) {
+    PassDesc d = base_desc(s);
+    set_axis0(d, vhat, cx, t0, cx, s.spec1, s.spec0);
+    d.basis = s.b0;
+    if (s.hb0.composite()) add_op(d, P_TO_ORTHO);
+    if (sv.has_pinv[0]) { d.pinv = sv.pinv[0]; add_op(d, P_MATVEC); }
+    if (sv.dense) { d.dense = sv.fwd; d.dense_rows = sv.m0; d.dense_cols = sv.m0; add_op(d, P_DENSE); }
+    run_pass(d, st);
+  }
+  PassDesc e = base_desc(s);
+  set_axis1(e, xpass ? t0 : vhat, cx, sv.dense ? t1 : vhat, cx, s.spec0, s.spec1, s.spec1);
+  e.basis = s.b1;
+  if (s.hb1.composite()) add_op(e, P_TO_ORTHO);
+  if (sv.has_pinv[1]) { e.pinv = sv.pinv[1]; add_op(e, P_MATVEC); }
+  if (k) { e.add = k; e.add_ls = s.spec1; add_op(e, P_ADD); }
+  e.fdma = sv.rows;
+  add_op(e, P_FDMA);
+  run_pass(e, st);
+  if (sv.dense) {
+    PassDesc f = base_desc(s);
+    set_axis0(f, t1, cx, vhat, cx, s.spec1, s.spec0);
     f.dense = sv.bwd; f.dense_rows = sv.m0; f.dense_cols = sv.m0;
     add_op(f, P_DENSE);
     run_pass(f, st);

@@ -103,6 +103,13 @@ void space_backward_ortho(const SpaceDev& s, const void* ortho, double* phys, vo
 void solver_solve(const SolverDev& sv, const SpaceDev& s, const void* in_ortho, void* out_spec, void* tmp,
                   cudaStream_t st);
 size_t tmp_elems(const SpaceDev& s);
+// Diffusion2D (src/navier/diffusion.rs): K = F pinv_x pinv_y C for the constant
+// ortho-space term C of the right-hand side (spec0 x spec1), and one update of
+// the composite state vhat in place (k may be null: C = 0).  Tensor (Hholtz)
+// solvers only.
+void diffusion_constant(const SolverDev& sv, const SpaceDev& s, const void* c_ortho, void* k_out, void* tmp,
+                        cudaStream_t st);
+void diffusion_step(const SolverDev& sv, const SpaceDev& s, void* vhat, const void* k, void* tmp, cudaStream_t st);
 
 // Batched 1-D operations (FP64) on `lanes` contiguous lanes of one
 // Chebyshev-family basis: forward, backward, to_ortho, from_ortho and the 1-D

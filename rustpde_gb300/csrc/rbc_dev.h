@@ -110,6 +110,12 @@ struct CaseDev {
   const void* bc_diff;    // mx x ny: dt*ka*(d2/dx2 + d2/dy2) fieldbc
   const double* bc_dx;    // nx x ny physical d/dx fieldbc
   const double* bc_dy;    // nx x ny physical d/dy fieldbc
+  const double* bc_v;     // nx x ny physical fieldbc
+
+  // solid-mask penalisation (navier.rs:551-560, 579-584, 603-608); null when
+  // the case has no solid.  The x pass then also transforms the temperature.
+  const double* solid_cm;   // nx x ny: (-1/eta) * mask, eta = 1e-2
+  const double* solid_val;  // nx x ny: temperature imposed inside the solid
 
   // scratch (per case)
   void* yw[6];   // y-pass outputs (Y0, Y1 for ux, uy, temp): mxc x ny

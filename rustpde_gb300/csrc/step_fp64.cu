@@ -96,10 +96,20 @@ size_t smem_y1(const CaseDev& c, int nr, bool cplx) {
   return base + 2 * (size_t)3 * nr * wld * 16 + 64;
 }
 
+// solid-mask damping of the convection products at physical point g
+// (navier.rs:551-560, 579-584, 603-608): conv -= (-1/eta) mask w with
+// w = ux, uy, and T + T_bc - value for the temperature (f = 2)
+__device__ __forceinline__ double solid_damp(const CaseDev& c, int f, size_t g, double p, double u, double v, double t) {
+  const double cm = c.solid_cm[g];
+  const double w = f == 0 ? u : f == 1 ? v : (t + c.bc_v[g]) - c.solid_val[g];
+  return p - cm * w;
+}
+
 // ============================================================================
 // Periodic X pass: one column j of the Y arrays.
 //  u = F^-1 Y0_ux, v = F^-1 Y0_uy;  for f: a = F^-1 (ik/s Y0_f), b = F^-1 Y1_f
 //  P_f = u a + v b (+ u dbc/dx + v dbc/dy for temp);  Q_f = F P_f, rows < kx
+//  With a solid mask a ninth lane carries T = F^-1 Y0_t for the damping term.
 // ============================================================================
 __global__ void __launch_bounds__(256) k_per_x(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
@@ -109,22 +119,24 @@ __global__ void __launch_bounds__(256) k_per_x(const CaseDev* __restrict__ cases
   const int mx = c.mx, nx = c.nx, ny = c.ny, M = c.fx.M;
   const int tid = threadIdx.x, nth = blockDim.x;
   const double inv_asp = 1.0 / c.aspect;
+  const bool solid = c.solid_cm != nullptr;
+  const int NL = solid ? 9 : 8;
   extern __shared__ double2 smem[];
   const int ild = mx + 1;         // input lanes (complex)
-  double2* IN = smem;             // 8 lanes
-  double2* WA = IN + 8 * ild;     // 8 lanes of M
-  double2* WB = WA + 8 * M;
-  double* PH = reinterpret_cast<double*>(IN);  // physical lanes alias the inputs (8 x nx reals)
-  // lane order: Y0u, Y0v, ikY0u, Y1u, ikY0v, Y1v, ikY0t, Y1t
-  for (int idx = tid; idx < 8 * mx; idx += nth) {
+  double2* IN = smem;             // NL lanes
+  double2* WA = IN + NL * ild;    // NL lanes of M
+  double2* WB = WA + NL * M;
+  double* PH = reinterpret_cast<double*>(IN);  // physical lanes alias the inputs (NL x nx reals)
+  // lane order: Y0u, Y0v, ikY0u, Y1u, ikY0v, Y1v, ikY0t, Y1t (, Y0t)
+  for (int idx = tid; idx < NL * mx; idx += nth) {
     int l = idx / mx, k = idx - l * mx;
-    int src = (l < 2) ? 2 * l : (l & 1 ? 2 * ((l - 2) >> 1) + 1 : 2 * ((l - 2) >> 1));
+    int src = (l == 8) ? 4 : (l < 2) ? 2 * l : (l & 1 ? 2 * ((l - 2) >> 1) + 1 : 2 * ((l - 2) >> 1));
     double2 v = static_cast<const double2*>(c.yw[src])[(size_t)k * ny + j];
-    if (l >= 2 && !(l & 1)) v = mul_ik(v, (double)k) * inv_asp;
+    if (l >= 2 && l < 8 && !(l & 1)) v = mul_ik(v, (double)k) * inv_asp;
     IN[l * ild + k] = v;
   }
   __syncthreads();
-  c2r(c.fx, IN, ild, 1, PH, nx, 8, WA, WB, M, tid, nth);
+  c2r(c.fx, IN, ild, 1, PH, nx, NL, WA, WB, M, tid, nth);
   // products into lanes 2, 4, 6
   const double* bx = c.bc_dx;
   const double* by = c.bc_dy;
@@ -137,6 +149,7 @@ __global__ void __launch_bounds__(256) k_per_x(const CaseDev* __restrict__ cases
       p = p + u * bx[(size_t)x * ny + j];
       p = p + v * by[(size_t)x * ny + j];
     }
+    if (solid) p = solid_damp(c, f, (size_t)x * ny + j, p, u, v, PH[8 * nx + x]);
     PH[(2 + 2 * f) * nx + x] = p;
   }
   __syncthreads();
@@ -145,9 +158,10 @@ __global__ void __launch_bounds__(256) k_per_x(const CaseDev* __restrict__ cases
 }
 
 size_t smem_per_x(const CaseDev& c) {
+  const size_t nl = c.solid_cm ? 9 : 8;
   size_t ild = c.mx + 1;
-  size_t in_bytes = std::max((size_t)8 * ild * 16, (size_t)8 * c.nx * 8);
-  return in_bytes + 2 * 8 * (size_t)c.fx.M * 16 + 64;
+  size_t in_bytes = std::max(nl * ild * 16, nl * c.nx * 8);
+  return in_bytes + 2 * nl * (size_t)c.fx.M * 16 + 64;
 }
 
 // ============================================================================
@@ -502,25 +516,27 @@ __global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ case
   const int ld = nx + 1;
   const int tid = threadIdx.x, nth = blockDim.x;
   const double inv_asp = 1.0 / c.aspect;
+  const bool solid = c.solid_cm != nullptr;
+  const int NL = solid ? 9 : 8;
   extern __shared__ double2 smem[];
-  double* IN = reinterpret_cast<double*>(smem);  // 8 lanes composite-x (mxc)
-  double* OR = IN + 8 * ld;                      // 8 ortho lanes (nx)
-  double* PH = OR + 8 * ld;                      // 8 physical lanes
-  double* TMP = PH + 8 * ld;                     // 8 lanes
-  double2* WA = reinterpret_cast<double2*>(TMP + 8 * ld + 2);
+  double* IN = reinterpret_cast<double*>(smem);  // NL lanes composite-x (mxc)
+  double* OR = IN + NL * ld;                     // NL ortho lanes (nx)
+  double* PH = OR + NL * ld;                     // NL physical lanes
+  double* TMP = PH + NL * ld;                    // NL lanes
+  double2* WA = reinterpret_cast<double2*>(TMP + NL * ld + 2);
   WA = reinterpret_cast<double2*>((reinterpret_cast<size_t>(WA) + 15) & ~size_t(15));
   const int wld = c.cx.use_fft ? c.cx.L : 1;
-  double2* WB = WA + 4 * wld;
-  // lanes: 0 Y0u, 1 Y0v, 2 Y0u(dx), 3 Y1u, 4 Y0v(dx), 5 Y1v, 6 Y0t(dx), 7 Y1t
-  for (int idx = tid; idx < 8 * mxc; idx += nth) {
+  double2* WB = WA + ((NL + 1) >> 1) * wld;
+  // lanes: 0 Y0u, 1 Y0v, 2 Y0u(dx), 3 Y1u, 4 Y0v(dx), 5 Y1v, 6 Y0t(dx), 7 Y1t (, 8 Y0t)
+  for (int idx = tid; idx < NL * mxc; idx += nth) {
     int l = idx / mxc, k = idx - l * mxc;
-    int src = (l < 2) ? 2 * l : (l & 1 ? 2 * ((l - 2) >> 1) + 1 : 2 * ((l - 2) >> 1));
+    int src = (l == 8) ? 4 : (l < 2) ? 2 * l : (l & 1 ? 2 * ((l - 2) >> 1) + 1 : 2 * ((l - 2) >> 1));
     IN[l * ld + k] = static_cast<const double*>(c.yw[src])[(size_t)k * ny + j];
   }
   __syncthreads();
-  // x stencils: lanes 0-5 use the velocity basis, 6-7 the temperature basis
+  // x stencils: lanes 0-5 use the velocity basis, 6-8 the temperature basis
   to_ortho<double>(c.xu, IN, ld, OR, ld, 6, tid, nth);
-  to_ortho<double>(c.xt, IN + 6 * ld, ld, OR + 6 * ld, ld, 2, tid, nth);
+  to_ortho<double>(c.xt, IN + 6 * ld, ld, OR + 6 * ld, ld, NL - 6, tid, nth);
   // d/dx for lanes 2, 4, 6 (in place through TMP)
   for (int f = 0; f < 3; f++) {
     double* lane = OR + (2 + 2 * f) * ld;
@@ -528,8 +544,8 @@ __global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ case
     for (int k = tid; k < nx; k += nth) lane[k] = TMP[k] * inv_asp;
     __syncthreads();
   }
-  if (c.cx.use_fft) dct1_fft_r(c.cx, false, OR, ld, PH, ld, 8, WA, WB, wld, tid, nth);
-  else dct1_dense<double>(c.cx, false, OR, ld, PH, ld, 8, tid, nth);
+  if (c.cx.use_fft) dct1_fft_r(c.cx, false, OR, ld, PH, ld, NL, WA, WB, wld, tid, nth);
+  else dct1_dense<double>(c.cx, false, OR, ld, PH, ld, NL, tid, nth);
   // products (lanes 2, 4, 6)
   for (int idx = tid; idx < 3 * nx; idx += nth) {
     int f = idx / nx, x = idx - f * nx;
@@ -539,6 +555,7 @@ __global__ void __launch_bounds__(256) k_box_x1(const CaseDev* __restrict__ case
       p = p + u * c.bc_dx[(size_t)x * ny + j];
       p = p + v * c.bc_dy[(size_t)x * ny + j];
     }
+    if (solid) p = solid_damp(c, f, (size_t)x * ny + j, p, u, v, PH[8 * ld + x]);
     TMP[f * ld + x] = p;
   }
   __syncthreads();
@@ -584,9 +601,10 @@ __global__ void __launch_bounds__(256) k_box_gpx(const CaseDev* __restrict__ cas
 size_t smem_box_gpx(const CaseDev& c) { return 3 * (size_t)(c.nx + 1) * 8 + 64; }
 
 size_t smem_box_x1(const CaseDev& c) {
+  const size_t nl = c.solid_cm ? 9 : 8;
   size_t ld = c.nx + 1;
   size_t wld = c.cx.use_fft ? c.cx.L : 1;
-  return 32 * ld * 8 + 2 * 4 * wld * 16 + 64;
+  return 4 * nl * ld * 8 + 2 * ((nl + 1) / 2) * wld * 16 + 64;
 }
 
 // Y2: rows i < nx (ortho x).  conv (y forward, dealiased), rhs, pinv_y -> s[1..3]
