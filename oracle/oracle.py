@@ -590,3 +590,54 @@ def solid_porosity_interpolate(nx, ny, diameter, porosity, n_fine=513):
         vc[:a, :b] = vh[:a, :b]
         out.append(coarse.backward(vc))
     return out[0], out[1]
+
+
+# ---------------------------------------------------------------------------
+# Diffusion2D (src/navier/diffusion.rs:113-238)
+# ---------------------------------------------------------------------------
+class Diffusion2D:
+    """Oracle Diffusion2D: Hholtz solver with c = [dt kappa, dt kappa]
+    (diffusion.rs:140-153); update = rhs = to_ortho(vhat), + dt force,
+    + dt kappa d2/dx2 fieldbc, + dt kappa d2/dy2 fieldbc, solve
+    (diffusion.rs:186-207), in the reference's operation order."""
+
+    def __init__(self, k0, n0, k1, n1, kappa, dt):
+        self.space = Space2(k0, n0, k1, n1)
+        self.solver = Solver(self.space, HHOLTZ, (dt * kappa, dt * kappa))
+        self.kappa, self.dt = kappa, dt
+        self.vhat = self.space._spec_arr(self.space.spec)
+        self.force = None
+        self.bc = None  # (space, vhat, v)
+        self.time = 0.0
+
+    def impulse(self):
+        """diffusion.rs:156-163"""
+        n, m = self.space.phys
+        v = np.zeros((n, m))
+        v[n // 2, m // 2] = 1.0
+        self.vhat = self.space.forward(v)
+
+    def add_force(self, force):
+        self.force = np.asarray(force, dtype=np.float64).copy()
+
+    def add_fieldbc(self, k0, k1, vhat):
+        sp = Space2(k0, self.space.phys[0], k1, self.space.phys[1])
+        self.bc = (sp, np.array(vhat), sp.backward(vhat))
+
+    def update(self, nsteps=1):
+        for _ in range(nsteps):
+            rhs = self.space.to_ortho(self.vhat)
+            if self.force is not None:
+                rhs = rhs + self.dt * self.force
+            if self.bc is not None:
+                sp, bvh, _ = self.bc
+                rhs = rhs + self.dt * self.kappa * sp.gradient(bvh, (2, 0), None)
+                rhs = rhs + self.dt * self.kappa * sp.gradient(bvh, (0, 2), None)
+            self.vhat = self.solver.solve(rhs)
+            self.time += self.dt
+
+    def physical(self, with_bc=False):
+        v = self.space.backward(self.vhat)
+        if with_bc and self.bc is not None:
+            v = v + self.bc[2]
+        return v

@@ -167,6 +167,20 @@ _SIGNATURES = {
     "fs_lanes_shape": (_I, [_P, _IP, _IP]),
     "fs_lanes_set_hholtz": (_I, [_P, _D]),
     "fs_lanes_apply": (_I, [_P, _I, _P, _P, _I, _P]),
+    "df_create": (_I, [_I, _I, _I, _I, _D, _D, ctypes.POINTER(_P)]),
+    "df_destroy": (_I, [_P]),
+    "df_shape": (_I, [_P, _I, _IP, _IP, _IP]),
+    "df_get_state": (_I, [_P, _DP, _SZ]),
+    "df_set_state": (_I, [_P, _DP, _SZ]),
+    "df_impulse": (_I, [_P]),
+    "df_add_force": (_I, [_P, _DP, _SZ]),
+    "df_add_fieldbc": (_I, [_P, _I, _I, _DP, _SZ]),
+    "df_step": (_I, [_P, _I]),
+    "df_synchronize": (_I, [_P]),
+    "df_get_time": (_I, [_P, _DP]),
+    "df_get_dt": (_I, [_P, _DP]),
+    "df_get_physical": (_I, [_P, _I, _DP, _SZ]),
+    "df_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "sv_create": (_I, [_P, _I, _DP, ctypes.POINTER(_P)]),
     "sv_destroy": (_I, [_P]),
     "sv_solve": (_I, [_P, _P, _P, _P]),
@@ -387,6 +401,97 @@ class Field2:
 
     def gradient(self, deriv, scale=None):
         return self.space.gradient(self.vhat, deriv, scale)
+
+
+class Diffusion2D:
+    """Diffusion2D (src/navier/diffusion.rs:113-238): the fully implicit 2-D
+    diffusion equation on the field's space, stepped on the GPU (df_* of the
+    C library).  ``Diffusion2D(field, kappa, dt)`` takes the field's space and
+    its current ``vhat`` as the initial state."""
+
+    def __init__(self, field: Field2, kappa, dt):
+        sp = field.space
+        h = _P()
+        _check(lib().df_create(sp.base0.kind, sp.base0.n, sp.base1.kind, sp.base1.n, float(kappa), float(dt),
+                               ctypes.byref(h)))
+        self._h = h
+        self.space = sp
+        self.kappa, self.dt = float(kappa), float(dt)
+        self._fieldbc = None
+        self.set_state(field.vhat)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.df_destroy(h)
+            self._h = None
+
+    def _cplx(self):
+        return np.complex128 if self.space.is_complex else np.float64
+
+    def get_state(self):
+        out = np.empty(self.space.spectral, dtype=self._cplx())
+        _check(lib().df_get_state(self._h, out.ctypes.data_as(_DP), out.size * (2 if self.space.is_complex else 1)))
+        return out
+
+    def set_state(self, vhat):
+        a = np.ascontiguousarray(vhat, dtype=self._cplx())
+        if a.shape != tuple(self.space.spectral):
+            raise ValueError(f"shape mismatch: got {a.shape}, expected {self.space.spectral}")
+        _check(lib().df_set_state(self._h, a.ctypes.data_as(_DP), a.size * (2 if self.space.is_complex else 1)))
+
+    @property
+    def vhat(self):
+        return self.get_state()
+
+    def impulse(self):
+        """diffusion.rs:156-163: unit impulse at (n/2, m/2), forward transform."""
+        _check(lib().df_impulse(self._h))
+
+    def add_force(self, force):
+        """diffusion.rs:168-171 (force with field.v's shape)."""
+        f = np.ascontiguousarray(force, dtype=np.float64)
+        if f.shape != tuple(self.space.physical):
+            raise ValueError(f"shape mismatch: got {f.shape}, expected {self.space.physical}")
+        _check(lib().df_add_force(self._h, _dptr(f), f.size))
+
+    def add_fieldbc(self, fieldbc: Field2):
+        """diffusion.rs:176-179: inhomogeneous boundary field (its vhat)."""
+        sp = fieldbc.space
+        if tuple(sp.physical) != tuple(self.space.physical):
+            raise ValueError("shape mismatch between the field and the boundary field")
+        a = np.ascontiguousarray(fieldbc.vhat, dtype=np.complex128 if sp.is_complex else np.float64)
+        _check(lib().df_add_fieldbc(self._h, sp.base0.kind, sp.base1.kind, a.ctypes.data_as(_DP),
+                                    a.size * (2 if sp.is_complex else 1)))
+        self._fieldbc = fieldbc
+
+    def update(self, nsteps: int = 1):
+        """Integrate::update (diffusion.rs:186-207), nsteps times (asynchronous)."""
+        _check(lib().df_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _check(lib().df_synchronize(self._h))
+
+    def get_time(self):
+        t = _D()
+        _check(lib().df_get_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    def get_dt(self):
+        return self.dt
+
+    def get_physical(self, with_bc=False):
+        out = np.empty(self.space.physical)
+        _check(lib().df_get_physical(self._h, int(bool(with_bc)), _dptr(out), out.size))
+        return out
+
+    def callback(self):
+        """The physical field as Diffusion2D::callback writes it (with the
+        boundary field added, diffusion.rs:214-225), returned instead of written."""
+        return self.get_physical(with_bc=True)
+
+    def exit(self):
+        return False
 
 
 OP_FORWARD, OP_BACKWARD, OP_TO_ORTHO, OP_FROM_ORTHO, OP_HHOLTZ = 0, 1, 2, 3, 4
@@ -855,9 +960,32 @@ class Server:
             pass
 
 
-def integrate(pde: Navier2D, max_time: float, save_intervall=None, callback=None):
+MAX_TIMESTEP = 10_000_000
+
+
+def integrate(pde, max_time: float, save_intervall=None, callback=None):
     """integrate() (src/lib.rs:155-187).  ``callback(pde)`` runs at each save
-    interval (Integrate::callback); returning True from it stops the loop."""
+    interval (Integrate::callback); returning True from it stops the loop.
+    A Navier2D runs the loop inside the C library (rbc_integrate); any other
+    object with the Integrate methods (update, get_time, get_dt, callback,
+    exit), e.g. Diffusion2D, runs the same loop here.  Returns the step count."""
+    if not isinstance(pde, Navier2D):
+        timestep = 0
+        dt = pde.get_dt()
+        eps_dt = dt * 1e-4
+        while True:
+            pde.update()
+            timestep += 1
+            t = pde.get_time()
+            if save_intervall:
+                r = t % save_intervall
+                if r < dt / 2.0 or r > save_intervall - dt / 2.0:
+                    out = pde.callback() if callback is None else callback(pde)
+                    if callback is not None and out:
+                        break
+            if t + eps_dt >= max_time or timestep >= MAX_TIMESTEP or pde.exit():
+                break
+        return timestep
     user_cb = callback if callback is not None else (lambda p: None)
 
     def _cb(_h, _t, _u):
