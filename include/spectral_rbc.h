@@ -383,6 +383,39 @@ int sv_create(FsSpace* s, int kind, const double c[2], SvSolver** out);
 int sv_destroy(SvSolver* sv);
 int sv_solve(SvSolver* sv, const double* d_in, double* d_out, void* stream);
 
+/* ---- Navier2DAdjoint (src/navier/navier_adjoint.rs) -----------------------
+ * rbc_adjoint_create replaces Navier2DAdjoint::new (navier_adjoint.rs:151-283,
+ * kind BOX_*) and ::new_periodic (:287-409): params as rbc_create, dt is the
+ * adjoint's pseudo time step, precision RBC_PREC_FP64.  rbc_adjoint_step is
+ * Integrate::update (:767-800): one Navier2D step with dt = 1e-2 gives the
+ * residual, (1 - D2) smooths it, the state advances with the adjoint
+ * convection, diffusion and a projection; one CUDA graph per update.
+ * Fields: RBC_TEMP, RBC_UX, RBC_UY, RBC_PRES, RBC_PSEUDO_PRES (the state,
+ * spectral, as rbc_get_state) and the smoothed residuals below.
+ * rbc_adjoint_eval: Nu, Nuvol, Re (:932-963), KE, |div|.  rbc_adjoint_residual:
+ * the L2 norms of the unsmoothed and the smoothed residual of ux, uy, temp
+ * (:866-874).  rbc_adjoint_exit: NaN divergence or smoothed residual < 1e-8
+ * (:889-906). */
+#define RBC_ADJ_TEMP_RES 10
+#define RBC_ADJ_UX_RES 11
+#define RBC_ADJ_UY_RES 12
+typedef struct RbcAdjoint RbcAdjoint;
+int rbc_adjoint_create(const RbcParams* params, RbcAdjoint** out);
+int rbc_adjoint_destroy(RbcAdjoint* a);
+int rbc_adjoint_set_velocity(RbcAdjoint* a, double amp, double m, double n);    /* :965-968 */
+int rbc_adjoint_set_temperature(RbcAdjoint* a, double amp, double m, double n); /* :969-971 */
+int rbc_adjoint_step(RbcAdjoint* a, int nsteps);
+int rbc_adjoint_synchronize(RbcAdjoint* a);
+int rbc_adjoint_get_time(const RbcAdjoint* a, double* t);
+int rbc_adjoint_set_time(RbcAdjoint* a, double t); /* reset_time :973-976 */
+int rbc_adjoint_field_shape(const RbcAdjoint* a, int field, int* n0, int* n1, int* is_complex);
+int rbc_adjoint_get_state(RbcAdjoint* a, int field, double* host, size_t n_doubles);
+int rbc_adjoint_set_state(RbcAdjoint* a, int field, const double* host, size_t n_doubles);
+int rbc_adjoint_eval(RbcAdjoint* a, int what, double* out);
+int rbc_adjoint_residual(RbcAdjoint* a, double out[6]);
+int rbc_adjoint_exit(RbcAdjoint* a, int* stop);
+int rbc_adjoint_get_stream(RbcAdjoint* a, void** stream);
+
 /* ---- Diffusion2D (src/navier/diffusion.rs:113-238) ------------------------
  * df_create replaces Diffusion2D::new(field, kappa, dt) (diffusion.rs:140-153)
  * for a field on the space (base0, n0) x (base1, n1): composite or Fourier

@@ -81,6 +81,21 @@ def lib():
                 "or_navier_set_time": (None, [P, D]),
                 "or_navier_eval": (D, [P, I]),
                 "or_navier_params": (None, [P, DP]),
+                "or_adjoint_new": (P, [I, I, D, D, D, D, I]),
+                "or_adjoint_free": (None, [P]),
+                "or_adjoint_tensor_pending": (I, [P, I, IP]),
+                "or_adjoint_tensor_get": (None, [P, I, DP, DP]),
+                "or_adjoint_tensor_set": (None, [P, I, DP, DP, DP]),
+                "or_adjoint_shape": (I, [P, I, IP, IP]),
+                "or_adjoint_get": (None, [P, I, DP]),
+                "or_adjoint_set": (None, [P, I, DP]),
+                "or_adjoint_set_velocity": (None, [P, D, D, D]),
+                "or_adjoint_set_temperature": (None, [P, D, D, D]),
+                "or_adjoint_update": (I, [P, I]),
+                "or_adjoint_time": (D, [P]),
+                "or_adjoint_eval": (D, [P, I]),
+                "or_adjoint_exit": (I, [P]),
+                "or_adjoint_residual": (None, [P, DP]),
                 "or_space_new": (P, [I, I, I, I]),
                 "or_space_free": (None, [P]),
                 "or_space_sizes": (I, [P, IP]),
@@ -641,3 +656,76 @@ class Diffusion2D:
         if with_bc and self.bc is not None:
             v = v + self.bc[2]
         return v
+
+
+
+# ---------------------------------------------------------------------------
+# Navier2DAdjoint (src/navier/navier_adjoint.rs)
+# ---------------------------------------------------------------------------
+# adjoint field ids: the state (TEMP, UX, UY, PRES0, PRES1) and the smoothed residuals
+TEMP_RES, UX_RES, UY_RES = 10, 11, 12
+
+
+class Navier2DAdjoint:
+    """Oracle Navier2DAdjoint (navier_adjoint.rs): kind as Navier2D."""
+
+    def __init__(self, nx, ny, ra, pr, dt, aspect, kind):
+        L = lib()
+        self._h = L.or_adjoint_new(int(nx), int(ny), float(ra), float(pr), float(dt), float(aspect), int(kind))
+        if not self._h:
+            raise RuntimeError(L.or_last_error().decode())
+        self.kind = kind
+        self.periodic = kind == PERIODIC
+        for k in range(5):
+            m = ctypes.c_int(0)
+            if L.or_adjoint_tensor_pending(self._h, k, ctypes.byref(m)):
+                mm = m.value
+                a0, c0 = np.zeros((mm, mm)), np.zeros((mm, mm))
+                L.or_adjoint_tensor_get(self._h, k, _dp(a0), _dp(c0))
+                lam, fwd, bwd = tensor_eig(a0, c0)
+                L.or_adjoint_tensor_set(self._h, k, _dp(lam), _dp(fwd), _dp(bwd))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            lib().or_adjoint_free(h)
+            self._h = None
+
+    def get(self, fid):
+        n0, n1 = ctypes.c_int(), ctypes.c_int()
+        cx = lib().or_adjoint_shape(self._h, fid, ctypes.byref(n0), ctypes.byref(n1))
+        out = np.zeros((n0.value, n1.value), dtype=np.complex128 if cx else np.float64)
+        lib().or_adjoint_get(self._h, fid, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        return out
+
+    def set(self, fid, arr):
+        n0, n1 = ctypes.c_int(), ctypes.c_int()
+        cx = lib().or_adjoint_shape(self._h, fid, ctypes.byref(n0), ctypes.byref(n1))
+        a = _f64(arr, (n0.value, n1.value), bool(cx))
+        lib().or_adjoint_set(self._h, fid, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+
+    def set_velocity(self, amp, m, n):
+        lib().or_adjoint_set_velocity(self._h, amp, m, n)
+
+    def set_temperature(self, amp, m, n):
+        lib().or_adjoint_set_temperature(self._h, amp, m, n)
+
+    def update(self, nsteps: int = 1):
+        if lib().or_adjoint_update(self._h, int(nsteps)) != 0:
+            raise RuntimeError(lib().or_last_error().decode())
+
+    @property
+    def time(self):
+        return lib().or_adjoint_time(self._h)
+
+    def eval(self, what):
+        return lib().or_adjoint_eval(self._h, what)
+
+    def exit(self):
+        return bool(lib().or_adjoint_exit(self._h))
+
+    def residual(self):
+        """(|u|, |v|, |T|) of the unsmoothed and of the smoothed residual."""
+        out = np.zeros(6)
+        lib().or_adjoint_residual(self._h, _dp(out))
+        return out

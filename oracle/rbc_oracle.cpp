@@ -1169,6 +1169,223 @@ template <> void Navier2D<cplx>::build(int nx, int ny, double ra_, double pr_, d
   fieldbc.forward();
 }
 
+// ---------------------------------------------------------------------------
+// Navier2DAdjoint (navier_adjoint.rs): adjoint descent towards steady states
+// (Farazmand 2016).  Each update runs one Navier2D step (dt_navier = 1e-2) to
+// form the residual, smooths it with (1 - D2) Hholtz solves, and advances the
+// state with the adjoint convection, explicit diffusion and a projection.
+// ---------------------------------------------------------------------------
+template <class T> struct Navier2DAdjoint {
+  Navier2D<T> navier;
+  Field2<T> field, temp[2], ux[2], uy[2], pres[2], fieldbc;
+  Solver2 solver;        // Poisson on pres[1]
+  Solver2 smoother[3];   // Hholtz (1 - D2) for ux, uy, temp
+  Arr2<T> unsmoothed[3];
+  double nu, ka, ra, pr, time = 0.0, dt, dt_navier = 1e-2;
+  double scale[2];
+  bool periodic = false;
+  bool dealias_on = true;
+  double res_tol = 1e-8;  // navier_adjoint.rs:120
+
+  void build(int nx, int ny, double ra_, double pr_, double dt_, double aspect, int kind) {
+    // navier_adjoint.rs:151-283 (box) and :287-409 (periodic)
+    periodic = kind == 2;
+    ra = ra_; pr = pr_; dt = dt_;
+    scale[0] = aspect; scale[1] = 1.0;
+    nu = get_nu(ra, pr, scale[1] * 2.0);
+    ka = get_ka(ra, pr, scale[1] * 2.0);
+    navier.build(nx, ny, ra, pr, dt_navier, aspect, kind);
+    int xu = periodic ? FOURIER : CD, xt = periodic ? FOURIER : (kind == 0 ? CN : CD);
+    int xo = periodic ? FOURIER : CHEB, xp = periodic ? FOURIER : CN;
+    for (int k = 0; k < 2; k++) {
+      ux[k] = Field2<T>(Space2<T>(Base(xu, nx), Base(CD, ny)));
+      uy[k] = Field2<T>(Space2<T>(Base(xu, nx), Base(CD, ny)));
+      temp[k] = Field2<T>(Space2<T>(Base(xt, nx), Base(CD, ny)));
+    }
+    pres[0] = Field2<T>(Space2<T>(Base(xo, nx), Base(CHEB, ny)));
+    pres[1] = Field2<T>(Space2<T>(Base(xp, nx), Base(CN, ny)));
+    field = Field2<T>(Space2<T>(Base(xo, nx), Base(CHEB, ny)));
+    double cp[2] = {1.0 / std::pow(scale[0], 2.0), 1.0 / std::pow(scale[1], 2.0)};
+    solver.build(pres[1].space, S_POISSON, cp);
+    const double w = 1e0;  // weight_laplacian
+    double cs[2] = {w / std::pow(scale[0], 2.0), w / std::pow(scale[1], 2.0)};
+    smoother[0].build(ux[1].space, S_HHOLTZ, cs);
+    smoother[1].build(uy[1].space, S_HHOLTZ, cs);
+    smoother[2].build(temp[1].space, S_HHOLTZ, cs);
+    // _scale (navier_adjoint.rs:419-438)
+    Field2<T>* fs[7] = {&temp[0], &ux[0], &uy[0], &pres[0], &temp[1], &ux[1], &uy[1]};
+    for (auto f : fs) {
+      for (auto& e : f->x[0]) e *= scale[0];
+      for (auto& e : f->x[1]) e *= scale[1];
+      for (auto& e : f->dx[0]) e *= scale[0];
+      for (auto& e : f->dx[1]) e *= scale[1];
+    }
+    fieldbc = navier.fieldbc;  // set_temp_bc(Navier2D::bc_rbc(nx, ny)), the same construction
+  }
+  Solver2* tensor_solver(int k) {
+    switch (k) {
+      case 0: return &navier.solver[3];
+      case 1: return &solver;
+      default: return &smoother[k - 2];
+    }
+  }
+  static void add(Arr2<double>& a, const Arr2<double>& b) { for (size_t i = 0; i < a.v.size(); i++) a.v[i] += b.v[i]; }
+  static T mulT(T a, T b) { return Navier2D<T>::mulT(a, b); }
+  // conv_term.rs:22-42 on this solver's `field`
+  Arr2<double> conv_term(const Field2<T>& f, const Arr2<double>& u, int d0, int d1) {
+    field.vhat = f.gradient(d0, d1, scale);
+    field.backward();
+    Arr2<double> r(u.n0, u.n1);
+    for (size_t i = 0; i < r.v.size(); i++) r.v[i] = u.v[i] * field.v.v[i];
+    return r;
+  }
+  Arr2<T> conv_finish(const Arr2<double>& conv) {
+    field.v = conv;
+    field.forward();
+    if (dealias_on) {  // navier.rs:1022-1032
+      Arr2<T>& vh = field.vhat;
+      int nxk = vh.n0 * 2 / 3, nyk = vh.n1 * 2 / 3;
+      for (int i = 0; i < vh.n0; i++)
+        for (int j = 0; j < vh.n1; j++)
+          if (i >= nxk || j >= nyk) vh(i, j) = T(0);
+    }
+    return field.vhat;
+  }
+  // navier_adjoint.rs:541-577
+  Arr2<T> conv_ux(const Arr2<double>& u, const Arr2<double>& v, const Arr2<double>& t) {
+    Arr2<double> c = conv_term(ux[1], u, 1, 0);
+    add(c, conv_term(ux[1], v, 0, 1));
+    add(c, conv_term(ux[1], u, 1, 0));
+    add(c, conv_term(uy[1], v, 1, 0));
+    add(c, conv_term(temp[1], t, 1, 0));
+    add(c, conv_term(temp[1], fieldbc.v, 1, 0));
+    return conv_finish(c);
+  }
+  // navier_adjoint.rs:579-611
+  Arr2<T> conv_uy(const Arr2<double>& u, const Arr2<double>& v, const Arr2<double>& t) {
+    Arr2<double> c = conv_term(uy[1], u, 1, 0);
+    add(c, conv_term(uy[1], v, 0, 1));
+    add(c, conv_term(ux[1], u, 0, 1));
+    add(c, conv_term(uy[1], v, 0, 1));
+    add(c, conv_term(temp[1], t, 0, 1));
+    add(c, conv_term(temp[1], fieldbc.v, 0, 1));
+    return conv_finish(c);
+  }
+  // navier_adjoint.rs:613-628
+  Arr2<T> conv_temp(const Arr2<double>& u, const Arr2<double>& v) {
+    Arr2<double> c = conv_term(temp[1], u, 1, 0);
+    add(c, conv_term(temp[1], v, 0, 1));
+    return conv_finish(c);
+  }
+  static void add_scaled(Arr2<T>& r, const Arr2<T>& x, double a) { for (size_t i = 0; i < r.v.size(); i++) r.v[i] += rmul(x.v[i], a); }
+  static void sub_scaled(Arr2<T>& r, const Arr2<T>& x, double a) { for (size_t i = 0; i < r.v.size(); i++) r.v[i] -= rmul(x.v[i], a); }
+  static void add_scaled2(Arr2<T>& r, const Arr2<T>& x, double a, double b) {
+    for (size_t i = 0; i < r.v.size(); i++) r.v[i] += rmul(rmul(x.v[i], a), b);
+  }
+  // navier_adjoint.rs:630-653 / 655-678: explicit update of the velocity
+  void solve_u(int which, const Arr2<double>& u, const Arr2<double>& v, const Arr2<double>& t) {
+    Field2<T>& f0 = which == 0 ? ux[0] : uy[0];
+    Field2<T>& f1 = which == 0 ? ux[1] : uy[1];
+    Arr2<T> rhs = f0.to_ortho();
+    sub_scaled(rhs, which == 0 ? pres[0].gradient(1, 0, scale) : pres[0].gradient(0, 1, scale), dt);
+    Arr2<T> conv = which == 0 ? conv_ux(u, v, t) : conv_uy(u, v, t);
+    add_scaled(rhs, conv, dt);
+    add_scaled2(rhs, f1.gradient(2, 0, scale), dt, nu);
+    add_scaled2(rhs, f1.gradient(0, 2, scale), dt, nu);
+    f0.from_ortho(rhs);
+  }
+  // navier_adjoint.rs:680-695
+  void solve_temp(const Arr2<double>& u, const Arr2<double>& v) {
+    Arr2<T> rhs = temp[0].to_ortho();
+    Arr2<T> conv = conv_temp(u, v);
+    add_scaled(rhs, conv, dt);
+    add_scaled(rhs, uy[1].to_ortho(), dt);
+    add_scaled2(rhs, temp[1].gradient(2, 0, scale), dt, ka);
+    add_scaled2(rhs, temp[1].gradient(0, 2, scale), dt, ka);
+    temp[0].from_ortho(rhs);
+  }
+  void project_velocity(double c) {  // navier_adjoint.rs:697-710
+    Arr2<T> dpdx = pres[1].gradient(1, 0, scale);
+    Arr2<T> dpdy = pres[1].gradient(0, 1, scale);
+    Arr2<T> ox = ux[0].vhat, oy = uy[0].vhat;
+    ux[0].from_ortho(dpdx);
+    uy[0].from_ortho(dpdy);
+    T cinto = T(-c);
+    for (size_t i = 0; i < ux[0].vhat.v.size(); i++) ux[0].vhat.v[i] = mulT(ux[0].vhat.v[i], cinto) + ox.v[i];
+    for (size_t i = 0; i < uy[0].vhat.v.size(); i++) uy[0].vhat.v[i] = mulT(uy[0].vhat.v[i], cinto) + oy.v[i];
+  }
+  Arr2<T> divergence() {  // navier_adjoint.rs:712-717
+    Arr2<T> r = ux[0].gradient(1, 0, scale);
+    Arr2<T> b = uy[0].gradient(0, 1, scale);
+    for (size_t i = 0; i < r.v.size(); i++) r.v[i] += b.v[i];
+    return r;
+  }
+  void solve_pres(const Arr2<T>& f) {  // navier_adjoint.rs:719-723
+    pres[1].vhat = solver.solve(f);
+    pres[1].vhat(0, 0) = T(0);
+  }
+  void update_pres() {  // navier_adjoint.rs:725-729
+    T inv_dt = T(1.0 / dt);
+    Arr2<T> p1o = pres[1].to_ortho();
+    for (size_t i = 0; i < p1o.v.size(); i++) pres[0].vhat.v[i] += mulT(p1o.v[i], inv_dt);
+  }
+  void update_residual() {  // navier_adjoint.rs:731-754
+    navier.ux.vhat = ux[0].vhat;
+    navier.uy.vhat = uy[0].vhat;
+    navier.temp.vhat = temp[0].vhat;
+    navier.update();
+    Field2<T>* nf[3] = {&navier.ux, &navier.uy, &navier.temp};
+    Field2<T>* sf[3] = {&ux[0], &uy[0], &temp[0]};
+    Field2<T>* rf[3] = {&ux[1], &uy[1], &temp[1]};
+    for (int k = 0; k < 3; k++) {
+      Arr2<T>& a = nf[k]->vhat;
+      for (size_t i = 0; i < a.v.size(); i++) a.v[i] = rdiv(a.v[i] - sf[k]->vhat.v[i], navier.dt);
+      unsmoothed[k] = nf[k]->to_ortho();
+      rf[k]->vhat = smoother[k].solve(unsmoothed[k]);
+      T rescale = T(-1.0);
+      for (auto& e : rf[k]->vhat.v) e = mulT(e, rescale);
+    }
+  }
+  void update() {  // navier_adjoint.rs:767-800
+    ux[0].backward();
+    uy[0].backward();
+    temp[0].backward();
+    Arr2<double> u = ux[0].v, v = uy[0].v, t = temp[0].v;
+    update_residual();
+    solve_u(0, u, v, t);
+    solve_u(1, u, v, t);
+    Arr2<T> div = divergence();
+    solve_pres(div);
+    project_velocity(1.0);
+    update_pres();
+    solve_temp(u, v);
+    time += dt;
+  }
+  static double norm_l2(const Arr2<T>& a) {  // navier_adjoint.rs:915-925
+    double s = 0.0;
+    for (const auto& e : a.v) s += Navier2D<T>::sq(e);
+    return std::sqrt(s);
+  }
+  bool exit() {  // navier_adjoint.rs:889-906
+    if (std::isnan(norm_l2(divergence()))) return true;
+    return norm_l2(ux[1].vhat) + norm_l2(uy[1].vhat) + norm_l2(temp[1].vhat) < res_tol;
+  }
+  // Nu, Nuvol, Re of the adjoint state (navier_adjoint.rs:932-963): the same
+  // functions on fields of the same spaces, evaluated through `navier`
+  double eval(int what) {
+    navier.ux.vhat = ux[0].vhat;
+    navier.uy.vhat = uy[0].vhat;
+    navier.temp.vhat = temp[0].vhat;
+    switch (what) {
+      case 0: return navier.eval_nu();
+      case 1: return navier.eval_nuvol();
+      case 2: return navier.eval_re();
+      case 3: return navier.eval_ke();
+      default: return norm_l2(divergence());
+    }
+  }
+};
+
 }  // namespace oracle
 
 // ===========================================================================
@@ -1381,6 +1598,110 @@ void or_navier_params(void* p, double* out) {  // nu, ka, ra, pr, dt, scale0, sc
   auto* h = (OrNavier*)p;
   if (h->periodic) { auto& n = h->per; double v[7] = {n.nu, n.ka, n.ra, n.pr, n.dt, n.scale[0], n.scale[1]}; std::memcpy(out, v, sizeof v); }
   else { auto& n = h->box; double v[7] = {n.nu, n.ka, n.ra, n.pr, n.dt, n.scale[0], n.scale[1]}; std::memcpy(out, v, sizeof v); }
+}
+
+// ---- Navier2DAdjoint ----------------------------------------------------------
+struct OrAdjoint {
+  bool periodic;
+  Navier2DAdjoint<double> box;
+  Navier2DAdjoint<cplx> per;
+};
+void* or_adjoint_new(int nx, int ny, double ra, double pr, double dt, double aspect, int kind) {
+  try {
+    auto* h = new OrAdjoint();
+    h->periodic = kind == 2;
+    if (h->periodic) h->per.build(nx, ny, ra, pr, dt, aspect, kind);
+    else h->box.build(nx, ny, ra, pr, dt, aspect, kind);
+    return h;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return nullptr;
+  }
+}
+void or_adjoint_free(void* p) { delete (OrAdjoint*)p; }
+// dense eigen-decompositions: k = 0 the inner Navier2D's Poisson, 1 the
+// adjoint's Poisson, 2..4 the smoothers of ux, uy, temp
+int or_adjoint_tensor_pending(void* p, int k, int* m) {
+  auto* h = (OrAdjoint*)p;
+  Solver2* s = h->periodic ? h->per.tensor_solver(k) : h->box.tensor_solver(k);
+  if (!s->tensor.pending) return 0;
+  *m = s->tensor.a0.n0;
+  return 1;
+}
+void or_adjoint_tensor_get(void* p, int k, double* a0, double* c0) {
+  auto* h = (OrAdjoint*)p;
+  Solver2* s = h->periodic ? h->per.tensor_solver(k) : h->box.tensor_solver(k);
+  std::memcpy(a0, s->tensor.a0.data(), 8 * s->tensor.a0.size());
+  std::memcpy(c0, s->tensor.c0.data(), 8 * s->tensor.c0.size());
+}
+void or_adjoint_tensor_set(void* p, int k, const double* lam, const double* fwd, const double* bwd) {
+  auto* h = (OrAdjoint*)p;
+  Solver2* s = h->periodic ? h->per.tensor_solver(k) : h->box.tensor_solver(k);
+  s->set_eig(lam, fwd, bwd);
+}
+}  // extern "C"
+// field ids: 0 temp, 1 ux, 2 uy, 3 pres[0], 4 pres[1], 10 temp[1], 11 ux[1], 12 uy[1]
+template <class T> static Field2<T>* adj_pick(Navier2DAdjoint<T>& a, int id) {
+  switch (id) {
+    case 0: return &a.temp[0];
+    case 1: return &a.ux[0];
+    case 2: return &a.uy[0];
+    case 3: return &a.pres[0];
+    case 4: return &a.pres[1];
+    case 10: return &a.temp[1];
+    case 11: return &a.ux[1];
+    case 12: return &a.uy[1];
+  }
+  return nullptr;
+}
+extern "C" {
+int or_adjoint_shape(void* p, int id, int* n0, int* n1) {
+  auto* h = (OrAdjoint*)p;
+  if (h->periodic) { auto* f = adj_pick(h->per, id); *n0 = f->vhat.n0; *n1 = f->vhat.n1; return 1; }
+  auto* f = adj_pick(h->box, id); *n0 = f->vhat.n0; *n1 = f->vhat.n1; return 0;
+}
+void or_adjoint_get(void* p, int id, double* out) {
+  auto* h = (OrAdjoint*)p;
+  if (h->periodic) put(adj_pick(h->per, id)->vhat, out); else put(adj_pick(h->box, id)->vhat, out);
+}
+void or_adjoint_set(void* p, int id, const double* in) {
+  auto* h = (OrAdjoint*)p;
+  if (h->periodic) { auto* f = adj_pick(h->per, id); f->vhat = mk<cplx>(in, f->vhat.n0, f->vhat.n1); }
+  else { auto* f = adj_pick(h->box, id); f->vhat = mk<double>(in, f->vhat.n0, f->vhat.n1); }
+}
+void or_adjoint_set_velocity(void* p, double amp, double m, double n) {  // navier_adjoint.rs:965-968
+  auto* h = (OrAdjoint*)p;
+  if (h->periodic) { Navier2D<cplx>::apply_mode(h->per.ux[0], amp, m, n, true); Navier2D<cplx>::apply_mode(h->per.uy[0], -amp, m, n, false); }
+  else { Navier2D<double>::apply_mode(h->box.ux[0], amp, m, n, true); Navier2D<double>::apply_mode(h->box.uy[0], -amp, m, n, false); }
+}
+void or_adjoint_set_temperature(void* p, double amp, double m, double n) {  // :969-971
+  auto* h = (OrAdjoint*)p;
+  if (h->periodic) Navier2D<cplx>::apply_mode(h->per.temp[0], -amp, m, n, false);
+  else Navier2D<double>::apply_mode(h->box.temp[0], -amp, m, n, false);
+}
+int or_adjoint_update(void* p, int nsteps) {
+  try {
+    auto* h = (OrAdjoint*)p;
+    for (int s = 0; s < nsteps; s++) {
+      if (h->periodic) h->per.update(); else h->box.update();
+    }
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
+}
+double or_adjoint_time(void* p) { auto* h = (OrAdjoint*)p; return h->periodic ? h->per.time : h->box.time; }
+double or_adjoint_eval(void* p, int what) { auto* h = (OrAdjoint*)p; return h->periodic ? h->per.eval(what) : h->box.eval(what); }
+int or_adjoint_exit(void* p) { auto* h = (OrAdjoint*)p; return h->periodic ? h->per.exit() : h->box.exit(); }
+// |unsmoothed residual| (u, v, T) and |smoothed residual| (u, v, T) (navier_adjoint.rs:866-874)
+void or_adjoint_residual(void* p, double* out) {
+  auto* h = (OrAdjoint*)p;
+  auto fill = [&](auto& a) {
+    for (int k = 0; k < 3; k++) out[k] = a.unsmoothed[k].v.empty() ? 0.0 : a.norm_l2(a.unsmoothed[k]);
+    out[3] = a.norm_l2(a.ux[1].vhat); out[4] = a.norm_l2(a.uy[1].vhat); out[5] = a.norm_l2(a.temp[1].vhat);
+  };
+  if (h->periodic) fill(h->per); else fill(h->box);
 }
 
 // ---- Space2 / Field2 primitives (funspace) ----------------------------------

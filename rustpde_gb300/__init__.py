@@ -34,6 +34,7 @@ RBC_ERR_NOMEM = -5
 BOX_ADIABATIC, BOX_CONDUCTING, PERIODIC = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 TEMP, UX, UY, PRES, PSEUDO_PRES, FIELDBC = 0, 1, 2, 3, 4, 5
+ADJ_TEMP_RES, ADJ_UX_RES, ADJ_UY_RES = 10, 11, 12
 NU, NUVOL, RE, KE, DIV_NORM = 0, 1, 2, 3, 4
 CHEBYSHEV, CHEB_DIRICHLET, CHEB_NEUMANN, CHEB_DIRICHLET_BC, CHEB_NEUMANN_BC, FOURIER_R2C = range(6)
 HHOLTZ, HHOLTZ_ADI, POISSON = 0, 1, 2
@@ -167,6 +168,21 @@ _SIGNATURES = {
     "fs_lanes_shape": (_I, [_P, _IP, _IP]),
     "fs_lanes_set_hholtz": (_I, [_P, _D]),
     "fs_lanes_apply": (_I, [_P, _I, _P, _P, _I, _P]),
+    "rbc_adjoint_create": (_I, [ctypes.POINTER(RbcParams), ctypes.POINTER(_P)]),
+    "rbc_adjoint_destroy": (_I, [_P]),
+    "rbc_adjoint_set_velocity": (_I, [_P, _D, _D, _D]),
+    "rbc_adjoint_set_temperature": (_I, [_P, _D, _D, _D]),
+    "rbc_adjoint_step": (_I, [_P, _I]),
+    "rbc_adjoint_synchronize": (_I, [_P]),
+    "rbc_adjoint_get_time": (_I, [_P, _DP]),
+    "rbc_adjoint_set_time": (_I, [_P, _D]),
+    "rbc_adjoint_field_shape": (_I, [_P, _I, _IP, _IP, _IP]),
+    "rbc_adjoint_get_state": (_I, [_P, _I, _DP, _SZ]),
+    "rbc_adjoint_set_state": (_I, [_P, _I, _DP, _SZ]),
+    "rbc_adjoint_eval": (_I, [_P, _I, _DP]),
+    "rbc_adjoint_residual": (_I, [_P, _DP]),
+    "rbc_adjoint_exit": (_I, [_P, _IP]),
+    "rbc_adjoint_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
     "df_create": (_I, [_I, _I, _I, _I, _D, _D, ctypes.POINTER(_P)]),
     "df_destroy": (_I, [_P]),
     "df_shape": (_I, [_P, _I, _IP, _IP, _IP]),
@@ -401,6 +417,107 @@ class Field2:
 
     def gradient(self, deriv, scale=None):
         return self.space.gradient(self.vhat, deriv, scale)
+
+
+class Navier2DAdjoint:
+    """Navier2DAdjoint (src/navier/navier_adjoint.rs): adjoint descent towards
+    a steady state of the Rayleigh-Benard equations, on the GPU.  ``dt`` is the
+    pseudo time step; each update runs one Navier2D step of dt = 1e-2."""
+
+    def __init__(self, nx, ny, ra, pr, dt, aspect, kind):
+        p = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(aspect), int(kind), PREC_FP64)
+        h = _P()
+        _check(lib().rbc_adjoint_create(ctypes.byref(p), ctypes.byref(h)))
+        self._h = h
+        self.nx, self.ny, self.kind, self.dt = int(nx), int(ny), int(kind), float(dt)
+
+    @classmethod
+    def new(cls, nx, ny, ra, pr, dt, aspect, adiabatic=True):
+        return cls(nx, ny, ra, pr, dt, aspect, BOX_ADIABATIC if adiabatic else BOX_CONDUCTING)
+
+    @classmethod
+    def new_periodic(cls, nx, ny, ra, pr, dt, aspect):
+        return cls(nx, ny, ra, pr, dt, aspect, PERIODIC)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib is not None:
+            _lib.rbc_adjoint_destroy(h)
+            self._h = None
+
+    def set_velocity(self, amp, m, n):
+        _check(lib().rbc_adjoint_set_velocity(self._h, float(amp), float(m), float(n)))
+
+    def set_temperature(self, amp, m, n):
+        _check(lib().rbc_adjoint_set_temperature(self._h, float(amp), float(m), float(n)))
+
+    def update(self, nsteps: int = 1):
+        _check(lib().rbc_adjoint_step(self._h, int(nsteps)))
+
+    def synchronize(self):
+        _check(lib().rbc_adjoint_synchronize(self._h))
+
+    def get_time(self):
+        t = _D()
+        _check(lib().rbc_adjoint_get_time(self._h, ctypes.byref(t)))
+        return t.value
+
+    def get_dt(self):
+        return self.dt
+
+    def reset_time(self):
+        _check(lib().rbc_adjoint_set_time(self._h, 0.0))
+
+    def shape(self, field):
+        a, b, c = _I(), _I(), _I()
+        _check(lib().rbc_adjoint_field_shape(self._h, field, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return (a.value, b.value), bool(c.value)
+
+    def get(self, field):
+        sh, cx = self.shape(field)
+        out = np.empty(sh, dtype=np.complex128 if cx else np.float64)
+        _check(lib().rbc_adjoint_get_state(self._h, field, out.ctypes.data_as(_DP), out.size * (2 if cx else 1)))
+        return out
+
+    def set(self, field, arr):
+        sh, cx = self.shape(field)
+        a = np.ascontiguousarray(arr, dtype=np.complex128 if cx else np.float64)
+        if a.shape != sh:
+            raise ValueError(f"shape mismatch: got {a.shape}, expected {sh}")
+        _check(lib().rbc_adjoint_set_state(self._h, field, a.ctypes.data_as(_DP), a.size * (2 if cx else 1)))
+
+    def eval(self, what):
+        v = _D()
+        _check(lib().rbc_adjoint_eval(self._h, what, ctypes.byref(v)))
+        return v.value
+
+    def eval_nu(self):
+        return self.eval(NU)
+
+    def eval_nuvol(self):
+        return self.eval(NUVOL)
+
+    def eval_re(self):
+        return self.eval(RE)
+
+    def residual(self):
+        """L2 norms (u, v, T) of the unsmoothed and of the smoothed residual."""
+        out = np.zeros(6)
+        _check(lib().rbc_adjoint_residual(self._h, _dptr(out)))
+        return out
+
+    def callback(self):
+        """The diagnostics Navier2DAdjoint::callback prints and logs
+        (navier_adjoint.rs:811-886), returned instead of written."""
+        r = self.residual()
+        return {"time": self.get_time(), "div": self.eval(DIV_NORM), "Nu": self.eval_nu(),
+                "Nuvol": self.eval_nuvol(), "Re": self.eval_re(), "res_unsmoothed": float(r[:3].sum()),
+                "res_smoothed": float(r[3:].sum())}
+
+    def exit(self):
+        s = _I()
+        _check(lib().rbc_adjoint_exit(self._h, ctypes.byref(s)))
+        return bool(s.value)
 
 
 class Diffusion2D:

@@ -22,7 +22,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libspectral_rbc.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["host_ops.cpp", "dense_ops.cpp", "solid_masks.cpp", "prims.cu", "lane_gemm.cu", "step_fp64.cu", "step_mixed.cu", "step_lanes.cu", "api.cu"]
+SOURCES = ["host_ops.cpp", "dense_ops.cpp", "solid_masks.cpp", "prims.cu", "lane_gemm.cu", "step_fp64.cu", "step_mixed.cu", "step_lanes.cu", "api.cu", "adjoint.cu"]
 EXTRA_SOURCES: list[str] = []
 
 

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "case_access.h"
 #include "dense_ops.h"
 #include "host_ops.h"
 #include "lane_gemm.h"
@@ -30,6 +31,7 @@ static int fail(int code, const std::string& m) {
   g_err = m;
   return code;
 }
+int set_last_error(int code, const std::string& m) { return fail(code, m); }
 
 #define API_BEGIN try {
 #define API_END                                              \
@@ -553,6 +555,33 @@ void capture_graph(RbcCase* c) {
   cuda_check(cudaGraphInstantiate(&c->gexec, g, 0), "graph instantiate");
 }
 
+}  // namespace
+
+namespace rbc {
+CaseAccess case_access(RbcCase* c) {
+  CaseAccess a;
+  a.temp = c->hd.temp;
+  a.ux = c->hd.ux;
+  a.uy = c->hd.uy;
+  a.p0 = c->hd.p0;
+  a.p1 = c->hd.p1;
+  a.bc_vhat = c->bc_vhat;
+  a.bc_phys = c->bc_phys;
+  a.stream = c->stream;
+  a.nu = c->nu;
+  a.ka = c->ka;
+  a.scale[0] = c->scale[0];
+  a.scale[1] = c->scale[1];
+  return a;
+}
+void case_enqueue_step(RbcCase* c, cudaStream_t st) {
+  if (!c->gexec) throw std::runtime_error("case_enqueue_step: the case belongs to a batch");
+  for (size_t k = 0; k < c->plan.launches.size(); k++)
+    cuda_check(launch_entry(c->plan.launches[k], c->dp, k, st, c->d_case), "step kernel launch");
+}
+}  // namespace rbc
+
+namespace {
 // physical initial condition -> spectral state (Field2::forward)
 void set_phys(RbcCase* c, int field, const std::vector<double>& v) {
   double* d = c->phys[0];

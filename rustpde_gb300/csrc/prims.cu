@@ -625,6 +625,41 @@ void space_backward(const SpaceDev& s, const void* spec, double* phys, void* tmp
   run_pass(e, st);
 }
 
+// backward(gradient(f)) on the physical grid in two passes, the field read
+// once per axis: x pass to_ortho, derivative, backward transform; y pass the
+// same with the 1/scale^deriv factor (conv_term.rs:22-42 does the gradient,
+// then Field2::backward of the ortho result).
+void space_gradient_physical(const SpaceDev& s, const void* spec, double* phys, int d0, int d1, const double* scale,
+                             void* tmp, cudaStream_t st) {
+  PassDesc d = base_desc(s);
+  set_axis0(d, spec, s.cplx, tmp, 0, s.spec1, s.spec0);
+  if (s.cplx) {
+    d.fx = s.f0;
+    if (d0 > 0) add_op(d, P_FDIFF, d0);
+    add_op(d, P_C2R);
+  } else {
+    d.cx = s.c0; d.basis = s.b0;
+    if (s.hb0.composite()) add_op(d, P_TO_ORTHO);
+    add_op(d, P_DIFF, d0);
+    add_op(d, P_DCT_BWD);
+  }
+  run_pass(d, st);
+  PassDesc e = base_desc(s);
+  set_axis1(e, tmp, 0, phys, 0, s.phys0, s.spec1, s.phys1);
+  e.cx = s.c1; e.basis = s.b1;
+  if (s.hb1.composite()) add_op(e, P_TO_ORTHO);
+  add_op(e, P_DIFF, d1);
+  if (scale) {
+    double s0 = 1.0, s1 = 1.0;
+    for (int i = 0; i < d0; i++) s0 *= scale[0];
+    for (int i = 0; i < d1; i++) s1 *= scale[1];
+    e.scale = 1.0 / (s0 * s1);
+    add_op(e, P_SCALE);
+  }
+  add_op(e, P_DCT_BWD);
+  run_pass(e, st);
+}
+
 void space_backward_ortho(const SpaceDev& s, const void* ortho, double* phys, void* tmp, cudaStream_t st) {
   PassDesc d = base_desc(s);
   set_axis0(d, ortho, s.cplx, tmp, 0, s.ortho1, s.ortho0);

@@ -98,6 +98,9 @@ void space_to_ortho(const SpaceDev& s, const void* spec, void* ortho, void* tmp,
 void space_from_ortho(const SpaceDev& s, const void* ortho, void* spec, void* tmp, cudaStream_t st);
 void space_gradient(const SpaceDev& s, const void* spec, void* ortho, int d0, int d1, const double* scale,
                     void* tmp, cudaStream_t st);
+// backward(gradient(spec)) onto the physical grid (two passes)
+void space_gradient_physical(const SpaceDev& s, const void* spec, double* phys, int d0, int d1, const double* scale,
+                             void* tmp, cudaStream_t st);
 // backward transform of an ortho-sized array (the `field` space of Navier2D)
 void space_backward_ortho(const SpaceDev& s, const void* ortho, double* phys, void* tmp, cudaStream_t st);
 void solver_solve(const SolverDev& sv, const SpaceDev& s, const void* in_ortho, void* out_spec, void* tmp,
