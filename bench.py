@@ -17,6 +17,9 @@ Workloads (--workload):
                       aspect=2), plain FP64, one case.
   serving             the serving loop alone (see run_serving).
   precision           batched 1-D stages, FP64 vs mixed (see run_precision).
+  extras              per-update device time of the solid-mask step, Diffusion2D
+                      and Navier2DAdjoint beside the oracle on the host cores
+                      (see run_extras).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
@@ -462,6 +465,81 @@ def run_precision(args):
 
 
 # ---------------------------------------------------------------------------
+# solid masks, Diffusion2D, Navier2DAdjoint: device time per update
+# ---------------------------------------------------------------------------
+def run_extras(args):
+    """Each solver on a fixed seeded case: K updates, each between CUDA events
+    on the solver's stream with L2 flushed in between, against the oracle on
+    all host cores (a bounded sample of updates of the same case)."""
+    import numpy as np
+
+    import rustpde_gb300 as R
+    from oracle import oracle as O
+    from rustpde_gb300 import build
+    from rustpde_gb300 import solid_masks as S
+    build.build()
+    O.build()
+    O.set_threads(os.cpu_count() or 1)
+    cu = Cudart()
+    flush = R.DeviceArray((256 * 1024 * 1024 // 8,))
+    K = min(args.steps, 50)
+
+    def device_ms(obj, stream):
+        obj.update(3)
+        return timed_steps(cu, stream, K, lambda: obj.update(1), flush) / K
+
+    def oracle_ms(obj, budget=3.0):
+        obj.update(1)
+        n, t0 = 0, time.perf_counter()
+        while n < 2 or (time.perf_counter() - t0 < budget and n < 200):
+            obj.update(1)
+            n += 1
+        return (time.perf_counter() - t0) / n * 1e3
+
+    out = {}
+    for name, (nx, ny, ra, dt, kind) in {"solid_box128": (128, 128, 1e6, 2e-3, R.BOX_ADIABATIC),
+                                         "solid_periodic256x129": (256, 129, 1e6, 2e-3, R.PERIODIC)}.items():
+        plain = R.Navier2D(nx, ny, ra, 1.0, dt, 1.0, kind, seed=None)
+        R.standard_ic(plain, 1)
+        g = R.Navier2D(nx, ny, ra, 1.0, dt, 1.0, kind, seed=None)
+        R.standard_ic(g, 1)
+        x, y = g.coords(R.TEMP)
+        g.solid = S.solid_cylinder_inner(x, y, 0.5 * (x[0] + x[-1]), 0.0, 0.3)
+        o = O.Navier2D(nx, ny, ra, 1.0, dt, 1.0, kind)
+        O.standard_ic(o, 1)
+        o.set_solid(*g.solid)
+        ms_plain, ms_solid = device_ms(plain, plain.stream()), device_ms(g, g.stream())
+        out[name] = {"ms_per_step_plain": ms_plain, "ms_per_step_solid": ms_solid,
+                     "solid_overhead": ms_solid / ms_plain - 1.0, "oracle_ms_per_step": oracle_ms(o),
+                     "grid_pt_steps_per_s": nx * ny / (ms_solid * 1e-3)}
+    for name, (k0, n0, k1, n1) in {"diffusion_cd256xcd256": (R.CHEB_DIRICHLET, 256, R.CHEB_DIRICHLET, 256),
+                                   "diffusion_f512xcd257": (R.FOURIER_R2C, 512, R.CHEB_DIRICHLET, 257)}.items():
+        f = R.Field2(R.Space2(R.Base(k0, n0), R.Base(k1, n1)))
+        g = R.Diffusion2D(f, 1.0, 1e-3)
+        g.impulse()
+        o = O.Diffusion2D(k0, n0, k1, n1, 1.0, 1e-3)
+        o.impulse()
+        ms = device_ms(g, g.stream())
+        out[name] = {"ms_per_update": ms, "oracle_ms_per_update": oracle_ms(o),
+                     "grid_pt_steps_per_s": n0 * n1 / (ms * 1e-3)}
+    for name, (nx, ny, kind) in {"adjoint_box64": (64, 64, R.BOX_ADIABATIC),
+                                 "adjoint_periodic128x65": (128, 65, R.PERIODIC)}.items():
+        g = R.Navier2DAdjoint(nx, ny, 1e5, 1.0, 0.02, 1.0, kind)
+        o = O.Navier2DAdjoint(nx, ny, 1e5, 1.0, 0.02, 1.0, kind)
+        for a in (g, o):
+            a.set_temperature(0.5, 1.0, 1.0)
+            a.set_velocity(0.5, 1.0, 1.0)
+        ms = device_ms(g, g.stream())
+        out[name] = {"ms_per_update": ms, "oracle_ms_per_update": oracle_ms(o),
+                     "grid_pt_steps_per_s": nx * ny / (ms * 1e-3)}
+    return {"metric": "ms per update", "workload": "extras", "steps": K, "unit": "ms", "higher_is_better": False,
+            "dtype": "f64", "data": "synthetic seeded fields",
+            "config": {"l2": "flushed between timed updates (256 MiB memset outside the events)",
+                       "oracle_cores": O.num_threads()},
+            "cases": out}
+
+
+# ---------------------------------------------------------------------------
 # single periodic 512x257 case, plain FP64
 # ---------------------------------------------------------------------------
 def run_periodic512(args, rank, world, local):
@@ -615,7 +693,8 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "periodic512", "serving", "precision"])
+    ap.add_argument("--workload", default="ensemble",
+                    choices=["ensemble", "periodic512", "serving", "precision", "extras"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
     ap.add_argument("--skip-plain", action="store_true",
@@ -635,6 +714,8 @@ def main():
         line = run_reference(args, rank, world)
     elif args.workload == "precision":
         line = run_precision(args)
+    elif args.workload == "extras":
+        line = run_extras(args)
     elif args.workload == "serving":
         from rustpde_gb300 import build
         build.build()

@@ -519,6 +519,11 @@ class Navier2DAdjoint:
         _check(lib().rbc_adjoint_exit(self._h, ctypes.byref(s)))
         return bool(s.value)
 
+    def stream(self):
+        s = _P()
+        _check(lib().rbc_adjoint_get_stream(self._h, ctypes.byref(s)))
+        return s.value
+
 
 class Diffusion2D:
     """Diffusion2D (src/navier/diffusion.rs:113-238): the fully implicit 2-D
@@ -606,6 +611,11 @@ class Diffusion2D:
         """The physical field as Diffusion2D::callback writes it (with the
         boundary field added, diffusion.rs:214-225), returned instead of written."""
         return self.get_physical(with_bc=True)
+
+    def stream(self):
+        s = _P()
+        _check(lib().df_get_stream(self._h, ctypes.byref(s)))
+        return s.value
 
     def exit(self):
         return False
