@@ -1,4 +1,5 @@
 // api.cu -- C ABI of the spectral RBC library (include/spectral_rbc.h).
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -187,7 +188,7 @@ struct RbcCase {
   double* d_red = nullptr;
   cudaStream_t stream = nullptr;
   StepPlan plan;
-  StepPlan plan_lanes;  // mixed form: the batch variant with one-thread-per-lane FP64 passes
+  std::vector<StepPlan> plan_alts;  // mixed form in batches: the other forms of the FP64 passes (autotuned)
   DevPlan dp;
   MixedOps mops;
   cudaGraph_t graph = nullptr;
@@ -523,8 +524,8 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   cuda_check(configure_step_kernels(), "configure step kernels");
   if (h.mixed) {
     cuda_check(configure_mixed_kernels(), "configure mixed kernels");
-    c->plan = build_mixed_plan(h, c->mops, false);
-    if (!with_graph) c->plan_lanes = build_mixed_plan(h, c->mops, true);
+    c->plan = build_mixed_plan(h, c->mops, 0);
+    if (!with_graph) c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2)};
   } else {
     c->plan = build_step_plan(h);
   }
@@ -1160,19 +1161,23 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     b->buckets[found].members.push_back(i);
   }
   for (auto& bk : b->buckets) {
-    std::vector<const StepPlan*> plans, lanes;
-    for (int m : bk.members) {
-      plans.push_back(&b->cases[m]->plan);
-      lanes.push_back(b->cases[m]->plan_lanes.launches.empty() ? &b->cases[m]->plan : &b->cases[m]->plan_lanes);
-    }
+    std::vector<const StepPlan*> plans;
+    for (int m : bk.members) plans.push_back(&b->cases[m]->plan);
     bk.plan = merge_plans(plans, bk.members, {});
     upload_plan(b->arena, bk.plan, bk.dp);
-    // autotune: where a pass has a one-thread-per-lane form, time both forms on
-    // this batch and keep the faster (the state is still zero; the choice is
-    // made once, so the batch's numbers do not depend on later timings)
-    StepPlan alt = merge_plans(lanes, bk.members, {});
-    DevPlan adp;
-    upload_plan(b->arena, alt, adp);
+    // autotune: where a pass has other forms (128-thread CTAs, one thread per
+    // sub-lane), time every form on this batch and keep the fastest (the state
+    // is still zero; the choice is made once, so the batch's numbers do not
+    // depend on later timings)
+    const size_t nalt = b->cases[bk.members[0]]->plan_alts.size();
+    std::vector<StepPlan> alts(nalt);
+    std::vector<DevPlan> adps(nalt);
+    for (size_t a = 0; a < nalt; a++) {
+      std::vector<const StepPlan*> ap;
+      for (int m : bk.members) ap.push_back(&b->cases[m]->plan_alts[a]);
+      alts[a] = merge_plans(ap, bk.members, {});
+      upload_plan(b->arena, alts[a], adps[a]);
+    }
     cuda_check(cudaDeviceSynchronize(), "batch set-up");
     cudaEvent_t e0, e1;
     cuda_check(cudaEventCreate(&e0), "event");
@@ -1192,12 +1197,27 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       return best;
     };
     for (size_t li = 0; li < bk.plan.launches.size(); li++) {
-      if (alt.launches[li].kernel == bk.plan.launches[li].kernel) continue;
-      const float t_cta = time_launch(bk.plan.launches[li], bk.dp, li);
-      const float t_lane = time_launch(alt.launches[li], adp, li);
-      b->tuning.push_back({bk.plan.launches[li].kernel, alt.launches[li].kernel, t_cta, t_lane});
-      if (t_lane < t_cta) {
-        bk.plan.launches[li] = alt.launches[li];
+      const int base_kernel = bk.plan.launches[li].kernel;
+      float t_base = -1.f, t_best_alt = 1e30f;
+      int best = -1, best_alt_kernel = base_kernel;
+      std::vector<int> seen{base_kernel};
+      for (size_t a = 0; a < nalt; a++) {
+        const int k = alts[a].launches[li].kernel;
+        if (std::find(seen.begin(), seen.end(), k) != seen.end()) continue;
+        seen.push_back(k);
+        if (t_base < 0) t_base = time_launch(bk.plan.launches[li], bk.dp, li);
+        const float t = time_launch(alts[a].launches[li], adps[a], li);
+        if (t < t_best_alt) {
+          t_best_alt = t;
+          best_alt_kernel = k;
+          if (t < t_base) best = (int)a;
+        }
+      }
+      if (t_base < 0) continue;  // no other form of this pass
+      b->tuning.push_back({base_kernel, best_alt_kernel, t_base, t_best_alt});
+      if (best >= 0) {
+        const DevPlan& adp = adps[best];
+        bk.plan.launches[li] = alts[best].launches[li];
         bk.dp.work[li] = adp.work[li];
         bk.dp.jobs[li] = adp.jobs[li];
         bk.dp.tiles[li] = adp.tiles[li];

@@ -53,7 +53,11 @@ struct MixedOps {
 };
 // lane_parallel: the FP64 passes run one thread per lane (many lanes: batches);
 // otherwise one CTA per lane (a single case)
-StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_parallel);
+// variant 0: a CTA per lane; 1: 128-thread CTAs where that form exists, else
+// one thread per lane; 2: one thread per (field, parity) sub-lane where that
+// form exists, else 128-thread CTAs
+StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant);
+int lane_kernel_subs(int kernel);
 cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work);
 constexpr int kLaneThreads = 128;  // lanes per CTA of the one-thread-per-lane kernels
 const char* step_kernel_name(int kernel);

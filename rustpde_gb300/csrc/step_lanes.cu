@@ -6,6 +6,11 @@
 // so every lane of every warp issues useful FP64 work and no scan, shuffle or
 // barrier is needed (the single-case kernels of step_fp64.cu use 16-thread
 // scans instead, because one case has too few lanes to fill the GPU).
+// The banded operators couple indices of equal parity only (offsets 0, +-2,
+// +-4), the Chebyshev derivative maps one parity onto the other, and the
+// fields are independent, so most passes split each lane into independent
+// (field, parity) sub-lanes (blockIdx.y): up to 6 threads per lane instead
+// of one, for latency hiding, with every recurrence still sequential.
 // Column lanes (x direction) are read and written coalesced across a warp;
 // row lanes (y direction) stream through L1, each thread along its own row.
 // Multi-pass kernels re-read their own earlier results from L1/L2.
@@ -135,98 +140,158 @@ __device__ __forceinline__ void from_ortho_lane(const BasisDev& b, const T* p, l
   }
 }
 
+// ---- parity chains: index q, q+2, q+4, ... of a lane --------------------------
+// largest index < n of parity q (or -1)
+__device__ __forceinline__ int top_par(int n, int q) { return ((n - 1 - q) & 1) ? n - 2 : n - 1; }
+
+// Chebyshev derivative d = D a on the indices of parity q, descending:
+// d_{n-1} = 0, d_i = 2(i+1) a_{i+1} + d_{i+2}, d_0 = a_1 + d_2 / 2; a(i)
+// supplies a_i (parity 1-q), store(i, d_i) receives the result
+template <class T, class A, class S>
+__device__ __forceinline__ void diff_par(int n, int q, A a, S store) {
+  T d2 = zero_v<T>();
+  for (int i = top_par(n, q); i >= 0; i -= 2) {
+    T d;
+    if (i == n - 1) d = zero_v<T>();
+    else if (i >= 1) d = fmas(d2, a(i + 1), 2.0 * (double)(i + 1));
+    else d = fmas(a(1), d2, 0.5);
+    store(i, d);
+    d2 = d;
+  }
+}
+
+// Fdma back substitution on the parity-q indices of a strided lane, in place
+template <class T>
+__device__ __forceinline__ void fdma_bwd_par(const FdmaRow& f, T* x, long long s, int q) {
+  T p2 = zero_v<T>(), p4 = zero_v<T>();
+#pragma unroll 4
+  for (int j = top_par(f.m, q); j >= 0; j -= 2) {
+    T v = scal(x[(long long)j * s], f.dinv[j]);
+    if (j + 2 < f.m) v = fmas(v, p2, f.up1[j]);
+    if (j + 4 < f.m) v = fmas(v, p4, f.up2[j]);
+    x[(long long)j * s] = v;
+    p4 = p2;
+    p2 = v;
+  }
+}
+
+// pinv rows fused with the Fdma forward elimination on the parity-q indices:
+// out_i = pinv_i(in) + low_{i-2} out_{i-2}, i < f.m
+template <class T>
+__device__ __forceinline__ void pinv_fwd_par(const PinvDev& p, const FdmaRow& f, const T* in, long long is, T* out,
+                                             long long os, int q) {
+  T xm2 = zero_v<T>();
+#pragma unroll 4
+  for (int i = q; i < f.m; i += 2) {
+    T v = pinv_lane<T>(p, in, is, i);
+    if (i >= 2) v = fmas(v, xm2, f.low[i - 2]);
+    out[(long long)i * os] = v;
+    xm2 = v;
+  }
+}
+
+// from_ortho (least squares, stride-2 tridiagonal) on the parity-q chain;
+// `in` and `out` may be the same lane
+template <class T>
+__device__ __forceinline__ void from_ortho_par(const BasisDev& b, const T* p, long long ps, T* out, long long os, int q) {
+  const int m = b.m;
+  T g2 = zero_v<T>();
+#pragma unroll 4
+  for (int i = q; i < m; i += 2) {
+    const T d = fmas(scal(p[(long long)i * ps], b.diag[i]), p[(long long)(i + 2) * ps], b.low2[i]);
+    const double qq = b.fo_dinv[i];
+    T g = scal(d, qq);
+    if (i >= 2) g = fmas(g, g2, -b.fo_off[i - 2] * qq);
+    out[(long long)i * os] = g;
+    g2 = g;
+  }
+  T x2 = zero_v<T>();
+#pragma unroll 4
+  for (int j = top_par(m, q); j >= 0; j -= 2) {
+    T x = out[(long long)j * os];
+    if (j + 2 < m) x = fmas(x, x2, -b.fo_w[j]);
+    out[(long long)j * os] = x;
+    x2 = x;
+  }
+}
+
 #define LANE_PROLOGUE                                                        \
   const int4 w = work[blockIdx.x];                                           \
   if ((int)threadIdx.x >= w.z) return;                                       \
   const CaseDev& c = cases[w.x];                                             \
   if (c.gate != nullptr && c.gate[1] == 0) return;                           \
-  const int lane = w.y + (int)threadIdx.x;
+  const int lane = w.y + (int)threadIdx.x;                                   \
+  const int sub = (int)blockIdx.y;                                           \
+  (void)sub;
 
-// ============================================================================
-// Box, x direction (lanes = columns, stride = row length)
-// ============================================================================
-// d/dx p0 / aspect -> s[0] (nx x ny), columns j < ny
+// d/dx p0 / aspect -> s[0] (nx x ny), columns j < ny; sub = parity of the output rows
 __global__ void __launch_bounds__(128) k_lp_box_gpx(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
   const int j = lane, nx = c.nx, ny = c.ny;
   const double inv_asp = 1.0 / c.aspect;
   const double* p0 = static_cast<const double*>(c.p0) + j;
   double* gp = static_cast<double*>(c.s[0]) + j;
-  DescDiff<double> D(nx);
-#pragma unroll 4
-  for (int i = nx - 1; i >= 0; i--) gp[(long long)i * ny] = D.step(i, p0[(long long)i * ny]) * inv_asp;
+  diff_par<double>(nx, sub, [&](int i) { return p0[(long long)i * ny]; },
+                   [&](int i, double d) { gp[(long long)i * ny] = d * inv_asp; });
 }
 
-// pinv_x and the ADI x solve of the three fields: s[1..3] -> s[4..6], columns j < myc
+// pinv_x and the ADI x solve of the three fields: s[1..3] -> s[4..6], columns
+// j < myc; sub = 2 * field + parity
 __global__ void __launch_bounds__(128) k_lp_box_x2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int j = lane, myc = c.myc, mxc = c.mxc;
-  for (int f = 0; f < 3; f++) {
-    const double* in = static_cast<const double*>(c.s[1 + f]) + j;
-    double* out = static_cast<double*>(c.s[4 + f]) + j;
-    const FdmaRow F = fdma_row(f < 2 ? c.hu_x : c.ht_x, 0);
-    // pinv fused with the forward elimination
-    double xm1 = 0.0, xm2 = 0.0;
-#pragma unroll 4
-    for (int i = 0; i < mxc; i++) {
-      double v = pinv_lane<double>(c.pinv_x, in, myc, i);
-      if (i >= 2) v = fma(xm2, F.low[i - 2], v);
-      out[(long long)i * myc] = v;
-      xm2 = xm1;
-      xm1 = v;
-    }
-    fdma_bwd_lane<double>(F, out, myc);
-  }
+  const int j = lane, myc = c.myc, f = sub >> 1, q = sub & 1;
+  const double* in = static_cast<const double*>(c.s[1 + f]) + j;
+  double* out = static_cast<double*>(c.s[4 + f]) + j;
+  const FdmaRow F = fdma_row(f < 2 ? c.hu_x : c.ht_x, 0);
+  pinv_fwd_par<double>(c.pinv_x, F, in, myc, out, myc, q);
+  fdma_bwd_par<double>(F, out, myc, q);
 }
 
 // divergence and pinv_x: A = s[1], B = s[2] (mxc x ny) -> div s[3] (nx x ny),
-// pinv_x div -> m_z (mxc x ny), columns j < ny
+// pinv_x div -> m_z (mxc x ny), columns j < ny; sub = parity of the rows
+// (Dx A on parity q from Sx A on parity 1 - q)
 __global__ void __launch_bounds__(128) k_lp_box_x3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int j = lane, nx = c.nx, ny = c.ny, mxc = c.mxc;
+  const int j = lane, nx = c.nx, ny = c.ny, mxc = c.mxc, q = sub;
   const double inv_asp = 1.0 / c.aspect;
   const double* A = static_cast<const double*>(c.s[1]) + j;
   const double* B = static_cast<const double*>(c.s[2]) + j;
   double* dv = static_cast<double*>(c.s[3]) + j;
-  DescDiff<double> D(nx);
-  for (int i = nx - 1; i >= 0; i--) {
-    const double da = D.step(i, stencil_lane<double>(c.xu, A, ny, i));
-    dv[(long long)i * ny] = fma(da, inv_asp, stencil_lane<double>(c.xu, B, ny, i));
-  }
+  diff_par<double>(nx, q, [&](int i) { return stencil_lane<double>(c.xu, A, ny, i); },
+                   [&](int i, double da) { dv[(long long)i * ny] = fma(da, inv_asp, stencil_lane<double>(c.xu, B, ny, i)); });
   double* z = static_cast<double*>(c.m_z) + j;
-  for (int r = 0; r < mxc; r++) z[(long long)r * ny] = pinv_lane<double>(c.pinv_x, dv, ny, r);
+#pragma unroll 4
+  for (int r = q; r < mxc; r += 2) z[(long long)r * ny] = pinv_lane<double>(c.pinv_x, dv, ny, r);
 }
 
 // projection along x from p1 (computed by the eigenbasis GEMM): p1[0][0] = 0;
 // Gp = Sx^N p1 -> s[0], E = Sx+ (Dx Sx^N p1 / s) -> s[1], Fv = Sx+ Sx^N p1 -> s[2]
-// (s arrays as mxc/nx x myc), columns j < myc
+// (s arrays as mxc/nx x myc), columns j < myc; sub q: Gp and Fv on the rows
+// of parity q, E on the rows of parity 1 - q
 __global__ void __launch_bounds__(128) k_lp_box_x4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int j = lane, nx = c.nx, myc = c.myc;
+  const int j = lane, nx = c.nx, myc = c.myc, q = sub;
   const double inv_asp = 1.0 / c.aspect;
   double* p1 = static_cast<double*>(c.p1) + j;
-  if (j == 0) p1[0] = 0.0;
+  if (j == 0 && q == 0) p1[0] = 0.0;
   double* gp = static_cast<double*>(c.s[0]) + j;
   double* e = static_cast<double*>(c.s[1]) + j;
   double* fv = static_cast<double*>(c.s[2]) + j;
-  DescDiff<double> D(nx);
 #pragma unroll 4
-  for (int i = nx - 1; i >= 0; i--) {
-    const double o = stencil_lane<double>(c.xp, p1, myc, i);
-    gp[(long long)i * myc] = o;
-    e[(long long)i * myc] = D.step(i, o) * inv_asp;  // scratch: from_ortho reads it below
-  }
-  from_ortho_lane<double>(c.xu, e, myc, e, myc);
-  from_ortho_lane<double>(c.xu, gp, myc, fv, myc);
+  for (int i = q; i < nx; i += 2) gp[(long long)i * myc] = stencil_lane<double>(c.xp, p1, myc, i);
+  diff_par<double>(nx, 1 - q, [&](int i) { return gp[(long long)i * myc]; },
+                   [&](int i, double d) { e[(long long)i * myc] = d * inv_asp; });
+  from_ortho_par<double>(c.xu, e, myc, e, myc, 1 - q);
+  from_ortho_par<double>(c.xu, gp, myc, fv, myc, q);
 }
 
-// ============================================================================
-// Box, y direction (lanes = rows, contiguous; stride 1)
-// ============================================================================
-// rows i < nx: convection (m_cv), x stencils of the state, right-hand sides, pinv_y -> s[1..3]
+// rows i < nx: convection (m_cv), x stencils of the state, right-hand sides,
+// pinv_y -> s[1..3].  sub = 2 * field + parity q: the field's right-hand side
+// and pinv rows on the columns of parity q (dP/dy on parity q comes from p0 on
+// parity 1 - q)
 __global__ void __launch_bounds__(128) k_lp_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, kx = c.kx, ky = c.ky;
+  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, kx = c.kx, ky = c.ky, f = sub >> 1, q = sub & 1;
   const double dt = c.dt;
   const void* f3[3] = {c.ux, c.uy, c.temp};
   const BasisDev* xb[3] = {&c.xu, &c.xu, &c.xt};
@@ -235,11 +300,11 @@ __global__ void __launch_bounds__(128) k_lp_box_y2(const CaseDev* __restrict__ c
   const double* gpx = static_cast<const double*>(c.s[0]) + (size_t)i * ny;
   const double* bco = static_cast<const double*>(c.bc_ortho) + (size_t)i * ny;
   const double* bcd = static_cast<const double*>(c.bc_diff) + (size_t)i * ny;
-  // x stencil of the state at row i, column k (the composite x basis of each field)
-  auto sx = [&](int f, int k) -> double {
+  // x stencil of field ff at row i, column k (the composite x basis of each field)
+  auto sx = [&](int ff, int k) -> double {
     if (k < 0 || k >= myc) return 0.0;
-    const double* a = static_cast<const double*>(f3[f]);
-    const BasisDev& b = *xb[f];
+    const double* a = static_cast<const double*>(f3[ff]);
+    const BasisDev& b = *xb[ff];
     double v = 0.0;
     bool has = false;
     if (i < mxc) { v = a[(size_t)i * myc + k] * b.diag[i]; has = true; }
@@ -249,132 +314,133 @@ __global__ void __launch_bounds__(128) k_lp_box_y2(const CaseDev* __restrict__ c
     }
     return v;
   };
-  // descending k: y stencil O_f,k (CD basis), dP/dy, right-hand sides, pinv rows
-  DescDiff<double> G(ny);
-  double R[3][5];  // R_f at k .. k+4
-  for (int f = 0; f < 3; f++)
-    for (int q = 0; q < 5; q++) R[f][q] = 0.0;
-  double* out[3] = {static_cast<double*>(c.s[1]) + (size_t)i * myc, static_cast<double*>(c.s[2]) + (size_t)i * myc,
-                    static_cast<double*>(c.s[3]) + (size_t)i * myc};
+  // y stencil O_k = diag_k SX_k + low2_{k-2} SX_{k-2} (CD basis)
+  auto oy = [&](int ff, int k) -> double {
+    double v = 0.0;
+    if (k < myc) v = sx(ff, k) * c.ycd.diag[k];
+    if (k >= 2 && k - 2 < myc) v = (k < myc) ? fma(sx(ff, k - 2), c.ycd.low2[k - 2], v) : sx(ff, k - 2) * c.ycd.low2[k - 2];
+    return v;
+  };
+  double* out = static_cast<double*>(c.s[1 + f]) + (size_t)i * myc;
   const PinvDev& pv = c.pinv_y;
-  for (int k = ny - 1; k >= 0; k--) {
-    double O[3];
-    for (int f = 0; f < 3; f++) {
-      // O_k = diag_k SX_k + low2_{k-2} SX_{k-2}
-      double v = 0.0;
-      if (k < myc) v = sx(f, k) * c.ycd.diag[k];
-      if (k >= 2 && k - 2 < myc) v = (k < myc) ? fma(sx(f, k - 2), c.ycd.low2[k - 2], v) : sx(f, k - 2) * c.ycd.low2[k - 2];
-      O[f] = v;
+  double r2 = 0.0, r4 = 0.0, g2 = 0.0;
+  for (int k = top_par(ny, q); k >= 0; k -= 2) {
+    double g = 0.0;
+    if (f == 1) {  // dP/dy at k (descending derivative recurrence)
+      if (k == ny - 1) g = 0.0;
+      else if (k >= 1) g = fmas(g2, P[k + 1], 2.0 * (double)(k + 1));
+      else g = fmas(P[1], g2, 0.5);
+      g2 = g;
     }
-    const double g = G.step(k, P[k]);
     const bool incv = i < kx && k < ky;
-    const double cvk0 = incv ? cv[((size_t)0 * kx + i) * ky + k] : 0.0;
-    const double cvk1 = incv ? cv[((size_t)1 * kx + i) * ky + k] : 0.0;
-    const double cvk2 = incv ? cv[((size_t)2 * kx + i) * ky + k] : 0.0;
-    for (int f = 0; f < 3; f++)
-      for (int q = 4; q > 0; q--) R[f][q] = R[f][q - 1];
-    R[0][0] = fnms(fnms(O[0], gpx[k], dt), cvk0, dt);
-    const double that = O[2] + bco[k];
-    R[1][0] = fnms(fmas(fnms(O[1], g, dt), that, dt), cvk1, dt);
-    R[2][0] = fnms(O[2] + bcd[k], cvk2, dt);
+    const double cvk = incv ? cv[((size_t)f * kx + i) * ky + k] : 0.0;
+    double r;
+    if (f == 0) r = fnms(fnms(oy(0, k), gpx[k], dt), cvk, dt);
+    else if (f == 1) r = fnms(fmas(fnms(oy(1, k), g, dt), oy(2, k) + bco[k], dt), cvk, dt);
+    else r = fnms(oy(2, k) + bcd[k], cvk, dt);
     if (k < myc) {
-      for (int f = 0; f < 3; f++) {
-        double v = R[f][0] * pv.dia[k];
-        if (k < myc - 2) v = fma(R[f][2], pv.up1[k], v);
-        if (k < myc - 4) v = fma(R[f][4], pv.up2[k], v);
-        out[f][k] = v;
-      }
+      double v = r * pv.dia[k];
+      if (k < myc - 2) v = fma(r2, pv.up1[k], v);
+      if (k < myc - 4) v = fma(r4, pv.up2[k], v);
+      out[k] = v;
     }
+    r4 = r2;
+    r2 = r;
   }
 }
 
 // rows i < mxc: ADI y solves; ux*, uy* in place (s[4], s[5]), temperature ->
-// state; A = Sy ux* -> s[1], B = Dy Sy uy* -> s[2] (mxc x ny)
+// state; A = Sy ux* -> s[1], B = Dy Sy uy* -> s[2] (mxc x ny).  sub = 2 *
+// field + parity q: the field's chain of parity q, then A on parity q (ux) or
+// B on parity 1 - q (uy)
 __global__ void __launch_bounds__(128) k_lp_box_y3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc;
-  double* F[3] = {static_cast<double*>(c.s[4]) + (size_t)i * myc, static_cast<double*>(c.s[5]) + (size_t)i * myc,
-                  static_cast<double*>(c.s[6]) + (size_t)i * myc};
-  bool bad = false;
-  for (int f = 0; f < 3; f++) {
-    const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, 0);
-    fdma_fwd_lane<double>(R, F[f], 1);
-    fdma_bwd_lane<double>(R, F[f], 1);
-  }
-  double* tt = static_cast<double*>(c.temp) + (size_t)i * myc;
-  for (int k = 0; k < myc; k++) {
-    const double t = F[2][k];
-    tt[k] = t;
-    bad |= !(isfinite(F[0][k]) && isfinite(F[1][k]) && isfinite(t));
-  }
-  double* A = static_cast<double*>(c.s[1]) + (size_t)i * ny;
-  double* B = static_cast<double*>(c.s[2]) + (size_t)i * ny;
-  DescDiff<double> D(ny);
+  const int i = lane, ny = c.ny, myc = c.myc, f = sub >> 1, q = sub & 1;
+  double* F = static_cast<double*>(c.s[4 + f]) + (size_t)i * myc;
+  const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, 0);
+  {
+    double xm2 = 0.0;
 #pragma unroll 4
-  for (int k = ny - 1; k >= 0; k--) {
-    A[k] = stencil_lane<double>(c.ycd, F[0], 1, k);
-    B[k] = D.step(k, stencil_lane<double>(c.ycd, F[1], 1, k));
+    for (int k = q; k < R.m; k += 2) {
+      double v = F[k];
+      if (k >= 2) v = fma(xm2, R.low[k - 2], v);
+      F[k] = v;
+      xm2 = v;
+    }
+  }
+  fdma_bwd_par<double>(R, F, 1, q);
+  bool bad = false;
+  if (f == 2) {
+    double* tt = static_cast<double*>(c.temp) + (size_t)i * myc;
+    for (int k = q; k < myc; k += 2) {
+      tt[k] = F[k];
+      bad |= !isfinite(F[k]);
+    }
+  } else {
+    for (int k = q; k < myc; k += 2) bad |= !isfinite(F[k]);
+  }
+  if (f == 0) {
+    double* A = static_cast<double*>(c.s[1]) + (size_t)i * ny;
+#pragma unroll 4
+    for (int k = q; k < ny; k += 2) A[k] = stencil_lane<double>(c.ycd, F, 1, k);
+  } else if (f == 1) {
+    double* B = static_cast<double*>(c.s[2]) + (size_t)i * ny;
+    diff_par<double>(ny, 1 - q, [&](int k) { return stencil_lane<double>(c.ycd, F, 1, k); },
+                     [&](int k, double d) { B[k] = d; });
   }
   if (bad) atomicOr(c.status, 1u);
 }
 
 // rows i < mxc: pinv_y of the eigenbasis-transformed divergence and the
-// Poisson row solve: s[6] (zf, mxc x ny) -> s[7] (mxc x myc)
+// Poisson row solve: s[6] (zf, mxc x ny) -> s[7] (mxc x myc); sub = parity
 __global__ void __launch_bounds__(128) k_lp_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
   const int i = lane, ny = c.ny, myc = c.myc;
   const double* zf = static_cast<const double*>(c.s[6]) + (size_t)i * ny;
   double* wv = static_cast<double*>(c.s[7]) + (size_t)i * myc;
   const FdmaRow R = fdma_row(c.pois_y, i);
-  double xm1 = 0.0, xm2 = 0.0;
-#pragma unroll 4
-  for (int k = 0; k < myc; k++) {
-    double v = pinv_lane<double>(c.pinv_y, zf, 1, k);
-    if (k >= 2) v = fma(xm2, R.low[k - 2], v);
-    wv[k] = v;
-    xm2 = xm1;
-    xm1 = v;
-  }
-  fdma_bwd_lane<double>(R, wv, 1);
+  pinv_fwd_par<double>(c.pinv_y, R, zf, 1, wv, 1, sub);
+  fdma_bwd_par<double>(R, wv, 1, sub);
 }
 
 // rows i < nx: ux = ux* - Sy+ Sy^N E ; uy = uy* - Sy+ Dy Sy^N Fv ;
-// p0 = (p0 - nu div) + Sy^N Gp / dt  (scratch rows: s[6], s[7])
+// p0 = (p0 - nu div) + Sy^N Gp / dt  (scratch rows: s[6], s[7]).
+// sub = 2 * part + parity q: part 0 ux, part 1 uy, part 2 p0, on parity q
 __global__ void __launch_bounds__(128) k_lp_box_y5(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc;
-  if (i < mxc) {
+  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, part = sub >> 1, q = sub & 1;
+  if (part == 2) {
+    const double* Gp = static_cast<const double*>(c.s[0]) + (size_t)i * myc;
+    double* p0 = static_cast<double*>(c.p0) + (size_t)i * ny;
+    const double* dv = static_cast<const double*>(c.s[3]) + (size_t)i * ny;
+#pragma unroll 4
+    for (int k = q; k < ny; k += 2) {
+      const double v = fnms(p0[k], dv[k], c.nu);
+      p0[k] = fmas(v, stencil_lane<double>(c.ycn, Gp, 1, k), c.inv_dt);
+    }
+    return;
+  }
+  if (i >= mxc) return;
+  double* d = static_cast<double*>(c.s[6 + part]) + (size_t)i * ny;
+  if (part == 0) {  // Sy^N E on parity q
     const double* E = static_cast<const double*>(c.s[1]) + (size_t)i * myc;
+#pragma unroll 4
+    for (int k = q; k < ny; k += 2) d[k] = stencil_lane<double>(c.ycn, E, 1, k);
+  } else {  // Dy Sy^N Fv on parity q (from Sy^N Fv on parity 1 - q)
     const double* Fv = static_cast<const double*>(c.s[2]) + (size_t)i * myc;
-    double* d0 = static_cast<double*>(c.s[6]) + (size_t)i * ny;  // Sy^N E (ortho), then its from_ortho
-    double* d1 = static_cast<double*>(c.s[7]) + (size_t)i * ny;  // Dy Sy^N Fv, then its from_ortho
-    DescDiff<double> D(ny);
-    for (int k = ny - 1; k >= 0; k--) {
-      d0[k] = stencil_lane<double>(c.ycn, E, 1, k);
-      d1[k] = D.step(k, stencil_lane<double>(c.ycn, Fv, 1, k));
-    }
-    from_ortho_lane<double>(c.ycd, d0, 1, d0, 1);
-    from_ortho_lane<double>(c.ycd, d1, 1, d1, 1);
-    double* ux = static_cast<double*>(c.ux) + (size_t)i * myc;
-    double* uy = static_cast<double*>(c.uy) + (size_t)i * myc;
-    const double* us = static_cast<const double*>(c.s[4]) + (size_t)i * myc;
-    const double* vs = static_cast<const double*>(c.s[5]) + (size_t)i * myc;
-    bool bad = false;
-    for (int k = 0; k < myc; k++) {
-      const double a = us[k] - d0[k], b = vs[k] - d1[k];
-      ux[k] = a;
-      uy[k] = b;
-      bad |= !(isfinite(a) && isfinite(b));
-    }
-    if (bad) atomicOr(c.status, 1u);
+    diff_par<double>(ny, q, [&](int k) { return stencil_lane<double>(c.ycn, Fv, 1, k); },
+                     [&](int k, double v) { d[k] = v; });
   }
-  const double* Gp = static_cast<const double*>(c.s[0]) + (size_t)i * myc;
-  double* p0 = static_cast<double*>(c.p0) + (size_t)i * ny;
-  const double* dv = static_cast<const double*>(c.s[3]) + (size_t)i * ny;
-  for (int k = 0; k < ny; k++) {
-    const double v = fnms(p0[k], dv[k], c.nu);
-    p0[k] = fmas(v, stencil_lane<double>(c.ycn, Gp, 1, k), c.inv_dt);
+  from_ortho_par<double>(c.ycd, d, 1, d, 1, q);
+  double* u = static_cast<double*>(part == 0 ? c.ux : c.uy) + (size_t)i * myc;
+  const double* us = static_cast<const double*>(c.s[4 + part]) + (size_t)i * myc;
+  bool bad = false;
+  for (int k = q; k < myc; k += 2) {
+    const double a = us[k] - d[k];
+    u[k] = a;
+    bad |= !isfinite(a);
   }
+  if (bad) atomicOr(c.status, 1u);
 }
 
 // ============================================================================
@@ -494,8 +560,17 @@ __global__ void __launch_bounds__(128) k_lp_per_y2(const CaseDev* __restrict__ c
 
 }  // namespace dev
 
+// sub-lanes per lane of each one-thread-per-lane kernel (blockIdx.y)
+int lane_kernel_subs(int kernel) {
+  switch (kernel) {
+    case K_LP_BOX_X2: case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y5: return 6;
+    case K_LP_BOX_GPX: case K_LP_BOX_X3: case K_LP_BOX_X4: case K_LP_BOX_Y4: return 2;
+    default: return 1;
+  }
+}
+
 cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work) {
-  dim3 g(nblocks), b(128);
+  dim3 g(nblocks, lane_kernel_subs(kernel)), b(128);
   switch (kernel) {
     case K_LP_BOX_GPX: dev::k_lp_box_gpx<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_BOX_X2: dev::k_lp_box_x2<<<g, b, 0, s>>>(cases, work); break;

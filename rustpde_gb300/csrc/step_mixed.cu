@@ -128,7 +128,9 @@ size_t smem_per_x_mixed(const CaseDev& c) {
 // ---------------------------------------------------------------------------
 static inline size_t clamp_smem_m(size_t s) { return (s + 127) & ~size_t(127); }
 
-StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_parallel) {
+StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
+  const bool lane_parallel = variant != 0;  // 128-thread or one-thread-per-lane forms
+  const bool lp = variant == 2;             // one-thread-per-lane forms wherever they exist
   StepPlan p;
   auto add = [&](int kernel, int lanes, size_t smem) {
     StepLaunch L;
@@ -179,7 +181,8 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
     // One CTA per row even in batches (a thread streaming a whole row through
     // its nine passes measured 1.7x slower: 3.9 vs 2.3 ms per ensemble step);
     // the batch variant launches it with 128 threads per row instead of 256
-    add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
+    if (lp) add_lp(K_LP_PER_Y2, mx);
+    else add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
     return p;
   }
   // ---- box
@@ -249,16 +252,15 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
                            ops.y2, ny, ky, 1.0, c.status));
   }
   // FP64: pressure gradient, Helmholtz (ADI), divergence, Poisson, projection.
-  // The batch variant (lane_parallel) offers each pass in a second form: one
-  // thread per lane where that measured faster on the 256-case ensemble (ms per
-  // step, CTA per lane vs thread per lane: gpx 0.16/0.12, x2 1.16/0.70, y3
-  // 1.34/1.06, y4 0.58/0.34, x4 0.54/0.48), and otherwise the same CTA kernel
-  // with 128 threads (y2 0.37/1.39, x3 0.24/0.42, y5 0.63/1.18 with threads per
-  // lane); rbc_batch_create times both variants of every pass on the batch and
-  // keeps the faster.
+  // Each pass has up to three forms: a CTA per lane (variant 0), the same
+  // kernel with 128 threads (variant 1, where it exists; otherwise the lane
+  // form) and one thread per (field, parity) sub-lane (variant 2, where it
+  // exists); rbc_batch_create times the forms of every pass on the batch and
+  // keeps the fastest.
   if (lane_parallel) add_lp(K_LP_BOX_GPX, ny);
   else add(K_BOX_GPX, ny, dev::smem_box_gpx(c));
-  add(lane_parallel ? K_BOX_Y2_PRE_T128 : K_BOX_Y2_PRE, nx, dev::smem_box_y2(c));
+  if (lp) add_lp(K_LP_BOX_Y2, nx);
+  else add(lane_parallel ? K_BOX_Y2_PRE_T128 : K_BOX_Y2_PRE, nx, dev::smem_box_y2(c));
   if (lane_parallel) {
     add_lp(K_LP_BOX_X2, myc);
     add_lp(K_LP_BOX_Y3, mxc);
@@ -266,7 +268,8 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
     add(K_BOX_X2, myc, dev::smem_box_x2(c));
     add(K_BOX_Y3, mxc, dev::smem_box_y3(c));
   }
-  add(lane_parallel ? K_BOX_X3_MIX_T128 : K_BOX_X3_MIX, ny, dev::smem_box_x3(c));
+  if (lp) add_lp(K_LP_BOX_X3, ny);
+  else add(lane_parallel ? K_BOX_X3_MIX_T128 : K_BOX_X3_MIX, ny, dev::smem_box_x3(c));
   {  // eigenbasis forward along x: s[6] = fwd * m_z (columns j < ny)
     void* zi[1] = {c.m_z};
     void* zo[1] = {c.s[6]};
@@ -283,7 +286,8 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, bool lane_paral
   }
   if (lane_parallel) add_lp(K_LP_BOX_X4, myc);
   else add(K_BOX_X4_MIX, myc, dev::smem_box_x4(c));
-  add(lane_parallel ? K_BOX_Y5_T128 : K_BOX_Y5, nx, dev::smem_box_y5(c));
+  if (lp) add_lp(K_LP_BOX_Y5, nx);
+  else add(lane_parallel ? K_BOX_Y5_T128 : K_BOX_Y5, nx, dev::smem_box_y5(c));
   return p;
 }
 
