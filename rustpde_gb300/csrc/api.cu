@@ -1166,9 +1166,9 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     bk.plan = merge_plans(plans, bk.members, {});
     upload_plan(b->arena, bk.plan, bk.dp);
     // autotune: where a pass has other forms (128-thread CTAs, one thread per
-    // sub-lane), time every form on this batch and keep the fastest (the state
-    // is still zero; the choice is made once, so the batch's numbers do not
-    // depend on later timings)
+    // sub-lane; a form may take several launches), time every form on this
+    // batch and keep the fastest (the state is still zero; the choice is made
+    // once, so the batch's numbers do not depend on later timings)
     const size_t nalt = b->cases[bk.members[0]]->plan_alts.size();
     std::vector<StepPlan> alts(nalt);
     std::vector<DevPlan> adps(nalt);
@@ -1196,35 +1196,55 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       }
       return best;
     };
-    for (size_t li = 0; li < bk.plan.launches.size(); li++) {
-      const int base_kernel = bk.plan.launches[li].kernel;
+    // launch indices of each pass, in order
+    auto passes = [](const StepPlan& P) {
+      std::vector<std::vector<size_t>> g;
+      for (size_t li = 0; li < P.launches.size(); li++) {
+        if (g.empty() || P.launches[g.back()[0]].pass != P.launches[li].pass) g.emplace_back();
+        g.back().push_back(li);
+      }
+      return g;
+    };
+    auto kernels_of = [](const StepPlan& P, const std::vector<size_t>& g) {
+      std::vector<int> k;
+      for (size_t li : g) k.push_back(P.launches[li].kernel);
+      return k;
+    };
+    const auto gb = passes(bk.plan);
+    std::vector<std::vector<std::vector<size_t>>> ga(nalt);
+    for (size_t a = 0; a < nalt; a++) {
+      ga[a] = passes(alts[a]);
+      if (ga[a].size() != gb.size()) throw std::runtime_error("autotune: plan forms of different pass structure");
+    }
+    StepPlan tuned;
+    for (size_t pi = 0; pi < gb.size(); pi++) {
+      auto group_time = [&](const StepPlan& P, const DevPlan& dp, const std::vector<size_t>& g) {
+        float t = 0.f;
+        for (size_t li : g) t += time_launch(P.launches[li], dp, li);
+        return t;
+      };
+      std::vector<std::vector<int>> seen{kernels_of(bk.plan, gb[pi])};
       float t_base = -1.f, t_best_alt = 1e30f;
-      int best = -1, best_alt_kernel = base_kernel;
-      std::vector<int> seen{base_kernel};
+      int best = -1, best_alt_kernel = bk.plan.launches[gb[pi][0]].kernel;
       for (size_t a = 0; a < nalt; a++) {
-        const int k = alts[a].launches[li].kernel;
-        if (std::find(seen.begin(), seen.end(), k) != seen.end()) continue;
-        seen.push_back(k);
-        if (t_base < 0) t_base = time_launch(bk.plan.launches[li], bk.dp, li);
-        const float t = time_launch(alts[a].launches[li], adps[a], li);
+        const auto ks = kernels_of(alts[a], ga[a][pi]);
+        if (std::find(seen.begin(), seen.end(), ks) != seen.end()) continue;
+        seen.push_back(ks);
+        if (t_base < 0) t_base = group_time(bk.plan, bk.dp, gb[pi]);
+        const float t = group_time(alts[a], adps[a], ga[a][pi]);
         if (t < t_best_alt) {
           t_best_alt = t;
-          best_alt_kernel = k;
+          best_alt_kernel = ks[0];
           if (t < t_base) best = (int)a;
         }
       }
-      if (t_base < 0) continue;  // no other form of this pass
-      b->tuning.push_back({base_kernel, best_alt_kernel, t_base, t_best_alt});
-      if (best >= 0) {
-        const DevPlan& adp = adps[best];
-        bk.plan.launches[li] = alts[best].launches[li];
-        bk.dp.work[li] = adp.work[li];
-        bk.dp.jobs[li] = adp.jobs[li];
-        bk.dp.tiles[li] = adp.tiles[li];
-        bk.dp.ntiles[li] = adp.ntiles[li];
-        bk.dp.max_nt[li] = adp.max_nt[li];
-      }
+      if (t_base >= 0) b->tuning.push_back({bk.plan.launches[gb[pi][0]].kernel, best_alt_kernel, t_base, t_best_alt});
+      const StepPlan& src = best >= 0 ? alts[best] : bk.plan;
+      for (size_t li : (best >= 0 ? ga[best][pi] : gb[pi])) tuned.launches.push_back(src.launches[li]);
     }
+    bk.plan = std::move(tuned);
+    bk.dp = DevPlan();
+    upload_plan(b->arena, bk.plan, bk.dp);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
   }

@@ -20,12 +20,16 @@ enum StepKernel {
   K_LP_PER_Y2,
   // the same CTA-per-lane kernels launched with 128 threads (more CTAs per SM)
   K_PER_Y2_PRE_T128, K_BOX_Y2_PRE_T128, K_BOX_X3_MIX_T128, K_BOX_Y5_T128,
+  // periodic Y2 as three one-thread-per-sub-lane launches (right-hand sides and
+  // Helmholtz solves; divergence and Poisson; projection and updates)
+  K_LP_PER_Y2A, K_LP_PER_Y2B, K_LP_PER_Y2C,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };
 
 struct StepLaunch {
   int kernel;
+  int pass = -1;  // launches of one pass share the id (the autotuner swaps whole passes)
   size_t smem;
   std::vector<int4> items;       // (case index, first lane, lane count, 0)
   std::vector<GemmJobDev> jobs;  // K_GEMM only
@@ -51,8 +55,6 @@ struct MixedOps {
   const float* pf = nullptr;  // Poisson eigenbasis forward: (nx - 2) x (nx - 2)
   const float* pb = nullptr;  // Poisson eigenbasis backward: (nx - 2) x (nx - 2)
 };
-// lane_parallel: the FP64 passes run one thread per lane (many lanes: batches);
-// otherwise one CTA per lane (a single case)
 // variant 0: a CTA per lane; 1: 128-thread CTAs where that form exists, else
 // one thread per lane; 2: one thread per (field, parity) sub-lane where that
 // form exists, else 128-thread CTAs

@@ -160,6 +160,19 @@ __device__ __forceinline__ void diff_par(int n, int q, A a, S store) {
   }
 }
 
+// Fdma forward elimination on the parity-q indices of a strided lane, in place
+template <class T>
+__device__ __forceinline__ void fdma_fwd_par(const FdmaRow& f, T* x, long long s, int q) {
+  T xm2 = zero_v<T>();
+#pragma unroll 4
+  for (int i = q; i < f.m; i += 2) {
+    T v = x[(long long)i * s];
+    if (i >= 2) v = fmas(v, xm2, f.low[i - 2]);
+    x[(long long)i * s] = v;
+    xm2 = v;
+  }
+}
+
 // Fdma back substitution on the parity-q indices of a strided lane, in place
 template <class T>
 __device__ __forceinline__ void fdma_bwd_par(const FdmaRow& f, T* x, long long s, int q) {
@@ -221,6 +234,19 @@ __device__ __forceinline__ void from_ortho_par(const BasisDev& b, const T* p, lo
   const CaseDev& c = cases[w.x];                                             \
   if (c.gate != nullptr && c.gate[1] == 0) return;                           \
   const int lane = w.y + (int)threadIdx.x;                                   \
+  const int sub = (int)blockIdx.y;                                           \
+  (void)sub;
+
+// row kernels: the two parity chains of a row run on adjacent threads of a
+// warp (q = threadIdx.x & 1), so a warp's loads of elements k and k + 1 share
+// sectors; blockIdx.y selects the field or part
+#define ROW_PROLOGUE                                                         \
+  const int4 w = work[blockIdx.x];                                           \
+  if ((int)(threadIdx.x >> 1) >= w.z) return;                                \
+  const CaseDev& c = cases[w.x];                                             \
+  if (c.gate != nullptr && c.gate[1] == 0) return;                           \
+  const int lane = w.y + (int)(threadIdx.x >> 1);                            \
+  const int q = (int)(threadIdx.x & 1);                                      \
   const int sub = (int)blockIdx.y;                                           \
   (void)sub;
 
@@ -289,9 +315,9 @@ __global__ void __launch_bounds__(128) k_lp_box_x4(const CaseDev* __restrict__ c
 // pinv_y -> s[1..3].  sub = 2 * field + parity q: the field's right-hand side
 // and pinv rows on the columns of parity q (dP/dy on parity q comes from p0 on
 // parity 1 - q)
-__global__ void __launch_bounds__(128) k_lp_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
-  LANE_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, kx = c.kx, ky = c.ky, f = sub >> 1, q = sub & 1;
+__global__ void __launch_bounds__(256) k_lp_box_y2(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, kx = c.kx, ky = c.ky, f = sub;
   const double dt = c.dt;
   const void* f3[3] = {c.ux, c.uy, c.temp};
   const BasisDev* xb[3] = {&c.xu, &c.xu, &c.xt};
@@ -353,9 +379,9 @@ __global__ void __launch_bounds__(128) k_lp_box_y2(const CaseDev* __restrict__ c
 // state; A = Sy ux* -> s[1], B = Dy Sy uy* -> s[2] (mxc x ny).  sub = 2 *
 // field + parity q: the field's chain of parity q, then A on parity q (ux) or
 // B on parity 1 - q (uy)
-__global__ void __launch_bounds__(128) k_lp_box_y3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
-  LANE_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, f = sub >> 1, q = sub & 1;
+__global__ void __launch_bounds__(256) k_lp_box_y3(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, f = sub;
   double* F = static_cast<double*>(c.s[4 + f]) + (size_t)i * myc;
   const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, 0);
   {
@@ -393,22 +419,22 @@ __global__ void __launch_bounds__(128) k_lp_box_y3(const CaseDev* __restrict__ c
 
 // rows i < mxc: pinv_y of the eigenbasis-transformed divergence and the
 // Poisson row solve: s[6] (zf, mxc x ny) -> s[7] (mxc x myc); sub = parity
-__global__ void __launch_bounds__(128) k_lp_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
-  LANE_PROLOGUE
+__global__ void __launch_bounds__(256) k_lp_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
   const int i = lane, ny = c.ny, myc = c.myc;
   const double* zf = static_cast<const double*>(c.s[6]) + (size_t)i * ny;
   double* wv = static_cast<double*>(c.s[7]) + (size_t)i * myc;
   const FdmaRow R = fdma_row(c.pois_y, i);
-  pinv_fwd_par<double>(c.pinv_y, R, zf, 1, wv, 1, sub);
-  fdma_bwd_par<double>(R, wv, 1, sub);
+  pinv_fwd_par<double>(c.pinv_y, R, zf, 1, wv, 1, q);
+  fdma_bwd_par<double>(R, wv, 1, q);
 }
 
 // rows i < nx: ux = ux* - Sy+ Sy^N E ; uy = uy* - Sy+ Dy Sy^N Fv ;
 // p0 = (p0 - nu div) + Sy^N Gp / dt  (scratch rows: s[6], s[7]).
 // sub = 2 * part + parity q: part 0 ux, part 1 uy, part 2 p0, on parity q
-__global__ void __launch_bounds__(128) k_lp_box_y5(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
-  LANE_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, part = sub >> 1, q = sub & 1;
+__global__ void __launch_bounds__(256) k_lp_box_y5(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, mxc = c.mxc, part = sub;
   if (part == 2) {
     const double* Gp = static_cast<const double*>(c.s[0]) + (size_t)i * myc;
     double* p0 = static_cast<double*>(c.p0) + (size_t)i * ny;
@@ -556,21 +582,170 @@ __global__ void __launch_bounds__(128) k_lp_per_y2(const CaseDev* __restrict__ c
   if (bad) atomicOr(c.status, 1u);
 }
 
+// ============================================================================
+// Periodic Y2 as three launches of one thread per sub-lane (rows i < mx,
+// complex).  Y2A writes the Helmholtz solutions to scratch (yw[3..5]) because
+// the uy right-hand side reads the old temperature; Y2C moves them into the
+// state.  Same operations as k_lp_per_y2 (navier.rs:622-721).
+// ============================================================================
+// Y2A, sub = 2 * field + parity q: right-hand side, pinv rows and the row's
+// banded Helmholtz solve of one field on the columns of parity q
+__global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, f = sub;
+  const double dt = c.dt, inv_asp = 1.0 / c.aspect, ki = (double)i;
+  const void* st3[3] = {c.ux, c.uy, c.temp};
+  const double2* Fo = static_cast<const double2*>(st3[f]) + (size_t)i * myc;
+  const double2* To = static_cast<const double2*>(c.temp) + (size_t)i * myc;
+  const double2* P = static_cast<const double2*>(c.p0) + (size_t)i * ny;
+  const double2* cv = static_cast<const double2*>(c.m_cv);
+  const double2* bco = static_cast<const double2*>(c.bc_ortho) + (size_t)i * ny;
+  const double2* bcd = static_cast<const double2*>(c.bc_diff) + (size_t)i * ny;
+  double2* out = static_cast<double2*>(c.yw[3 + f]) + (size_t)i * ny;
+  const PinvDev& pv = c.pinv_y;
+  double2 r2 = c2(0.0, 0.0), r4 = c2(0.0, 0.0), g2 = c2(0.0, 0.0);
+  for (int k = top_par(ny, q); k >= 0; k -= 2) {
+    const double2 o = stencil_lane<double2>(c.ycd, Fo, 1, k);
+    const bool incv = i < kx && k < ky;
+    const double2 cvk = incv ? cv[((size_t)f * kx + i) * ky + k] : c2(0.0, 0.0);
+    double2 r;
+    if (f == 0) {
+      const double2 gx = mul_ik(P[k], ki) * inv_asp;
+      r = fnms(fnms(o, gx, dt), cvk, dt);
+    } else if (f == 1) {  // dP/dy at k (descending derivative recurrence), buoyancy
+      double2 g;
+      if (k == ny - 1) g = c2(0.0, 0.0);
+      else if (k >= 1) g = fmas(g2, P[k + 1], 2.0 * (double)(k + 1));
+      else g = fmas(P[1], g2, 0.5);
+      g2 = g;
+      const double2 that = stencil_lane<double2>(c.ycd, To, 1, k) + bco[k];
+      r = fnms(fmas(fnms(o, g, dt), that, dt), cvk, dt);
+    } else {
+      r = fnms(o + bcd[k], cvk, dt);
+    }
+    if (k < myc) {
+      double2 v = scal(r, pv.dia[k]);
+      if (k < myc - 2) v = fmas(v, r2, pv.up1[k]);
+      if (k < myc - 4) v = fmas(v, r4, pv.up2[k]);
+      out[k] = v;
+    }
+    r4 = r2;
+    r2 = r;
+  }
+  const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, i);
+  fdma_fwd_par<double2>(R, out, 1, q);
+  fdma_bwd_par<double2>(R, out, 1, q);
+}
+
+// Y2B, sub = parity q: divergence ik/s Sy ux* + Dy Sy uy* on parity q (from
+// uy* on parity 1 - q), pinv rows and the Poisson row solve -> p1 (p1[0,0] = 0)
+__global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc;
+  const double inv_asp = 1.0 / c.aspect, ki = (double)i;
+  const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
+  const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
+  double2* dvr = static_cast<double2*>(c.yw[0]) + (size_t)i * ny;
+  double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
+  const PinvDev& pv = c.pinv_y;
+  double2 g2 = c2(0.0, 0.0), w2 = c2(0.0, 0.0), w4 = c2(0.0, 0.0);
+  for (int k = top_par(ny, q); k >= 0; k -= 2) {
+    const double2 o0 = stencil_lane<double2>(c.ycd, U, 1, k);
+    double2 g;
+    if (k == ny - 1) g = c2(0.0, 0.0);
+    else if (k >= 1) g = fmas(g2, stencil_lane<double2>(c.ycd, V, 1, k + 1), 2.0 * (double)(k + 1));
+    else g = fmas(stencil_lane<double2>(c.ycd, V, 1, 1), g2, 0.5);
+    g2 = g;
+    const double2 d = mul_ik(o0, ki) * inv_asp + g;
+    dvr[k] = d;
+    if (k < myc) {
+      double2 v = scal(d, pv.dia[k]);
+      if (k < myc - 2) v = fmas(v, w2, pv.up1[k]);
+      if (k < myc - 4) v = fmas(v, w4, pv.up2[k]);
+      p1[k] = v;
+    }
+    w4 = w2;
+    w2 = d;
+  }
+  const FdmaRow R = fdma_row(c.pois_y, i);
+  fdma_fwd_par<double2>(R, p1, 1, q);
+  fdma_bwd_par<double2>(R, p1, 1, q);
+  if (i == 0 && q == 0) p1[0] = c2(0.0, 0.0);
+}
+
+// Y2C, sub = 2 * parity q + part: part 0: O1 = Sy^N p1, dp/dx, pres[0] and
+// ux, temperature on parity q; part 1: dp/dy on parity 1 - q and uy there
+__global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  const int i = lane, ny = c.ny, myc = c.myc, part = sub;
+  const double inv_asp = 1.0 / c.aspect, ki = (double)i;
+  const double2* p1 = static_cast<const double2*>(c.p1) + (size_t)i * myc;
+  bool bad = false;
+  if (part == 0) {
+    double2* dpx = static_cast<double2*>(c.yw[1]) + (size_t)i * ny;
+    double2* P = static_cast<double2*>(c.p0) + (size_t)i * ny;
+    const double2* dvr = static_cast<const double2*>(c.yw[0]) + (size_t)i * ny;
+#pragma unroll 4
+    for (int k = q; k < ny; k += 2) {
+      const double2 o1 = stencil_lane<double2>(c.ycn, p1, 1, k);
+      dpx[k] = mul_ik(o1, ki) * inv_asp;
+      const double2 v = fnms(P[k], dvr[k], c.nu);
+      P[k] = fmas(v, o1, c.inv_dt);
+    }
+    from_ortho_par<double2>(c.ycd, dpx, 1, dpx, 1, q);
+    const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
+    const double2* T = static_cast<const double2*>(c.yw[5]) + (size_t)i * ny;
+    double2* ux = static_cast<double2*>(c.ux) + (size_t)i * myc;
+    double2* tt = static_cast<double2*>(c.temp) + (size_t)i * myc;
+    for (int k = q; k < myc; k += 2) {
+      const double2 a = U[k] - dpx[k];
+      const double2 t = T[k];
+      ux[k] = a;
+      tt[k] = t;
+      bad |= !(finite_v(a) && finite_v(t));
+    }
+  } else {
+    double2* dpy = static_cast<double2*>(c.yw[2]) + (size_t)i * ny;
+    diff_par<double2>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
+                      [&](int k, double2 d) { dpy[k] = d; });
+    from_ortho_par<double2>(c.ycd, dpy, 1, dpy, 1, 1 - q);
+    const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
+    double2* uy = static_cast<double2*>(c.uy) + (size_t)i * myc;
+    for (int k = 1 - q; k < myc; k += 2) {
+      const double2 b = V[k] - dpy[k];
+      uy[k] = b;
+      bad |= !finite_v(b);
+    }
+  }
+  if (bad) atomicOr(c.status, 1u);
+}
+
 #undef LANE_PROLOGUE
 
 }  // namespace dev
 
-// sub-lanes per lane of each one-thread-per-lane kernel (blockIdx.y)
+// grid.y of each one-thread-per-lane kernel: column kernels put (field,
+// parity) sub-lanes there; row kernels put the field or part there and the
+// parity on adjacent threads (256 threads for 128 lanes)
 int lane_kernel_subs(int kernel) {
   switch (kernel) {
-    case K_LP_BOX_X2: case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y5: return 6;
-    case K_LP_BOX_GPX: case K_LP_BOX_X3: case K_LP_BOX_X4: case K_LP_BOX_Y4: return 2;
+    case K_LP_BOX_X2: return 6;
+    case K_LP_BOX_GPX: case K_LP_BOX_X3: case K_LP_BOX_X4: return 2;
+    case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y5: case K_LP_PER_Y2A: return 3;
+    case K_LP_PER_Y2C: return 2;
     default: return 1;
+  }
+}
+static bool lane_kernel_rows(int kernel) {
+  switch (kernel) {
+    case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y4: case K_LP_BOX_Y5:
+    case K_LP_PER_Y2A: case K_LP_PER_Y2B: case K_LP_PER_Y2C: return true;
+    default: return false;
   }
 }
 
 cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work) {
-  dim3 g(nblocks, lane_kernel_subs(kernel)), b(128);
+  dim3 g(nblocks, lane_kernel_subs(kernel)), b(lane_kernel_rows(kernel) ? 256 : 128);
   switch (kernel) {
     case K_LP_BOX_GPX: dev::k_lp_box_gpx<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_BOX_X2: dev::k_lp_box_x2<<<g, b, 0, s>>>(cases, work); break;
@@ -581,6 +756,9 @@ cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const Ca
     case K_LP_BOX_Y4: dev::k_lp_box_y4<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_BOX_Y5: dev::k_lp_box_y5<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_PER_Y2: dev::k_lp_per_y2<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_PER_Y2A: dev::k_lp_per_y2a<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_PER_Y2B: dev::k_lp_per_y2b<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_PER_Y2C: dev::k_lp_per_y2c<<<g, b, 0, s>>>(cases, work); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

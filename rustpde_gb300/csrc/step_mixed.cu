@@ -132,12 +132,19 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   const bool lane_parallel = variant != 0;  // 128-thread or one-thread-per-lane forms
   const bool lp = variant == 2;             // one-thread-per-lane forms wherever they exist
   StepPlan p;
+  // pass ids: one per pass, the same in every variant; `group` >= 0 gives the
+  // following launches one shared id (a pass made of several launches)
+  int npass = 0, group = -1;
+  auto push = [&](StepLaunch& L) {
+    L.pass = group >= 0 ? group : npass++;
+    p.launches.push_back(L);
+  };
   auto add = [&](int kernel, int lanes, size_t smem) {
     StepLaunch L;
     L.kernel = kernel;
     L.smem = clamp_smem_m(smem);
     for (int i = 0; i < lanes; i++) L.items.push_back(make_int4(0, i, 1, 0));
-    p.launches.push_back(L);
+    push(L);
   };
   // one-thread-per-lane kernel: items of up to kLaneThreads consecutive lanes
   auto add_lp = [&](int kernel, int lanes) {
@@ -145,14 +152,14 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     L.kernel = kernel;
     L.smem = 0;
     for (int i = 0; i < lanes; i += kLaneThreads) L.items.push_back(make_int4(0, i, std::min(kLaneThreads, lanes - i), 0));
-    p.launches.push_back(L);
+    push(L);
   };
   auto add_gemm = [&](const GemmJobDev& j) {
     StepLaunch L;
     L.kernel = K_GEMM;
     L.smem = gemm_smem_bytes(j.NT);
     L.jobs.push_back(j);
-    p.launches.push_back(L);
+    push(L);
   };
   const int mx = c.mx, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
   if (c.kind == KIND_PERIODIC) {
@@ -177,12 +184,18 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     for (int f = 0; f < 3; f++) cvp[f] = static_cast<double2*>(c.m_cv) + (size_t)f * kx * ky;
     LaneSideDev co = lane_rows(cvp, 3, kx, ky, ky, LT_F64, true);
     add_gemm(make_gemm_job(qi, co, ops.y2, ny, ky, 1.0, c.status));
-    // Y2: FP64 right-hand sides, banded solves, projection, pressure update.
-    // One CTA per row even in batches (a thread streaming a whole row through
-    // its nine passes measured 1.7x slower: 3.9 vs 2.3 ms per ensemble step);
-    // the batch variant launches it with 128 threads per row instead of 256
-    if (lp) add_lp(K_LP_PER_Y2, mx);
-    else add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
+    // Y2: FP64 right-hand sides, banded solves, projection, pressure update:
+    // one CTA per row (256 or 128 threads), or three launches of one thread
+    // per (field, parity) sub-lane
+    if (lp) {
+      group = npass++;
+      add_lp(K_LP_PER_Y2A, mx);
+      add_lp(K_LP_PER_Y2B, mx);
+      add_lp(K_LP_PER_Y2C, mx);
+      group = -1;
+    } else {
+      add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
+    }
     return p;
   }
   // ---- box
@@ -208,6 +221,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   {
     StepLaunch L;
     L.kernel = K_GEMM;
+    L.pass = npass++;
     void* a_in[2] = {c.m_y[0], c.m_y[1]};
     void* a_out[2] = {c.m_ph[0], c.m_ph[1]};
     L.jobs.push_back(make_gemm_job(lane_rows(a_in, 2, ny, mxc, mxc, LT_F32, false),
@@ -343,6 +357,7 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
       case K_LP_BOX_Y5: kernel = K_BOX_Y5; break;
       case K_LP_PER_Y2: kernel = K_PER_Y2_PRE; break;
       case K_PER_Y2_PRE_T128: kernel = K_PER_Y2_PRE; break;
+      case K_LP_PER_Y2B: case K_LP_PER_Y2C: kernel = -1; break;  // counted with Y2A
       case K_BOX_Y2_PRE_T128: kernel = K_BOX_Y2_PRE; break;
       case K_BOX_X3_MIX_T128: kernel = K_BOX_X3_MIX; break;
       case K_BOX_Y5_T128: kernel = K_BOX_Y5; break;
@@ -351,6 +366,7 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
     switch (kernel) {
       case K_Y1_C: case K_Y1_R: v = 3 * myc * z + 6 * ny * z; break;
       case K_PER_X: v = 6 * mx * z + 2 * nx * 8 + 3 * kx * z; break;
+      case K_LP_PER_Y2A:  // the three launches of the periodic Y2 pass move the Y2 arrays once
       case K_PER_Y2: case K_PER_Y2_PRE:
         v = (kernel == K_PER_Y2 ? 3 * ny : 3 * ky) * z + 2 * 3 * myc * z + 2 * ny * z + 2 * ny * z + 12 * myc * 8 +
             myc * z;
@@ -388,7 +404,8 @@ const char* step_kernel_name(int kernel) {
                                 "box_y2_pre", "box_x3_mix", "box_x4_mix", "box_gpx", "lanes_box_gpx",
                                 "lanes_box_x2", "lanes_box_x3", "lanes_box_x4", "lanes_box_y2", "lanes_box_y3",
                                 "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2", "periodic_y2_pre_t128",
-                                "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128"};
+                                "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128", "lanes_periodic_y2a",
+                                "lanes_periodic_y2b", "lanes_periodic_y2c"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";
