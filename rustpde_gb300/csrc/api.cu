@@ -119,6 +119,10 @@ static StepPlan merge_plans(const std::vector<const StepPlan*>& plans, const std
         L.jobs.push_back(j);
       }
     }
+    // items that carry a cost (one-thread-per-lane kernels): most expensive
+    // first, so the last CTAs to start are the cheapest
+    if (!L.items.empty() && L.items[0].w > 0)
+      std::stable_sort(L.items.begin(), L.items.end(), [](const int4& a, const int4& b) { return a.w > b.w; });
   }
   return P;
 }

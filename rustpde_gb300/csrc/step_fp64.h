@@ -60,8 +60,13 @@ struct MixedOps {
 // form exists, else 128-thread CTAs
 StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant);
 int lane_kernel_subs(int kernel);
+bool lane_kernel_rows(int kernel);
 cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work);
-constexpr int kLaneThreads = 128;  // lanes per CTA of the one-thread-per-lane kernels
+// one-thread-per-lane kernels: 64 threads per CTA, i.e. 64 column lanes or 32
+// row lanes (two parity threads each) per work item; small items, sorted by
+// cost (item.w = lanes x lane length) in merged plans, keep the SMs evenly busy
+constexpr int kLaneBlock = 64;
+inline int lane_item_lanes(int kernel) { return lane_kernel_rows(kernel) ? kLaneBlock / 2 : kLaneBlock; }
 const char* step_kernel_name(int kernel);
 // serving gate of the cases members[0..n) of `cases` (see CaseDev::gate)
 cudaError_t launch_gate(const CaseDev* cases, const int* members, int n, cudaStream_t s);

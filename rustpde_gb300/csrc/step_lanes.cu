@@ -736,7 +736,7 @@ int lane_kernel_subs(int kernel) {
     default: return 1;
   }
 }
-static bool lane_kernel_rows(int kernel) {
+bool lane_kernel_rows(int kernel) {
   switch (kernel) {
     case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y4: case K_LP_BOX_Y5:
     case K_LP_PER_Y2A: case K_LP_PER_Y2B: case K_LP_PER_Y2C: return true;
@@ -745,7 +745,7 @@ static bool lane_kernel_rows(int kernel) {
 }
 
 cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work) {
-  dim3 g(nblocks, lane_kernel_subs(kernel)), b(lane_kernel_rows(kernel) ? 256 : 128);
+  dim3 g(nblocks, lane_kernel_subs(kernel)), b(kLaneBlock);
   switch (kernel) {
     case K_LP_BOX_GPX: dev::k_lp_box_gpx<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_BOX_X2: dev::k_lp_box_x2<<<g, b, 0, s>>>(cases, work); break;

@@ -146,12 +146,17 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     for (int i = 0; i < lanes; i++) L.items.push_back(make_int4(0, i, 1, 0));
     push(L);
   };
-  // one-thread-per-lane kernel: items of up to kLaneThreads consecutive lanes
-  auto add_lp = [&](int kernel, int lanes) {
+  // one-thread-per-lane kernel: items of lane_item_lanes() consecutive lanes
+  // of length `len` (item.w = the item's cost, lanes x len)
+  auto add_lp = [&](int kernel, int lanes, int len) {
     StepLaunch L;
     L.kernel = kernel;
     L.smem = 0;
-    for (int i = 0; i < lanes; i += kLaneThreads) L.items.push_back(make_int4(0, i, std::min(kLaneThreads, lanes - i), 0));
+    const int per = lane_item_lanes(kernel);
+    for (int i = 0; i < lanes; i += per) {
+      const int n = std::min(per, lanes - i);
+      L.items.push_back(make_int4(0, i, n, n * len));
+    }
     push(L);
   };
   auto add_gemm = [&](const GemmJobDev& j) {
@@ -189,9 +194,9 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     // per (field, parity) sub-lane
     if (lp) {
       group = npass++;
-      add_lp(K_LP_PER_Y2A, mx);
-      add_lp(K_LP_PER_Y2B, mx);
-      add_lp(K_LP_PER_Y2C, mx);
+      add_lp(K_LP_PER_Y2A, mx, ny);
+      add_lp(K_LP_PER_Y2B, mx, ny);
+      add_lp(K_LP_PER_Y2C, mx, ny);
       group = -1;
     } else {
       add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
@@ -271,18 +276,18 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   // form) and one thread per (field, parity) sub-lane (variant 2, where it
   // exists); rbc_batch_create times the forms of every pass on the batch and
   // keeps the fastest.
-  if (lane_parallel) add_lp(K_LP_BOX_GPX, ny);
+  if (lane_parallel) add_lp(K_LP_BOX_GPX, ny, nx);
   else add(K_BOX_GPX, ny, dev::smem_box_gpx(c));
-  if (lp) add_lp(K_LP_BOX_Y2, nx);
+  if (lp) add_lp(K_LP_BOX_Y2, nx, ny);
   else add(lane_parallel ? K_BOX_Y2_PRE_T128 : K_BOX_Y2_PRE, nx, dev::smem_box_y2(c));
   if (lane_parallel) {
-    add_lp(K_LP_BOX_X2, myc);
-    add_lp(K_LP_BOX_Y3, mxc);
+    add_lp(K_LP_BOX_X2, myc, mxc);
+    add_lp(K_LP_BOX_Y3, mxc, ny);
   } else {
     add(K_BOX_X2, myc, dev::smem_box_x2(c));
     add(K_BOX_Y3, mxc, dev::smem_box_y3(c));
   }
-  if (lp) add_lp(K_LP_BOX_X3, ny);
+  if (lp) add_lp(K_LP_BOX_X3, ny, nx);
   else add(lane_parallel ? K_BOX_X3_MIX_T128 : K_BOX_X3_MIX, ny, dev::smem_box_x3(c));
   {  // eigenbasis forward along x: s[6] = fwd * m_z (columns j < ny)
     void* zi[1] = {c.m_z};
@@ -290,7 +295,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     add_gemm(make_gemm_job(lane_cols(zi, 1, ny, mxc, ny, LT_F64, 0), lane_cols(zo, 1, ny, mxc, ny, LT_F64, 0), ops.pf,
                            mxc, mxc, 1.0, c.status));
   }
-  if (lane_parallel) add_lp(K_LP_BOX_Y4, mxc);
+  if (lane_parallel) add_lp(K_LP_BOX_Y4, mxc, ny);
   else add(K_BOX_Y4, mxc, dev::smem_box_y4(c));
   {  // eigenbasis backward along x: p1 = bwd * s[7] (columns j < myc)
     void* wi[1] = {c.s[7]};
@@ -298,9 +303,9 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     add_gemm(make_gemm_job(lane_cols(wi, 1, myc, mxc, myc, LT_F64, 0), lane_cols(po, 1, myc, mxc, myc, LT_F64, 0),
                            ops.pb, mxc, mxc, 1.0, c.status));
   }
-  if (lane_parallel) add_lp(K_LP_BOX_X4, myc);
+  if (lane_parallel) add_lp(K_LP_BOX_X4, myc, nx);
   else add(K_BOX_X4_MIX, myc, dev::smem_box_x4(c));
-  if (lp) add_lp(K_LP_BOX_Y5, nx);
+  if (lp) add_lp(K_LP_BOX_Y5, nx, ny);
   else add(lane_parallel ? K_BOX_Y5_T128 : K_BOX_Y5, nx, dev::smem_box_y5(c));
   return p;
 }
