@@ -234,6 +234,8 @@ def run_ensemble(args, rank, world, local):
 
     # ---- per-kernel profile of the batched step (each launch alone) and roofline
     prof = B.profile_step(3)
+    per_launch = [{"bucket": b_, "pass": p_, "kernel": k_, "ms": round(m_, 4), "bytes": b2_}
+                  for b_, p_, k_, m_, b2_ in B.profile_launches(3)]
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_bytes = prof[dom]
     pk, pk_src = peaks()
@@ -255,7 +257,8 @@ def run_ensemble(args, rank, world, local):
 
     if args.skip_plain:  # profiling runs: the batched mixed step only
         return {"metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "steps": K, "warmup": W,
-                "cases": len(params), "mode": "batched mixed only", "kernels_ms_per_step": {k: v[0] for k, v in prof.items()}}
+                "cases": len(params), "mode": "batched mixed only", "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
+                "launches": per_launch}
 
     # ---- plain FP64, case by case, same ensemble and initial fields
     plain_ms = 0.0
@@ -312,6 +315,7 @@ def run_ensemble(args, rank, world, local):
                 "how": "per step: rbc_batch_set_state_all (pinned h2d), rbc_batch_step(1), rbc_batch_get_state_all"},
         "gpu_launches": K * launches,
         "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
+        "launches_ms": per_launch,
         "autotuner": [{"pass": t[0], "ms_cta_per_lane": t[1], "ms_thread_per_lane": t[2], "chosen": t[3]}
                       for t in tuning],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",

@@ -200,6 +200,10 @@ int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* st
  * batch (ms per launch) and kept the faster.  *n = number of decisions; entry k
  * (if 0 <= k < *n) is written to the non-null outputs (kernel ids: see
  * rbc_kernel_name). */
+/* every launch of the batch step timed alone, in step order: kernel id
+ * (rbc_kernel_name), bucket, pass id, mean ms, algorithmic bytes (may be NULL) */
+int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket, int* pass, double* ms,
+                               double* bytes, int max_launches, int* nlaunches);
 int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
                      int* n);
 int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes);

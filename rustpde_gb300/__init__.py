@@ -142,6 +142,7 @@ _SIGNATURES = {
     "rbc_server_destroy": (_I, [_P]),
     "rbc_batch_profile_step": (_I, [_P, _I, _DP, _DP, _IP, _I, _IP]),
     "rbc_batch_tuning": (_I, [_P, _I, _IP, _IP, _DP, _DP, _IP]),
+    "rbc_batch_profile_launches": (_I, [_P, _I, _IP, _IP, _IP, _DP, _DP, _I, _IP]),
     "rbc_stage_bytes": (_I, [_P, _I, _DP]),
     "rbc_kernel_name": (ctypes.c_char_p, [_I]),
     "rbc_batch_state_offset": (_I, [_P, _I, ctypes.POINTER(_SZ)]),
@@ -999,6 +1000,16 @@ class Batch:
         n = _I()
         _check(lib().rbc_batch_profile_step(self._h, int(nsteps), ms, by, kd, cap, ctypes.byref(n)))
         return {lib().rbc_kernel_name(kd[k]).decode(): (ms[k], by[k]) for k in range(n.value)}
+
+    def profile_launches(self, nsteps=3):
+        """[(bucket, pass, kernel name, mean ms, algorithmic bytes)] for every
+        launch of the step, each timed alone (advances the batch by nsteps)."""
+        cap = 256
+        kd, bk, ps = (ctypes.c_int * cap)(), (ctypes.c_int * cap)(), (ctypes.c_int * cap)()
+        ms, by = (ctypes.c_double * cap)(), (ctypes.c_double * cap)()
+        n = _I()
+        _check(lib().rbc_batch_profile_launches(self._h, int(nsteps), kd, bk, ps, ms, by, cap, ctypes.byref(n)))
+        return [(bk[k], ps[k], lib().rbc_kernel_name(kd[k]).decode(), ms[k], by[k]) for k in range(min(n.value, cap))]
 
     def tuning(self):
         """Autotuner decisions: [(pass, ms one CTA per lane, ms one thread per lane, chosen)]."""

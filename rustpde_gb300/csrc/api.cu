@@ -1458,6 +1458,51 @@ int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* st
   API_END
 }
 
+// every launch of the batch step timed alone, in step order (bucket by
+// bucket): kernel id, bucket, pass id, mean ms and algorithmic bytes
+int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket, int* pass, double* ms_out,
+                               double* bytes_out, int max_launches, int* nlaunches) {
+  API_BEGIN
+  require(b && kernel && bucket && pass && ms_out && nlaunches && nsteps > 0, "rbc_batch_profile_launches: invalid argument");
+  std::vector<CaseDev> hd;
+  for (RbcCase* c : b->cases) hd.push_back(c->hd);
+  std::vector<double> acc;
+  int n = 0;
+  for (size_t k = 0; k < b->buckets.size(); k++)
+    for (auto& L : b->buckets[k].plan.launches) {
+      if (n < max_launches) {
+        kernel[n] = L.kernel;
+        bucket[n] = (int)k;
+        pass[n] = L.pass;
+        if (bytes_out) bytes_out[n] = launch_algorithmic_bytes(L, hd.data());
+      }
+      n++;
+    }
+  acc.assign(n, 0.0);
+  cudaEvent_t e0, e1;
+  cuda_check(cudaEventCreate(&e0), "event create");
+  cuda_check(cudaEventCreate(&e1), "event create");
+  for (int s = 0; s < nsteps; s++) {
+    int idx = 0;
+    for (auto& bk : b->buckets)
+      for (size_t li = 0; li < bk.plan.launches.size(); li++, idx++) {
+        cuda_check(cudaEventRecord(e0, b->stream), "event record");
+        cuda_check(launch_entry(bk.plan.launches[li], bk.dp, li, b->stream, b->d_cases), "stage launch");
+        cuda_check(cudaEventRecord(e1, b->stream), "event record");
+        cuda_check(cudaEventSynchronize(e1), "event sync");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "elapsed");
+        acc[idx] += ms;
+      }
+    for (RbcCase* c : b->cases) c->time += c->p.dt;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (int k = 0; k < n && k < max_launches; k++) ms_out[k] = acc[k] / nsteps;
+  *nlaunches = n;
+  API_END
+}
+
 const char* rbc_kernel_name(int kernel) { return step_kernel_name(kernel); }
 
 const char* rbc_stage_name(const RbcCase* c, int k) {
