@@ -174,7 +174,10 @@ const char* rbc_kernel_name(int kernel);
  * group, groups run as parallel branches, and the whole batch step is one
  * CUDA graph.  Case handles
  * from rbc_batch_case are borrowed (do not destroy them); they share the batch
- * stream, so their state/diagnostic calls are ordered after rbc_batch_step. */
+ * stream, so their state/diagnostic calls are ordered after rbc_batch_step.
+ * Mixed-precision batches time the forms of each FP64 pass at creation and
+ * keep the fastest (rbc_batch_tuning); the environment variable
+ * RBC_BATCH_FORM=0|1|2 pins one form instead (profiling runs). */
 typedef struct RbcBatch RbcBatch;
 int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out);
 int rbc_batch_destroy(RbcBatch* b);

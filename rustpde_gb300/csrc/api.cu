@@ -2,6 +2,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -1220,6 +1221,11 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       ga[a] = passes(alts[a]);
       if (ga[a].size() != gb.size()) throw std::runtime_error("autotune: plan forms of different pass structure");
     }
+    // RBC_BATCH_FORM=0|1|2 pins the form of every pass that has it (profiling
+    // runs: a profiler's per-launch overhead distorts the timings)
+    int forced = -1;
+    if (const char* f = std::getenv("RBC_BATCH_FORM"))
+      if (f[0] >= '0' && f[0] <= '2' && f[1] == '\0') forced = f[0] - '0';
     StepPlan tuned;
     for (size_t pi = 0; pi < gb.size(); pi++) {
       auto group_time = [&](const StepPlan& P, const DevPlan& dp, const std::vector<size_t>& g) {
@@ -1243,6 +1249,8 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
         }
       }
       if (t_base >= 0) b->tuning.push_back({bk.plan.launches[gb[pi][0]].kernel, best_alt_kernel, t_base, t_best_alt});
+      if (forced == 0) best = -1;
+      else if (forced > 0 && (size_t)forced <= nalt) best = forced - 1;
       const StepPlan& src = best >= 0 ? alts[best] : bk.plan;
       for (size_t li : (best >= 0 ? ga[best][pi] : gb[pi])) tuned.launches.push_back(src.launches[li]);
     }

@@ -284,24 +284,30 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
           stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
       }
       __syncthreads();
+      // FP32 outputs of scale 1 are stored as they are (a round trip through
+      // FP64 would run at the FP64 rate on this GPU)
+      auto store_all = [&](auto store) {
 #pragma unroll 4
-      for (int it = 0; it < 4096 / kGemmThreads; it++) {
-        const int q = tid + kGemmThreads * it;
-        int l, n;
-        if (J.out.lane_fast) { l = q & 127; n = q >> 7; }
-        else {
-          const int p = q % P;
-          n = (q / P) & 31;
-          l = (q / (32 * P)) * P + p;
+        for (int it = 0; it < 4096 / kGemmThreads; it++) {
+          const int q = tid + kGemmThreads * it;
+          int l, n;
+          if (J.out.lane_fast) { l = q & 127; n = q >> 7; }
+          else {
+            const int p = q % P;
+            n = (q / P) & 31;
+            l = (q / (32 * P)) * P + p;
+          }
+          char* base = ob[l];
+          const int nl = cc + n, ng = nbase + nl;
+          if (base != nullptr && nl < NT && ng < J.N) store(base, (long long)ng * oes, stage[l * 33 + n]);
         }
-        char* base = ob[l];
-        const int nl = cc + n, ng = nbase + nl;
-        if (base != nullptr && nl < NT && ng < J.N) {
-          const double v = (double)stage[l * 33 + n] * scale;
-          if (otype == LT_F64) reinterpret_cast<double*>(base)[(long long)ng * oes] = v;
-          else reinterpret_cast<float*>(base)[(long long)ng * oes] = (float)v;
-        }
-      }
+      };
+      if (otype == LT_F64)
+        store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f * scale; });
+      else if (scale == 1.0)
+        store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = f; });
+      else
+        store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = (float)((double)f * scale); });
       __syncthreads();
     }
   } else if (tid == 0 && J.status != nullptr) {
