@@ -230,6 +230,7 @@ def run_ensemble(args, rank, world, local):
     status = [c.status() for c in B.cases]
     mixed_nu = [c.eval(R.NU) for c in B.cases]
     mixed_ke = [c.eval(R.KE) for c in B.cases]
+    mixed_temp = [c.get(R.TEMP) for c in B.cases]
     value = gp * K / (total_ms * 1e-3) * world
 
     # ---- per-kernel profile of the batched step (each launch alone) and roofline
@@ -262,7 +263,7 @@ def run_ensemble(args, rank, world, local):
 
     # ---- plain FP64, case by case, same ensemble and initial fields
     plain_ms = 0.0
-    err_nu, err_ke = [], []
+    err_nu, err_ke, err_t, ke_ref = [], [], [], []
     t_plain = time.perf_counter()
     for i, p in enumerate(params):
         nav = R.Navier2D(*p, precision=R.PREC_FP64, seed=None)
@@ -279,10 +280,13 @@ def run_ensemble(args, rank, world, local):
         for lst, what, ref in ((err_nu, R.NU, mixed_nu[i]), (err_ke, R.KE, mixed_ke[i])):
             v = nav.eval(what)
             lst.append(abs(ref - v) / max(abs(v), 1e-300))
+        ke_ref.append(nav.eval(R.KE))
+        t64 = nav.get(R.TEMP)
+        err_t.append(float(np.linalg.norm(mixed_temp[i] - t64) / max(np.linalg.norm(t64), 1e-300)))
         del nav
     t_plain = time.perf_counter() - t_plain
     plain_value = gp * K / (plain_ms * 1e-3) * world
-    err_nu, err_ke = np.array(err_nu), np.array(err_ke)
+    err_nu, err_ke, err_t = np.array(err_nu), np.array(err_ke), np.array(err_t)
 
     line = {
         "metric": METRIC,
@@ -307,8 +311,12 @@ def run_ensemble(args, rank, world, local):
         "speedup_vs_plain_fp64": value / plain_value,
         "mixed_error": {"steps": W + K, "nu_max_rel": float(err_nu.max()), "nu_median_rel": float(np.median(err_nu)),
                         "ke_max_rel": float(err_ke.max()), "ke_median_rel": float(np.median(err_ke)),
-                        "worst_ke_cases": [{"case": int(i), "params": list(params[i]), "ke_rel": float(err_ke[i])}
-                                           for i in np.argsort(err_ke)[::-1][:3]],
+                        "temp_l2_max_rel": float(err_t.max()), "temp_l2_median_rel": float(np.median(err_t)),
+                        "cases_nu_ke_within_1e-6": int(np.sum((err_nu <= 1e-6) & (err_ke <= 1e-6))),
+                        "worst_ke_cases": [{"case": int(i), "params": list(params[i]), "ke_rel": float(err_ke[i]),
+                                            "nu_rel": float(err_nu[i]), "ke": float(ke_ref[i]),
+                                            "temp_l2_rel": float(err_t[i])}
+                                           for i in np.argsort(err_ke)[::-1][:5]],
                         "against": "the plain FP64 GPU path (parity with the FP64 oracle <= 1e-9)"},
         "e2e": {"value": gp * Ke / e2e_s * world, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes, "steps": Ke,

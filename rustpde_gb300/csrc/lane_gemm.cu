@@ -6,10 +6,18 @@
 //     straight into the K-major core-matrix layout the tensor core reads
 //     (8 rows x 16 bytes per core matrix, no swizzle);
 //   * the matching chunk of the pre-split operator W is copied as-is;
-//   * one thread issues 4 k-steps x 3 tcgen05.mma (lo*hi, hi*lo, hi*hi) into
-//     an FP32 accumulator in tensor memory and commits to an mbarrier;
-//   * after the last chunk each warp reads its 32 accumulator lanes back with
-//     tcgen05.ld, stages them through shared memory and stores them coalesced.
+//   * one thread issues 4 k-steps x 3 tcgen05.mma (lo*hi, hi*lo, hi*hi) and
+//     commits to an mbarrier.  The hi*hi products of each chunk go to a fresh
+//     partial accumulator in tensor memory (two, used alternately); while the
+//     next chunk's MMAs run, the threads add the finished partial into an FP32
+//     running total with round-to-nearest.  The tensor core's accumulation
+//     truncates, so summing the whole K range in one accumulator biased every
+//     output by about (K/8) ulp; per-chunk partials keep that to 4 ulp of a
+//     partial.  The small lo*hi + hi*lo corrections accumulate over all of K
+//     in a third accumulator;
+//   * after the last chunk each warp reads its 32 lanes of total + corrections
+//     back with tcgen05.ld, stages them through shared memory and stores them
+//     coalesced.
 // Every wait is bounded: on time-out the kernel sets kStatusGemmTimeout, skips
 // the stores, frees its tensor memory and returns.
 #include "lane_gemm.h"
@@ -93,11 +101,50 @@ __device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// tensor-memory columns of a tile: a power of two >= 2 NT (main sum and corrections)
+// tensor-memory columns of a tile: a power of two holding the two chunk
+// partials, the corrections and the running total (NT each), with the last
+// region padded to whole 32-column epilogue loads
 __host__ __device__ inline uint32_t gemm_tmem_cols(int NT) {
+  const uint32_t need = 3u * (uint32_t)NT + (((uint32_t)NT + 31u) & ~31u);
   uint32_t c = 32;
-  while (c < 2u * (uint32_t)NT) c <<= 1;
+  while (c < need) c <<= 1;
   return c;
+}
+
+__device__ __forceinline__ void tmem_ld8(uint32_t addr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(addr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
+}
+__device__ __forceinline__ void tmem_st8(uint32_t addr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(addr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+
+// running total += chunk partial (or = partial for the first chunk), all 8
+// warps: warp w covers tensor-memory lanes 32 (w % 4) .. + 31 and every other
+// 8-column block (from block w / 4)
+__device__ __forceinline__ void tmem_accumulate(uint32_t tmem, uint32_t part, uint32_t total, int NT, bool first,
+                                                int warp) {
+  const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+  for (int cb = (warp >> 2) * 8; cb < NT; cb += 16) {
+    float p[8], t[8];
+    tmem_ld8(tmem + lane_base + part + (uint32_t)cb, p);
+    if (!first) {
+      tmem_ld8(tmem + lane_base + total + (uint32_t)cb, t);
+#pragma unroll
+      for (int j = 0; j < 8; j++) p[j] = __fadd_rn(t[j], p[j]);
+    }
+    tmem_st8(tmem + lane_base + total + (uint32_t)cb, p);
+  }
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 constexpr long kWaitLimit = 1L << 22;  // try_wait polls before a completion wait is declared lost
@@ -203,12 +250,13 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   const float* wsrc = J.w + (size_t)tile_n * J.kchunks * 2 * NT * kGemmKC;
   w_issue(wsrc, 0, NT, Wb[0], tid);  // operator chunk 0 in flight during the set-up
   cp_async_commit();
-  // two accumulators of NT columns: the hi*hi products and, apart, the small
-  // lo*hi + hi*lo corrections (added to the main sum with round-to-nearest at
-  // the end; accumulated into the main sum they would lose bits to the tensor
-  // core's truncating accumulation)
+  // tensor-memory columns: chunk partials of the hi*hi products at 0 and NT
+  // (alternate chunks), the lo*hi + hi*lo corrections at 2 NT, the running
+  // total at 3 NT; corrections and total are added with round-to-nearest at
+  // the end (accumulated into the hi*hi sum the corrections would lose bits
+  // to the tensor core's truncating accumulation)
   const uint32_t ncols = gemm_tmem_cols(NT);
-  const uint32_t corr = ncols / 2;
+  const uint32_t corr = 2u * (uint32_t)NT, total = 3u * (uint32_t)NT;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
                  "r"(ncols));
@@ -244,6 +292,7 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     if (tid == 0) {
       unsigned char* Whi = Wb[c & 1];
       unsigned char* Wlo = Whi + NT * 128;
+      const uint32_t part = (uint32_t)((c & 1) * NT);
 #pragma unroll
       for (int s = 0; s < kGemmKC / 8; s++) {
         const uint64_t ah = umma_desc(smem_u32(Ahi) + s * 2 * a_lbo, a_lbo, 128);
@@ -253,18 +302,26 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
         const uint32_t acc = (c > 0 || s > 0) ? 1u : 0u;
         mma_tf32(tmem + corr, al, wh, idesc, acc);
         mma_tf32(tmem + corr, ah, wlo, idesc, 1u);
-        mma_tf32(tmem, ah, wh, idesc, acc);
+        mma_tf32(tmem + part, ah, wh, idesc, s > 0 ? 1u : 0u);  // fresh partial per chunk
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                        smem_u32(mbar))
                    : "memory");
     }
+    // the previous chunk's partial into the running total, while chunk c multiplies
+    if (c > 0) tmem_accumulate(tmem, (uint32_t)(((c - 1) & 1) * NT), total, NT, c == 1, warp);
     // next input chunk in flight while the tensor core works
     if (c + 1 < J.kchunks) a_load<T>(a, J, ib, (c + 1) * kGemmKC, tid);
   }
   if (ok) {
     ok = mma_wait(mbar, (uint32_t)((J.kchunks - 1) & 1));
     tc_fence_after();
+    if (ok) {
+      tmem_accumulate(tmem, (uint32_t)(((J.kchunks - 1) & 1) * NT), total, NT, J.kchunks == 1, warp);
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+    }
   }
   asm volatile("cp.async.wait_all;" ::: "memory");
 
@@ -277,7 +334,7 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     for (int cc = 0; cc < NT; cc += 32) {
       if (warp < 4) {  // warp w reads accumulator lanes 32w .. 32w+31
         uint32_t r[32], q[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)cc, r);
+        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + total + (uint32_t)cc, r);
         tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
 #pragma unroll
         for (int j = 0; j < 32; j++)
@@ -343,11 +400,12 @@ __global__ void __launch_bounds__(kGemmThreads, 2) k_lane_gemm_one(const __grid_
 // host side
 // ---------------------------------------------------------------------------
 int gemm_tile_n(int N) {
-  // at most 128 outputs per tile: two operator buffers of 32 KB and two CTAs
-  // per SM; wider outputs are split into equal tiles
+  // at most 64 outputs per tile: 4 NT tensor-memory columns per CTA (two chunk
+  // partials, corrections, total) and two CTAs per SM; wider outputs are split
+  // into equal tiles
   auto r16 = [](int v) { return (v + 15) & ~15; };
-  if (N <= 128) return r16(N);
-  int t = (N + 127) / 128;
+  if (N <= 64) return r16(N);
+  int t = (N + 63) / 64;
   return r16((N + t - 1) / t);
 }
 
@@ -412,10 +470,10 @@ cudaError_t configure_gemm_kernels() {
   static bool done = false;
   if (done) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(dev::k_lane_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)gemm_smem_bytes(256));
+                                       (int)gemm_smem_bytes(64));  // tiles hold at most 64 outputs
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(dev::k_lane_gemm_one, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)gemm_smem_bytes(256));
+                           (int)gemm_smem_bytes(64));
   if (e == cudaSuccess) done = true;
   return e;
 }
