@@ -715,7 +715,7 @@ def main():
     ap.add_argument("--horizon-scale", type=float, default=0.01, help="serving: horizon multiplier")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 50 if args.workload == "ensemble" else 200
+        args.steps = 500 if args.workload == "ensemble" else 200
     rank, world, local = dist_info()
     if world > 1 and args.impl == "ours":
         import torch

@@ -138,7 +138,8 @@ struct CaseDev {
   void* m_cv;     // FP64 convection term, spectral: 3 x (kx x ky)
   void* m_ph[8];  // box: FP32 physical fields (nx x ny)
   void* m_p[3];   // box: FP32 products, then their x transforms
-  void* m_z;      // box: FP64 pinv_x of the divergence (mxc x ny)
+  void* m_z;      // box: FP32 pinv_x of the divergence (mxc x ny), then the FP32 Poisson row solutions (mxc x myc)
+  void* m_s32;    // FP32 copy of ux, uy, temp (3 x mxc x myc, interleaved re/im when periodic): the y GEMM's input
   const float* m_bcx;  // FP32 d(fieldbc)/dx, transposed: ny x nx
   const float* m_bcy;  // FP32 d(fieldbc)/dy, transposed: ny x nx
 };

@@ -806,9 +806,9 @@ __global__ void __launch_bounds__(256) k_box_x3(const CaseDev* __restrict__ case
   }
   __syncthreads();
   matvec_pinv<double>(c.pinv_x, DV, ld, Z, ld, 1, tid, nth);
-  if (MIX) {
-    double* mz = static_cast<double*>(c.m_z);
-    for (int r = tid; r < mxc; r += nth) mz[(size_t)r * ny + j] = Z[r];
+  if (MIX) {  // FP32: the input of the eigenbasis GEMM
+    float* mz = static_cast<float*>(c.m_z);
+    for (int r = tid; r < mxc; r += nth) mz[(size_t)r * ny + j] = (float)Z[r];
     return;
   }
   // dense eigenbasis forward along x
@@ -840,6 +840,11 @@ __global__ void __launch_bounds__(256) k_box_y4(const CaseDev* __restrict__ case
   __syncthreads();
   matvec_pinv<double>(c.pinv_y, IN, ld, OUT, ld, 1, tid, nth);
   fdma_solve<double>(c.pois_y, OUT, ld, 1, i, 0, tid, nth);
+  if (c.mixed) {  // FP32 into m_z: the input of the eigenbasis GEMM
+    float* wf = static_cast<float*>(c.m_z);
+    for (int k = tid; k < myc; k += nth) wf[(size_t)i * myc + k] = (float)OUT[k];
+    return;
+  }
   double* wv = static_cast<double*>(c.s[7]);
   for (int k = tid; k < myc; k += nth) wv[(size_t)i * myc + k] = OUT[k];
 }

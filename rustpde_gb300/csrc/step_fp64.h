@@ -23,6 +23,8 @@ enum StepKernel {
   // periodic Y2 as three one-thread-per-sub-lane launches (right-hand sides and
   // Helmholtz solves; divergence and Poisson; projection and updates)
   K_LP_PER_Y2A, K_LP_PER_Y2B, K_LP_PER_Y2C,
+  // FP32 copy of the state rows for the y GEMM (mixed form)
+  K_STATE_F32,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };

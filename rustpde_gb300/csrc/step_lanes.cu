@@ -285,9 +285,9 @@ __global__ void __launch_bounds__(128) k_lp_box_x3(const CaseDev* __restrict__ c
   double* dv = static_cast<double*>(c.s[3]) + j;
   diff_par<double>(nx, q, [&](int i) { return stencil_lane<double>(c.xu, A, ny, i); },
                    [&](int i, double da) { dv[(long long)i * ny] = fma(da, inv_asp, stencil_lane<double>(c.xu, B, ny, i)); });
-  double* z = static_cast<double*>(c.m_z) + j;
+  float* z = static_cast<float*>(c.m_z) + j;  // FP32: the input of the eigenbasis GEMM
 #pragma unroll 4
-  for (int r = q; r < mxc; r += 2) z[(long long)r * ny] = pinv_lane<double>(c.pinv_x, dv, ny, r);
+  for (int r = q; r < mxc; r += 2) z[(long long)r * ny] = (float)pinv_lane<double>(c.pinv_x, dv, ny, r);
 }
 
 // projection along x from p1 (computed by the eigenbasis GEMM): p1[0][0] = 0;
@@ -426,7 +426,19 @@ __global__ void __launch_bounds__(256) k_lp_box_y4(const CaseDev* __restrict__ c
   double* wv = static_cast<double*>(c.s[7]) + (size_t)i * myc;
   const FdmaRow R = fdma_row(c.pois_y, i);
   pinv_fwd_par<double>(c.pinv_y, R, zf, 1, wv, 1, q);
-  fdma_bwd_par<double>(R, wv, 1, q);
+  // back substitution (FP64 in place), each result also rounded into m_z:
+  // the FP32 input of the eigenbasis GEMM
+  float* wf = static_cast<float*>(c.m_z) + (size_t)i * myc;
+  double p2 = 0.0, p4 = 0.0;
+#pragma unroll 4
+  for (int j = top_par(R.m, q); j >= 0; j -= 2) {
+    double v = wv[j] * R.dinv[j];
+    if (j + 2 < R.m) v = fma(p2, R.up1[j], v);
+    if (j + 4 < R.m) v = fma(p4, R.up2[j], v);
+    wf[j] = (float)v;
+    p4 = p2;
+    p2 = v;
+  }
 }
 
 // rows i < nx: ux = ux* - Sy+ Sy^N E ; uy = uy* - Sy+ Dy Sy^N Fv ;

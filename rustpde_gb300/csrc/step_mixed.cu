@@ -117,6 +117,23 @@ __global__ void k_gate(const CaseDev* __restrict__ cases, const int* __restrict_
   g[0] -= run;
 }
 
+// FP32 copy of row i of ux, uy, temp (the y GEMM's input, rounded once here
+// instead of once per output tile inside the GEMM; the GEMM rounds FP64 input
+// to FP32 the same way)
+__global__ void __launch_bounds__(128) k_state_f32(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;
+  const int i = w.y;
+  const size_t rl = (size_t)c.myc * (c.kind == KIND_PERIODIC ? 2 : 1);  // doubles per row
+  const size_t fs = (size_t)c.mxc * rl;
+  const double* src[3] = {static_cast<const double*>(c.ux), static_cast<const double*>(c.uy),
+                          static_cast<const double*>(c.temp)};
+  float* dst = static_cast<float*>(c.m_s32);
+  for (int f = 0; f < 3; f++)
+    for (size_t k = threadIdx.x; k < rl; k += blockDim.x) dst[f * fs + i * rl + k] = (float)src[f][i * rl + k];
+}
+
 size_t smem_per_x_mixed(const CaseDev& c) {
   return ((size_t)8 * (c.mx + 1) + (size_t)16 * c.fx.M) * 8 + 64;
 }
@@ -167,10 +184,14 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     push(L);
   };
   const int mx = c.mx, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
+  // FP32 copy of the state rows, read by G1
+  void* s32[3];
+  for (int f = 0; f < 3; f++)
+    s32[f] = static_cast<float*>(c.m_s32) + (size_t)f * c.mxc * myc * (c.kind == KIND_PERIODIC ? 2 : 1);
+  add(K_STATE_F32, c.mxc, 0);
   if (c.kind == KIND_PERIODIC) {
-    // G1: rows of ux, uy, temp (complex, FP64) -> [Y0 | Y1] (FP32), stored transposed
-    void* st[3] = {c.ux, c.uy, c.temp};
-    LaneSideDev in = lane_rows(st, 3, mx, myc, myc, LT_F64, true);
+    // G1: rows of ux, uy, temp (complex) -> [Y0 | Y1] (FP32), stored transposed
+    LaneSideDev in = lane_rows(s32, 3, mx, myc, myc, LT_F32, true);
     LaneSideDev out;
     std::memset(&out, 0, sizeof out);
     for (int f = 0; f < 3; f++) out.ptr[f] = c.m_y[f];
@@ -215,11 +236,10 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     return sd;
   };
   auto fptr = [](void* base, size_t off_floats) { return static_cast<void*>(static_cast<float*>(base) + off_floats); };
-  // G1: rows of ux, uy, temp (FP64, mxc x myc) -> [Y0 | Y1] transposed (2 ny x mxc, FP32)
+  // G1: rows of ux, uy, temp (FP32 copy, mxc x myc) -> [Y0 | Y1] transposed (2 ny x mxc, FP32)
   {
-    void* st[3] = {c.ux, c.uy, c.temp};
     void* yo[3] = {c.m_y[0], c.m_y[1], c.m_y[2]};
-    add_gemm(make_gemm_job(lane_rows(st, 3, mxc, myc, myc, LT_F64, false),
+    add_gemm(make_gemm_job(lane_rows(s32, 3, mxc, myc, myc, LT_F32, false),
                            side(yo, 3, mxc, 2 * ny, 1, mxc, LT_F32, 1), ops.y1, myc, 2 * ny, 1.0, c.status));
   }
   // GX: x stencils, derivatives and backward transforms -> physical (transposed), one launch of 4 jobs
@@ -292,15 +312,15 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   {  // eigenbasis forward along x: s[6] = fwd * m_z (columns j < ny)
     void* zi[1] = {c.m_z};
     void* zo[1] = {c.s[6]};
-    add_gemm(make_gemm_job(lane_cols(zi, 1, ny, mxc, ny, LT_F64, 0), lane_cols(zo, 1, ny, mxc, ny, LT_F64, 0), ops.pf,
+    add_gemm(make_gemm_job(lane_cols(zi, 1, ny, mxc, ny, LT_F32, 0), lane_cols(zo, 1, ny, mxc, ny, LT_F64, 0), ops.pf,
                            mxc, mxc, 1.0, c.status));
   }
   if (lane_parallel) add_lp(K_LP_BOX_Y4, mxc, ny);
   else add(K_BOX_Y4, mxc, dev::smem_box_y4(c));
-  {  // eigenbasis backward along x: p1 = bwd * s[7] (columns j < myc)
-    void* wi[1] = {c.s[7]};
+  {  // eigenbasis backward along x: p1 = bwd * W (FP32 Poisson row solutions in m_z, columns j < myc)
+    void* wi[1] = {c.m_z};
     void* po[1] = {c.p1};
-    add_gemm(make_gemm_job(lane_cols(wi, 1, myc, mxc, myc, LT_F64, 0), lane_cols(po, 1, myc, mxc, myc, LT_F64, 0),
+    add_gemm(make_gemm_job(lane_cols(wi, 1, myc, mxc, myc, LT_F32, 0), lane_cols(po, 1, myc, mxc, myc, LT_F64, 0),
                            ops.pb, mxc, mxc, 1.0, c.status));
   }
   if (lane_parallel) add_lp(K_LP_BOX_X4, myc, nx);
@@ -324,6 +344,7 @@ cudaError_t launch_mixed_kernel(int kernel, int nblocks, size_t smem, cudaStream
                                 const int4* work) {
   switch (kernel) {
     case K_PER_X_MIXED: dev::k_per_x_mixed<<<nblocks, 256, smem, s>>>(cases, work); break;
+    case K_STATE_F32: dev::k_state_f32<<<nblocks, 128, 0, s>>>(cases, work); break;
     case K_BOX_PROD_MIXED: dev::k_box_prod_mixed<<<nblocks, 256, 0, s>>>(cases, work); break;
     default: return launch_lane_kernel(kernel, nblocks, s, cases, work);
   }
@@ -377,6 +398,7 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
             myc * z;
         break;
       case K_PER_X_MIXED: v = 6 * mx * 8 + 2 * nx * 4 + 3 * kx * 8; break;
+      case K_STATE_F32: v = 3 * myc * (z + z / 2); break;
       case K_BOX_X1: v = 6 * mxc * 8 + 3 * nx * 8 + 3 * kx * 8 + nx * 8; break;
       case K_BOX_Y2: case K_BOX_Y2_PRE:
         v = (kernel == K_BOX_Y2 ? 3 * ny : 3 * ky) * 8 + 6 * myc * 8 + 4 * ny * 8 + 3 * myc * 8;
@@ -410,7 +432,7 @@ const char* step_kernel_name(int kernel) {
                                 "lanes_box_x2", "lanes_box_x3", "lanes_box_x4", "lanes_box_y2", "lanes_box_y3",
                                 "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2", "periodic_y2_pre_t128",
                                 "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128", "lanes_periodic_y2a",
-                                "lanes_periodic_y2b", "lanes_periodic_y2c"};
+                                "lanes_periodic_y2b", "lanes_periodic_y2c", "state_f32"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";
