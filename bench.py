@@ -153,6 +153,18 @@ class Cudart:
             self.lib.cudaEventDestroy(e)
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ensemble step of
+# each kernel of the batched mixed step, from one ncu capture of the 256-case
+# ensemble (the launch list in profiles/launches_ensemble256_mixed.md); the
+# roofline's `traffic` for the dominant kernel, per step like its `achieved`
+NCU_DRAM_BYTES_PER_STEP = {
+    "lane_gemm": 754e6, "lanes_periodic_y2a": 380e6, "lanes_box_y2": 251e6, "lanes_periodic_y2b": 109e6,
+    "lanes_periodic_y2c": 265e6, "lanes_box_x4": 40e6, "lanes_box_y5": 266e6, "lanes_box_y3": 181e6,
+    "lanes_box_x3": 49e6, "lanes_box_y4": 131e6, "periodic_x_mixed": 93e6, "lanes_box_x2": 116e6,
+    "box_prod_mixed": 128e6, "lanes_box_gpx": 23e6, "state_f32": 141e6,
+}
+
+
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -327,7 +339,9 @@ def run_ensemble(args, rank, world, local):
         "autotuner": [{"pass": t[0], "ms_cta_per_lane": t[1], "ms_thread_per_lane": t[2], "chosen": t[3]}
                       for t in tuning],
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_launch": dom_bytes,
+                     "frac": achieved / hbm, "traffic": NCU_DRAM_BYTES_PER_STEP.get(dom),
+                     "traffic_source": "ncu dram bytes per step, profiles/launches_ensemble256_mixed.md",
+                     "algorithmic_bytes_per_step": dom_bytes,
                      "peak_source": pk_src},
         "clocks": clk,
         "status_nonzero_cases": int(sum(1 for s in status if s)),
