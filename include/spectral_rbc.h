@@ -422,6 +422,10 @@ int rbc_adjoint_eval(RbcAdjoint* a, int what, double* out);
 int rbc_adjoint_residual(RbcAdjoint* a, double out[6]);
 int rbc_adjoint_exit(RbcAdjoint* a, int* stop);
 int rbc_adjoint_get_stream(RbcAdjoint* a, void** stream);
+/* Navier2DAdjoint::write / read (navier_adjoint.rs:991-1040) in the snapshot
+ * format of rbc_write_snapshot; read restores temp, ux, uy and time */
+int rbc_adjoint_write_snapshot(RbcAdjoint* a, const char* path);
+int rbc_adjoint_read_snapshot(RbcAdjoint* a, const char* path);
 
 /* ---- Diffusion2D (src/navier/diffusion.rs:113-238) ------------------------
  * df_create replaces Diffusion2D::new(field, kappa, dt) (diffusion.rs:140-153)

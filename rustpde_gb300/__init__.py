@@ -184,6 +184,8 @@ _SIGNATURES = {
     "rbc_adjoint_residual": (_I, [_P, _DP]),
     "rbc_adjoint_exit": (_I, [_P, _IP]),
     "rbc_adjoint_get_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "rbc_adjoint_write_snapshot": (_I, [_P, ctypes.c_char_p]),
+    "rbc_adjoint_read_snapshot": (_I, [_P, ctypes.c_char_p]),
     "df_create": (_I, [_I, _I, _I, _I, _D, _D, ctypes.POINTER(_P)]),
     "df_destroy": (_I, [_P]),
     "df_shape": (_I, [_P, _I, _IP, _IP, _IP]),
@@ -524,6 +526,14 @@ class Navier2DAdjoint:
         s = _P()
         _check(lib().rbc_adjoint_get_stream(self._h, ctypes.byref(s)))
         return s.value
+
+    def write(self, filename):
+        """Navier2DAdjoint::write (navier_adjoint.rs:1005-1040)."""
+        _check(lib().rbc_adjoint_write_snapshot(self._h, filename.encode()))
+
+    def read(self, filename):
+        """Navier2DAdjoint::read (navier_adjoint.rs:991-999): temp, ux, uy, time."""
+        _check(lib().rbc_adjoint_read_snapshot(self._h, filename.encode()))
 
 
 class Diffusion2D:

@@ -496,6 +496,43 @@ int rbc_adjoint_exit(RbcAdjoint* a, int* stop) {
   ADJ_END
 }
 
+// Navier2DAdjoint::write (navier_adjoint.rs:1005-1040): temp (plus the boundary
+// field), ux, uy, pres and the scalars, through the inner case's snapshot
+// writer on a copy of the adjoint state (the header's dt is the inner step's)
+int rbc_adjoint_write_snapshot(RbcAdjoint* a, const char* path) {
+  ADJ_BEGIN
+  need(a && path, "rbc_adjoint_write_snapshot: null argument");
+  state_to_nav(a);
+  cuda_check(cudaMemcpyAsync(a->na.p0, a->p0, a->n_p0 * 8, cudaMemcpyDeviceToDevice, a->st), "copy state");
+  a->sync();
+  double t_nav = 0.0;
+  rbc_get_time(a->nav, &t_nav);
+  rbc_set_time(a->nav, a->time);
+  int rc = rbc_write_snapshot(a->nav, path);
+  rbc_set_time(a->nav, t_nav);
+  if (rc != RBC_OK) throw AdjError(rc, rbc_last_error());
+  ADJ_END
+}
+
+// Navier2DAdjoint::read (navier_adjoint.rs:991-999): temp, ux, uy and time
+int rbc_adjoint_read_snapshot(RbcAdjoint* a, const char* path) {
+  ADJ_BEGIN
+  need(a && path, "rbc_adjoint_read_snapshot: null argument");
+  double t_nav = 0.0;
+  rbc_get_time(a->nav, &t_nav);
+  int rc = rbc_read_snapshot(a->nav, path);
+  if (rc != RBC_OK) throw AdjError(rc, rbc_last_error());
+  double t = 0.0;
+  rbc_get_time(a->nav, &t);
+  rbc_set_time(a->nav, t_nav);
+  a->time = t;
+  cuda_check(cudaMemcpyAsync(a->ux0, a->na.ux, a->n_spec_u * 8, cudaMemcpyDeviceToDevice, a->st), "copy state");
+  cuda_check(cudaMemcpyAsync(a->uy0, a->na.uy, a->n_spec_u * 8, cudaMemcpyDeviceToDevice, a->st), "copy state");
+  cuda_check(cudaMemcpyAsync(a->t0, a->na.temp, a->n_spec_t * 8, cudaMemcpyDeviceToDevice, a->st), "copy state");
+  a->sync();
+  ADJ_END
+}
+
 int rbc_adjoint_get_stream(RbcAdjoint* a, void** stream) {
   ADJ_BEGIN
   need(a && stream, "rbc_adjoint_get_stream: null argument");

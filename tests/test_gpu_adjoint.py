@@ -106,3 +106,20 @@ def test_state_round_trip_and_errors(R):
         g.set(O.TEMP, np.zeros((3, 3)))
     with pytest.raises(R.RbcError):
         R.Navier2DAdjoint(32, 32, -1.0, 1.0, 0.02, 1.0, O.BOX_ADIABATIC)
+
+
+def test_snapshot_write_read(R, tmp_path):
+    """write() stores the adjoint state; read() restores temp, ux, uy and time."""
+    from rustpde_gb300.snapshot import read_snapshot
+    _, g = pair(R, "box32")
+    g.update(3)
+    path = str(tmp_path / "adjoint.rbc")
+    g.write(path)
+    snap = read_snapshot(path)
+    np.testing.assert_array_equal(snap["datasets"]["ux/vhat"], g.get(O.UX))
+    assert abs(snap["scalars"]["time"] - g.get_time()) < 1e-15
+    h = R.Navier2DAdjoint(*CASES["box32"])
+    h.read(path)
+    for f in (O.TEMP, O.UX, O.UY):
+        np.testing.assert_array_equal(h.get(f), g.get(f))
+    assert abs(h.get_time() - g.get_time()) < 1e-15
