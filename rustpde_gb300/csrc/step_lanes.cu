@@ -144,87 +144,176 @@ __device__ __forceinline__ void from_ortho_lane(const BasisDev& b, const T* p, l
 // largest index < n of parity q (or -1)
 __device__ __forceinline__ int top_par(int n, int q) { return ((n - 1 - q) & 1) ? n - 2 : n - 1; }
 
+// Each chain below loads kPB elements (and their coefficients) into registers
+// before running their recurrence steps: the chains are latency-bound, and
+// loads issued one step at a time behind the previous step's store (which
+// the compiler cannot reorder) left about 15 stall cycles per instruction.
+// The arithmetic and its order are those of the one-element-at-a-time form.
+constexpr int kPB = 8;
+// box y3 and y5 measured faster with one element at a time (0.28 / 0.31 ms per
+// ensemble step against 0.33 / 0.36 with 8 and 0.40 / 0.47 with 4)
+constexpr int kPBRow = 1;
+
 // Chebyshev derivative d = D a on the indices of parity q, descending:
 // d_{n-1} = 0, d_i = 2(i+1) a_{i+1} + d_{i+2}, d_0 = a_1 + d_2 / 2; a(i)
 // supplies a_i (parity 1-q), store(i, d_i) receives the result
-template <class T, class A, class S>
+template <class T, int PB = kPB, class A, class S>
 __device__ __forceinline__ void diff_par(int n, int q, A a, S store) {
   T d2 = zero_v<T>();
-  for (int i = top_par(n, q); i >= 0; i -= 2) {
-    T d;
-    if (i == n - 1) d = zero_v<T>();
-    else if (i >= 1) d = fmas(d2, a(i + 1), 2.0 * (double)(i + 1));
-    else d = fmas(a(1), d2, 0.5);
-    store(i, d);
-    d2 = d;
+  for (int i0 = top_par(n, q); i0 >= 0; i0 -= 2 * PB) {
+    T av[PB];
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 - 2 * e;
+      av[e] = (i >= 0 && i < n - 1) ? a(i + 1) : zero_v<T>();
+    }
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 - 2 * e;
+      if (i < 0) break;
+      T d;
+      if (i == n - 1) d = zero_v<T>();
+      else if (i >= 1) d = fmas(d2, av[e], 2.0 * (double)(i + 1));
+      else d = fmas(av[e], d2, 0.5);
+      store(i, d);
+      d2 = d;
+    }
   }
 }
 
 // Fdma forward elimination on the parity-q indices of a strided lane, in place
-template <class T>
+template <class T, int PB = kPB>
 __device__ __forceinline__ void fdma_fwd_par(const FdmaRow& f, T* x, long long s, int q) {
   T xm2 = zero_v<T>();
-#pragma unroll 4
-  for (int i = q; i < f.m; i += 2) {
-    T v = x[(long long)i * s];
-    if (i >= 2) v = fmas(v, xm2, f.low[i - 2]);
-    x[(long long)i * s] = v;
-    xm2 = v;
+  for (int i0 = q; i0 < f.m; i0 += 2 * PB) {
+    T xv[PB];
+    double lv[PB];
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 + 2 * e;
+      xv[e] = i < f.m ? x[(long long)i * s] : zero_v<T>();
+      lv[e] = (i < f.m && i >= 2) ? __ldg(f.low + i - 2) : 0.0;
+    }
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 + 2 * e;
+      if (i >= f.m) break;
+      T v = xv[e];
+      if (i >= 2) v = fmas(v, xm2, lv[e]);
+      x[(long long)i * s] = v;
+      xm2 = v;
+    }
   }
 }
 
 // Fdma back substitution on the parity-q indices of a strided lane, in place
-template <class T>
+template <class T, int PB = kPB>
 __device__ __forceinline__ void fdma_bwd_par(const FdmaRow& f, T* x, long long s, int q) {
   T p2 = zero_v<T>(), p4 = zero_v<T>();
-#pragma unroll 4
-  for (int j = top_par(f.m, q); j >= 0; j -= 2) {
-    T v = scal(x[(long long)j * s], f.dinv[j]);
-    if (j + 2 < f.m) v = fmas(v, p2, f.up1[j]);
-    if (j + 4 < f.m) v = fmas(v, p4, f.up2[j]);
-    x[(long long)j * s] = v;
-    p4 = p2;
-    p2 = v;
+  for (int j0 = top_par(f.m, q); j0 >= 0; j0 -= 2 * PB) {
+    T xv[PB];
+    double dv[PB], u1[PB], u2[PB];
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int j = j0 - 2 * e;
+      const bool in = j >= 0;
+      xv[e] = in ? x[(long long)j * s] : zero_v<T>();
+      dv[e] = in ? __ldg(f.dinv + j) : 0.0;
+      u1[e] = (in && j + 2 < f.m) ? __ldg(f.up1 + j) : 0.0;
+      u2[e] = (in && j + 4 < f.m) ? __ldg(f.up2 + j) : 0.0;
+    }
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int j = j0 - 2 * e;
+      if (j < 0) break;
+      T v = scal(xv[e], dv[e]);
+      if (j + 2 < f.m) v = fmas(v, p2, u1[e]);
+      if (j + 4 < f.m) v = fmas(v, p4, u2[e]);
+      x[(long long)j * s] = v;
+      p4 = p2;
+      p2 = v;
+    }
   }
 }
 
 // pinv rows fused with the Fdma forward elimination on the parity-q indices:
-// out_i = pinv_i(in) + low_{i-2} out_{i-2}, i < f.m
-template <class T>
+// out_i = pinv_i(in) + low_{i-2} out_{i-2}, i < f.m (in and out are different lanes)
+template <class T, int PB = kPB>
 __device__ __forceinline__ void pinv_fwd_par(const PinvDev& p, const FdmaRow& f, const T* in, long long is, T* out,
                                              long long os, int q) {
   T xm2 = zero_v<T>();
-#pragma unroll 4
-  for (int i = q; i < f.m; i += 2) {
-    T v = pinv_lane<T>(p, in, is, i);
-    if (i >= 2) v = fmas(v, xm2, f.low[i - 2]);
-    out[(long long)i * os] = v;
-    xm2 = v;
+  for (int i0 = q; i0 < f.m; i0 += 2 * PB) {
+    T pv[PB];
+    double lv[PB];
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 + 2 * e;
+      pv[e] = i < f.m ? pinv_lane<T>(p, in, is, i) : zero_v<T>();
+      lv[e] = (i < f.m && i >= 2) ? __ldg(f.low + i - 2) : 0.0;
+    }
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 + 2 * e;
+      if (i >= f.m) break;
+      T v = pv[e];
+      if (i >= 2) v = fmas(v, xm2, lv[e]);
+      out[(long long)i * os] = v;
+      xm2 = v;
+    }
   }
 }
 
 // from_ortho (least squares, stride-2 tridiagonal) on the parity-q chain;
-// `in` and `out` may be the same lane
-template <class T>
+// `in` and `out` may be the same lane (a batch reads its inputs, including
+// p_{i+2} of its last element, before writing)
+template <class T, int PB = kPB>
 __device__ __forceinline__ void from_ortho_par(const BasisDev& b, const T* p, long long ps, T* out, long long os, int q) {
   const int m = b.m;
   T g2 = zero_v<T>();
-#pragma unroll 4
-  for (int i = q; i < m; i += 2) {
-    const T d = fmas(scal(p[(long long)i * ps], b.diag[i]), p[(long long)(i + 2) * ps], b.low2[i]);
-    const double qq = b.fo_dinv[i];
-    T g = scal(d, qq);
-    if (i >= 2) g = fmas(g, g2, -b.fo_off[i - 2] * qq);
-    out[(long long)i * os] = g;
-    g2 = g;
+  for (int i0 = q; i0 < m; i0 += 2 * PB) {
+    T dv[PB];
+    double qv[PB], ov[PB];
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 + 2 * e;
+      if (i < m) {
+        dv[e] = fmas(scal(p[(long long)i * ps], __ldg(b.diag + i)), p[(long long)(i + 2) * ps], __ldg(b.low2 + i));
+        qv[e] = __ldg(b.fo_dinv + i);
+        ov[e] = i >= 2 ? __ldg(b.fo_off + i - 2) : 0.0;
+      } else {
+        dv[e] = zero_v<T>();
+        qv[e] = ov[e] = 0.0;
+      }
+    }
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int i = i0 + 2 * e;
+      if (i >= m) break;
+      T g = scal(dv[e], qv[e]);
+      if (i >= 2) g = fmas(g, g2, -ov[e] * qv[e]);
+      out[(long long)i * os] = g;
+      g2 = g;
+    }
   }
   T x2 = zero_v<T>();
-#pragma unroll 4
-  for (int j = top_par(m, q); j >= 0; j -= 2) {
-    T x = out[(long long)j * os];
-    if (j + 2 < m) x = fmas(x, x2, -b.fo_w[j]);
-    out[(long long)j * os] = x;
-    x2 = x;
+  for (int j0 = top_par(m, q); j0 >= 0; j0 -= 2 * PB) {
+    T xv[PB];
+    double wv[PB];
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int j = j0 - 2 * e;
+      xv[e] = j >= 0 ? out[(long long)j * os] : zero_v<T>();
+      wv[e] = (j >= 0 && j + 2 < m) ? __ldg(b.fo_w + j) : 0.0;
+    }
+#pragma unroll
+    for (int e = 0; e < PB; e++) {
+      const int j = j0 - 2 * e;
+      if (j < 0) break;
+      T x = xv[e];
+      if (j + 2 < m) x = fmas(x, x2, -wv[e]);
+      out[(long long)j * os] = x;
+      x2 = x;
+    }
   }
 }
 
@@ -394,7 +483,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y3(const CaseDev* __restrict__ c
       xm2 = v;
     }
   }
-  fdma_bwd_par<double>(R, F, 1, q);
+  fdma_bwd_par<double, kPBRow>(R, F, 1, q);
   bool bad = false;
   if (f == 2) {
     double* tt = static_cast<double*>(c.temp) + (size_t)i * myc;
@@ -411,7 +500,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y3(const CaseDev* __restrict__ c
     for (int k = q; k < ny; k += 2) A[k] = stencil_lane<double>(c.ycd, F, 1, k);
   } else if (f == 1) {
     double* B = static_cast<double*>(c.s[2]) + (size_t)i * ny;
-    diff_par<double>(ny, 1 - q, [&](int k) { return stencil_lane<double>(c.ycd, F, 1, k); },
+    diff_par<double, kPBRow>(ny, 1 - q, [&](int k) { return stencil_lane<double>(c.ycd, F, 1, k); },
                      [&](int k, double d) { B[k] = d; });
   }
   if (bad) atomicOr(c.status, 1u);
@@ -466,10 +555,10 @@ __global__ void __launch_bounds__(256) k_lp_box_y5(const CaseDev* __restrict__ c
     for (int k = q; k < ny; k += 2) d[k] = stencil_lane<double>(c.ycn, E, 1, k);
   } else {  // Dy Sy^N Fv on parity q (from Sy^N Fv on parity 1 - q)
     const double* Fv = static_cast<const double*>(c.s[2]) + (size_t)i * myc;
-    diff_par<double>(ny, q, [&](int k) { return stencil_lane<double>(c.ycn, Fv, 1, k); },
+    diff_par<double, kPBRow>(ny, q, [&](int k) { return stencil_lane<double>(c.ycn, Fv, 1, k); },
                      [&](int k, double v) { d[k] = v; });
   }
-  from_ortho_par<double>(c.ycd, d, 1, d, 1, q);
+  from_ortho_par<double, kPBRow>(c.ycd, d, 1, d, 1, q);
   double* u = static_cast<double*>(part == 0 ? c.ux : c.uy) + (size_t)i * myc;
   const double* us = static_cast<const double*>(c.s[4 + part]) + (size_t)i * myc;
   bool bad = false;
