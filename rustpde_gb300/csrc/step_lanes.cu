@@ -705,33 +705,52 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
   double2* out = static_cast<double2*>(c.yw[3 + f]) + (size_t)i * ny;
   const PinvDev& pv = c.pinv_y;
   double2 r2 = c2(0.0, 0.0), r4 = c2(0.0, 0.0), g2 = c2(0.0, 0.0);
-  for (int k = top_par(ny, q); k >= 0; k -= 2) {
-    const double2 o = stencil_lane<double2>(c.ycd, Fo, 1, k);
-    const bool incv = i < kx && k < ky;
-    const double2 cvk = incv ? cv[((size_t)f * kx + i) * ky + k] : c2(0.0, 0.0);
-    double2 r;
-    if (f == 0) {
-      const double2 gx = mul_ik(P[k], ki) * inv_asp;
-      r = fnms(fnms(o, gx, dt), cvk, dt);
-    } else if (f == 1) {  // dP/dy at k (descending derivative recurrence), buoyancy
-      double2 g;
-      if (k == ny - 1) g = c2(0.0, 0.0);
-      else if (k >= 1) g = fmas(g2, P[k + 1], 2.0 * (double)(k + 1));
-      else g = fmas(P[1], g2, 0.5);
-      g2 = g;
-      const double2 that = stencil_lane<double2>(c.ycd, To, 1, k) + bco[k];
-      r = fnms(fmas(fnms(o, g, dt), that, dt), cvk, dt);
-    } else {
-      r = fnms(o + bcd[k], cvk, dt);
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPB) {
+    // the batch's loads first (stencil, convection, pressure, boundary terms)
+    double2 ov[kPB], cvv[kPB], pk[kPB], xv[kPB];
+#pragma unroll
+    for (int e = 0; e < kPB; e++) {
+      const int k = k0 - 2 * e;
+      ov[e] = cvv[e] = pk[e] = xv[e] = c2(0.0, 0.0);
+      if (k < 0) continue;
+      ov[e] = stencil_lane<double2>(c.ycd, Fo, 1, k);
+      if (i < kx && k < ky) cvv[e] = cv[((size_t)f * kx + i) * ky + k];
+      if (f == 0) pk[e] = P[k];
+      else if (f == 1) {
+        if (k < ny - 1) pk[e] = P[k + 1];
+        xv[e] = stencil_lane<double2>(c.ycd, To, 1, k) + bco[k];
+      } else {
+        xv[e] = bcd[k];
+      }
     }
-    if (k < myc) {
-      double2 v = scal(r, pv.dia[k]);
-      if (k < myc - 2) v = fmas(v, r2, pv.up1[k]);
-      if (k < myc - 4) v = fmas(v, r4, pv.up2[k]);
-      out[k] = v;
+#pragma unroll
+    for (int e = 0; e < kPB; e++) {
+      const int k = k0 - 2 * e;
+      if (k < 0) break;
+      const double2 o = ov[e], cvk = cvv[e];
+      double2 r;
+      if (f == 0) {
+        const double2 gx = mul_ik(pk[e], ki) * inv_asp;
+        r = fnms(fnms(o, gx, dt), cvk, dt);
+      } else if (f == 1) {  // dP/dy at k (descending derivative recurrence), buoyancy
+        double2 g;
+        if (k == ny - 1) g = c2(0.0, 0.0);
+        else if (k >= 1) g = fmas(g2, pk[e], 2.0 * (double)(k + 1));
+        else g = fmas(pk[e], g2, 0.5);
+        g2 = g;
+        r = fnms(fmas(fnms(o, g, dt), xv[e], dt), cvk, dt);
+      } else {
+        r = fnms(o + xv[e], cvk, dt);
+      }
+      if (k < myc) {
+        double2 v = scal(r, pv.dia[k]);
+        if (k < myc - 2) v = fmas(v, r2, pv.up1[k]);
+        if (k < myc - 4) v = fmas(v, r4, pv.up2[k]);
+        out[k] = v;
+      }
+      r4 = r2;
+      r2 = r;
     }
-    r4 = r2;
-    r2 = r;
   }
   const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, i);
   fdma_fwd_par<double2>(R, out, 1, q);
@@ -750,23 +769,36 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
   double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
   const PinvDev& pv = c.pinv_y;
   double2 g2 = c2(0.0, 0.0), w2 = c2(0.0, 0.0), w4 = c2(0.0, 0.0);
-  for (int k = top_par(ny, q); k >= 0; k -= 2) {
-    const double2 o0 = stencil_lane<double2>(c.ycd, U, 1, k);
-    double2 g;
-    if (k == ny - 1) g = c2(0.0, 0.0);
-    else if (k >= 1) g = fmas(g2, stencil_lane<double2>(c.ycd, V, 1, k + 1), 2.0 * (double)(k + 1));
-    else g = fmas(stencil_lane<double2>(c.ycd, V, 1, 1), g2, 0.5);
-    g2 = g;
-    const double2 d = mul_ik(o0, ki) * inv_asp + g;
-    dvr[k] = d;
-    if (k < myc) {
-      double2 v = scal(d, pv.dia[k]);
-      if (k < myc - 2) v = fmas(v, w2, pv.up1[k]);
-      if (k < myc - 4) v = fmas(v, w4, pv.up2[k]);
-      p1[k] = v;
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPB) {
+    double2 ov[kPB], vv[kPB];  // Sy ux* at k, Sy uy* at k + 1
+#pragma unroll
+    for (int e = 0; e < kPB; e++) {
+      const int k = k0 - 2 * e;
+      ov[e] = vv[e] = c2(0.0, 0.0);
+      if (k < 0) continue;
+      ov[e] = stencil_lane<double2>(c.ycd, U, 1, k);
+      if (k < ny - 1) vv[e] = stencil_lane<double2>(c.ycd, V, 1, k + 1);
     }
-    w4 = w2;
-    w2 = d;
+#pragma unroll
+    for (int e = 0; e < kPB; e++) {
+      const int k = k0 - 2 * e;
+      if (k < 0) break;
+      double2 g;
+      if (k == ny - 1) g = c2(0.0, 0.0);
+      else if (k >= 1) g = fmas(g2, vv[e], 2.0 * (double)(k + 1));
+      else g = fmas(vv[e], g2, 0.5);
+      g2 = g;
+      const double2 d = mul_ik(ov[e], ki) * inv_asp + g;
+      dvr[k] = d;
+      if (k < myc) {
+        double2 v = scal(d, pv.dia[k]);
+        if (k < myc - 2) v = fmas(v, w2, pv.up1[k]);
+        if (k < myc - 4) v = fmas(v, w4, pv.up2[k]);
+        p1[k] = v;
+      }
+      w4 = w2;
+      w2 = d;
+    }
   }
   const FdmaRow R = fdma_row(c.pois_y, i);
   fdma_fwd_par<double2>(R, p1, 1, q);
@@ -786,12 +818,25 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     double2* dpx = static_cast<double2*>(c.yw[1]) + (size_t)i * ny;
     double2* P = static_cast<double2*>(c.p0) + (size_t)i * ny;
     const double2* dvr = static_cast<const double2*>(c.yw[0]) + (size_t)i * ny;
-#pragma unroll 4
-    for (int k = q; k < ny; k += 2) {
-      const double2 o1 = stencil_lane<double2>(c.ycn, p1, 1, k);
-      dpx[k] = mul_ik(o1, ki) * inv_asp;
-      const double2 v = fnms(P[k], dvr[k], c.nu);
-      P[k] = fmas(v, o1, c.inv_dt);
+    for (int k0 = q; k0 < ny; k0 += 2 * kPB) {
+      double2 ov[kPB], pv0[kPB], dv[kPB];
+#pragma unroll
+      for (int e = 0; e < kPB; e++) {
+        const int k = k0 + 2 * e;
+        ov[e] = pv0[e] = dv[e] = c2(0.0, 0.0);
+        if (k >= ny) continue;
+        ov[e] = stencil_lane<double2>(c.ycn, p1, 1, k);
+        pv0[e] = P[k];
+        dv[e] = dvr[k];
+      }
+#pragma unroll
+      for (int e = 0; e < kPB; e++) {
+        const int k = k0 + 2 * e;
+        if (k >= ny) break;
+        dpx[k] = mul_ik(ov[e], ki) * inv_asp;
+        const double2 v = fnms(pv0[e], dv[e], c.nu);
+        P[k] = fmas(v, ov[e], c.inv_dt);
+      }
     }
     from_ortho_par<double2>(c.ycd, dpx, 1, dpx, 1, q);
     const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
