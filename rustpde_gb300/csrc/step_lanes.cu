@@ -439,28 +439,50 @@ __global__ void __launch_bounds__(256) k_lp_box_y2(const CaseDev* __restrict__ c
   double* out = static_cast<double*>(c.s[1 + f]) + (size_t)i * myc;
   const PinvDev& pv = c.pinv_y;
   double r2 = 0.0, r4 = 0.0, g2 = 0.0;
-  for (int k = top_par(ny, q); k >= 0; k -= 2) {
-    double g = 0.0;
-    if (f == 1) {  // dP/dy at k (descending derivative recurrence)
-      if (k == ny - 1) g = 0.0;
-      else if (k >= 1) g = fmas(g2, P[k + 1], 2.0 * (double)(k + 1));
-      else g = fmas(P[1], g2, 0.5);
-      g2 = g;
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPB) {
+    // the batch's loads first: stencils of the state, convection, pressure, boundary terms
+    double ov[kPB], cvv[kPB], pk[kPB], xv[kPB];
+#pragma unroll
+    for (int e = 0; e < kPB; e++) {
+      const int k = k0 - 2 * e;
+      ov[e] = cvv[e] = pk[e] = xv[e] = 0.0;
+      if (k < 0) continue;
+      ov[e] = oy(f, k);
+      if (i < kx && k < ky) cvv[e] = cv[((size_t)f * kx + i) * ky + k];
+      if (f == 0) pk[e] = gpx[k];
+      else if (f == 1) {
+        if (k < ny - 1) pk[e] = P[k + 1];
+        xv[e] = oy(2, k) + bco[k];
+      } else {
+        xv[e] = bcd[k];
+      }
     }
-    const bool incv = i < kx && k < ky;
-    const double cvk = incv ? cv[((size_t)f * kx + i) * ky + k] : 0.0;
-    double r;
-    if (f == 0) r = fnms(fnms(oy(0, k), gpx[k], dt), cvk, dt);
-    else if (f == 1) r = fnms(fmas(fnms(oy(1, k), g, dt), oy(2, k) + bco[k], dt), cvk, dt);
-    else r = fnms(oy(2, k) + bcd[k], cvk, dt);
-    if (k < myc) {
-      double v = r * pv.dia[k];
-      if (k < myc - 2) v = fma(r2, pv.up1[k], v);
-      if (k < myc - 4) v = fma(r4, pv.up2[k], v);
-      out[k] = v;
+#pragma unroll
+    for (int e = 0; e < kPB; e++) {
+      const int k = k0 - 2 * e;
+      if (k < 0) break;
+      double r;
+      if (f == 0) {
+        r = fnms(fnms(ov[e], pk[e], dt), cvv[e], dt);
+      } else if (f == 1) {  // dP/dy at k (descending derivative recurrence), buoyancy
+        double g;
+        if (k == ny - 1) g = 0.0;
+        else if (k >= 1) g = fmas(g2, pk[e], 2.0 * (double)(k + 1));
+        else g = fmas(pk[e], g2, 0.5);
+        g2 = g;
+        r = fnms(fmas(fnms(ov[e], g, dt), xv[e], dt), cvv[e], dt);
+      } else {
+        r = fnms(ov[e] + xv[e], cvv[e], dt);
+      }
+      if (k < myc) {
+        double v = r * pv.dia[k];
+        if (k < myc - 2) v = fma(r2, pv.up1[k], v);
+        if (k < myc - 4) v = fma(r4, pv.up2[k], v);
+        out[k] = v;
+      }
+      r4 = r2;
+      r2 = r;
     }
-    r4 = r2;
-    r2 = r;
   }
 }
 

@@ -84,12 +84,18 @@ MIX_PARAMS = [(64, 33, 1e5, 1.0, 0.005, 1.0, O.PERIODIC), (128, 64, 1e6, 0.7, 2e
               (64, 64, 1e5, 1.0, 0.02, 1.0, O.BOX_ADIABATIC)]
 
 
+# Forms of the FP64 passes (CTA scans, 128-thread CTAs, sub-lane chains) round
+# differently in the last bit; in the mixed step a last-bit FP64 difference
+# can flip the FP32 rounding of a value fed to the next tensor-core transform,
+# so two forms agree to the mixed form's own precision, not to FP64's.
+FORMS_TOL = 1e-7
+
+
 def test_mixed_batch_matches_batch_of_one(R):
-    # batches choose per pass between the one-CTA-per-lane and one-thread-per-
-    # lane forms of the FP64 passes (autotuned on the batch), so a case's
-    # numbers match its batch of one up to the roundings of the two forms;
-    # bitwise identity alone vs in a mix is the serving loop's guarantee
-    # (test_gpu_serving.py)
+    # batches choose per pass between the forms of the FP64 passes (autotuned
+    # on the batch), so a case's numbers match its batch of one up to the
+    # roundings of the forms; bitwise identity alone vs in a mix is the
+    # serving loop's guarantee (test_gpu_serving.py)
     b = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     print("autotuner:", b.tuning())
     for i in range(len(MIX_PARAMS)):
@@ -103,7 +109,7 @@ def test_mixed_batch_matches_batch_of_one(R):
         one.synchronize()
         for f in FIELDS:
             e = rel(b.cases[i].get(f), one.cases[0].get(f))
-            assert e < 1e-10, (i, f, e)
+            assert e < FORMS_TOL, (i, f, e)
 
 
 def test_mixed_batch_matches_single_case(R):
@@ -123,4 +129,4 @@ def test_mixed_batch_matches_single_case(R):
     for i, s in enumerate(singles):
         for f in FIELDS:
             e = rel(b.cases[i].get(f), s.get(f))
-            assert e < 1e-10, (i, f, e)
+            assert e < FORMS_TOL, (i, f, e)
