@@ -128,21 +128,40 @@ __device__ __forceinline__ void tmem_st8(uint32_t addr, const float (&v)[8]) {
                : "memory");
 }
 
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t addr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(addr));
+}
+
 // running total += chunk partial (or = partial for the first chunk), all 8
 // warps: warp w covers tensor-memory lanes 32 (w % 4) .. + 31 and every other
-// 8-column block (from block w / 4)
+// 8-column block (from block w / 4), at most 4 blocks (NT <= 64).  All loads
+// are issued before one wait, so a flush costs one tensor-memory round trip.
 __device__ __forceinline__ void tmem_accumulate(uint32_t tmem, uint32_t part, uint32_t total, int NT, bool first,
                                                 int warp) {
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-  for (int cb = (warp >> 2) * 8; cb < NT; cb += 16) {
-    float p[8], t[8];
-    tmem_ld8(tmem + lane_base + part + (uint32_t)cb, p);
-    if (!first) {
-      tmem_ld8(tmem + lane_base + total + (uint32_t)cb, t);
+  const int cb0 = (warp >> 2) * 8;
+  uint32_t p[4][8], t[4][8];
 #pragma unroll
-      for (int j = 0; j < 8; j++) p[j] = __fadd_rn(t[j], p[j]);
+  for (int b = 0; b < 4; b++) {
+    const int cb = cb0 + 16 * b;
+    if (cb < NT) {
+      tmem_ld8_nowait(tmem + lane_base + part + (uint32_t)cb, p[b]);
+      if (!first) tmem_ld8_nowait(tmem + lane_base + total + (uint32_t)cb, t[b]);
     }
-    tmem_st8(tmem + lane_base + total + (uint32_t)cb, p);
+  }
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    const int cb = cb0 + 16 * b;
+    if (cb < NT) {
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        v[j] = first ? __uint_as_float(p[b][j]) : __fadd_rn(__uint_as_float(t[b][j]), __uint_as_float(p[b][j]));
+      tmem_st8(tmem + lane_base + total + (uint32_t)cb, v);
+    }
   }
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
