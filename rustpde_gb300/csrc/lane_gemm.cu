@@ -89,7 +89,8 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, 
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
-__device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
+// 32 columns of a warp's 32 tensor-memory lanes; the caller waits (tcgen05.wait::ld)
+__device__ __forceinline__ void tmem_ld32_nowait(uint32_t addr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
       "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -98,7 +99,6 @@ __device__ __forceinline__ void tmem_ld32(uint32_t addr, uint32_t (&r)[32]) {
         "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
         "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(addr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // tensor-memory columns of a tile: a power of two holding the two chunk
@@ -111,15 +111,6 @@ __host__ __device__ inline uint32_t gemm_tmem_cols(int NT) {
   return c;
 }
 
-__device__ __forceinline__ void tmem_ld8(uint32_t addr, float (&v)[8]) {
-  uint32_t r[8];
-  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
-               : "r"(addr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int j = 0; j < 8; j++) v[j] = __uint_as_float(r[j]);
-}
 __device__ __forceinline__ void tmem_st8(uint32_t addr, const float (&v)[8]) {
   asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(addr),
                "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
@@ -353,8 +344,9 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     for (int cc = 0; cc < NT; cc += 32) {
       if (warp < 4) {  // warp w reads accumulator lanes 32w .. 32w+31
         uint32_t r[32], q[32];
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + total + (uint32_t)cc, r);
-        tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
+        tmem_ld32_nowait(tmem + ((uint32_t)(warp * 32) << 16) + total + (uint32_t)cc, r);
+        tmem_ld32_nowait(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int j = 0; j < 32; j++)
           stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
