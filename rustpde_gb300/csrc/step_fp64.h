@@ -25,6 +25,8 @@ enum StepKernel {
   K_LP_PER_Y2A, K_LP_PER_Y2B, K_LP_PER_Y2C,
   // FP32 copy of the state rows for the y GEMM (mixed form)
   K_STATE_F32,
+  // the periodic FP32 x pass launched with 128 threads
+  K_PER_X_MIXED_T128,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };

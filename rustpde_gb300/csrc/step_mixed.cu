@@ -198,8 +198,8 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     out.nf = 3; out.rows = mx; out.parts = 2; out.type = LT_F32;
     out.lane_stride = 2; out.part_stride = 1; out.elem_stride = 2LL * mx; out.len = 2 * ny; out.lane_fast = 1;
     add_gemm(make_gemm_job(in, out, ops.y1, myc, 2 * ny, 1.0, c.status));
-    // X: FP32 convection, one CTA per column
-    add(K_PER_X_MIXED, ny, dev::smem_per_x_mixed(c));
+    // X: FP32 convection, one CTA per column (256 threads, or 128 in the batch forms)
+    add(lane_parallel ? K_PER_X_MIXED_T128 : K_PER_X_MIXED, ny, dev::smem_per_x_mixed(c));
     // G2: y transform of the x-transformed products (FP32, transposed) -> m_cv (FP64)
     LaneSideDev qi;
     std::memset(&qi, 0, sizeof qi);
@@ -345,6 +345,7 @@ cudaError_t launch_mixed_kernel(int kernel, int nblocks, size_t smem, cudaStream
   switch (kernel) {
     case K_PER_X_MIXED: dev::k_per_x_mixed<<<nblocks, 256, smem, s>>>(cases, work); break;
     case K_STATE_F32: dev::k_state_f32<<<nblocks, 128, 0, s>>>(cases, work); break;
+    case K_PER_X_MIXED_T128: dev::k_per_x_mixed<<<nblocks, 128, smem, s>>>(cases, work); break;
     case K_BOX_PROD_MIXED: dev::k_box_prod_mixed<<<nblocks, 256, 0, s>>>(cases, work); break;
     default: return launch_lane_kernel(kernel, nblocks, s, cases, work);
   }
@@ -384,6 +385,7 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
       case K_LP_PER_Y2: kernel = K_PER_Y2_PRE; break;
       case K_PER_Y2_PRE_T128: kernel = K_PER_Y2_PRE; break;
       case K_LP_PER_Y2B: case K_LP_PER_Y2C: kernel = -1; break;  // counted with Y2A
+      case K_PER_X_MIXED_T128: kernel = K_PER_X_MIXED; break;
       case K_BOX_Y2_PRE_T128: kernel = K_BOX_Y2_PRE; break;
       case K_BOX_X3_MIX_T128: kernel = K_BOX_X3_MIX; break;
       case K_BOX_Y5_T128: kernel = K_BOX_Y5; break;
@@ -432,7 +434,7 @@ const char* step_kernel_name(int kernel) {
                                 "lanes_box_x2", "lanes_box_x3", "lanes_box_x4", "lanes_box_y2", "lanes_box_y3",
                                 "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2", "periodic_y2_pre_t128",
                                 "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128", "lanes_periodic_y2a",
-                                "lanes_periodic_y2b", "lanes_periodic_y2c", "state_f32"};
+                                "lanes_periodic_y2b", "lanes_periodic_y2c", "state_f32", "periodic_x_mixed_t128"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";
