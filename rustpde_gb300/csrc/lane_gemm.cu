@@ -165,11 +165,18 @@ __device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
 
-// bounded wait for completion phase `parity` of the MMA barrier; true when
-// every thread of the CTA saw it complete
+// bounded wait for completion phase `parity` of the MMA barrier; true when it
+// completed.  Warp 0 polls the barrier and the other warps wait at
+// __syncthreads (256 polling threads took the issue slots of the SM's other
+// CTA); the callers' tcgen05.fence::after_thread_sync orders every thread's
+// later tensor-memory and shared-memory accesses after the completion.
 __device__ __forceinline__ bool mma_wait(uint64_t* mbar, uint32_t parity) {
-  bool done = false;
-  for (long i = 0; i < kWaitLimit && !done; i++) done = mbar_try(mbar, parity);
+  int done = 1;
+  if (threadIdx.x < 32) {
+    bool d = false;
+    for (long i = 0; i < kWaitLimit && !d; i++) d = mbar_try(mbar, parity);
+    done = d ? 1 : 0;
+  }
   return __syncthreads_and(done) != 0;
 }
 
