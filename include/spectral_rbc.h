@@ -177,7 +177,10 @@ const char* rbc_kernel_name(int kernel);
  * stream, so their state/diagnostic calls are ordered after rbc_batch_step.
  * Mixed-precision batches time the forms of each FP64 pass at creation and
  * keep the fastest (rbc_batch_tuning); the environment variable
- * RBC_BATCH_FORM=0|1|2 pins one form instead (profiling runs). */
+ * RBC_BATCH_FORM=0|1|2 pins one form instead (profiling runs).  The group
+ * whose step takes longest runs on a high-priority branch, so its thread
+ * blocks are dispatched first; RBC_BATCH_PRIORITY=0 gives every branch the
+ * default priority. */
 typedef struct RbcBatch RbcBatch;
 int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out);
 int rbc_batch_destroy(RbcBatch* b);

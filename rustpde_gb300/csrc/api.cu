@@ -1265,11 +1265,50 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   cuda_check(cudaMemsetAsync(b->d_state, 0, b->state_bytes, b->stream), "clear state");
   for (RbcCase* c : b->cases) cuda_check(cudaMemsetAsync(c->hd.status, 0, 16, b->stream), "clear status");
   cuda_check(cudaDeviceSynchronize(), "batch set-up");
-  // graph: one branch per bucket
+  // graph: one branch per bucket.  The branches run side by side; the one
+  // with the longest step (timed here, launches in sequence) is the critical
+  // path and is captured on a high-priority stream, so its thread blocks are
+  // dispatched first and the other branches fill the SMs it leaves idle
+  // (kernel nodes take the capturing stream's priority)
   size_t nb = b->buckets.size();
+  std::vector<float> bucket_ms(nb, 0.f);
+  {
+    cudaEvent_t e0, e1;
+    cuda_check(cudaEventCreate(&e0), "event");
+    cuda_check(cudaEventCreate(&e1), "event");
+    for (size_t k = 0; k < nb; k++) {
+      const auto& bk = b->buckets[k];
+      float best = 1e30f;
+      for (int r = 0; r < 2; r++) {
+        cuda_check(cudaEventRecord(e0, b->stream), "event");
+        for (size_t li = 0; li < bk.plan.launches.size(); li++)
+          cuda_check(launch_entry(bk.plan.launches[li], bk.dp, li, b->stream, b->d_cases), "bucket timing launch");
+        cuda_check(cudaEventRecord(e1, b->stream), "event");
+        cuda_check(cudaEventSynchronize(e1), "event");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, e0, e1), "event");
+        best = std::min(best, ms);
+      }
+      bucket_ms[k] = best;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cuda_check(cudaMemsetAsync(b->d_state, 0, b->state_bytes, b->stream), "clear state");
+    for (RbcCase* c : b->cases) cuda_check(cudaMemsetAsync(c->hd.status, 0, 16, b->stream), "clear status");
+    cuda_check(cudaStreamSynchronize(b->stream), "batch set-up");
+  }
+  const size_t critical = (size_t)(std::max_element(bucket_ms.begin(), bucket_ms.end()) - bucket_ms.begin());
+  bool use_priority = nb > 1;
+  if (const char* f = std::getenv("RBC_BATCH_PRIORITY"))
+    if (f[0] == '0' && f[1] == '\0') use_priority = false;
+  int prio_low = 0, prio_high = 0;
+  cuda_check(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high), "stream priority range");
   b->branch.resize(nb);
   b->events.resize(nb + 1);
-  for (size_t k = 0; k < nb; k++) cuda_check(cudaStreamCreateWithFlags(&b->branch[k], cudaStreamNonBlocking), "stream");
+  for (size_t k = 0; k < nb; k++) {
+    const int prio = !use_priority ? 0 : (k == critical ? prio_high : prio_low);
+    cuda_check(cudaStreamCreateWithPriority(&b->branch[k], cudaStreamNonBlocking, prio), "stream");
+  }
   for (auto& e : b->events) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
   cuda_check(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t le = cudaEventRecord(b->events[nb], b->stream);
@@ -1289,7 +1328,8 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   cuda_check(le, "batch capture");
   cuda_check(ce, "end capture");
   b->graph = g;
-  cuda_check(cudaGraphInstantiate(&b->gexec, g, 0), "graph instantiate");
+  cuda_check(cudaGraphInstantiate(&b->gexec, g, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
+             "graph instantiate");
   *out = b.release();
   API_END
 }

@@ -24,6 +24,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 namespace rbc {
 namespace dev {
@@ -189,33 +190,71 @@ struct AChunk {
   T v[kItems][4];
 };
 
+// A thread's items are the same in every chunk of a tile: item it of thread
+// tid is q = tid + 256 it, lane l and quad kq as below.  With lanes fast in
+// memory (columns) a thread keeps one lane and steps kq by 2; with rows it
+// keeps kq and steps the lane by 32.  The lane addresses (element 4 kq of each
+// item's lane) are formed once per tile.
 template <class T>
-__device__ __forceinline__ void a_load(AChunk<T>& a, const GemmJobDev& J, const char* const* ib, int k0, int tid) {
-  const long long es = J.in.elem_stride;
+struct ATile {
+  const T* src[kItems];  // nullptr: lane past the job's end (zeros)
+  int es;               // element stride of the lanes (a row length at most)
+  int soff0, sstep;     // shared-memory byte offset of item 0, step per item
+};
+
+__device__ __forceinline__ void item_lane_quad(int q, bool lane_fast, int& l, int& kq) {
+  const int llo = q & 7, r = q >> 3;
+  l = lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
+  kq = lane_fast ? r >> 4 : r & 7;
+}
+
+template <class T>
+__device__ __forceinline__ void a_setup(ATile<T>& t, const GemmJobDev& J, const char* const* ib, int tid) {
+  const bool lf = J.in.lane_fast != 0;
+  t.es = (int)J.in.elem_stride;
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    const int q = tid + kGemmThreads * it;
-    const int llo = q & 7, r = q >> 3;
-    const int l = J.in.lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
-    const int kq = J.in.lane_fast ? r >> 4 : r & 7;
-    const T* base = reinterpret_cast<const T*>(ib[l]);
+    int l, kq;
+    item_lane_quad(tid + kGemmThreads * it, lf, l, kq);
+    const T* b = reinterpret_cast<const T*>(ib[l]);
+    t.src[it] = b != nullptr ? b + (long long)(kq * 4) * t.es : nullptr;
+    if (it == 0) t.soff0 = cm_off(l, kq * 4, kGemmLanes);
+  }
+  // item it+1 is 2 quads further (lanes fast) or 32 lanes further (rows)
+  t.sstep = lf ? 2 * (kGemmLanes / 8) * 128 : 4 * 128;
+}
+
+// loads of chunk k0 .. k0+31; only the job's last chunk checks k < K
+template <class T>
+__device__ __forceinline__ void a_load(AChunk<T>& a, const ATile<T>& t, int k0, int K, bool lane_fast, int tid) {
+  const int o = k0 * t.es;
+  if (k0 + kGemmKC <= K) {
 #pragma unroll
-    for (int e = 0; e < 4; e++) {
-      const int k = k0 + kq * 4 + e;
-      a.v[it][e] = (base != nullptr && k < J.K) ? __ldg(base + (long long)k * es) : T(0);
+    for (int it = 0; it < kItems; it++) {
+      const T* p = t.src[it];
+#pragma unroll
+      for (int e = 0; e < 4; e++) a.v[it][e] = p != nullptr ? __ldg(p + o + e * t.es) : T(0);
+    }
+  } else {
+#pragma unroll
+    for (int it = 0; it < kItems; it++) {
+      int l, kq;
+      item_lane_quad(tid + kGemmThreads * it, lane_fast, l, kq);
+      const T* p = t.src[it];
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        const int k = k0 + kq * 4 + e;
+        a.v[it][e] = (p != nullptr && k < K) ? __ldg(p + o + e * t.es) : T(0);
+      }
     }
   }
 }
 
 template <class T>
-__device__ __forceinline__ void a_store(const AChunk<T>& a, const GemmJobDev& J, unsigned char* Ahi,
-                                        unsigned char* Alo, int tid) {
+__device__ __forceinline__ void a_store(const AChunk<T>& a, const ATile<T>& t, unsigned char* Ahi,
+                                        unsigned char* Alo) {
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
-    const int q = tid + kGemmThreads * it;
-    const int llo = q & 7, r = q >> 3;
-    const int l = J.in.lane_fast ? (r & 15) * 8 + llo : (r >> 3) * 8 + llo;
-    const int kq = J.in.lane_fast ? r >> 4 : r & 7;
     float4 hi, lo;
     float x;
     // lo is rounded to TF32 here: left to the tensor core it would be
@@ -224,7 +263,7 @@ __device__ __forceinline__ void a_store(const AChunk<T>& a, const GemmJobDev& J,
     x = (float)a.v[it][1]; hi.y = tf32_rna(x); lo.y = tf32_rna(x - hi.y);
     x = (float)a.v[it][2]; hi.z = tf32_rna(x); lo.z = tf32_rna(x - hi.z);
     x = (float)a.v[it][3]; hi.w = tf32_rna(x); lo.w = tf32_rna(x - hi.w);
-    const int off = cm_off(l, kq * 4, kGemmLanes);
+    const int off = t.soff0 + it * t.sstep;
     *reinterpret_cast<float4*>(Ahi + off) = hi;
     *reinterpret_cast<float4*>(Alo + off) = lo;
   }
@@ -288,18 +327,24 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NT >> 3) << 17) | ((128u >> 4) << 24);
   const uint32_t a_lbo = (kGemmLanes / 8) * 128, w_lbo = (uint32_t)(NT / 8) * 128;
   bool ok = true;
+  const int K = J.K, kchunks = J.kchunks;
+  const bool in_lf = J.in.lane_fast != 0;
+  ATile<T> at;
+  a_setup<T>(at, J, ib, tid);
   AChunk<T> a;
-  a_load<T>(a, J, ib, 0, tid);
+  a_load<T>(a, at, 0, K, in_lf, tid);
 
-  for (int c = 0; c < J.kchunks; c++) {
+  for (int c = 0; c < kchunks; c++) {
     // the A buffer and operator buffer (c+1)&1 were read by MMA c-1
     if (c > 0) {
       ok = mma_wait(mbar, (uint32_t)((c - 1) & 1));
       tc_fence_after();
       if (!ok) break;
     }
-    a_store<T>(a, J, Ahi, Alo, tid);
-    if (c + 1 < J.kchunks) w_issue(wsrc, c + 1, NT, Wb[(c + 1) & 1], tid);
+    a_store<T>(a, at, Ahi, Alo);
+    // next input chunk in flight through the barrier, the MMAs and the flush
+    if (c + 1 < kchunks) a_load<T>(a, at, (c + 1) * kGemmKC, K, in_lf, tid);
+    if (c + 1 < kchunks) w_issue(wsrc, c + 1, NT, Wb[(c + 1) & 1], tid);
     cp_async_commit();
     cp_async_wait1();  // operator chunk c has landed (this thread's copies)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -327,14 +372,12 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     }
     // the previous chunk's partial into the running total, while chunk c multiplies
     if (c > 0) tmem_accumulate(tmem, (uint32_t)(((c - 1) & 1) * NT), total, NT, c == 1, warp);
-    // next input chunk in flight while the tensor core works
-    if (c + 1 < J.kchunks) a_load<T>(a, J, ib, (c + 1) * kGemmKC, tid);
   }
   if (ok) {
-    ok = mma_wait(mbar, (uint32_t)((J.kchunks - 1) & 1));
+    ok = mma_wait(mbar, (uint32_t)((kchunks - 1) & 1));
     tc_fence_after();
     if (ok) {
-      tmem_accumulate(tmem, (uint32_t)(((J.kchunks - 1) & 1) * NT), total, NT, J.kchunks == 1, warp);
+      tmem_accumulate(tmem, (uint32_t)(((kchunks - 1) & 1) * NT), total, NT, kchunks == 1, warp);
       tc_fence_before();
       __syncthreads();
       tc_fence_after();
@@ -343,11 +386,15 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   asm volatile("cp.async.wait_all;" ::: "memory");
 
   if (ok) {
-    const int P = J.out.parts;
+    // output mapping of staged element q = tid + 256 it -> (lane l, column n):
+    // 0: lanes fast in memory (columns); 1: real rows; 2: complex rows (re, im
+    // lanes of one row interleaved)
+    const int omode = J.out.lane_fast ? 0 : (J.out.parts == 2 ? 2 : 1);
     const long long oes = J.out.elem_stride;
     const int otype = J.out.type;
     const double scale = J.scale;
     const int nbase = tile_n * NT;
+    const int nvalid = min(NT, J.N - nbase);  // valid columns of this tile
     for (int cc = 0; cc < NT; cc += 32) {
       if (warp < 4) {  // warp w reads accumulator lanes 32w .. 32w+31
         uint32_t r[32], q[32];
@@ -361,28 +408,33 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
       __syncthreads();
       // FP32 outputs of scale 1 are stored as they are (a round trip through
       // FP64 would run at the FP64 rate on this GPU)
-      auto store_all = [&](auto store) {
+      auto store_all = [&](auto store, auto mode) {
+        constexpr int M = decltype(mode)::value;
 #pragma unroll 4
         for (int it = 0; it < 4096 / kGemmThreads; it++) {
           const int q = tid + kGemmThreads * it;
           int l, n;
-          if (J.out.lane_fast) { l = q & 127; n = q >> 7; }
-          else {
-            const int p = q % P;
-            n = (q / P) & 31;
-            l = (q / (32 * P)) * P + p;
-          }
+          if constexpr (M == 0) { l = q & 127; n = q >> 7; }
+          else if constexpr (M == 1) { l = q >> 5; n = q & 31; }
+          else { l = (q >> 6) * 2 + (q & 1); n = (q >> 1) & 31; }
           char* base = ob[l];
-          const int nl = cc + n, ng = nbase + nl;
-          if (base != nullptr && nl < NT && ng < J.N) store(base, (long long)ng * oes, stage[l * 33 + n]);
+          const int nl = cc + n;
+          if (base != nullptr && nl < nvalid) store(base, (long long)(nbase + nl) * oes, stage[l * 33 + n]);
         }
       };
-      if (otype == LT_F64)
-        store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f * scale; });
-      else if (scale == 1.0)
-        store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = f; });
-      else
-        store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = (float)((double)f * scale); });
+      auto store_typed = [&](auto mode) {
+        if (otype == LT_F64)
+          store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f * scale; },
+                    mode);
+        else if (scale == 1.0)
+          store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = f; }, mode);
+        else
+          store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = (float)((double)f * scale); },
+                    mode);
+      };
+      if (omode == 0) store_typed(std::integral_constant<int, 0>());
+      else if (omode == 1) store_typed(std::integral_constant<int, 1>());
+      else store_typed(std::integral_constant<int, 2>());
       __syncthreads();
     }
   } else if (tid == 0 && J.status != nullptr) {
