@@ -134,25 +134,28 @@ __device__ __forceinline__ void tmem_accumulate(uint32_t tmem, uint32_t part, ui
                                                 int warp) {
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const int cb0 = (warp >> 2) * 8;
-  uint32_t p[4][8], t[4][8];
 #pragma unroll
-  for (int b = 0; b < 4; b++) {
-    const int cb = cb0 + 16 * b;
-    if (cb < NT) {
-      tmem_ld8_nowait(tmem + lane_base + part + (uint32_t)cb, p[b]);
-      if (!first) tmem_ld8_nowait(tmem + lane_base + total + (uint32_t)cb, t[b]);
+  for (int h = 0; h < 2; h++) {
+    uint32_t p[2][8], t[2][8];
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      const int cb = cb0 + 16 * (2 * h + b);
+      if (cb < NT) {
+        tmem_ld8_nowait(tmem + lane_base + part + (uint32_t)cb, p[b]);
+        if (!first) tmem_ld8_nowait(tmem + lane_base + total + (uint32_t)cb, t[b]);
+      }
     }
-  }
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int b = 0; b < 4; b++) {
-    const int cb = cb0 + 16 * b;
-    if (cb < NT) {
-      float v[8];
+    for (int b = 0; b < 2; b++) {
+      const int cb = cb0 + 16 * (2 * h + b);
+      if (cb < NT) {
+        float v[8];
 #pragma unroll
-      for (int j = 0; j < 8; j++)
-        v[j] = first ? __uint_as_float(p[b][j]) : __fadd_rn(__uint_as_float(t[b][j]), __uint_as_float(p[b][j]));
-      tmem_st8(tmem + lane_base + total + (uint32_t)cb, v);
+        for (int j = 0; j < 8; j++)
+          v[j] = first ? __uint_as_float(p[b][j]) : __fadd_rn(__uint_as_float(t[b][j]), __uint_as_float(p[b][j]));
+        tmem_st8(tmem + lane_base + total + (uint32_t)cb, v);
+      }
     }
   }
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -522,6 +525,11 @@ void gemm_tiles(const std::vector<GemmJobDev>& jobs, std::vector<int4>& tiles) {
   for (size_t j = 0; j < jobs.size(); j++)
     for (int l0 = 0; l0 < jobs[j].lanes; l0 += kGemmLanes)
       for (int t = 0; t < jobs[j].ntiles; t++) tiles.push_back(make_int4((int)j, l0, t, 0));
+  // longest tiles (most K chunks) first, so the last wave holds short ones;
+  // the sort is stable, so the output tiles of one lane block stay adjacent
+  // and share its input in L2
+  std::stable_sort(tiles.begin(), tiles.end(),
+                   [&](const int4& a, const int4& b) { return jobs[a.x].kchunks > jobs[b.x].kchunks; });
 }
 
 size_t gemm_smem_bytes(int NT) {
