@@ -54,8 +54,19 @@ __device__ __forceinline__ double fnms(double a, double b, double s) { return fm
 __device__ __forceinline__ double2 fnms(double2 a, double2 b, double s) { return c2(fma(-b.x, s, a.x), fma(-b.y, s, a.y)); }
 __device__ __forceinline__ double fmas(double a, double b, double s) { return fma(b, s, a); }
 __device__ __forceinline__ double2 fmas(double2 a, double2 b, double s) { return c2(fma(b.x, s, a.x), fma(b.y, s, a.y)); }
-__device__ __forceinline__ bool finite_v(double a) { return isfinite(a); }
-__device__ __forceinline__ bool finite_v(double2 a) { return isfinite(a.x) && isfinite(a.y); }
+// finiteness from the exponent bits (integer operations: comparisons and
+// conversions of doubles run at the FP64 rate on this GPU)
+__device__ __forceinline__ bool finite_v(double a) {
+  return ((unsigned long long)__double_as_longlong(a) & 0x7FF0000000000000ull) != 0x7FF0000000000000ull;
+}
+__device__ __forceinline__ bool finite_v(double2 a) { return finite_v(a.x) && finite_v(a.y); }
+// n (1 <= n < 2^31) as a double, assembled from its bits with integer
+// operations; equal to (double)n
+__device__ __forceinline__ double exact_double(int n) {
+  const int e = 31 - __clz(n);  // 2^e <= n < 2^(e+1)
+  const unsigned long long mant = ((unsigned long long)(unsigned)n << (52 - e)) & ((1ull << 52) - 1ull);
+  return __longlong_as_double((long long)(((unsigned long long)(1023 + e) << 52) | mant));
+}
 
 // multiply by i*k / s  (Fourier derivative of order 1, then division by the scale)
 __device__ __forceinline__ double2 mul_ik(double2 a, double k) { return c2(-a.y * k, a.x * k); }

@@ -90,6 +90,18 @@ BasisDev upload_basis(Arena& a, const HostBasis& b) {
   d.fo_off = a.upload(b.fo_off);
   d.fo_w = a.upload(b.fo_w);
   d.fo_dinv = a.upload(b.fo_dinv);
+  if (!b.fo_dinv.empty()) {
+    const int m = b.m;
+    std::vector<double> fa(m), fb(m), fc(m, 0.0);
+    for (int i = 0; i < m; i++) {
+      fa[i] = b.diag[i] * b.fo_dinv[i];
+      fb[i] = b.low2[i] * b.fo_dinv[i];
+      if (i >= 2) fc[i] = -b.fo_off[i - 2] * b.fo_dinv[i];
+    }
+    d.fo_a = a.upload(fa);
+    d.fo_b = a.upload(fb);
+    d.fo_c = a.upload(fc);
+  }
   for (int i = 0; i < 2; i++) { d.t0[i] = b.t0[i]; d.t1[i] = b.t1[i]; }
   for (int i = 0; i < 4; i++) d.bc_inv[i] = b.bc_inv[i];
   return d;

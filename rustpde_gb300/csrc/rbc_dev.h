@@ -19,6 +19,11 @@ struct BasisDev {
   const double* fo_off;   // from_ortho tdma off-diagonal (m-2)
   const double* fo_w;     // from_ortho tdma ratios (m-2)
   const double* fo_dinv;  // from_ortho tdma 1/denominators (m)
+  // forward sweep of from_ortho with its factors multiplied out:
+  // g_i = fo_a_i p_i + fo_b_i p_{i+2} + fo_c_i g_{i-2}
+  const double* fo_a;     // diag_i / den_i (m)
+  const double* fo_b;     // low2_i / den_i (m)
+  const double* fo_c;     // -off_{i-2} / den_i, 0 for i < 2 (m)
   double t0[2], t1[2];    // boundary stencil
   double bc_inv[4];       // boundary least-squares inverse
 };

@@ -38,7 +38,7 @@ struct DescDiff {
   __device__ __forceinline__ T step(int i, T a_i) {
     T d;
     if (i == n - 1) d = zero_v<T>();
-    else if (i >= 1) d = fmas(d2, a_next, 2.0 * (double)(i + 1));
+    else if (i >= 1) d = fmas(d2, a_next, exact_double(2 * i + 2));
     else d = fmas(a_next, d2, 0.5);
     d2 = d1;
     d1 = d;
@@ -173,7 +173,7 @@ __device__ __forceinline__ void diff_par(int n, int q, A a, S store) {
       if (i < 0) break;
       T d;
       if (i == n - 1) d = zero_v<T>();
-      else if (i >= 1) d = fmas(d2, av[e], 2.0 * (double)(i + 1));
+      else if (i >= 1) d = fmas(d2, av[e], exact_double(2 * i + 2));
       else d = fmas(av[e], d2, 0.5);
       store(i, d);
       d2 = d;
@@ -263,7 +263,8 @@ __device__ __forceinline__ void pinv_fwd_par(const PinvDev& p, const FdmaRow& f,
   }
 }
 
-// from_ortho (least squares, stride-2 tridiagonal) on the parity-q chain;
+// from_ortho (least squares, stride-2 tridiagonal) on the parity-q chain, the
+// forward sweep with its factors multiplied out at set-up (BasisDev::fo_a..c);
 // `in` and `out` may be the same lane (a batch reads its inputs, including
 // p_{i+2} of its last element, before writing)
 template <class T, int PB = kPB>
@@ -272,25 +273,23 @@ __device__ __forceinline__ void from_ortho_par(const BasisDev& b, const T* p, lo
   T g2 = zero_v<T>();
   for (int i0 = q; i0 < m; i0 += 2 * PB) {
     T dv[PB];
-    double qv[PB], ov[PB];
+    double cv[PB];
 #pragma unroll
     for (int e = 0; e < PB; e++) {
       const int i = i0 + 2 * e;
       if (i < m) {
-        dv[e] = fmas(scal(p[(long long)i * ps], __ldg(b.diag + i)), p[(long long)(i + 2) * ps], __ldg(b.low2 + i));
-        qv[e] = __ldg(b.fo_dinv + i);
-        ov[e] = i >= 2 ? __ldg(b.fo_off + i - 2) : 0.0;
+        dv[e] = fmas(scal(p[(long long)i * ps], __ldg(b.fo_a + i)), p[(long long)(i + 2) * ps], __ldg(b.fo_b + i));
+        cv[e] = __ldg(b.fo_c + i);
       } else {
         dv[e] = zero_v<T>();
-        qv[e] = ov[e] = 0.0;
+        cv[e] = 0.0;
       }
     }
 #pragma unroll
     for (int e = 0; e < PB; e++) {
       const int i = i0 + 2 * e;
       if (i >= m) break;
-      T g = scal(dv[e], qv[e]);
-      if (i >= 2) g = fmas(g, g2, -ov[e] * qv[e]);
+      const T g = fmas(dv[e], g2, cv[e]);  // fo_c is 0 for i < 2
       out[(long long)i * os] = g;
       g2 = g;
     }
@@ -381,23 +380,40 @@ __global__ void __launch_bounds__(128) k_lp_box_x3(const CaseDev* __restrict__ c
 
 // projection along x from p1 (computed by the eigenbasis GEMM): p1[0][0] = 0;
 // Gp = Sx^N p1 -> s[0], E = Sx+ (Dx Sx^N p1 / s) -> s[1], Fv = Sx+ Sx^N p1 -> s[2]
-// (s arrays as mxc/nx x myc), columns j < myc; sub q: Gp and Fv on the rows
-// of parity q, E on the rows of parity 1 - q
+// (s arrays as mxc/nx x myc), columns j < myc.  sub = 2 * part + parity q:
+// part 0: Gp and Fv on the rows of parity q; part 1: E on the rows of parity
+// 1 - q, from Gp of parity q formed again from p1 (the two parts share no
+// intermediate, so they run on different threads)
 __global__ void __launch_bounds__(128) k_lp_box_x4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   LANE_PROLOGUE
-  const int j = lane, nx = c.nx, myc = c.myc, q = sub;
-  const double inv_asp = 1.0 / c.aspect;
+  const int j = lane, nx = c.nx, myc = c.myc, q = sub & 1, part = sub >> 1;
   double* p1 = static_cast<double*>(c.p1) + j;
-  if (j == 0 && q == 0) p1[0] = 0.0;
-  double* gp = static_cast<double*>(c.s[0]) + j;
-  double* e = static_cast<double*>(c.s[1]) + j;
-  double* fv = static_cast<double*>(c.s[2]) + j;
+  // p1[0][0] = 0 is stored for the later passes; within this pass it is read
+  // as zero, so no thread reads the element while it is written
+  if (j == 0 && q == 0 && part == 0) p1[0] = 0.0;
+  const bool z0 = j == 0;
+  auto gp_at = [&](int i) {  // (Sx^N p1)_i
+    const BasisDev& b = c.xp;
+    auto pv = [&](int r) { return (z0 && r == 0) ? 0.0 : p1[(long long)r * myc]; };
+    if (b.kind == 0 || b.kind == 5) return pv(i);
+    double v = 0.0;
+    if (i < b.m) v = pv(i) * b.diag[i];
+    if (i >= 2 && i - 2 < b.m) v = (i < b.m) ? fma(pv(i - 2), b.low2[i - 2], v) : pv(i - 2) * b.low2[i - 2];
+    return v;
+  };
+  if (part == 0) {
+    double* gp = static_cast<double*>(c.s[0]) + j;
+    double* fv = static_cast<double*>(c.s[2]) + j;
 #pragma unroll 4
-  for (int i = q; i < nx; i += 2) gp[(long long)i * myc] = stencil_lane<double>(c.xp, p1, myc, i);
-  diff_par<double>(nx, 1 - q, [&](int i) { return gp[(long long)i * myc]; },
-                   [&](int i, double d) { e[(long long)i * myc] = d * inv_asp; });
-  from_ortho_par<double>(c.xu, e, myc, e, myc, 1 - q);
-  from_ortho_par<double>(c.xu, gp, myc, fv, myc, q);
+    for (int i = q; i < nx; i += 2) gp[(long long)i * myc] = gp_at(i);
+    from_ortho_par<double>(c.xu, gp, myc, fv, myc, q);
+  } else {
+    const double inv_asp = 1.0 / c.aspect;
+    double* e = static_cast<double*>(c.s[1]) + j;
+    diff_par<double>(nx, 1 - q, [&](int i) { return gp_at(i); },
+                     [&](int i, double d) { e[(long long)i * myc] = d * inv_asp; });
+    from_ortho_par<double>(c.xu, e, myc, e, myc, 1 - q);
+  }
 }
 
 // rows i < nx: convection (m_cv), x stencils of the state, right-hand sides,
@@ -467,7 +483,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y2(const CaseDev* __restrict__ c
       } else if (f == 1) {  // dP/dy at k (descending derivative recurrence), buoyancy
         double g;
         if (k == ny - 1) g = 0.0;
-        else if (k >= 1) g = fmas(g2, pk[e], 2.0 * (double)(k + 1));
+        else if (k >= 1) g = fmas(g2, pk[e], exact_double(2 * k + 2));
         else g = fmas(pk[e], g2, 0.5);
         g2 = g;
         r = fnms(fmas(fnms(ov[e], g, dt), xv[e], dt), cvv[e], dt);
@@ -511,10 +527,10 @@ __global__ void __launch_bounds__(256) k_lp_box_y3(const CaseDev* __restrict__ c
     double* tt = static_cast<double*>(c.temp) + (size_t)i * myc;
     for (int k = q; k < myc; k += 2) {
       tt[k] = F[k];
-      bad |= !isfinite(F[k]);
+      bad |= !finite_v(F[k]);
     }
   } else {
-    for (int k = q; k < myc; k += 2) bad |= !isfinite(F[k]);
+    for (int k = q; k < myc; k += 2) bad |= !finite_v(F[k]);
   }
   if (f == 0) {
     double* A = static_cast<double*>(c.s[1]) + (size_t)i * ny;
@@ -587,7 +603,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y5(const CaseDev* __restrict__ c
   for (int k = q; k < myc; k += 2) {
     const double a = us[k] - d[k];
     u[k] = a;
-    bad |= !isfinite(a);
+    bad |= !finite_v(a);
   }
   if (bad) atomicOr(c.status, 1u);
 }
@@ -716,7 +732,7 @@ __global__ void __launch_bounds__(128) k_lp_per_y2(const CaseDev* __restrict__ c
 __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   ROW_PROLOGUE
   const int i = lane, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, f = sub;
-  const double dt = c.dt, inv_asp = 1.0 / c.aspect, ki = (double)i;
+  const double dt = c.dt, inv_asp = 1.0 / c.aspect, kis = (double)i * inv_asp;  // ik/s
   const void* st3[3] = {c.ux, c.uy, c.temp};
   const double2* Fo = static_cast<const double2*>(st3[f]) + (size_t)i * myc;
   const double2* To = static_cast<const double2*>(c.temp) + (size_t)i * myc;
@@ -752,12 +768,12 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
       const double2 o = ov[e], cvk = cvv[e];
       double2 r;
       if (f == 0) {
-        const double2 gx = mul_ik(pk[e], ki) * inv_asp;
+        const double2 gx = mul_ik(pk[e], kis);
         r = fnms(fnms(o, gx, dt), cvk, dt);
       } else if (f == 1) {  // dP/dy at k (descending derivative recurrence), buoyancy
         double2 g;
         if (k == ny - 1) g = c2(0.0, 0.0);
-        else if (k >= 1) g = fmas(g2, pk[e], 2.0 * (double)(k + 1));
+        else if (k >= 1) g = fmas(g2, pk[e], exact_double(2 * k + 2));
         else g = fmas(pk[e], g2, 0.5);
         g2 = g;
         r = fnms(fmas(fnms(o, g, dt), xv[e], dt), cvk, dt);
@@ -784,7 +800,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
 __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   ROW_PROLOGUE
   const int i = lane, ny = c.ny, myc = c.myc;
-  const double inv_asp = 1.0 / c.aspect, ki = (double)i;
+  const double inv_asp = 1.0 / c.aspect, kis = (double)i * inv_asp;  // ik/s
   const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
   const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
   double2* dvr = static_cast<double2*>(c.yw[0]) + (size_t)i * ny;
@@ -807,10 +823,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
       if (k < 0) break;
       double2 g;
       if (k == ny - 1) g = c2(0.0, 0.0);
-      else if (k >= 1) g = fmas(g2, vv[e], 2.0 * (double)(k + 1));
+      else if (k >= 1) g = fmas(g2, vv[e], exact_double(2 * k + 2));
       else g = fmas(vv[e], g2, 0.5);
       g2 = g;
-      const double2 d = mul_ik(ov[e], ki) * inv_asp + g;
+      const double2 d = c2(fma(-ov[e].y, kis, g.x), fma(ov[e].x, kis, g.y));  // ik/s Sy ux* + g
       dvr[k] = d;
       if (k < myc) {
         double2 v = scal(d, pv.dia[k]);
@@ -833,7 +849,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
 __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   ROW_PROLOGUE
   const int i = lane, ny = c.ny, myc = c.myc, part = sub;
-  const double inv_asp = 1.0 / c.aspect, ki = (double)i;
+  const double inv_asp = 1.0 / c.aspect, kis = (double)i * inv_asp;  // ik/s
   const double2* p1 = static_cast<const double2*>(c.p1) + (size_t)i * myc;
   bool bad = false;
   if (part == 0) {
@@ -855,7 +871,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
       for (int e = 0; e < kPB; e++) {
         const int k = k0 + 2 * e;
         if (k >= ny) break;
-        dpx[k] = mul_ik(ov[e], ki) * inv_asp;
+        dpx[k] = mul_ik(ov[e], kis);
         const double2 v = fnms(pv0[e], dv[e], c.nu);
         P[k] = fmas(v, ov[e], c.inv_dt);
       }
@@ -898,7 +914,8 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
 int lane_kernel_subs(int kernel) {
   switch (kernel) {
     case K_LP_BOX_X2: return 6;
-    case K_LP_BOX_GPX: case K_LP_BOX_X3: case K_LP_BOX_X4: return 2;
+    case K_LP_BOX_GPX: case K_LP_BOX_X3: return 2;
+    case K_LP_BOX_X4: return 4;
     case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y5: case K_LP_PER_Y2A: return 3;
     case K_LP_PER_Y2C: return 2;
     default: return 1;
