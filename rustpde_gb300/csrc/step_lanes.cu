@@ -153,6 +153,8 @@ constexpr int kPB = 8;
 // box y3 and y5 measured faster with one element at a time (0.28 / 0.31 ms per
 // ensemble step against 0.33 / 0.36 with 8 and 0.40 / 0.47 with 4)
 constexpr int kPBRow = 1;
+// complex (periodic Y2) chains: elements of two doubles each
+constexpr int kPBC = 4;
 
 // Chebyshev derivative d = D a on the indices of parity q, descending:
 // d_{n-1} = 0, d_i = 2(i+1) a_{i+1} + d_{i+2}, d_0 = a_1 + d_2 / 2; a(i)
@@ -743,11 +745,11 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
   double2* out = static_cast<double2*>(c.yw[3 + f]) + (size_t)i * ny;
   const PinvDev& pv = c.pinv_y;
   double2 r2 = c2(0.0, 0.0), r4 = c2(0.0, 0.0), g2 = c2(0.0, 0.0);
-  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPB) {
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPBC) {
     // the batch's loads first (stencil, convection, pressure, boundary terms)
-    double2 ov[kPB], cvv[kPB], pk[kPB], xv[kPB];
+    double2 ov[kPBC], cvv[kPBC], pk[kPBC], xv[kPBC];
 #pragma unroll
-    for (int e = 0; e < kPB; e++) {
+    for (int e = 0; e < kPBC; e++) {
       const int k = k0 - 2 * e;
       ov[e] = cvv[e] = pk[e] = xv[e] = c2(0.0, 0.0);
       if (k < 0) continue;
@@ -762,7 +764,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
       }
     }
 #pragma unroll
-    for (int e = 0; e < kPB; e++) {
+    for (int e = 0; e < kPBC; e++) {
       const int k = k0 - 2 * e;
       if (k < 0) break;
       const double2 o = ov[e], cvk = cvv[e];
@@ -791,8 +793,8 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
     }
   }
   const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, i);
-  fdma_fwd_par<double2>(R, out, 1, q);
-  fdma_bwd_par<double2>(R, out, 1, q);
+  fdma_fwd_par<double2, kPBC>(R, out, 1, q);
+  fdma_bwd_par<double2, kPBC>(R, out, 1, q);
 }
 
 // Y2B, sub = parity q: divergence ik/s Sy ux* + Dy Sy uy* on parity q (from
@@ -807,10 +809,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
   double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
   const PinvDev& pv = c.pinv_y;
   double2 g2 = c2(0.0, 0.0), w2 = c2(0.0, 0.0), w4 = c2(0.0, 0.0);
-  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPB) {
-    double2 ov[kPB], vv[kPB];  // Sy ux* at k, Sy uy* at k + 1
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPBC) {
+    double2 ov[kPBC], vv[kPBC];  // Sy ux* at k, Sy uy* at k + 1
 #pragma unroll
-    for (int e = 0; e < kPB; e++) {
+    for (int e = 0; e < kPBC; e++) {
       const int k = k0 - 2 * e;
       ov[e] = vv[e] = c2(0.0, 0.0);
       if (k < 0) continue;
@@ -818,7 +820,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
       if (k < ny - 1) vv[e] = stencil_lane<double2>(c.ycd, V, 1, k + 1);
     }
 #pragma unroll
-    for (int e = 0; e < kPB; e++) {
+    for (int e = 0; e < kPBC; e++) {
       const int k = k0 - 2 * e;
       if (k < 0) break;
       double2 g;
@@ -839,8 +841,8 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
     }
   }
   const FdmaRow R = fdma_row(c.pois_y, i);
-  fdma_fwd_par<double2>(R, p1, 1, q);
-  fdma_bwd_par<double2>(R, p1, 1, q);
+  fdma_fwd_par<double2, kPBC>(R, p1, 1, q);
+  fdma_bwd_par<double2, kPBC>(R, p1, 1, q);
   if (i == 0 && q == 0) p1[0] = c2(0.0, 0.0);
 }
 
@@ -856,10 +858,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     double2* dpx = static_cast<double2*>(c.yw[1]) + (size_t)i * ny;
     double2* P = static_cast<double2*>(c.p0) + (size_t)i * ny;
     const double2* dvr = static_cast<const double2*>(c.yw[0]) + (size_t)i * ny;
-    for (int k0 = q; k0 < ny; k0 += 2 * kPB) {
-      double2 ov[kPB], pv0[kPB], dv[kPB];
+    for (int k0 = q; k0 < ny; k0 += 2 * kPBC) {
+      double2 ov[kPBC], pv0[kPBC], dv[kPBC];
 #pragma unroll
-      for (int e = 0; e < kPB; e++) {
+      for (int e = 0; e < kPBC; e++) {
         const int k = k0 + 2 * e;
         ov[e] = pv0[e] = dv[e] = c2(0.0, 0.0);
         if (k >= ny) continue;
@@ -868,7 +870,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
         dv[e] = dvr[k];
       }
 #pragma unroll
-      for (int e = 0; e < kPB; e++) {
+      for (int e = 0; e < kPBC; e++) {
         const int k = k0 + 2 * e;
         if (k >= ny) break;
         dpx[k] = mul_ik(ov[e], kis);
@@ -876,7 +878,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
         P[k] = fmas(v, ov[e], c.inv_dt);
       }
     }
-    from_ortho_par<double2>(c.ycd, dpx, 1, dpx, 1, q);
+    from_ortho_par<double2, kPBC>(c.ycd, dpx, 1, dpx, 1, q);
     const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
     const double2* T = static_cast<const double2*>(c.yw[5]) + (size_t)i * ny;
     double2* ux = static_cast<double2*>(c.ux) + (size_t)i * myc;
@@ -890,9 +892,9 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     }
   } else {
     double2* dpy = static_cast<double2*>(c.yw[2]) + (size_t)i * ny;
-    diff_par<double2>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
+    diff_par<double2, kPBC>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
                       [&](int k, double2 d) { dpy[k] = d; });
-    from_ortho_par<double2>(c.ycd, dpy, 1, dpy, 1, 1 - q);
+    from_ortho_par<double2, kPBC>(c.ycd, dpy, 1, dpy, 1, 1 - q);
     const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
     double2* uy = static_cast<double2*>(c.uy) + (size_t)i * myc;
     for (int k = 1 - q; k < myc; k += 2) {
