@@ -83,7 +83,7 @@ __device__ __forceinline__ T stencil_at(const BasisDev& b, const T* c, int i) {
     return zero_v<T>();
   }
   T v = zero_v<T>();
-  if (i < m) v = scal(c[i], b.diag[i]);
+  if (i < m) v = b.unit_diag ? c[i] : scal(c[i], b.diag[i]);
   if (i >= 2 && i - 2 < m) v = (i < m) ? fmas(v, c[i - 2], b.low2[i - 2]) : scal(c[i - 2], b.low2[i - 2]);
   (void)n;
   return v;
@@ -127,7 +127,7 @@ static __device__ void from_ortho(const BasisDev& b, const T* in, int in_ld, T* 
   for (int idx = tid; idx < nl * m; idx += nth) {
     int l = dm(idx), i = idx - l * m;
     const T* p = in + l * in_ld;
-    out[l * out_ld + i] = fmas(scal(p[i], b.diag[i]), p[i + 2], b.low2[i]);
+    out[l * out_ld + i] = fmas(b.unit_diag ? p[i] : scal(p[i], b.diag[i]), p[i + 2], b.low2[i]);
   }
   __syncthreads();
   // forward g_i = (d_i - a_{i-2} g_{i-2}) / den_i, then x_j = g_j - w_j x_{j+2},
@@ -186,7 +186,7 @@ static __device__ void cheb_diff(const T* in, int in_ld, T* out, int out_ld, int
       const T* a = src + l * src_ld;
       T v;
       if (i == 0) v = a[1];
-      else if (i < n - 1) v = scal(a[i + 1], 2.0 * (double)(i + 1));
+      else if (i < n - 1) v = scal(a[i + 1], exact_double(2 * i + 2));
       else v = zero_v<T>();
       dst[l * dst_ld + i] = v;
     }

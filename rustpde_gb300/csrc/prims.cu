@@ -1,5 +1,6 @@
 // prims.cu -- generic 2-D funspace / solver operations (see prims.h).
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <stdexcept>
 
@@ -86,6 +87,7 @@ BasisDev upload_basis(Arena& a, const HostBasis& b) {
   d.n = b.n;
   d.m = b.m;
   d.diag = a.upload(b.diag);
+  d.unit_diag = !b.diag.empty() && std::all_of(b.diag.begin(), b.diag.end(), [](double v) { return v == 1.0; });
   d.low2 = a.upload(b.low2);
   d.fo_off = a.upload(b.fo_off);
   d.fo_w = a.upload(b.fo_w);

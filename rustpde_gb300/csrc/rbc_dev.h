@@ -13,7 +13,8 @@ struct BasisDev {
   int kind;   // BaseKind
   int n;      // physical / ortho length (Fourier: physical length)
   int m;      // spectral length
-  int pad_;
+  int unit_diag;          // 1 when every diag_i is 1 (the composite bases here): the
+                          // stencils skip the product, which is exact either way
   const double* diag;     // composite stencil diag (m)
   const double* low2;     // composite stencil low2 (m)
   const double* fo_off;   // from_ortho tdma off-diagonal (m-2)

@@ -663,7 +663,7 @@ __global__ void __launch_bounds__(256) k_box_y2(const CaseDev* __restrict__ case
     const BasisDev& b = *xb[f];
     double v = 0.0;
     bool has = false;
-    if (i < mxc) { v = a[(size_t)i * myc + k] * b.diag[i]; has = true; }
+    if (i < mxc) { v = b.unit_diag ? a[(size_t)i * myc + k] : a[(size_t)i * myc + k] * b.diag[i]; has = true; }
     if (i >= 2 && i - 2 < mxc) {
       double t = a[(size_t)(i - 2) * myc + k];
       v = has ? fma(t, b.low2[i - 2], v) : t * b.low2[i - 2];

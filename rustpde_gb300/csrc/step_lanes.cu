@@ -54,7 +54,7 @@ __device__ __forceinline__ T stencil_lane(const BasisDev& b, const T* c, long lo
   if (b.kind == 0 || b.kind == 5) return c[(long long)i * s];
   const int m = b.m;
   T v = zero_v<T>();
-  if (i < m) v = scal(c[(long long)i * s], b.diag[i]);
+  if (i < m) v = b.unit_diag ? c[(long long)i * s] : scal(c[(long long)i * s], b.diag[i]);
   if (i >= 2 && i - 2 < m) {
     const T t = c[(long long)(i - 2) * s];
     v = (i < m) ? fmas(v, t, b.low2[i - 2]) : scal(t, b.low2[i - 2]);
@@ -121,7 +121,7 @@ __device__ __forceinline__ void from_ortho_lane(const BasisDev& b, const T* p, l
   T g1 = zero_v<T>(), g2 = zero_v<T>();
 #pragma unroll 4
   for (int i = 0; i < m; i++) {
-    const T d = fmas(scal(p[(long long)i * ps], b.diag[i]), p[(long long)(i + 2) * ps], b.low2[i]);
+    const T d = fmas(b.unit_diag ? p[(long long)i * ps] : scal(p[(long long)i * ps], b.diag[i]), p[(long long)(i + 2) * ps], b.low2[i]);
     const double q = b.fo_dinv[i];
     T g = scal(d, q);
     if (i >= 2) g = fmas(g, g2, -b.fo_off[i - 2] * q);
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(128) k_lp_box_x4(const CaseDev* __restrict__ c
     auto pv = [&](int r) { return (z0 && r == 0) ? 0.0 : p1[(long long)r * myc]; };
     if (b.kind == 0 || b.kind == 5) return pv(i);
     double v = 0.0;
-    if (i < b.m) v = pv(i) * b.diag[i];
+    if (i < b.m) v = b.unit_diag ? pv(i) : pv(i) * b.diag[i];
     if (i >= 2 && i - 2 < b.m) v = (i < b.m) ? fma(pv(i - 2), b.low2[i - 2], v) : pv(i - 2) * b.low2[i - 2];
     return v;
   };
@@ -440,7 +440,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y2(const CaseDev* __restrict__ c
     const BasisDev& b = *xb[ff];
     double v = 0.0;
     bool has = false;
-    if (i < mxc) { v = a[(size_t)i * myc + k] * b.diag[i]; has = true; }
+    if (i < mxc) { v = b.unit_diag ? a[(size_t)i * myc + k] : a[(size_t)i * myc + k] * b.diag[i]; has = true; }
     if (i >= 2 && i - 2 < mxc) {
       const double t = a[(size_t)(i - 2) * myc + k];
       v = has ? fma(t, b.low2[i - 2], v) : t * b.low2[i - 2];
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y2(const CaseDev* __restrict__ c
   // y stencil O_k = diag_k SX_k + low2_{k-2} SX_{k-2} (CD basis)
   auto oy = [&](int ff, int k) -> double {
     double v = 0.0;
-    if (k < myc) v = sx(ff, k) * c.ycd.diag[k];
+    if (k < myc) v = c.ycd.unit_diag ? sx(ff, k) : sx(ff, k) * c.ycd.diag[k];
     if (k >= 2 && k - 2 < myc) v = (k < myc) ? fma(sx(ff, k - 2), c.ycd.low2[k - 2], v) : sx(ff, k - 2) * c.ycd.low2[k - 2];
     return v;
   };
