@@ -20,6 +20,8 @@ Workloads (--workload):
   extras              per-update device time of the solid-mask step, Diffusion2D
                       and Navier2DAdjoint beside the oracle on the host cores
                       (see run_extras).
+  profile-step        one batched ensemble step between cudaProfilerStart/Stop,
+                      for `ncu --profile-from-start off` (see run_profile_step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
@@ -250,6 +252,7 @@ def run_ensemble(args, rank, world, local):
     total_ms = max_over_ranks(total_ms, world)
     nb, launches = B.layout()
     tuning = B.tuning()
+    tuning_forms = B.tuning_forms()
     status = [c.status() for c in B.cases]
     mixed_nu = [c.eval(R.NU) for c in B.cases]
     mixed_ke = [c.eval(R.KE) for c in B.cases]
@@ -283,7 +286,8 @@ def run_ensemble(args, rank, world, local):
 
     if args.skip_plain:  # profiling runs: the batched mixed step only
         return {"metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "steps": K, "warmup": W,
-                "cases": len(params), "mode": "batched mixed only", "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
+                "cases": len(params), "mode": "batched mixed only", "autotuner_forms": tuning_forms,
+                "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
                 "launches": per_launch}
 
     # ---- plain FP64, case by case, same ensemble and initial fields
@@ -354,6 +358,7 @@ def run_ensemble(args, rank, world, local):
         "launches_ms": per_launch,
         "autotuner": [{"pass": t[0], "ms_cta_per_lane": t[1], "ms_thread_per_lane": t[2], "chosen": t[3]}
                       for t in tuning],
+        "autotuner_forms": tuning_forms,
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": NCU_DRAM_BYTES_PER_STEP.get(dom),
                      "traffic_source": "ncu dram bytes per step, profiles/launches_ensemble256_mixed.md",
@@ -729,6 +734,33 @@ def run_reference(args, rank, world):
     }
 
 
+def run_profile_step(args):
+    """The ensemble's batched mixed step for a profiler: the batch (forms from
+    the autotuner, or pinned by RBC_BATCH_FORM), W warm-up steps, then ONE step
+    between cudaProfilerStart and cudaProfilerStop, so that
+    `ncu --profile-from-start off` captures exactly the launches of one step."""
+    import rustpde_gb300 as R
+    from rustpde_gb300 import build
+    from rustpde_gb300.ensemble import draw_ensemble
+    build.build()
+    cu = Cudart()
+    cu.lib.cudaProfilerStart.argtypes = []
+    cu.lib.cudaProfilerStop.argtypes = []
+    params = draw_ensemble(args.cases, ENSEMBLE_SEED)
+    B = R.Batch(params, precision=R.PREC_MIXED)
+    for i, c in enumerate(B.cases):
+        R.standard_ic(c, seed=1000 + i)
+    B.update(args.warmup)
+    B.synchronize()
+    cu.lib.cudaProfilerStart()
+    B.update(1)
+    B.synchronize()
+    cu.lib.cudaProfilerStop()
+    nb, launches = B.layout()
+    return {"workload": "profile-step", "cases": len(params), "warmup": args.warmup, "launches_in_step": launches,
+            "autotuner_forms": B.tuning_forms(), "status_max": max(c.status() for c in B.cases)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -736,7 +768,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ensemble",
-                    choices=["ensemble", "periodic512", "serving", "precision", "extras"])
+                    choices=["ensemble", "periodic512", "serving", "precision", "extras", "profile-step"])
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
     ap.add_argument("--skip-plain", action="store_true",
@@ -758,6 +790,8 @@ def main():
         line = run_precision(args)
     elif args.workload == "extras":
         line = run_extras(args)
+    elif args.workload == "profile-step":
+        line = run_profile_step(args)
     elif args.workload == "serving":
         from rustpde_gb300 import build
         build.build()

@@ -177,7 +177,8 @@ const char* rbc_kernel_name(int kernel);
  * stream, so their state/diagnostic calls are ordered after rbc_batch_step.
  * Mixed-precision batches time the forms of each FP64 pass at creation and
  * keep the fastest (rbc_batch_tuning); the environment variable
- * RBC_BATCH_FORM=0|1|2 pins one form instead (profiling runs).  The group
+ * RBC_BATCH_FORM pins the forms instead (profiling runs): one digit 0|1|2 for
+ * every pass, or the list rbc_batch_tuning_forms returns.  The group
  * whose step takes longest runs on a high-priority branch, so its thread
  * blocks are dispatched first; RBC_BATCH_PRIORITY=0 gives every branch the
  * default priority. */
@@ -201,17 +202,23 @@ int rbc_batch_get_stream(RbcBatch* b, void** stream);
  * bytes per step (stage_bytes and stage_kernel may be NULL). */
 int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* stage_bytes, int* stage_kernel,
                            int max_stages, int* nstages);
-/* Autotuner record of a batch: for the passes that have a one-thread-per-lane
- * form beside the one-CTA-per-lane form, rbc_batch_create timed both on the
- * batch (ms per launch) and kept the faster.  *n = number of decisions; entry k
- * (if 0 <= k < *n) is written to the non-null outputs (kernel ids: see
- * rbc_kernel_name). */
 /* every launch of the batch step timed alone, in step order: kernel id
  * (rbc_kernel_name), bucket, pass id, mean ms, algorithmic bytes (may be NULL) */
 int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket, int* pass, double* ms,
                                double* bytes, int max_launches, int* nlaunches);
+/* Autotuner record of a batch: for the passes that have other forms beside
+ * the one-CTA-per-lane form, rbc_batch_create timed every form on the batch
+ * (ms per step) and kept the fastest.  *n = number of decisions; entry k (if
+ * 0 <= k < *n) is written to the non-null outputs: the CTA form's kernel and
+ * time, the fastest other form's kernel and time (kernel ids: see
+ * rbc_kernel_name). */
 int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
                      int* n);
+/* The forms kept, one digit per decision of rbc_batch_tuning, comma-separated
+ * (0: a CTA per lane, 1: 128-thread CTAs, 2: a thread per sub-lane), NUL-
+ * terminated in buf (len bytes).  Passed as RBC_BATCH_FORM it makes another
+ * batch of the same cases keep the same forms without timing them. */
+int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len);
 int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes);
 int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
 int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes);

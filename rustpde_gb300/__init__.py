@@ -142,6 +142,7 @@ _SIGNATURES = {
     "rbc_server_destroy": (_I, [_P]),
     "rbc_batch_profile_step": (_I, [_P, _I, _DP, _DP, _IP, _I, _IP]),
     "rbc_batch_tuning": (_I, [_P, _I, _IP, _IP, _DP, _DP, _IP]),
+    "rbc_batch_tuning_forms": (_I, [_P, ctypes.c_char_p, ctypes.c_size_t]),
     "rbc_batch_profile_launches": (_I, [_P, _I, _IP, _IP, _IP, _DP, _DP, _I, _IP]),
     "rbc_stage_bytes": (_I, [_P, _I, _DP]),
     "rbc_kernel_name": (ctypes.c_char_p, [_I]),
@@ -1033,6 +1034,12 @@ class Batch:
             out.append((lib().rbc_kernel_name(a.value).decode(), ta.value, tb.value,
                         "lanes" if tb.value < ta.value else "cta"))
         return out
+
+    def tuning_forms(self):
+        """The forms the autotuner kept, as the RBC_BATCH_FORM list ("2,0,...")."""
+        buf = ctypes.create_string_buffer(256)
+        _check(lib().rbc_batch_tuning_forms(self._h, buf, len(buf)))
+        return buf.value.decode()
 
     def state_bytes(self):
         n = _SZ()

@@ -1099,6 +1099,7 @@ struct RbcBatch {
   struct Tuned {
     int kernel_cta, kernel_lanes;
     float ms_cta, ms_lanes;
+    int form;  // form kept: 0 CTA per lane, 1 and 2 the other plan variants
   };
   std::vector<Tuned> tuning;          // autotuner decisions (rbc_batch_tuning)
   char* d_state = nullptr;            // every case's spectral state, contiguous
@@ -1222,11 +1223,14 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       ga[a] = passes(alts[a]);
       if (ga[a].size() != gb.size()) throw std::runtime_error("autotune: plan forms of different pass structure");
     }
-    // RBC_BATCH_FORM=0|1|2 pins the form of every pass that has it (profiling
-    // runs: a profiler's per-launch overhead distorts the timings)
-    int forced = -1;
+    // RBC_BATCH_FORM pins the forms instead (profiling runs: a profiler's
+    // per-launch overhead distorts the timings): one digit 0|1|2 for every pass
+    // that has forms, or a comma-separated list with one digit per such pass,
+    // in the order of rbc_batch_tuning
+    std::vector<int> forced_list;
     if (const char* f = std::getenv("RBC_BATCH_FORM"))
-      if (f[0] >= '0' && f[0] <= '2' && f[1] == '\0') forced = f[0] - '0';
+      for (const char* q = f; *q; q++)
+        if (*q >= '0' && *q <= '2') forced_list.push_back(*q - '0');
     StepPlan tuned;
     for (size_t pi = 0; pi < gb.size(); pi++) {
       auto group_time = [&](const StepPlan& P, const DevPlan& dp, const std::vector<size_t>& g) {
@@ -1249,9 +1253,14 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
           if (t < t_base) best = (int)a;
         }
       }
-      if (t_base >= 0) b->tuning.push_back({bk.plan.launches[gb[pi][0]].kernel, best_alt_kernel, t_base, t_best_alt});
-      if (forced == 0) best = -1;
-      else if (forced > 0 && (size_t)forced <= nalt) best = forced - 1;
+      if (t_base >= 0) {
+        int forced = -1;
+        if (forced_list.size() == 1) forced = forced_list[0];
+        else if (b->tuning.size() < forced_list.size()) forced = forced_list[b->tuning.size()];
+        if (forced == 0) best = -1;
+        else if (forced > 0 && (size_t)forced <= nalt) best = forced - 1;
+        b->tuning.push_back({bk.plan.launches[gb[pi][0]].kernel, best_alt_kernel, t_base, t_best_alt, best + 1});
+      }
       const StepPlan& src = best >= 0 ? alts[best] : bk.plan;
       for (size_t li : (best >= 0 ? ga[best][pi] : gb[pi])) tuned.launches.push_back(src.launches[li]);
     }
@@ -1385,6 +1394,19 @@ int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lane
     if (ms_cta) *ms_cta = t.ms_cta;
     if (ms_lanes) *ms_lanes = t.ms_lanes;
   }
+  API_END
+}
+
+int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len) {
+  API_BEGIN
+  require(b && buf && len > 0, "rbc_batch_tuning_forms: invalid argument");
+  std::string s;
+  for (const auto& t : b->tuning) {
+    if (!s.empty()) s += ',';
+    s += (char)('0' + t.form);
+  }
+  require(s.size() < len, "rbc_batch_tuning_forms: buffer too small");
+  std::memcpy(buf, s.c_str(), s.size() + 1);
   API_END
 }
 

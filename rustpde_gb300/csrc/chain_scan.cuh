@@ -11,7 +11,8 @@
 //   second order  (x_t, x_{t-1}) = [[a_t, c_t], [1, 0]] (x_{t-1}, x_{t-2}) + (b_t, 0)
 // phase 1 composes each thread's block of E = ceil(len / T) maps, phase 2 scans
 // the T block maps with shuffles, phase 3 replays the block from the exclusive
-// prefix.  Coefficients are real; values are double or double2.
+// prefix.  Coefficients are real; values are double or double2.  Warps with
+// no chain left skip the rounds (the CTA-wide calls often have 2 chains).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -35,8 +36,12 @@ template <> __device__ __forceinline__ double2 zero_val<double2>() { return make
 // CTA call this (uniformly); it contains no barrier.
 template <int T, class V, class LenF, class CoefF, class StoreF>
 __device__ __forceinline__ void chains1(int nch, LenF len_of, CoefF coef, StoreF store, int tid, int nth) {
+  static_assert(T <= 32 && (32 % T) == 0, "a group lies within one warp");
   const int g = tid / T, gl = tid % T, ng = nth / T;
   for (int base = 0; base < nch; base += ng) {
+    // a warp whose groups all lie past the last chain has no work here or in
+    // later rounds (its shuffles involve only itself)
+    if (base + (tid & ~31) / T >= nch) break;
     const int c = base + g;
     const bool on = c < nch;
     const int len = on ? len_of(c) : 0;
@@ -75,8 +80,10 @@ __device__ __forceinline__ void chains1(int nch, LenF len_of, CoefF coef, StoreF
 // Second-order chains: x_t = a_t x_{t-1} + c_t x_{t-2} + b_t.  coef(c, t, a, cc, b).
 template <int T, class V, class LenF, class CoefF, class StoreF>
 __device__ __forceinline__ void chains2(int nch, LenF len_of, CoefF coef, StoreF store, int tid, int nth) {
+  static_assert(T <= 32 && (32 % T) == 0, "a group lies within one warp");
   const int g = tid / T, gl = tid % T, ng = nth / T;
   for (int base = 0; base < nch; base += ng) {
+    if (base + (tid & ~31) / T >= nch) break;  // as in chains1
     const int c = base + g;
     const bool on = c < nch;
     const int len = on ? len_of(c) : 0;
