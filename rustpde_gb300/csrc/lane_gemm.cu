@@ -426,7 +426,9 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
         }
       };
       auto store_typed = [&](auto mode) {
-        if (otype == LT_F64)
+        if (otype == LT_F64 && scale == 1.0)  // no FP64 product (the conversion alone runs at the FP64 rate)
+          store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f; }, mode);
+        else if (otype == LT_F64)
           store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f * scale; },
                     mode);
         else if (scale == 1.0)
