@@ -162,10 +162,10 @@ class Cudart:
 # ensemble (the launch list in profiles/launches_ensemble256_mixed.md); the
 # roofline's `traffic` for the dominant kernel, per step like its `achieved`
 NCU_DRAM_BYTES_PER_STEP = {
-    "lane_gemm": 754e6, "lanes_periodic_y2a": 380e6, "lanes_box_y2": 251e6, "lanes_periodic_y2b": 109e6,
-    "lanes_periodic_y2c": 265e6, "lanes_box_x4": 40e6, "lanes_box_y5": 266e6, "lanes_box_y3": 181e6,
-    "lanes_box_x3": 49e6, "lanes_box_y4": 131e6, "periodic_x_mixed": 93e6, "lanes_box_x2": 116e6,
-    "box_prod_mixed": 128e6, "lanes_box_gpx": 23e6, "state_f32": 141e6,
+    "state_f32": 144e6, "lane_gemm": 738e6, "periodic_x_mixed_t128": 93e6, "lanes_periodic_y2a": 404e6,
+    "lanes_periodic_y2b": 108e6, "lanes_periodic_y2c": 260e6, "box_prod_mixed": 128e6, "lanes_box_gpx": 23e6,
+    "box_y2_pre": 237e6, "lanes_box_x2": 112e6, "lanes_box_y3": 179e6, "box_x3_mix_t128": 50e6,
+    "lanes_box_y4": 131e6, "lanes_box_x4": 45e6, "lanes_box_y5": 263e6,
 }
 
 
