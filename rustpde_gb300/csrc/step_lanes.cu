@@ -150,9 +150,11 @@ __device__ __forceinline__ int top_par(int n, int q) { return ((n - 1 - q) & 1) 
 // the compiler cannot reorder) left about 15 stall cycles per instruction.
 // The arithmetic and its order are those of the one-element-at-a-time form.
 constexpr int kPB = 8;
-// box y3 and y5 measured faster with one element at a time (0.28 / 0.31 ms per
-// ensemble step against 0.33 / 0.36 with 8 and 0.40 / 0.47 with 4)
-constexpr int kPBRow = 1;
+// box y3 and y5 (row chains, 40 registers) measured best with 2 and 1 elements
+// ahead: y3 0.23 / 0.26 / 0.35 ms per ensemble step with 2 / 1 / 4, y5 0.29 /
+// 0.30 with 1 / 4
+constexpr int kPBY3 = 2;
+constexpr int kPBY5 = 1;
 // complex (periodic Y2) chains: elements of two doubles each
 constexpr int kPBC = 4;
 
@@ -523,7 +525,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y3(const CaseDev* __restrict__ c
       xm2 = v;
     }
   }
-  fdma_bwd_par<double, kPBRow>(R, F, 1, q);
+  fdma_bwd_par<double, kPBY3>(R, F, 1, q);
   bool bad = false;
   if (f == 2) {
     double* tt = static_cast<double*>(c.temp) + (size_t)i * myc;
@@ -540,7 +542,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y3(const CaseDev* __restrict__ c
     for (int k = q; k < ny; k += 2) A[k] = stencil_lane<double>(c.ycd, F, 1, k);
   } else if (f == 1) {
     double* B = static_cast<double*>(c.s[2]) + (size_t)i * ny;
-    diff_par<double, kPBRow>(ny, 1 - q, [&](int k) { return stencil_lane<double>(c.ycd, F, 1, k); },
+    diff_par<double, kPBY3>(ny, 1 - q, [&](int k) { return stencil_lane<double>(c.ycd, F, 1, k); },
                      [&](int k, double d) { B[k] = d; });
   }
   if (bad) atomicOr(c.status, 1u);
@@ -595,10 +597,10 @@ __global__ void __launch_bounds__(256) k_lp_box_y5(const CaseDev* __restrict__ c
     for (int k = q; k < ny; k += 2) d[k] = stencil_lane<double>(c.ycn, E, 1, k);
   } else {  // Dy Sy^N Fv on parity q (from Sy^N Fv on parity 1 - q)
     const double* Fv = static_cast<const double*>(c.s[2]) + (size_t)i * myc;
-    diff_par<double, kPBRow>(ny, q, [&](int k) { return stencil_lane<double>(c.ycn, Fv, 1, k); },
+    diff_par<double, kPBY5>(ny, q, [&](int k) { return stencil_lane<double>(c.ycn, Fv, 1, k); },
                      [&](int k, double v) { d[k] = v; });
   }
-  from_ortho_par<double, kPBRow>(c.ycd, d, 1, d, 1, q);
+  from_ortho_par<double, kPBY5>(c.ycd, d, 1, d, 1, q);
   double* u = static_cast<double*>(part == 0 ? c.ux : c.uy) + (size_t)i * myc;
   const double* us = static_cast<const double*>(c.s[4 + part]) + (size_t)i * myc;
   bool bad = false;
