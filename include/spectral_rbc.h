@@ -217,7 +217,7 @@ int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lane
 /* The forms kept, one digit per decision of rbc_batch_tuning, comma-separated
  * (0: a CTA per lane, 1: 128-thread CTAs, 2: a thread per sub-lane), NUL-
  * terminated in buf (len bytes).  Passed as RBC_BATCH_FORM it makes another
- * batch of the same cases keep the same forms without timing them. */
+ * batch of the same cases keep the same forms, whatever its own timings say. */
 int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len);
 int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes);
 int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
