@@ -130,3 +130,42 @@ def test_mixed_batch_matches_single_case(R):
         for f in FIELDS:
             e = rel(b.cases[i].get(f), s.get(f))
             assert e < FORMS_TOL, (i, f, e)
+
+
+def test_mixed_batch_forms_replay(R, monkeypatch):
+    # the autotuner's forms, replayed through RBC_BATCH_FORM, rebuild the same
+    # step: bitwise the same numbers
+    b1 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
+    forms = b1.tuning_forms()
+    assert forms and all(ch in "012," for ch in forms), forms
+    monkeypatch.setenv("RBC_BATCH_FORM", forms)
+    b2 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
+    assert b2.tuning_forms() == forms
+    for b in (b1, b2):
+        for i in range(len(MIX_PARAMS)):
+            R.standard_ic(b.cases[i], seed=40 + i)
+        b.update(4)
+        b.synchronize()
+    for i in range(len(MIX_PARAMS)):
+        for f in FIELDS:
+            assert np.array_equal(b1.cases[i].get(f), b2.cases[i].get(f)), (i, f)
+
+
+def test_mixed_batch_one_call_equals_single_steps(R, monkeypatch):
+    # rbc_batch_step(n) runs the same graph n times as n calls of one step
+    # (both batches keep the same forms: the second replays the first's)
+    b0 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
+    monkeypatch.setenv("RBC_BATCH_FORM", b0.tuning_forms())
+    bs = [b0, R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)]
+    for b in bs:
+        for i in range(len(MIX_PARAMS)):
+            R.standard_ic(b.cases[i], seed=60 + i)
+    bs[0].update(3)
+    for _ in range(3):
+        bs[1].update(1)
+    for b in bs:
+        b.synchronize()
+    for i in range(len(MIX_PARAMS)):
+        assert bs[0].cases[i].get_time() == bs[1].cases[i].get_time()
+        for f in FIELDS:
+            assert np.array_equal(bs[0].cases[i].get(f), bs[1].cases[i].get(f)), (i, f)
