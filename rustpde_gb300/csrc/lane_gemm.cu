@@ -63,11 +63,6 @@ __device__ __forceinline__ const char* lane_addr(const LaneSideDev& s, int l) {
   return static_cast<const char*>(s.ptr[f]) + ((long long)r * s.lane_stride + (long long)p * s.part_stride) * es;
 }
 
-__device__ __forceinline__ float load_elem(const char* base, long long idx, int type) {
-  if (type == LT_F64) return (float)__ldg(reinterpret_cast<const double*>(base) + idx);
-  return __ldg(reinterpret_cast<const float*>(base) + idx);
-}
-
 __device__ __forceinline__ void mbar_init(uint64_t* m, int count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(m)), "r"(count));
 }
@@ -128,8 +123,9 @@ __device__ __forceinline__ void tmem_ld8_nowait(uint32_t addr, uint32_t (&r)[8])
 
 // running total += chunk partial (or = partial for the first chunk), all 8
 // warps: warp w covers tensor-memory lanes 32 (w % 4) .. + 31 and every other
-// 8-column block (from block w / 4), at most 4 blocks (NT <= 64).  All loads
-// are issued before one wait, so a flush costs one tensor-memory round trip.
+// 8-column block (from block w / 4), at most 4 blocks (NT <= 64), in two
+// halves of two blocks: each half issues its loads before one wait (two round
+// trips per flush; all four blocks at once needed registers that spilled).
 __device__ __forceinline__ void tmem_accumulate(uint32_t tmem, uint32_t part, uint32_t total, int NT, bool first,
                                                 int warp) {
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
