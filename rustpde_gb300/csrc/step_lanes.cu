@@ -155,8 +155,12 @@ constexpr int kPB = 8;
 // 0.30 with 1 / 4
 constexpr int kPBY3 = 2;
 constexpr int kPBY5 = 1;
-// complex (periodic Y2) chains: elements of two doubles each
+// complex (periodic Y2) chains, elements of two doubles each: Y2A 4 (8 took
+// 196 registers and left the launch at 1.3 waves), Y2B 6, Y2C 8, each the
+// fastest measured
 constexpr int kPBC = 4;
+constexpr int kPBCB = 6;
+constexpr int kPBCC = 8;
 
 // Chebyshev derivative d = D a on the indices of parity q, descending:
 // d_{n-1} = 0, d_i = 2(i+1) a_{i+1} + d_{i+2}, d_0 = a_1 + d_2 / 2; a(i)
@@ -811,10 +815,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
   double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
   const PinvDev& pv = c.pinv_y;
   double2 g2 = c2(0.0, 0.0), w2 = c2(0.0, 0.0), w4 = c2(0.0, 0.0);
-  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPBC) {
-    double2 ov[kPBC], vv[kPBC];  // Sy ux* at k, Sy uy* at k + 1
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPBCB) {
+    double2 ov[kPBCB], vv[kPBCB];  // Sy ux* at k, Sy uy* at k + 1
 #pragma unroll
-    for (int e = 0; e < kPBC; e++) {
+    for (int e = 0; e < kPBCB; e++) {
       const int k = k0 - 2 * e;
       ov[e] = vv[e] = c2(0.0, 0.0);
       if (k < 0) continue;
@@ -822,7 +826,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
       if (k < ny - 1) vv[e] = stencil_lane<double2>(c.ycd, V, 1, k + 1);
     }
 #pragma unroll
-    for (int e = 0; e < kPBC; e++) {
+    for (int e = 0; e < kPBCB; e++) {
       const int k = k0 - 2 * e;
       if (k < 0) break;
       double2 g;
@@ -843,8 +847,8 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
     }
   }
   const FdmaRow R = fdma_row(c.pois_y, i);
-  fdma_fwd_par<double2, kPBC>(R, p1, 1, q);
-  fdma_bwd_par<double2, kPBC>(R, p1, 1, q);
+  fdma_fwd_par<double2, kPBCB>(R, p1, 1, q);
+  fdma_bwd_par<double2, kPBCB>(R, p1, 1, q);
   if (i == 0 && q == 0) p1[0] = c2(0.0, 0.0);
 }
 
@@ -860,10 +864,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     double2* dpx = static_cast<double2*>(c.yw[1]) + (size_t)i * ny;
     double2* P = static_cast<double2*>(c.p0) + (size_t)i * ny;
     const double2* dvr = static_cast<const double2*>(c.yw[0]) + (size_t)i * ny;
-    for (int k0 = q; k0 < ny; k0 += 2 * kPBC) {
-      double2 ov[kPBC], pv0[kPBC], dv[kPBC];
+    for (int k0 = q; k0 < ny; k0 += 2 * kPBCC) {
+      double2 ov[kPBCC], pv0[kPBCC], dv[kPBCC];
 #pragma unroll
-      for (int e = 0; e < kPBC; e++) {
+      for (int e = 0; e < kPBCC; e++) {
         const int k = k0 + 2 * e;
         ov[e] = pv0[e] = dv[e] = c2(0.0, 0.0);
         if (k >= ny) continue;
@@ -872,7 +876,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
         dv[e] = dvr[k];
       }
 #pragma unroll
-      for (int e = 0; e < kPBC; e++) {
+      for (int e = 0; e < kPBCC; e++) {
         const int k = k0 + 2 * e;
         if (k >= ny) break;
         dpx[k] = mul_ik(ov[e], kis);
@@ -880,7 +884,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
         P[k] = fmas(v, ov[e], c.inv_dt);
       }
     }
-    from_ortho_par<double2, kPBC>(c.ycd, dpx, 1, dpx, 1, q);
+    from_ortho_par<double2, kPBCC>(c.ycd, dpx, 1, dpx, 1, q);
     const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
     const double2* T = static_cast<const double2*>(c.yw[5]) + (size_t)i * ny;
     double2* ux = static_cast<double2*>(c.ux) + (size_t)i * myc;
@@ -894,9 +898,9 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     }
   } else {
     double2* dpy = static_cast<double2*>(c.yw[2]) + (size_t)i * ny;
-    diff_par<double2, kPBC>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
+    diff_par<double2, kPBCC>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
                       [&](int k, double2 d) { dpy[k] = d; });
-    from_ortho_par<double2, kPBC>(c.ycd, dpy, 1, dpy, 1, 1 - q);
+    from_ortho_par<double2, kPBCC>(c.ycd, dpy, 1, dpy, 1, 1 - q);
     const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
     double2* uy = static_cast<double2*>(c.uy) + (size_t)i * myc;
     for (int k = 1 - q; k < myc; k += 2) {
