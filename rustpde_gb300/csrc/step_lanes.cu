@@ -156,7 +156,7 @@ constexpr int kPB = 8;
 constexpr int kPBY3 = 2;
 constexpr int kPBY5 = 1;
 // complex (periodic Y2) chains, elements of two doubles each: Y2A 4 (8 took
-// 196 registers and left the launch at 1.3 waves), Y2B 6, Y2C 8, each the
+// 196 registers, five 64-thread blocks per SM), Y2B 6, Y2C 8, each the
 // fastest measured
 constexpr int kPBC = 4;
 constexpr int kPBCB = 6;
