@@ -516,14 +516,26 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
       std::vector<double> hx((size_t)nx * ny), hy((size_t)nx * ny);
       cuda_check(cudaMemcpy(hx.data(), bdx, hx.size() * 8, cudaMemcpyDeviceToHost), "copy bc dx");
       cuda_check(cudaMemcpy(hy.data(), bdy, hy.size() * 8, cudaMemcpyDeviceToHost), "copy bc dy");
+      // The boundary convection term u dbc/dx + v dbc/dy splits into g0 v,
+      // with g0 the mean of dbc/dy, and the remainder u dbc/dx + v (dbc/dy - g0).
+      // The FP32 products carry only the remainder (rounding-level for the
+      // conduction profile, which is linear in y); the FP64 pass that forms the
+      // temperature right-hand side adds g0 * dealias(to_ortho(uy)), the exact
+      // forward transform of g0 v (rbc_dev.h m_bclin).
+      double g0 = 0.0;
+      for (double v : hy) g0 += v;
+      g0 /= (double)hy.size();
       std::vector<float> tx((size_t)nx * ny), ty((size_t)nx * ny);
       for (int i = 0; i < nx; i++)
         for (int j = 0; j < ny; j++) {
           tx[(size_t)j * nx + i] = (float)hx[(size_t)i * ny + j];
-          ty[(size_t)j * nx + i] = (float)hy[(size_t)i * ny + j];
+          ty[(size_t)j * nx + i] = (float)(hy[(size_t)i * ny + j] - g0);
         }
       cuda_check(cudaMemcpy(const_cast<float*>(h.m_bcx), tx.data(), tx.size() * 4, cudaMemcpyHostToDevice), "bc dx");
       cuda_check(cudaMemcpy(const_cast<float*>(h.m_bcy), ty.data(), ty.size() * 4, cudaMemcpyHostToDevice), "bc dy");
+      h.m_bclin = 1;
+      h.m_bcg = g0;
+      cuda_check(cudaMemcpy(c->d_case, &h, sizeof(CaseDev), cudaMemcpyHostToDevice), "copy case descriptor");
     }
   }
   // ---- step plan, work tables and the CUDA graph of one update()

@@ -54,6 +54,14 @@ __device__ __forceinline__ double fnms(double a, double b, double s) { return fm
 __device__ __forceinline__ double2 fnms(double2 a, double2 b, double s) { return c2(fma(-b.x, s, a.x), fma(-b.y, s, a.y)); }
 __device__ __forceinline__ double fmas(double a, double b, double s) { return fma(b, s, a); }
 __device__ __forceinline__ double2 fmas(double2 a, double2 b, double s) { return c2(fma(b.x, s, a.x), fma(b.y, s, a.y)); }
+// Temperature convection term plus the boundary-field term of a boundary
+// field linear in y (CaseDev::m_bclin): ct + g * o with o = to_ortho(uy) at
+// the same (dealiased) index.  On a Fourier axis, row 0 takes the real part of
+// o only, as the c2r -> r2c round trip of the product does.
+__device__ __forceinline__ double add_bclin(double ct, double o, double g, int) { return fma(o, g, ct); }
+__device__ __forceinline__ double2 add_bclin(double2 ct, double2 o, double g, int row) {
+  return row == 0 ? c2(fma(o.x, g, ct.x), ct.y) : c2(fma(o.x, g, ct.x), fma(o.y, g, ct.y));
+}
 // finiteness from the exponent bits (integer operations: comparisons and
 // conversions of doubles run at the FP64 rate on this GPU)
 __device__ __forceinline__ bool finite_v(double a) {

@@ -138,7 +138,15 @@ struct CaseDev {
   // mixed-precision form (precision RBC_PREC_MIXED): the dense transforms run
   // as tensor-core lane GEMMs, the convection products in FP32
   int mixed;
-  int pad_m;
+  // Mixed form: the boundary convection term's part m_bcg * uy, with m_bcg the
+  // mean of d(fieldbc)/dy, is added in FP64 by the pass that forms the
+  // temperature right-hand side, as m_bcg times the dealiased to_ortho(uy)
+  // (the exact forward transform of m_bcg * uy).  It is linear in the state
+  // and drives the convective instability; carried through the FP32 products
+  // and two tensor-core transforms, their truncation bias shifted the growth
+  // rate of near-critical cases.  m_bcy holds d(fieldbc)/dy - m_bcg.
+  int m_bclin;
+  double m_bcg;
   void* m_y[3];   // FP32 y-pass outputs [Y0 | Y1] per field, stored transposed: (2 ny) x mx
   void* m_q;      // FP32 x-transformed products, transposed: 3 x (ny x kx)
   void* m_cv;     // FP64 convection term, spectral: 3 x (kx x ky)
@@ -147,7 +155,7 @@ struct CaseDev {
   void* m_z;      // box: FP32 pinv_x of the divergence (mxc x ny), then the FP32 Poisson row solutions (mxc x myc)
   void* m_s32;    // FP32 copy of ux, uy, temp (3 x mxc x myc, interleaved re/im when periodic): the y GEMM's input
   const float* m_bcx;  // FP32 d(fieldbc)/dx, transposed: ny x nx
-  const float* m_bcy;  // FP32 d(fieldbc)/dy, transposed: ny x nx
+  const float* m_bcy;  // FP32 d(fieldbc)/dy - m_bcg, transposed: ny x nx
 };
 
 }  // namespace rbc

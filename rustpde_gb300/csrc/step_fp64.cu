@@ -270,6 +270,7 @@ __global__ void __launch_bounds__(256) k_per_y2(const CaseDev* __restrict__ case
   for (int k = tid; k < ny; k += nth) {
     double2 gx = mul_ik(P[k], ki) * inv_asp;
     double2 cu = CV[k], cvv = CV[ld + k], ct = CV[2 * ld + k];
+    if (PRE && c.m_bclin && i < kx && k < ky) ct = add_bclin(ct, O[ld + k], c.m_bcg, i);
     R[k] = fnms(fnms(O[k], gx, dt), cu, dt);
     double2 that = O[2 * ld + k] + bco[(size_t)i * ny + k];
     R[ld + k] = fnms(fmas(fnms(O[ld + k], G[k], dt), that, dt), cvv, dt);
@@ -682,7 +683,9 @@ __global__ void __launch_bounds__(256) k_box_y2(const CaseDev* __restrict__ case
     R[k] = fnms(fnms(O[k], gpx[(size_t)i * ny + k], dt), CV[k], dt);
     double that = O[2 * ld + k] + bco[(size_t)i * ny + k];
     R[ld + k] = fnms(fmas(fnms(O[ld + k], G[k], dt), that, dt), CV[ld + k], dt);
-    R[2 * ld + k] = fnms(O[2 * ld + k] + bcd[(size_t)i * ny + k], CV[2 * ld + k], dt);
+    double ct = CV[2 * ld + k];
+    if (PRE && c.m_bclin && i < kx && k < ky) ct = add_bclin(ct, O[ld + k], c.m_bcg, i);
+    R[2 * ld + k] = fnms(O[2 * ld + k] + bcd[(size_t)i * ny + k], ct, dt);
   }
   __syncthreads();
   matvec_pinv<double>(c.pinv_y, R, ld, O, ld, 3, tid, nth);

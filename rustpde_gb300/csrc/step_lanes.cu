@@ -479,6 +479,7 @@ __global__ void __launch_bounds__(256) k_lp_box_y2(const CaseDev* __restrict__ c
         xv[e] = oy(2, k) + bco[k];
       } else {
         xv[e] = bcd[k];
+        if (c.m_bclin && i < kx && k < ky) cvv[e] = add_bclin(cvv[e], oy(1, k), c.m_bcg, i);
       }
     }
 #pragma unroll
@@ -653,7 +654,8 @@ __global__ void __launch_bounds__(128) k_lp_per_y2(const CaseDev* __restrict__ c
       const bool incv = i < kx && k < ky;
       const double2 c0 = incv ? cv[((size_t)0 * kx + i) * ky + k] : c2(0.0, 0.0);
       const double2 c1 = incv ? cv[((size_t)1 * kx + i) * ky + k] : c2(0.0, 0.0);
-      const double2 cc2 = incv ? cv[((size_t)2 * kx + i) * ky + k] : c2(0.0, 0.0);
+      double2 cc2 = incv ? cv[((size_t)2 * kx + i) * ky + k] : c2(0.0, 0.0);
+      if (incv && c.m_bclin) cc2 = add_bclin(cc2, O[1], c.m_bcg, i);
       for (int f = 0; f < 3; f++)
         for (int q = 4; q > 0; q--) R[f][q] = R[f][q - 1];
       const double2 gx = mul_ik(pk, ki) * inv_asp;
@@ -744,6 +746,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
   const void* st3[3] = {c.ux, c.uy, c.temp};
   const double2* Fo = static_cast<const double2*>(st3[f]) + (size_t)i * myc;
   const double2* To = static_cast<const double2*>(c.temp) + (size_t)i * myc;
+  const double2* Uo = static_cast<const double2*>(c.uy) + (size_t)i * myc;
   const double2* P = static_cast<const double2*>(c.p0) + (size_t)i * ny;
   const double2* cv = static_cast<const double2*>(c.m_cv);
   const double2* bco = static_cast<const double2*>(c.bc_ortho) + (size_t)i * ny;
@@ -767,6 +770,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
         xv[e] = stencil_lane<double2>(c.ycd, To, 1, k) + bco[k];
       } else {
         xv[e] = bcd[k];
+        if (c.m_bclin && i < kx && k < ky) cvv[e] = add_bclin(cvv[e], stencil_lane<double2>(c.ycd, Uo, 1, k), c.m_bcg, i);
       }
     }
 #pragma unroll

@@ -25,7 +25,8 @@ namespace dev {
 // ============================================================================
 // Periodic X pass in FP32: column j of the transposed y-pass outputs.
 //  u = F^-1 Y0_ux, v = F^-1 Y0_uy;  for f: a = F^-1 (ik/s Y0_f), b = F^-1 Y1_f
-//  P_f = u a + v b (+ u dbc/dx + v dbc/dy for temp);  Q_f = F P_f, rows < kx
+//  P_f = u a + v b (+ u dbc/dx + v (dbc/dy - g0) for temp; the Y2 pass adds the
+//  g0 v part in FP64);  Q_f = F P_f, rows < kx
 // (navier.rs:538-616, conv_term.rs:22-42)
 // ============================================================================
 __global__ void __launch_bounds__(256) k_per_x_mixed(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
@@ -75,7 +76,8 @@ __global__ void __launch_bounds__(256) k_per_x_mixed(const CaseDev* __restrict__
 // ============================================================================
 // Box products in FP32 (one y index n per CTA, transposed physical arrays):
 //   P_u = u du/dx + v du/dy,  P_v = u dv/dx + v dv/dy,
-//   P_t = u dT/dx + v dT/dy + u dbc/dx + v dbc/dy          (navier.rs:538-616)
+//   P_t = u dT/dx + v dT/dy + u dbc/dx + v (dbc/dy - g0)   (navier.rs:538-616;
+//   the y2 pass adds the g0 v part in FP64)
 // m_ph: 0 [u | du/dx], 1 [v | dv/dx] (ny x 2nx), 2 du/dy, 3 dv/dy, 4 dT/dx,
 // 5 dT/dy (ny x nx).  m_p[f]: ny x nx.
 // ============================================================================

@@ -37,3 +37,33 @@ def test_mixed_ensemble_matches_fp64(R):
             worst = max(worst, e)
             assert e <= NU_KE_TOL, (i, p, what, a, ref)
     print("worst relative Nu/KE deviation:", worst)
+
+
+def test_mixed_headline_ensemble_505_steps(R):
+    """The benchmark's own ensemble (256 cases, seed 2024, initial fields seeded
+    1000 + i) after 505 steps: every case's Nusselt number and kinetic energy
+    within 1e-6 relative of FP64 (navier.rs:890-921 diagnostics).  The FP64
+    side is an FP64 batch, whose cases are bit-identical to each case stepped
+    alone (tests/test_gpu_batch.py)."""
+    from rustpde_gb300.ensemble import draw_ensemble
+    params = draw_ensemble(256, seed=2024)
+    steps = 505
+    res = {}
+    for prec in (R.PREC_MIXED, R.PREC_FP64):
+        b = R.Batch(params, precision=prec)
+        for i, c in enumerate(b.cases):
+            R.standard_ic(c, seed=1000 + i)
+        b.update(steps)
+        b.synchronize()
+        assert all(c.status() == 0 for c in b.cases)
+        res[prec] = [(c.eval(R.NU), c.eval(R.KE)) for c in b.cases]
+        del b
+    bad, worst = [], 0.0
+    for i, p in enumerate(params):
+        for (a, ref), name in zip(zip(res[R.PREC_MIXED][i], res[R.PREC_FP64][i]), ("Nu", "KE")):
+            e = abs(a - ref) / abs(ref)
+            worst = max(worst, e)
+            if e > NU_KE_TOL:
+                bad.append((i, name, e, p))
+    print("worst relative Nu/KE deviation over 256 cases:", worst)
+    assert not bad, bad
