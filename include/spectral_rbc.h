@@ -35,6 +35,7 @@ extern "C" {
 #define RBC_ERR_NUMERIC (-3)     /* non-finite value detected in the state */
 #define RBC_ERR_UNSUPPORTED (-4) /* valid request the library does not implement */
 #define RBC_ERR_NOMEM (-5)       /* device allocation failed / budget exceeded */
+#define RBC_ERR_CANCELLED (-6)   /* serving: the request was cancelled (rbc_server_cancel) */
 
 /* ---- enums -------------------------------------------------------------- */
 /* case kinds: Navier2D::new(adiabatic=true/false), Navier2D::new_periodic */
@@ -127,13 +128,20 @@ int rbc_synchronize(RbcCase* c);
 int rbc_get_time(const RbcCase* c, double* t);   /* Integrate::get_time lib.rs:139 */
 int rbc_set_time(RbcCase* c, double t);          /* Navier2D::reset_time navier.rs:951 */
 int rbc_get_dt(const RbcCase* c, double* dt);    /* Integrate::get_dt lib.rs:141 */
-/* bit 0: a non-finite value was written to the state since creation */
+/* Status word of the case (bits stay set until the case is destroyed; a
+ * batch clears its cases' words when it is created):
+ *   bit 0 (1): a non-finite value was written to the state;
+ *   bit 1 (2): RBC_PREC_MIXED only -- a tensor-core completion wait of a lane
+ *              GEMM timed out, so that step's results are incomplete (the
+ *              kernel skipped its stores and returned instead of hanging). */
 int rbc_status(RbcCase* c, int* status);
 /* Integrate::exit (navier.rs:855-862): *stop = 1 if ||div|| is NaN */
 int rbc_exit(RbcCase* c, int* stop);
 /* integrate() (lib.rs:155-187): step until max_time; call cb(case, time, user)
  * whenever time % save_intervall is within dt/2 (save_intervall <= 0: never);
- * a non-zero return of cb stops the loop.  steps_done may be NULL. */
+ * a non-zero return of cb stops the loop.  steps_done may be NULL.  Stops
+ * after MAX_TIMESTEP (1e7) steps, or when exit() holds (the divergence norm is
+ * NaN), as the reference does; returns RBC_ERR_CUDA when status bit 1 is set. */
 typedef int (*rbc_callback)(RbcCase* c, double time, void* user);
 int rbc_integrate(RbcCase* c, double max_time, double save_intervall, rbc_callback cb, void* user,
                   long* steps_done);
@@ -279,8 +287,9 @@ typedef struct RbcServerConfig {
 } RbcServerConfig;
 typedef struct RbcRequestResult {
   long long id;
-  int status;      /* RBC_OK, RBC_ERR_NUMERIC (non-finite state) or RBC_ERR_NOMEM (never fits) */
-  int steps;       /* steps advanced */
+  int status;      /* RBC_OK, RBC_ERR_NUMERIC (non-finite state), RBC_ERR_NOMEM (never fits),
+                      RBC_ERR_CUDA (status bit 1, see rbc_status) or RBC_ERR_CANCELLED */
+  int steps;       /* steps advanced (fewer than requested when cancelled) */
   double sim_time; /* simulated time reached */
   double t_submit, t_admit, t_done; /* server clock, seconds */
   double nu, ke;   /* eval_nu and kinetic energy at the horizon */
@@ -297,6 +306,14 @@ typedef struct RbcServerStats {
 int rbc_server_create(const RbcServerConfig* cfg, RbcServer** out);
 /* params->precision selects the form of the case (RBC_PREC_FP64 / RBC_PREC_MIXED) */
 int rbc_server_submit(RbcServer* s, const RbcParams* params, double horizon, uint64_t seed, long long* id);
+/* Cancel a request: *found = 1 if it had not finished.  A request still
+ * queued is answered at once; one being built, waiting for a slot or
+ * advancing stops at the scheduler's next chunk boundary (no step of it is in
+ * flight when its memory is freed).  Either way a result with status
+ * RBC_ERR_CANCELLED and the steps it advanced is queued; the other requests'
+ * numbers are unaffected.  No reference counterpart (the reference runs one
+ * case to completion). */
+int rbc_server_cancel(RbcServer* s, long long id, int* found);
 /* completed results (at most max_results, *n of them; non-blocking) */
 int rbc_server_poll(RbcServer* s, RbcRequestResult* out, int max_results, int* n);
 /* wait until nothing is pending or running (or timeout); *idle = 1 when idle */
@@ -361,7 +378,9 @@ int fs_gradient(FsSpace* s, const double* d_spec, double* d_ortho, int deriv0, i
  * space's device current.  All calls on one device share the buffer, so two
  * calls that may run at the same time (on different streams, or from
  * different threads without ordering) race on it; calls ordered on one
- * stream do not. */
+ * stream do not.  The looked-up address is kept per device ordinal for the
+ * life of the process; after cudaDeviceReset it no longer names the buffer,
+ * so do not call this entry point on a device that was reset. */
 #define FS_NOALLOC_SCRATCH_BYTES (4u * 1024u * 1024u)
 int fs_forward_noalloc(FsSpace* s, const double* d_phys, double* d_spec, void* stream);
 
@@ -387,6 +406,18 @@ int fs_lanes_shape(const FsLanes* p, int* n, int* m);
 /* coefficient c of (I - c D2) for FS_OP_HHOLTZ (HholtzAdi::new(field, [c]) along this axis) */
 int fs_lanes_set_hholtz(FsLanes* p, double c);
 int fs_lanes_apply(FsLanes* p, int op, const double* d_in, double* d_out, int lanes, void* stream);
+/* Waits for `stream`, then returns and clears the status word of the applies
+ * enqueued so far: bit 1 (2) when a tensor-core completion wait of an
+ * RBC_PREC_MIXED apply timed out (its output is incomplete); 0 otherwise. */
+int fs_lanes_status(FsLanes* p, void* stream, unsigned int* status);
+
+/* Test hook (no counterpart in the reference): the poll limit of the lane
+ * GEMM's bounded completion waits on the current device; a negative value
+ * restores the default (2^22 polls).  A limit of 0 makes every wait run out at
+ * once, so that the time-out path -- status bit 1 set, stores skipped, the
+ * MMAs in flight drained, tensor memory freed -- can be exercised without a
+ * hung GPU.  It applies to every RBC_PREC_MIXED handle on the device. */
+int rbc_set_gemm_wait_limit(long long polls);
 
 /* ---- solvers ----------------------------------------------------------------
  * Hholtz::new (src/solver/hholtz.rs:42-76), HholtzAdi::new (hholtz_adi.rs:44-63),

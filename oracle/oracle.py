@@ -281,6 +281,11 @@ class Navier2D:
     def eval(self, what):
         return lib().or_navier_eval(self._h, what)
 
+    def exit(self):
+        """Integrate::exit for Navier2D (navier.rs:855-862): the L2 norm of the
+        divergence is NaN."""
+        return bool(np.isnan(self.eval(DIVNORM)))
+
     def eval_nu(self):
         return self.eval(NU)
 
@@ -729,3 +734,32 @@ class Navier2DAdjoint:
         out = np.zeros(6)
         lib().or_adjoint_residual(self._h, _dp(out))
         return out
+
+
+MAX_TIMESTEP = 10_000_000
+
+
+def integrate(pde, dt, max_time, save_intervall=None, callback=None):
+    """integrate() (src/lib.rs:155-187) over the oracle: update, the save
+    test on time % save_intervall within dt/2 (callback(pde) there), then the
+    time limit with eps_dt = dt * 1e-4, MAX_TIMESTEP and exit().  Returns the
+    step count."""
+    timestep = 0
+    eps_dt = dt * 1e-4
+    while True:
+        pde.update(1)
+        timestep += 1
+        t = pde.time
+        if save_intervall is not None:
+            r = t % save_intervall
+            if r < dt / 2.0 or r > save_intervall - dt / 2.0:
+                if callback is not None:
+                    callback(pde)
+        if t + eps_dt >= max_time:
+            break
+        if timestep >= MAX_TIMESTEP:
+            break
+        if pde.exit():
+            break
+    return timestep
+

@@ -30,6 +30,7 @@ RBC_ERR_CUDA = -2
 RBC_ERR_NUMERIC = -3
 RBC_ERR_UNSUPPORTED = -4
 RBC_ERR_NOMEM = -5
+RBC_ERR_CANCELLED = -6
 
 BOX_ADIABATIC, BOX_CONDUCTING, PERIODIC = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
@@ -137,6 +138,7 @@ _SIGNATURES = {
     "rbc_server_create": (_I, [ctypes.POINTER(RbcServerConfig), ctypes.POINTER(_P)]),
     "rbc_server_submit": (_I, [_P, ctypes.POINTER(RbcParams), _D, ctypes.c_uint64, ctypes.POINTER(ctypes.c_longlong)]),
     "rbc_server_poll": (_I, [_P, ctypes.POINTER(RbcRequestResult), _I, _IP]),
+    "rbc_server_cancel": (_I, [_P, ctypes.c_longlong, _IP]),
     "rbc_server_wait_idle": (_I, [_P, _D, _IP]),
     "rbc_server_stats": (_I, [_P, ctypes.POINTER(RbcServerStats)]),
     "rbc_server_destroy": (_I, [_P]),
@@ -170,6 +172,8 @@ _SIGNATURES = {
     "fs_lanes_shape": (_I, [_P, _IP, _IP]),
     "fs_lanes_set_hholtz": (_I, [_P, _D]),
     "fs_lanes_apply": (_I, [_P, _I, _P, _P, _I, _P]),
+    "fs_lanes_status": (_I, [_P, _P, ctypes.POINTER(ctypes.c_uint)]),
+    "rbc_set_gemm_wait_limit": (_I, [ctypes.c_longlong]),
     "rbc_adjoint_create": (_I, [ctypes.POINTER(RbcParams), ctypes.POINTER(_P)]),
     "rbc_adjoint_destroy": (_I, [_P]),
     "rbc_adjoint_set_velocity": (_I, [_P, _D, _D, _D]),
@@ -659,6 +663,13 @@ class Lanes:
     def apply_dev(self, op, d_in, d_out, lanes, stream=None):
         _check(lib().fs_lanes_apply(self._h, int(op), d_in.ptr, d_out.ptr, int(lanes), stream))
 
+    def status(self, stream=None):
+        """Wait for `stream` and return (and clear) the status word of the
+        applies so far: bit 1 when a tensor-core completion wait timed out."""
+        v = ctypes.c_uint()
+        _check(lib().fs_lanes_status(self._h, stream, ctypes.byref(v)))
+        return v.value
+
     def apply(self, op, a):
         a = np.ascontiguousarray(a, dtype=np.float64)
         il, ol = self.lengths(op)
@@ -1082,6 +1093,13 @@ class Server:
         _check(lib().rbc_server_submit(self._h, ctypes.byref(p), float(horizon), int(seed), ctypes.byref(rid)))
         return rid.value
 
+    def cancel(self, rid):
+        """Cancel request `rid`; True if it had not finished.  Its result
+        (status RBC_ERR_CANCELLED, the steps it advanced) arrives through poll()."""
+        found = _I()
+        _check(lib().rbc_server_cancel(self._h, int(rid), ctypes.byref(found)))
+        return bool(found.value)
+
     def poll(self, max_results=1024):
         buf = (RbcRequestResult * max_results)()
         n = _I()
@@ -1116,6 +1134,13 @@ class Server:
 
 
 MAX_TIMESTEP = 10_000_000
+
+
+def set_gemm_wait_limit(polls: int):
+    """Test hook: poll limit of the lane GEMM's bounded completion waits on
+    the current device (negative: the default).  0 makes every wait time out,
+    which exercises the time-out path without a hung GPU."""
+    _check(lib().rbc_set_gemm_wait_limit(int(polls)))
 
 
 def integrate(pde, max_time: float, save_intervall=None, callback=None):

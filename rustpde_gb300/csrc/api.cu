@@ -1006,6 +1006,11 @@ int rbc_integrate(RbcCase* c, double max_time, double save_intervall, rbc_callba
     unsigned int s = 0;
     cuda_check(cudaMemcpyAsync(&s, c->hd.status, 4, cudaMemcpyDeviceToHost, c->stream), "d2h");
     c->sync();
+    if (s & kStatusGemmTimeout) {
+      if (steps_done) *steps_done = timestep;
+      throw ApiError(RBC_ERR_CUDA, "rbc_integrate: a tensor-core completion wait timed out (the step's results are "
+                                   "incomplete)");
+    }
     if (s & 1u) {
       int stop = 0;
       double d = eval_case(c, RBC_DIV_NORM);
@@ -1717,8 +1722,12 @@ void* noalloc_scratch_for_current_device() {
   void* p = g_noalloc_addr[dev].load(std::memory_order_acquire);
   if (p) return p;
   cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-  if (e != cudaSuccess || p == nullptr)
+  if (e != cudaSuccess || p == nullptr) {
+    // clear the runtime's last error: the launch check of the next call would
+    // otherwise report this failure as its own
+    (void)cudaGetLastError();
     throw ApiError(RBC_ERR_CUDA, std::string("fs_forward_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+  }
   g_noalloc_addr[dev].store(p, std::memory_order_release);
   return p;
 }
@@ -1789,6 +1798,22 @@ int fs_lanes_set_hholtz(FsLanes* p, double c) {
   require(p != nullptr, "null argument");
   require(std::isfinite(c), "fs_lanes_set_hholtz: coefficient must be finite");
   lanes_set_hholtz(p->arena, p->L, c);
+  API_END
+}
+int fs_lanes_status(FsLanes* p, void* stream, unsigned int* status) {
+  API_BEGIN
+  require(p && status, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned int v = 0;
+  cuda_check(cudaMemcpyAsync(&v, p->d_status, 4, cudaMemcpyDeviceToHost, st), "d2h");
+  cuda_check(cudaMemsetAsync(p->d_status, 0, 4, st), "clear status");
+  cuda_check(cudaStreamSynchronize(st), "synchronize");
+  *status = v;
+  API_END
+}
+int rbc_set_gemm_wait_limit(long long polls) {
+  API_BEGIN
+  cuda_check(set_gemm_wait_limit(polls), "set the lane GEMM wait limit");
   API_END
 }
 int fs_lanes_apply(FsLanes* p, int op, const double* d_in, double* d_out, int lanes, void* stream) {
@@ -2101,6 +2126,7 @@ int df_get_stream(DfCase* d, void** stream) {
 #include <condition_variable>
 #include <deque>
 #include <thread>
+#include <unordered_set>
 
 struct RbcServer {
   RbcServerConfig cfg{};
@@ -2130,11 +2156,15 @@ struct RbcServer {
     long left;
     double t_admit;
     size_t bytes;
+    bool cancelled;
   };
   std::deque<Req> pending;      // submitted, not yet taken by a set-up worker
   std::deque<Slot> ready;       // built, initial fields set, waiting for a slot
   std::vector<Slot> active;     // advancing
   std::deque<RbcRequestResult> done;
+  // ids being built by a set-up worker, and ids cancelled while building,
+  // ready or active (the thread that holds the case retires it)
+  std::unordered_set<long long> building_ids, cancelled;
   int building = 0;
   long long next_id = 0;
   size_t bytes_in_use = 0;      // building (reserved), ready and active cases
@@ -2202,6 +2232,7 @@ static void server_worker(RbcServer* S) {
         S->pending.pop_front();
         S->bytes_in_use += reserve;
         S->building++;
+        S->building_ids.insert(r.id);
       }
       std::unique_ptr<RbcCase> c(new RbcCase());
       c->p = r.p;
@@ -2231,11 +2262,13 @@ static void server_worker(RbcServer* S) {
       const size_t bytes = c->arena.bytes();
       std::lock_guard<std::mutex> lk(S->mu);
       S->building--;
+      S->building_ids.erase(r.id);
       S->bytes_in_use -= reserve;
-      if (!fits) {
+      const bool cancelled = S->cancelled.erase(r.id) > 0;
+      if (!fits || cancelled) {
         RbcRequestResult res{};
         res.id = r.id;
-        res.status = RBC_ERR_NOMEM;
+        res.status = cancelled ? RBC_ERR_CANCELLED : RBC_ERR_NOMEM;
         res.t_submit = r.t_submit;
         res.t_admit = res.t_done = S->now();
         res.grid_points = (long long)r.p.nx * r.p.ny;
@@ -2245,7 +2278,7 @@ static void server_worker(RbcServer* S) {
       } else {
         S->bytes_in_use += bytes;
         c->stream = S->stream;
-        S->ready.push_back(RbcServer::Slot{r, c.release(), r.steps, 0.0, bytes});
+        S->ready.push_back(RbcServer::Slot{r, c.release(), r.steps, 0.0, bytes, false});
       }
       S->cv.notify_all();
     }
@@ -2261,6 +2294,25 @@ static void server_worker(RbcServer* S) {
 // Move built cases into free slots.
 static void server_admit(RbcServer* S) {
   std::lock_guard<std::mutex> lk(S->mu);
+  // cases cancelled while they waited for a slot: retired without a step
+  for (size_t i = 0; i < S->ready.size();) {
+    RbcServer::Slot& sl = S->ready[i];
+    if (!S->cancelled.erase(sl.r.id)) {
+      i++;
+      continue;
+    }
+    RbcRequestResult res{};
+    res.id = sl.r.id;
+    res.status = RBC_ERR_CANCELLED;
+    res.t_submit = sl.r.t_submit;
+    res.t_admit = res.t_done = S->now();
+    res.grid_points = (long long)sl.r.p.nx * sl.r.p.ny;
+    delete sl.c;
+    S->bytes_in_use -= sl.bytes;
+    S->done.push_back(res);
+    S->completed++;
+    S->ready.erase(S->ready.begin() + i);
+  }
   while (!S->ready.empty() && (int)S->active.size() < S->cfg.max_active) {
     RbcServer::Slot sl = S->ready.front();
     S->ready.pop_front();
@@ -2340,18 +2392,25 @@ static void server_rebuild(RbcServer* S) {
 }
 
 static void server_finish(RbcServer* S) {
+  {
+    // active cases cancelled during the chunk stop here, between chunks
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (auto& sl : S->active)
+      if (S->cancelled.erase(sl.r.id)) sl.cancelled = true;
+  }
   for (int i = (int)S->active.size() - 1; i >= 0; i--) {
     RbcServer::Slot& sl = S->active[i];
-    if (sl.left > 0) continue;
+    if (sl.left > 0 && !sl.cancelled) continue;
     RbcRequestResult res{};
     res.id = sl.r.id;
-    res.steps = (int)sl.r.steps;
+    res.steps = (int)(sl.r.steps - sl.left);
     res.sim_time = sl.c->time;
     res.t_submit = sl.r.t_submit;
     res.t_admit = sl.t_admit;
     unsigned int st = 0;
     cuda_check(cudaMemcpy(&st, sl.c->hd.status, sizeof st, cudaMemcpyDeviceToHost), "status");
     res.status = st == 0 ? RBC_OK : ((st & 1u) ? RBC_ERR_NUMERIC : RBC_ERR_CUDA);
+    if (sl.cancelled) res.status = RBC_ERR_CANCELLED;
     res.nu = eval_case(sl.c, RBC_NU);
     res.ke = eval_case(sl.c, RBC_KE);
     res.t_done = S->now();
@@ -2448,6 +2507,37 @@ int rbc_server_submit(RbcServer* S, const RbcParams* p, double horizon, uint64_t
   r.steps = std::max<long>(1, std::lround(horizon / p->dt));
   S->pending.push_back(r);
   *id = r.id;
+  S->cv.notify_all();
+  API_END
+}
+
+int rbc_server_cancel(RbcServer* S, long long id, int* found) {
+  API_BEGIN
+  require(S && found, "null argument");
+  std::lock_guard<std::mutex> lk(S->mu);
+  *found = 0;
+  for (auto it = S->pending.begin(); it != S->pending.end(); ++it) {
+    if (it->id != id) continue;
+    RbcRequestResult res{};
+    res.id = id;
+    res.status = RBC_ERR_CANCELLED;
+    res.t_submit = it->t_submit;
+    res.t_admit = res.t_done = S->now();
+    res.grid_points = (long long)it->p.nx * it->p.ny;
+    S->pending.erase(it);
+    S->done.push_back(res);
+    S->completed++;
+    *found = 1;
+    S->cv.notify_all();
+    return RBC_OK;
+  }
+  bool live = S->building_ids.count(id) > 0;
+  for (auto& sl : S->ready) live = live || sl.r.id == id;
+  for (auto& sl : S->active) live = live || sl.r.id == id;
+  if (live) {
+    S->cancelled.insert(id);
+    *found = 1;
+  }
   S->cv.notify_all();
   API_END
 }

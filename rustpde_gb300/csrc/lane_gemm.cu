@@ -19,7 +19,8 @@
 //     back with tcgen05.ld, stages them through shared memory and stores them
 //     coalesced.
 // Every wait is bounded: on time-out the kernel sets kStatusGemmTimeout, skips
-// the stores, frees its tensor memory and returns.
+// the stores, drains its MMA in flight (again bounded), frees its tensor memory
+// and returns.
 #include "lane_gemm.h"
 
 #include <algorithm>
@@ -157,7 +158,12 @@ __device__ __forceinline__ void tmem_accumulate(uint32_t tmem, uint32_t part, ui
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-constexpr long kWaitLimit = 1L << 22;  // try_wait polls before a completion wait is declared lost
+constexpr long long kWaitLimit = 1LL << 22;  // try_wait polls before a completion wait is declared lost
+// The poll limit of the completion waits on this device (kWaitLimit unless a
+// test lowers it through set_gemm_wait_limit to make the time-out path run).
+// After a time-out the kernel still drains its MMA in flight with kWaitLimit
+// polls before it frees tensor memory.
+__device__ long long g_gemm_wait_limit = kWaitLimit;
 
 __device__ __forceinline__ void cp_async16(uint32_t saddr, const void* g) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
@@ -170,11 +176,11 @@ __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_g
 // __syncthreads (256 polling threads took the issue slots of the SM's other
 // CTA); the callers' tcgen05.fence::after_thread_sync orders every thread's
 // later tensor-memory and shared-memory accesses after the completion.
-__device__ __forceinline__ bool mma_wait(uint64_t* mbar, uint32_t parity) {
+__device__ __forceinline__ bool mma_wait(uint64_t* mbar, uint32_t parity, long long limit) {
   int done = 1;
   if (threadIdx.x < 32) {
     bool d = false;
-    for (long i = 0; i < kWaitLimit && !d; i++) d = mbar_try(mbar, parity);
+    for (long long i = 0; i < limit && !d; i++) d = mbar_try(mbar, parity);
     done = d ? 1 : 0;
   }
   return __syncthreads_and(done) != 0;
@@ -326,6 +332,8 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NT >> 3) << 17) | ((128u >> 4) << 24);
   const uint32_t a_lbo = (kGemmLanes / 8) * 128, w_lbo = (uint32_t)(NT / 8) * 128;
   bool ok = true;
+  const long long wait_limit = g_gemm_wait_limit;
+  uint32_t pending = 0;  // phase parity of the commit a failed wait left in flight
   const int K = J.K, kchunks = J.kchunks;
   const bool in_lf = J.in.lane_fast != 0;
   ATile<T> at;
@@ -336,7 +344,8 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   for (int c = 0; c < kchunks; c++) {
     // the A buffer and operator buffer (c+1)&1 were read by MMA c-1
     if (c > 0) {
-      ok = mma_wait(mbar, (uint32_t)((c - 1) & 1));
+      pending = (uint32_t)((c - 1) & 1);
+      ok = mma_wait(mbar, pending, wait_limit);
       tc_fence_after();
       if (!ok) break;
     }
@@ -373,7 +382,8 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
     if (c > 0) tmem_accumulate(tmem, (uint32_t)(((c - 1) & 1) * NT), total, NT, c == 1, warp);
   }
   if (ok) {
-    ok = mma_wait(mbar, (uint32_t)((kchunks - 1) & 1));
+    pending = (uint32_t)((kchunks - 1) & 1);
+    ok = mma_wait(mbar, pending, wait_limit);
     tc_fence_after();
     if (ok) {
       tmem_accumulate(tmem, (uint32_t)(((kchunks - 1) & 1) * NT), total, NT, kchunks == 1, warp);
@@ -438,8 +448,13 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
       else store_typed(std::integral_constant<int, 2>());
       __syncthreads();
     }
-  } else if (tid == 0 && J.status != nullptr) {
-    atomicOr(J.status, kStatusGemmTimeout);
+  } else {
+    if (tid == 0 && J.status != nullptr) atomicOr(J.status, kStatusGemmTimeout);
+    // the MMAs of the commit that was not seen to complete may still read
+    // shared memory and write tensor memory: wait for them (bounded) before
+    // the shared memory and the columns are given back
+    mma_wait(mbar, pending, kWaitLimit);
+    tc_fence_after();
   }
   tc_fence_before();
   __syncthreads();
@@ -552,6 +567,11 @@ cudaError_t configure_gemm_kernels() {
                            (int)gemm_smem_bytes(64));
   if (e == cudaSuccess) done = true;
   return e;
+}
+
+cudaError_t set_gemm_wait_limit(long long polls) {
+  const long long v = polls < 0 ? dev::kWaitLimit : polls;
+  return cudaMemcpyToSymbol(dev::g_gemm_wait_limit, &v, sizeof v);
 }
 
 cudaError_t launch_lane_gemm_one(const GemmJobDev& job, cudaStream_t st) {

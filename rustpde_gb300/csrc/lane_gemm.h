@@ -64,6 +64,12 @@ cudaError_t configure_gemm_kernels();
 cudaError_t launch_lane_gemm(const GemmJobDev* jobs, const int4* tiles, int ntiles_total, int max_nt,
                              cudaStream_t st);
 
+// Poll limit of the kernel's bounded completion waits on the current device
+// (negative: the default, 2^22 polls).  A small limit makes the waits run out
+// so that the time-out path (status bit, no stores, tensor memory freed) can
+// be tested; it affects every lane GEMM launched on the device afterwards.
+cudaError_t set_gemm_wait_limit(long long polls);
+
 // One job passed by value (no tables): lanes tiled in order.
 cudaError_t launch_lane_gemm_one(const GemmJobDev& job, cudaStream_t st);
 GemmJobDev make_gemm_job(const LaneSideDev& in, const LaneSideDev& out, const float* w, int K, int N, double scale,

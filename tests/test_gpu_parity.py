@@ -41,6 +41,13 @@ CASES = {
     "periodic64x33": (O.PERIODIC, 64, 33, 1e5, 1.0, 0.005, 1.0),
     "periodic512x257": (O.PERIODIC, 512, 257, 1e7, 1.0, 1e-3, 2.0),
 }
+# the ensemble's box sizes: the Poisson eigen-decompositions of 126 and 254
+# modes come from the library's own eigensolver on the GPU side and from
+# LAPACK geev (numpy) on the oracle's
+LARGE_BOX = {
+    "box128": (O.BOX_ADIABATIC, 128, 128, 1e6, 1.0, 5e-3, 1.5),
+    "box256": (O.BOX_ADIABATIC, 256, 256, 1e7, 0.7, 2e-3, 2.0),
+}
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -84,6 +91,63 @@ def test_config0_100_steps_nu_ke(R):
     for what in (O.NU, O.KE):
         a, b = g.eval(what), o.eval(what)
         assert abs(a - b) <= 1e-9 * abs(b), (what, a, b)
+
+
+def _qz_eig(a0, c0):
+    """FdmaTensor::from_matrix's decomposition by the generalized QZ route
+    (scipy.linalg.eig(a0, c0)) instead of geev on inv(c0) a0: the same
+    operator, another backward-stable algorithm."""
+    import scipy.linalg as sl
+    lam_c, evec_c = sl.eig(a0, c0)
+    lam, evec = lam_c.real.copy(), evec_c.real.copy()
+    perm = np.argsort(lam, kind="stable")[::-1]
+    lam, evec = np.ascontiguousarray(lam[perm]), np.ascontiguousarray(evec[:, perm])
+    return lam, np.ascontiguousarray(np.linalg.inv(evec) @ np.linalg.inv(c0)), evec
+
+
+@pytest.mark.parametrize("name", list(LARGE_BOX))
+def test_ten_steps_large_box(R, name):
+    """Every state field <= 1e-10 after 10 steps.  The pseudo pressure pres[1]
+    is the eigenbasis Poisson solution itself, and at 126-254 modes the
+    eigenvector matrix is ill-conditioned enough that two LAPACK-grade
+    decompositions (geev, QZ) already move it by 5e-11-9e-10; the GPU (own
+    Hessenberg + Francis QR solver) must stay within 4x of that spread,
+    measured here on the same case."""
+    o, g = pair(R, *LARGE_BOX[name])
+    orig = O.tensor_eig
+    O.tensor_eig = _qz_eig
+    try:
+        o2 = O.Navier2D(*LARGE_BOX[name][1:], LARGE_BOX[name][0])
+        O.standard_ic(o2, 1)
+    finally:
+        O.tensor_eig = orig
+    for x in (o, o2, g):
+        x.update(10)
+    spread = rel(o2.get(O.PRES1), o.get(O.PRES1))
+    for f in FIELDS:
+        e = rel(g.get(f), o.get(f))
+        tol = max(1e-10, 4.0 * spread) if f == O.PRES1 else 1e-10
+        print(name, f, "gpu vs oracle", e, "geev vs QZ", rel(o2.get(f), o.get(f)))
+        assert e < tol, (name, f, e, tol)
+    assert g.status() == 0
+
+
+def test_config1_1000_steps(R):
+    """Navier2D::new_periodic(512, 257, 1e7, 1, 1e-3, 2) after 1000 steps: per
+    field relative L2, Nu and KE against the oracle (the deviation this
+    configuration is reported with)."""
+    o, g = pair(R, *CASES["periodic512x257"])
+    o.update(1000)
+    g.update(1000)
+    errs = {f: rel(g.get(f), o.get(f)) for f in FIELDS}
+    for what in (O.NU, O.KE):
+        a, b = g.eval(what), o.eval(what)
+        errs[("eval", what)] = abs(a - b) / abs(b)
+    print("config 1 after 1000 steps, relative deviation from the oracle:", errs)
+    for f in FIELDS:
+        assert errs[f] < 1e-9, (f, errs[f])
+    for what in (O.NU, O.KE):
+        assert errs[("eval", what)] < 1e-9, (what, errs[("eval", what)])
 
 
 def test_step_is_deterministic(R):

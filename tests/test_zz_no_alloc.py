@@ -53,6 +53,10 @@ def test_noalloc_matches_fs_forward_twice(R, sp):
 
 
 def test_noalloc_allocates_nothing(R):
+    """Free device memory is unchanged across three calls.  mem_get_info
+    reports the whole device at the allocator's page granularity (2 MiB), so
+    this rules out allocations of a page or more, not smaller ones; that the
+    entry point calls no allocator at all is a property of its code."""
     s = R.Space2(R.Base(0, 512), R.Base(0, 257))
     v = np.random.default_rng(3).standard_normal(s.physical)
     d_in = R.DeviceArray.from_host(v)
@@ -64,6 +68,28 @@ def test_noalloc_allocates_nothing(R):
         s.forward_noalloc_dev(d_in, d_out)
     R._check(R.lib().rbc_device_synchronize())
     assert _mem_free() == before
+
+
+def test_noalloc_exact_limit_accepted_one_more_column_refused(R):
+    """Chebyshev 512 x 1024: the intermediate is 512 * 1024 doubles, exactly the
+    4 MiB of fixed scratch, and is accepted (bit-identical to fs_forward); one
+    more column (512 x 1025) is refused before anything is enqueued."""
+    s = R.Space2(R.Base(0, 512), R.Base(0, 1024))
+    assert s.physical[0] * s.spectral[1] * 8 == 4 * 1024 * 1024
+    v = np.random.default_rng(5).standard_normal(s.physical)
+    d_in = R.DeviceArray.from_host(v)
+    d_ref = R.DeviceArray(s.spectral, s.is_complex)
+    d_out = R.DeviceArray(s.spectral, s.is_complex)
+    s.forward_dev(d_in, d_ref)
+    s.forward_noalloc_dev(d_in, d_out)
+    R._check(R.lib().rbc_device_synchronize())
+    assert np.array_equal(d_out.to_host(), d_ref.to_host())
+    s2 = R.Space2(R.Base(0, 512), R.Base(0, 1025))
+    d_in2 = R.DeviceArray(s2.physical, False)
+    d_out2 = R.DeviceArray(s2.spectral, s2.is_complex)
+    with pytest.raises(R.RbcError) as e:
+        s2.forward_noalloc_dev(d_in2, d_out2)
+    assert e.value.code == -1
 
 
 def test_noalloc_rejects_oversized_space(R):
