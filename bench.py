@@ -157,18 +157,6 @@ class Cudart:
             self.lib.cudaEventDestroy(e)
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per ensemble step of
-# each kernel of the batched mixed step, from one ncu capture of the 256-case
-# ensemble (the launch list in profiles/launches_ensemble256_mixed.md); the
-# roofline's `traffic` for the dominant kernel, per step like its `achieved`
-NCU_DRAM_BYTES_PER_STEP = {
-    "state_f32": 144e6, "lane_gemm": 738e6, "periodic_x_mixed_t128": 93e6, "lanes_periodic_y2a": 404e6,
-    "lanes_periodic_y2b": 108e6, "lanes_periodic_y2c": 260e6, "box_prod_mixed": 128e6, "lanes_box_gpx": 23e6,
-    "box_y2_pre": 237e6, "lanes_box_x2": 112e6, "lanes_box_y3": 179e6, "box_x3_mix_t128": 50e6,
-    "lanes_box_y4": 131e6, "lanes_box_x4": 45e6, "lanes_box_y5": 263e6,
-}
-
-
 def peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -210,6 +198,74 @@ def barrier(world):
 # ---------------------------------------------------------------------------
 # ensemble workload (default)
 # ---------------------------------------------------------------------------
+def ensemble_config(params):
+    """The workload's `config`, shared by both arms (what is run, not how)."""
+    return {"workload": WORKLOAD_ENS, "cases": len(params), "grid_points": sum(p[0] * p[1] for p in params),
+            "seeds": "ensemble 2024, initial fields 1000 + case index"}
+
+
+def transform_flops(params):
+    """Useful flops per ensemble step of the dense transforms (the tensor-core
+    work): per grid-point-step 26 (nx + ny) + 4 nx for a box and 26 ny for a
+    periodic case (13 transforms of 2N flops per point, plus the two box
+    eigenbasis products)."""
+    f = 0.0
+    for nx, ny, _ra, _pr, _dt, _asp, kind in params:
+        per = 26 * ny if kind == 2 else 26 * (nx + ny) + 4 * nx
+        f += float(per) * nx * ny
+    return f
+
+
+def step_state_bytes(params):
+    """Compulsory HBM bytes per ensemble step: read and write of the spectral
+    state {ux, uy, temp, pres[1]} (composite) and pres[0] (ortho), complex for
+    periodic cases."""
+    b = 0.0
+    for nx, ny, _ra, _pr, _dt, _asp, kind in params:
+        if kind == 2:
+            sc, so, w = (nx // 2 + 1) * (ny - 2), (nx // 2 + 1) * ny, 2
+        else:
+            sc, so, w = (nx - 2) * (ny - 2), nx * ny, 1
+        b += 2 * 8 * w * (4 * sc + so)
+    return b
+
+
+def side_file(name, obj):
+    """Per-launch detail that would crowd the JSON line, next to the run's logs."""
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    with open(os.path.join(ROOT, "gpurun_out", name), "w") as f:
+        json.dump(obj, f, indent=1)
+
+
+def ensemble_accuracy(R, params, steps):
+    """Nu, KE and temperature of the batched mixed form against an FP64 batch
+    (each FP64 batch case is bit-identical to the case stepped alone) after
+    `steps` steps from the benchmark's initial fields."""
+    import numpy as np
+    out = {}
+    for prec in (R.PREC_MIXED, R.PREC_FP64):
+        b = R.Batch(params, precision=prec)
+        for i, c in enumerate(b.cases):
+            R.standard_ic(c, seed=1000 + i)
+        b.update(steps)
+        b.synchronize()
+        out[prec] = ([c.eval(R.NU) for c in b.cases], [c.eval(R.KE) for c in b.cases],
+                     [c.get(R.TEMP) for c in b.cases], [c.status() for c in b.cases])
+        del b
+    m, d = out[R.PREC_MIXED], out[R.PREC_FP64]
+    nu = np.array([abs(a - r) / abs(r) for a, r in zip(m[0], d[0])])
+    ke = np.array([abs(a - r) / abs(r) for a, r in zip(m[1], d[1])])
+    tl = np.array([np.linalg.norm(a - r) / np.linalg.norm(r) for a, r in zip(m[2], d[2])])
+    w = int(np.argmax(np.maximum(nu, ke)))
+    return {"steps": steps, "against": "FP64 batch (= each case alone in FP64, <= 1e-9 of the oracle)",
+            "nu_max_rel": float(nu.max()), "ke_max_rel": float(ke.max()), "temp_l2_max_rel": float(tl.max()),
+            "nu_median_rel": float(np.median(nu)), "ke_median_rel": float(np.median(ke)),
+            "status_nonzero": int(sum(1 for s in m[3] + d[3] if s)),
+            "worst_case": {"case": w, "params": [round(x, 6) if isinstance(x, float) else x for x in params[w]],
+                           "nu_rel": float(nu[w]), "ke_rel": float(ke[w])},
+            "cases_nu_ke_within_1e-6": int(np.sum((nu <= 1e-6) & (ke <= 1e-6)))}
+
+
 def run_ensemble(args, rank, world, local):
     import numpy as np
 
@@ -236,8 +292,7 @@ def run_ensemble(args, rank, world, local):
     clocks = ClockSampler(local)
     clocks.start()
     # K steps in one rbc_batch_step call, as a user advances the ensemble, L2
-    # flushed once before (as for the plain FP64 arm below); the groups' graph
-    # branches run their steps independently within the call
+    # flushed once before (the state, 221 MB, and each step's scratch exceed L2)
     t_wall = time.perf_counter()
     e0, e1 = cu.event(), cu.event()
     cu.memset(flush.ptr, 0x5A, flush.nbytes, stream)
@@ -251,25 +306,42 @@ def run_ensemble(args, rank, world, local):
     barrier(world)
     total_ms = max_over_ranks(total_ms, world)
     nb, launches = B.layout()
-    tuning = B.tuning()
-    tuning_forms = B.tuning_forms()
-    status = [c.status() for c in B.cases]
-    mixed_nu = [c.eval(R.NU) for c in B.cases]
-    mixed_ke = [c.eval(R.KE) for c in B.cases]
-    mixed_temp = [c.get(R.TEMP) for c in B.cases]
-    # K more steps, one call each, L2 flushed before every step (reported beside)
+    status_bad = int(sum(1 for c in B.cases if c.status()))
+    # the same K steps, one call each with L2 flushed before every step
     flushed_ms = max_over_ranks(timed_steps(cu, stream, K, lambda: B.update(1), flush), world)
     value = gp * K / (total_ms * 1e-3) * world
 
-    # ---- per-kernel profile of the batched step (each launch alone) and roofline
+    # ---- every launch of the step timed alone: the dominant kernel's roofline
     prof = B.profile_step(3)
     per_launch = [{"bucket": b_, "pass": p_, "kernel": k_, "ms": round(m_, 4), "bytes": b2_}
                   for b_, p_, k_, m_, b2_ in B.profile_launches(3)]
+    tuning = [{"pass": t[0], "ms_cta_per_lane": t[1], "ms_thread_per_lane": t[2], "chosen": t[3]}
+              for t in B.tuning()]
+    forms = B.tuning_forms()
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_bytes = prof[dom]
     pk, pk_src = peaks()
     hbm = pk.get("hbm_gbs", 6800.0)
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    step_bytes = step_state_bytes(params)
+    if dom == "lane_gemm":
+        # the tensor-core kernel: useful transform flops over its time, against
+        # the TF32 dense rate (half the measured bf16 rate)
+        tf32 = pk.get("bf16_tflops", 1900.0) / 2.0
+        flops = transform_flops(params)
+        achieved = flops / (dom_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": tf32, "unit": "TFLOP/s",
+                "frac": achieved / tf32, "traffic": None, "flops_per_step": flops,
+                "ms_per_step": dom_ms, "launches_per_step": sum(1 for x in per_launch if x["kernel"] == dom),
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops / 2 (TF32 dense rate), " + pk_src,
+                "hbm_view": {"algorithmic_bytes": dom_bytes, "gbs": dom_bytes / (dom_ms * 1e-3) / 1e9}}
+    else:
+        achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": None, "algorithmic_bytes_per_step": dom_bytes,
+                "ms_per_step": dom_ms, "peak_source": pk_src}
+    roof["traffic_note"] = "not measured in this run (no profiler in the timed process); ncu DRAM bytes in profiles/"
+    roof["step_hbm"] = {"bytes": step_bytes, "gbs": step_bytes / (total_ms / K * 1e-3) / 1e9,
+                        "frac": step_bytes / (total_ms / K * 1e-3) / 1e9 / hbm}
 
     # ---- end to end through the public API (whole ensemble state in and out every step)
     nbytes = B.state_bytes()
@@ -283,17 +355,22 @@ def run_ensemble(args, rank, world, local):
         B.get_state_all(host.array)
     e2e_s = time.perf_counter() - t0
     del B
+    side_file("bench_ensemble_detail.json", {"launches_ms": per_launch, "autotuner": tuning, "forms": forms,
+                                              "kernels_ms_per_step": {k: v[0] for k, v in prof.items()}})
 
+    line = {
+        "metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 state/solves, tf32x3 tensor-core transforms, f32 products",
+        "data": "synthetic seeded ensemble and fields",
+        "config": ensemble_config(params),
+    }
     if args.skip_plain:  # profiling runs: the batched mixed step only
-        return {"metric": METRIC, "value": value, "unit": "grid-pt-steps/s", "steps": K, "warmup": W,
-                "cases": len(params), "mode": "batched mixed only", "autotuner_forms": tuning_forms,
-                "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
-                "launches": per_launch}
+        line.update({"autotuner_forms": forms, "kernels_ms_per_step": {k: v[0] for k, v in prof.items()}})
+        return line
 
     # ---- plain FP64, case by case, same ensemble and initial fields
     plain_ms = 0.0
-    err_nu, err_ke, err_t, ke_ref = [], [], [], []
-    t_plain = time.perf_counter()
     for i, p in enumerate(params):
         nav = R.Navier2D(*p, precision=R.PREC_FP64, seed=None)
         R.standard_ic(nav, seed=1000 + i)
@@ -306,101 +383,64 @@ def run_ensemble(args, rank, world, local):
         cu.record(e1, st)
         plain_ms += cu.elapsed(e0, e1)
         cu.destroy(e0, e1)
-        for lst, what, ref in ((err_nu, R.NU, mixed_nu[i]), (err_ke, R.KE, mixed_ke[i])):
-            v = nav.eval(what)
-            lst.append(abs(ref - v) / max(abs(v), 1e-300))
-        ke_ref.append(nav.eval(R.KE))
-        t64 = nav.get(R.TEMP)
-        err_t.append(float(np.linalg.norm(mixed_temp[i] - t64) / max(np.linalg.norm(t64), 1e-300)))
         del nav
-    t_plain = time.perf_counter() - t_plain
     plain_value = gp * K / (plain_ms * 1e-3) * world
-    err_nu, err_ke, err_t = np.array(err_nu), np.array(err_ke), np.array(err_t)
 
-    line = {
-        "metric": METRIC,
-        "value": value,
-        "unit": "grid-pt-steps/s",
-        "n_gpus": world,
-        "steps": K,
-        "warmup": W,
-        "ms_per_step": total_ms / K,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f64 state and solves, tf32x3 tensor-core transforms, f32 products",
-        "data": "synthetic: seeded ensemble draw; set_velocity(0.2,1,1) + splitmix64 temperature noise 1e-3 per case",
-        "config": {"workload": WORKLOAD_ENS, "cases": len(params), "grid_points": gp, "precision": "mixed",
-                   "buckets": nb, "launches_per_step": launches, "parallelism": f"replicas{world}",
-                   "l2": "flushed once before the K timed steps (256 MiB memset outside the events); the "
-                         "ensemble state (221 MB) and each step's scratch exceed L2",
-                   "one_call_per_step_l2_flushed": {"value": gp * K / (flushed_ms * 1e-3) * world,
-                                                    "ms_per_step": flushed_ms / K},
-                   "setup_s": t_setup, "wall_s_timed_region": t_wall},
-        "plain_fp64": {"value": plain_value, "unit": "grid-pt-steps/s", "ms_per_ensemble_step": plain_ms / K,
-                       "how": "each case alone through rbc_step (its own CUDA graph), K steps between CUDA events, "
-                              "cases one after another; L2 flushed before each case", "wall_s": t_plain},
-        "speedup_vs_plain_fp64": value / plain_value,
-        "mixed_error": {"steps": W + K, "nu_max_rel": float(err_nu.max()), "nu_median_rel": float(np.median(err_nu)),
-                        "ke_max_rel": float(err_ke.max()), "ke_median_rel": float(np.median(err_ke)),
-                        "temp_l2_max_rel": float(err_t.max()), "temp_l2_median_rel": float(np.median(err_t)),
-                        "cases_nu_ke_within_1e-6": int(np.sum((err_nu <= 1e-6) & (err_ke <= 1e-6))),
-                        "worst_ke_cases": [{"case": int(i), "params": list(params[i]), "ke_rel": float(err_ke[i]),
-                                            "nu_rel": float(err_nu[i]), "ke": float(ke_ref[i]),
-                                            "temp_l2_rel": float(err_t[i])}
-                                           for i in np.argsort(err_ke)[::-1][:5]],
-                        "against": "the plain FP64 GPU path (parity with the FP64 oracle <= 1e-9)"},
+    line.update({
+        "gpu_launches": K * launches,
         "e2e": {"value": gp * Ke / e2e_s * world, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes, "steps": Ke,
-                "how": "per step: rbc_batch_set_state_all (pinned h2d), rbc_batch_step(1), rbc_batch_get_state_all"},
-        "gpu_launches": K * launches,
-        "kernels_ms_per_step": {k: v[0] for k, v in prof.items()},
-        "launches_ms": per_launch,
-        "autotuner": [{"pass": t[0], "ms_cta_per_lane": t[1], "ms_thread_per_lane": t[2], "chosen": t[3]}
-                      for t in tuning],
-        "autotuner_forms": tuning_forms,
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": NCU_DRAM_BYTES_PER_STEP.get(dom),
-                     "traffic_source": "ncu dram bytes per step, profiles/launches_ensemble256_mixed.md",
-                     "algorithmic_bytes_per_step": dom_bytes,
-                     "peak_source": pk_src},
+                "how": "per step: rbc_batch_set_state_all (pinned), rbc_batch_step(1), rbc_batch_get_state_all"},
+        "roofline": roof,
         "clocks": clk,
-        "status_nonzero_cases": int(sum(1 for s in status if s)),
-    }
+        "timing": {"l2": "flushed before the timed call (256 MiB memset outside the events); state 221 MB > L2",
+                   "one_call_per_step_l2_flushed": gp * K / (flushed_ms * 1e-3) * world,
+                   "setup_s": round(t_setup, 3), "wall_s_timed_region": round(t_wall, 4), "buckets": nb,
+                   "launches_per_step": launches, "status_nonzero_cases": status_bad},
+    })
     if rank == 0 and world == 1:
         line["serving"] = run_serving(args, args.requests, args.horizon_scale)
-        line["cpu_baseline"] = cpu_baseline_ensemble(params, budget_s=args.cpu_budget)
+        line["cpu_baseline"] = cpu_baseline_ensemble(params, steps=args.cpu_steps)
+    line["plain_fp64"] = {"value": plain_value, "ms_per_ensemble_step": plain_ms / K,
+                          "how": "each case alone through rbc_step, cases one after another"}
+    line["speedup_vs_plain_fp64"] = value / plain_value
+    line["mixed_error"] = ensemble_accuracy(R, params, args.accuracy_steps)
     return line
 
 
-def cpu_baseline_ensemble(params, budget_s=15.0, steps_per_case=2):
-    """The oracle (CPU restatement of the reference algorithm, OpenMP over
-    lanes, all host threads) on the leading cases of the same ensemble."""
+def cpu_ensemble_sample(O, params, steps, warmup):
+    """The oracle on every case of the ensemble: `warmup` untimed steps, then
+    `steps` timed ensemble steps (each advances every case once).  The one CPU
+    sample of the ensemble, used by cpu_baseline and by the reference arm."""
+    objs = []
+    for i, p in enumerate(params):
+        nx, ny, ra, pr, dt, asp, kind = p
+        o = O.Navier2D(nx, ny, ra, pr, dt, asp, kind)
+        O.standard_ic(o, 1000 + i)
+        o.update(max(warmup, 0))
+        objs.append((o, nx * ny))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for o, _g in objs:
+            o.update(1)
+    secs = time.perf_counter() - t0
+    gp = sum(g for _, g in objs)
+    return gp * steps / secs, secs
+
+
+def cpu_baseline_ensemble(params, steps=3):
     from oracle import oracle as O
     O.build()
     O.set_threads(os.cpu_count() or 1)
-    done_gp, t_acc, ncase = 0, 0.0, 0
-    for p in params:
-        nx, ny, ra, pr, dt, asp, kind = p
-        o = O.Navier2D(nx, ny, ra, pr, dt, asp, kind)
-        O.standard_ic(o, 1)
-        o.update(1)
-        t0 = time.perf_counter()
-        o.update(steps_per_case)
-        t_acc += time.perf_counter() - t0
-        done_gp += nx * ny * steps_per_case
-        ncase += 1
-        if t_acc > budget_s:
-            break
-    return {"value": done_gp / t_acc, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
-            "sample": f"first {ncase} ensemble cases x {steps_per_case} steps after 1 warm-up step each "
-                      f"({t_acc:.1f} s timed)"}
+    v, secs = cpu_ensemble_sample(O, params, steps, 1)
+    return {"value": v, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"all {len(params)} cases x {steps} ensemble steps after 1 warm-up step ({secs:.1f} s)"}
 
 
 # ---------------------------------------------------------------------------
 # serving: Poisson arrivals of solve requests, continuous batching
 # ---------------------------------------------------------------------------
-def run_serving(args, n_requests, horizon_scale, n_check=12):
+def run_serving(args, n_requests, horizon_scale, n_check=8):
     """Requests of rustpde_gb300.ensemble.draw_requests (50/s, seed 7, 5 %
     512x257) with horizons scaled by `horizon_scale`, submitted at their
     arrival times to the serving loop (mixed precision, 150 GB budget).
@@ -446,13 +486,10 @@ def run_serving(args, n_requests, horizon_scale, n_check=12):
         "failed": int(sum(1 for r in res if r["status"] != 0)),
         "p50_latency_s": float(np.percentile(lat, 50)), "p99_latency_s": float(np.percentile(lat, 99)),
         "p50_queue_and_setup_s": float(np.percentile(setup, 50)),
-        "aggregate_grid_pt_steps_per_s": gp_steps / span, "span_s": span,
-        "steps_launched": st["steps_launched"], "graph_rebuilds": st["rebuilds"],
+        "aggregate_grid_pt_steps_per_s": gp_steps / span, "span_s": round(span, 2),
+        "graph_rebuilds": st["rebuilds"], "peak_device_gb": round(st["peak_bytes_in_use"] / 1e9, 2),
         "nu_max_rel_vs_fp64": float(max(errs_nu)), "ke_max_rel_vs_fp64": float(max(errs_ke)),
-        "checked": len(errs_nu),
-        "workload": (f"{n_requests} requests, Poisson 50/s (seed 7), sizes as the ensemble + 512x257 at 5 %, "
-                     f"horizon U[1,20] time units x {horizon_scale} (scaled so the run fits in minutes), "
-                     "mixed precision, 150 GB budget, max 256 active, 8 steps per round"),
+        "checked": len(errs_nu), "horizon_scale": horizon_scale,
     }
 
 
@@ -686,51 +723,34 @@ def run_reference(args, rank, world):
     from oracle import oracle as O
     O.build()
     O.set_threads(os.cpu_count() or 1)
-    budget = 90.0
     if args.workload == "periodic512":
-        cases = [(NX, NY, RA, PR, DT, ASPECT, O.PERIODIC)]
+        o = O.Navier2D(NX, NY, RA, PR, DT, ASPECT, O.PERIODIC)
+        O.standard_ic(o, 1)
+        o.update(args.warmup)
+        K = max(1, args.steps)
+        t0 = time.perf_counter()
+        o.update(K)
+        secs = time.perf_counter() - t0
+        v = NX * NY * K / secs
         config = {"workload": WORKLOAD_512, "nx": NX, "ny": NY}
+        sample = f"{K} steps after {args.warmup} warm-up steps"
     else:
         from rustpde_gb300.ensemble import draw_ensemble
-        cases = draw_ensemble(args.cases, ENSEMBLE_SEED)
-        config = {"workload": WORKLOAD_ENS.replace("batched mixed precision", "case by case, FP64"),
-                  "cases": len(cases)}
-    # one timed "step" advances every sampled case once; the sample is the
-    # leading cases of the workload that fit the time budget
-    objs, per_case = [], []
-    for p in cases:
-        nx, ny, ra, pr, dt, asp, kind = p
-        o = O.Navier2D(nx, ny, ra, pr, dt, asp, kind)
-        O.standard_ic(o, 1)
-        t0 = time.perf_counter()
-        o.update(1)
-        per_case.append(time.perf_counter() - t0)
-        objs.append((o, nx * ny))
-        if sum(per_case) * max(args.steps, 1) > budget:
-            break
-    warm = min(args.warmup, 2)
-    for o, _ in objs:
-        o.update(warm)
-    K = max(1, args.steps)
-    t0 = time.perf_counter()
-    done = 0
-    for _ in range(K):
-        for o, _g in objs:
-            o.update(1)
-        done += 1
-        if time.perf_counter() - t0 > budget:
-            break
-    dt_s = time.perf_counter() - t0
-    gp = sum(g for _, g in objs)
-    v = gp * done / dt_s
+        params = draw_ensemble(args.cases, ENSEMBLE_SEED)
+        K = max(1, args.steps)
+        v, secs = cpu_ensemble_sample(O, params, K, args.warmup)
+        config = ensemble_config(params)
+        sample = f"all {len(params)} cases x {K} ensemble steps after {args.warmup} warm-up steps"
     return {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "grid-pt-steps/s", "n_gpus": world,
-        "steps": done, "warmup": warm, "ms_per_step": dt_s / done * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded fields", "config": config,
+        "steps": K, "warmup": args.warmup, "ms_per_step": secs / K * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic seeded ensemble and fields",
+        "config": config,
         "cpu_baseline": {"value": v, "unit": "grid-pt-steps/s", "cores": O.num_threads(), "kind": "port",
-                         "sample": f"{len(objs)} of {len(cases)} cases, {done} steps each (bounded to ~{budget:.0f} s)"},
+                         "sample": sample},
         "e2e": {"value": v, "unit": "grid-pt-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "reference is Rust (no toolchain here or on the box); timed: the C++ restatement in oracle/",
+        "note": "the reference is Rust (no toolchain here or on the box): the C++ restatement in oracle/, "
+                "FP64 case by case on all host threads",
     }
 
 
@@ -769,12 +789,15 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ensemble",
                     choices=["ensemble", "periodic512", "serving", "precision", "extras", "profile-step"])
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="periodic512: oracle seconds")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="ensemble: oracle ensemble steps in cpu_baseline")
+    ap.add_argument("--accuracy-steps", type=int, default=505,
+                    help="ensemble: steps of the mixed-vs-FP64 comparison (the configuration's horizon)")
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
     ap.add_argument("--skip-plain", action="store_true",
                     help="time the batched mixed step only (profiling runs; prints a reduced line)")
-    ap.add_argument("--requests", type=int, default=300, help="serving: number of requests")
-    ap.add_argument("--horizon-scale", type=float, default=0.01, help="serving: horizon multiplier")
+    ap.add_argument("--requests", type=int, default=100, help="serving: number of requests")
+    ap.add_argument("--horizon-scale", type=float, default=0.1, help="serving: horizon multiplier")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 500 if args.workload == "ensemble" else 200

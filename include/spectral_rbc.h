@@ -302,6 +302,8 @@ typedef struct RbcServerStats {
   size_t bytes_in_use;
   double grid_point_steps; /* advanced so far */
   long long steps_launched, rebuilds;
+  size_t peak_bytes_in_use; /* largest bytes_in_use so far (never above the budget but for a
+                               single case admitted alone) */
 } RbcServerStats;
 int rbc_server_create(const RbcServerConfig* cfg, RbcServer** out);
 /* params->precision selects the form of the case (RBC_PREC_FP64 / RBC_PREC_MIXED) */

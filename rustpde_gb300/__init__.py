@@ -80,7 +80,7 @@ class RbcServerStats(ctypes.Structure):
     _fields_ = [("now", ctypes.c_double), ("pending", ctypes.c_int), ("active", ctypes.c_int),
                 ("completed", ctypes.c_longlong), ("bytes_in_use", ctypes.c_size_t),
                 ("grid_point_steps", ctypes.c_double), ("steps_launched", ctypes.c_longlong),
-                ("rebuilds", ctypes.c_longlong)]
+                ("rebuilds", ctypes.c_longlong), ("peak_bytes_in_use", ctypes.c_size_t)]
 
 
 _SIGNATURES = {

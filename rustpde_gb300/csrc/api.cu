@@ -2168,6 +2168,7 @@ struct RbcServer {
   int building = 0;
   long long next_id = 0;
   size_t bytes_in_use = 0;      // building (reserved), ready and active cases
+  size_t peak_bytes = 0;        // largest bytes_in_use so far
   double gp_steps = 0;
   long long steps_launched = 0, rebuilds = 0, completed = 0;
   std::chrono::steady_clock::time_point t0;
@@ -2231,6 +2232,7 @@ static void server_worker(RbcServer* S) {
         r = S->pending.front();
         S->pending.pop_front();
         S->bytes_in_use += reserve;
+        S->peak_bytes = std::max(S->peak_bytes, S->bytes_in_use);
         S->building++;
         S->building_ids.insert(r.id);
       }
@@ -2277,6 +2279,7 @@ static void server_worker(RbcServer* S) {
         c.reset();
       } else {
         S->bytes_in_use += bytes;
+        S->peak_bytes = std::max(S->peak_bytes, S->bytes_in_use);
         c->stream = S->stream;
         S->ready.push_back(RbcServer::Slot{r, c.release(), r.steps, 0.0, bytes, false});
       }
@@ -2579,6 +2582,7 @@ int rbc_server_stats(RbcServer* S, RbcServerStats* st) {
   st->grid_point_steps = S->gp_steps;
   st->steps_launched = S->steps_launched;
   st->rebuilds = S->rebuilds;
+  st->peak_bytes_in_use = S->peak_bytes;
   API_END
 }
 

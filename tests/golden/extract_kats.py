@@ -6,7 +6,7 @@ parsed from the reference source at the cited file:line and stored verbatim.
 The inputs of each test are rebuilt in tests/test_oracle_kats.py from the same
 test code (cited there).  Run from the repository root:
 
-    python tests/golden/extract_kats.py [/path/to/rustpde]
+    python tests/golden/extract_kats.py /path/to/rustpde
 """
 from __future__ import annotations
 
@@ -104,6 +104,8 @@ def main(ref_root: str, out_path: str):
 
 
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/extract_kats.py /path/to/rustpde")
+    root = sys.argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     main(root, os.path.join(here, "reference_kats.json"))

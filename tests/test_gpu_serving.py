@@ -78,3 +78,24 @@ def test_budget_rejection(R):
     out = srv.poll()
     srv.close()
     assert len(out) == 1 and out[0]["id"] == rid and out[0]["status"] == -5
+
+
+def test_admission_under_memory_pressure(R):
+    """A budget of about two cases' worth: every request still completes, the
+    device bytes held by the loop (reservations of cases being built, built
+    and active cases) never exceed the budget, and each result equals the
+    request served alone with a large budget."""
+    budget = 24 * 10**6
+    reqs = [((64, 64, 1e5, 1.0, 0.02, 1.0, 0), 0.1, 40 + k) for k in range(5)]
+    srv = R.Server(hbm_budget_bytes=budget, max_active=8, chunk_steps=4)
+    ids = [srv.submit(p, h, seed) for p, h, seed in reqs]
+    assert srv.wait_idle(120.0)
+    res = {r["id"]: r for r in srv.poll()}
+    st = srv.stats()
+    srv.close()
+    assert 0 < st["peak_bytes_in_use"] <= budget
+    for k, rid in enumerate(ids):
+        r = res[rid]
+        assert r["status"] == 0 and r["steps"] == 5
+        alone, _ = serve(R, [reqs[k]])
+        assert alone[0]["nu"] == r["nu"] and alone[0]["ke"] == r["ke"]
