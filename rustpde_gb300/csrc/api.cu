@@ -726,7 +726,7 @@ static void validate_params(const RbcParams& p) {
   require(p.ra > 0 && p.pr > 0 && p.dt > 0 && p.aspect > 0, "rbc_create: ra, pr, dt, aspect must be positive");
   require(p.ny >= 8 && p.ny <= 4097, "rbc_create: ny must be in [8, 4097]");
   if (p.kind == RBC_PERIODIC)
-    require(p.nx >= 8 && p.nx <= 8192 && is_pow2(p.nx), "rbc_create: periodic nx must be a power of two in [8, 8192]");
+    require(p.nx >= 8 && p.nx <= 8192, "rbc_create: periodic nx must be in [8, 8192]");
   else require(p.nx >= 8 && p.nx <= 4097, "rbc_create: nx must be in [8, 4097]");
   require(p.precision == RBC_PREC_FP64 || p.precision == RBC_PREC_MIXED, "rbc_create: unknown precision");
 
@@ -1646,7 +1646,6 @@ int fs_space_create(int base0, int n0, int base1, int n1, FsSpace** out) {
   *out = nullptr;
   require(base0 >= 0 && base0 <= 5 && base1 >= 0 && base1 <= 4, "fs_space_create: unknown base (Fourier along axis 0 only)");
   require(n0 >= 4 && n1 >= 4 && n0 <= 8192 && n1 <= 8192, "fs_space_create: sizes must be in [4, 8192]");
-  if (base0 == FS_FOURIER_R2C) require(is_pow2(n0), "fs_space_create: Fourier length must be a power of two");
   cuda_check(configure_prim_kernels(), "configure kernels");
   std::unique_ptr<FsSpace> s(new FsSpace());
   build_space(s->arena, s->s, base0, n0, base1, n1);
@@ -1932,7 +1931,6 @@ int df_create(int base0, int n0, int base1, int n1, double kappa, double dt, DfC
   *out = nullptr;
   require(base0 >= 0 && base0 <= 5 && base1 >= 0 && base1 <= 4, "df_create: unknown base (Fourier along axis 0 only)");
   require(n0 >= 6 && n1 >= 6 && n0 <= 8192 && n1 <= 8192, "df_create: sizes must be in [6, 8192]");
-  if (base0 == FS_FOURIER_R2C) require(is_pow2(n0), "df_create: Fourier length must be a power of two");
   require(kappa > 0 && dt > 0, "df_create: kappa and dt must be positive");
   cuda_check(configure_prim_kernels(), "configure kernels");
   std::unique_ptr<DfCase> d(new DfCase());

@@ -337,6 +337,102 @@ __device__ __forceinline__ double2* fft_pow2(double2* a, double2* b, int L, int 
   return a;
 }
 
+// ------------------------------------------------------------------ FFT of any length
+// Complex arithmetic for the two lane types (the FP64 form and the FP32
+// mixed form share the mixed-radix FFT below).
+__device__ __forceinline__ double2 cx_add(double2 a, double2 b) { return c2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cx_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 cx_sub(double2 a, double2 b) { return c2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cx_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// a * w (forward) or a * conj(w) (inverse)
+__device__ __forceinline__ double2 cx_tw(double2 a, double2 w, bool inv) { return inv ? cmulc(a, w) : cmul(a, w); }
+__device__ __forceinline__ float2 cx_tw(float2 a, float2 w, bool inv) {
+  return inv ? make_float2(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y)
+             : make_float2(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+}
+// a * (-i) (forward) or a * (+i) (inverse)
+__device__ __forceinline__ double2 cx_rot(double2 a, bool inv) { return inv ? c2(-a.y, a.x) : c2(a.y, -a.x); }
+__device__ __forceinline__ float2 cx_rot(float2 a, bool inv) {
+  return inv ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// Stockham autosort FFT of nl lanes of length L = rad[0] * ... * rad[nrad-1]
+// (lane stride ld), unnormalised, exp(-+2 pi i jk / L).  tw[t] =
+// exp(-2 pi i t / twL) with L dividing twL.  Stage s of radix p, after
+// sub-transforms of length Ns: input j + r L/p (r < p) is twiddled by
+// w^(r (j mod Ns)), w = exp(-2 pi i / (Ns p)), and the p-point DFT's output q
+// goes to (j - j mod Ns) p + (j mod Ns) + q Ns.  Radix 4 and 2 use the
+// butterflies; other radices the direct p-point DFT through the same table.
+// Returns the buffer that holds the result (a or b).
+template <class C>
+__device__ C* fft_mixed(C* a, C* b, int L, const int* rad, int nrad, int nl, int ld, const C* __restrict__ tw,
+                        int twL, bool inv, int tid, int nth) {
+  int Ns = 1;
+  for (int st = 0; st < nrad; st++) {
+    const int p = rad[st];
+    const int Lp = L / p;
+    const int tstep = twL / (Ns * p);  // w = tw[tstep]
+    const int pstep = twL / p;         // exp(-2 pi i / p) = tw[pstep]
+    for (int idx = tid; idx < nl * Lp; idx += nth) {
+      const int l = idx / Lp, j = idx - l * Lp;
+      const int jm = j % Ns;
+      const C* src = a + (size_t)l * ld + j;
+      C* dst = b + (size_t)l * ld + (j - jm) * p + jm;
+      if (p == 4) {
+        C v0 = src[0], v1 = src[Lp], v2 = src[2 * Lp], v3 = src[3 * Lp];
+        if (jm) {
+          const int e = jm * tstep;
+          v1 = cx_tw(v1, tw[e], inv);
+          v2 = cx_tw(v2, tw[2 * e], inv);
+          v3 = cx_tw(v3, tw[3 * e], inv);
+        }
+        const C s0 = cx_add(v0, v2), d0 = cx_sub(v0, v2), s1 = cx_add(v1, v3);
+        const C r = cx_rot(cx_sub(v1, v3), inv);
+        dst[0] = cx_add(s0, s1);
+        dst[Ns] = cx_add(d0, r);
+        dst[2 * Ns] = cx_sub(s0, s1);
+        dst[3 * Ns] = cx_sub(d0, r);
+      } else if (p == 2) {
+        C v0 = src[0], v1 = src[Lp];
+        if (jm) v1 = cx_tw(v1, tw[jm * tstep], inv);
+        dst[0] = cx_add(v0, v1);
+        dst[Ns] = cx_sub(v0, v1);
+      } else if (p <= 8) {
+        C v[8];
+        for (int r = 0; r < p; r++) {
+          v[r] = src[(size_t)r * Lp];
+          if (jm && r) v[r] = cx_tw(v[r], tw[r * jm * tstep], inv);
+        }
+        for (int q = 0; q < p; q++) {
+          C acc = v[0];
+          for (int r = 1; r < p; r++) {
+            const int e = (r * q) % p;
+            acc = cx_add(acc, e ? cx_tw(v[r], tw[e * pstep], inv) : v[r]);
+          }
+          dst[q * Ns] = acc;
+        }
+      } else {  // a large prime factor: the inputs are twiddled again for every output
+        for (int q = 0; q < p; q++) {
+          C acc = src[0];
+          for (int r = 1; r < p; r++) {
+            C vr = src[(size_t)r * Lp];
+            if (jm) vr = cx_tw(vr, tw[r * jm * tstep], inv);
+            const int e = (r * q) % p;
+            acc = cx_add(acc, e ? cx_tw(vr, tw[e * pstep], inv) : vr);
+          }
+          dst[q * Ns] = acc;
+        }
+      }
+    }
+    __syncthreads();
+    C* t = a;
+    a = b;
+    b = t;
+    Ns *= p;
+  }
+  return a;
+}
+
 // ------------------------------------------------------------------ Chebyshev transforms
 // pre/post factors of ortho.rs:235-312 for index k of length n (N = n-1)
 __device__ __forceinline__ double cheb_fwd_post(int k, int n, double inv_nm1) {
@@ -526,13 +622,74 @@ static __device__ void dct1_dense(const ChebXformDev& cx, bool forward, const T*
 }
 
 // ------------------------------------------------------------------ Fourier (x)
-// c2r: in = M+1 complex per lane (DC imag and Nyquist imag ignored), out = 2M reals.
+// length-M complex FFT of the Fourier descriptor (radix-4/2 or mixed radix)
+__device__ __forceinline__ double2* fourier_fft(const FourierXformDev& fx, double2* wa, double2* wb, int nl, int wld,
+                                                bool inv, int tid, int nth) {
+  if (fx.log2M >= 0) return fft_pow2(wa, wb, fx.M, fx.log2M, nl, wld, fx.tw, fx.n, inv, tid, nth);
+  return fft_mixed<double2>(wa, wb, fx.M, fx.rad, fx.nrad, nl, wld, fx.tw, fx.n, inv, tid, nth);
+}
+// lane and element of a flat index over nl lanes of M
+__device__ __forceinline__ void fourier_split(const FourierXformDev& fx, int idx, int& l, int& k) {
+  if (fx.log2M >= 0) {
+    l = idx >> fx.log2M;
+    k = idx & (fx.M - 1);
+  } else {
+    l = idx / fx.M;
+    k = idx - l * fx.M;
+  }
+}
+
+// Odd n: c2r and r2c through a full-length complex FFT (M = n).
+static __device__ void c2r_odd(const FourierXformDev& fx, const double2* in, int in_ld, int in_stride, double* out,
+                               int out_ld, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  const int n = fx.n, h = n / 2;
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l, k;
+    fourier_split(fx, idx, l, k);
+    const double2* X = in + l * in_ld;
+    double2 v = k <= h ? X[k * in_stride] : conj2(X[(n - k) * in_stride]);
+    if (k == 0) v.y = 0.0;
+    wa[l * wld + k] = v;
+  }
+  __syncthreads();
+  double2* r = fourier_fft(fx, wa, wb, nl, wld, true, tid, nth);
+  const double s = 1.0 / (double)n;
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l, k;
+    fourier_split(fx, idx, l, k);
+    out[l * out_ld + k] = r[l * wld + k].x * s;
+  }
+  __syncthreads();
+}
+static __device__ void r2c_odd(const FourierXformDev& fx, const double* in, int in_ld, double2* out, int out_ld,
+                               int out_stride, int keep, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  const int n = fx.n;
+  for (int idx = tid; idx < nl * n; idx += nth) {
+    int l, k;
+    fourier_split(fx, idx, l, k);
+    wa[l * wld + k] = c2(in[l * in_ld + k], 0.0);
+  }
+  __syncthreads();
+  double2* r = fourier_fft(fx, wa, wb, nl, wld, false, tid, nth);
+  for (int idx = tid; idx < nl * keep; idx += nth) {
+    const int l = idx / keep, k = idx - l * keep;
+    out[l * out_ld + k * out_stride] = r[l * wld + k];
+  }
+  __syncthreads();
+}
+
+// c2r: in = n/2+1 complex per lane (DC imag and Nyquist imag ignored), out = n reals.
 // Lane l reads in[l*in_ld + k*in_stride].
 static __device__ void c2r(const FourierXformDev& fx, const double2* in, int in_ld, int in_stride, double* out, int out_ld,
                     int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  if (fx.n & 1) {
+    c2r_odd(fx, in, in_ld, in_stride, out, out_ld, nl, wa, wb, wld, tid, nth);
+    return;
+  }
   int M = fx.M;
   for (int idx = tid; idx < nl * M; idx += nth) {
-    int l = idx >> fx.log2M, k = idx & (M - 1);
+    int l, k;
+    fourier_split(fx, idx, l, k);
     const double2* X = in + l * in_ld;
     double2 xk = X[k * in_stride];
     double2 xm = X[(M - k) * in_stride];
@@ -543,10 +700,11 @@ static __device__ void c2r(const FourierXformDev& fx, const double2* in, int in_
     wa[l * wld + k] = c2(xk.x + xc.x - t.y, xk.y + xc.y + t.x);
   }
   __syncthreads();
-  double2* r = fft_pow2(wa, wb, M, fx.log2M, nl, wld, fx.tw, fx.n, true, tid, nth);
+  double2* r = fourier_fft(fx, wa, wb, nl, wld, true, tid, nth);
   double s = 1.0 / (double)fx.n;
   for (int idx = tid; idx < nl * M; idx += nth) {
-    int l = idx >> fx.log2M, k = idx & (M - 1);
+    int l, k;
+    fourier_split(fx, idx, l, k);
     double2 v = r[l * wld + k];
     out[l * out_ld + 2 * k] = v.x * s;
     out[l * out_ld + 2 * k + 1] = v.y * s;
@@ -554,21 +712,26 @@ static __device__ void c2r(const FourierXformDev& fx, const double2* in, int in_
   __syncthreads();
 }
 
-// r2c: in = 2M reals per lane, out = first `keep` (<= M+1) complex values;
+// r2c: in = n reals per lane, out = first `keep` (<= n/2+1) complex values;
 // lane l writes out[l*out_ld + k*out_stride].
 static __device__ void r2c(const FourierXformDev& fx, const double* in, int in_ld, double2* out, int out_ld, int out_stride,
                     int keep, int nl, double2* wa, double2* wb, int wld, int tid, int nth) {
+  if (fx.n & 1) {
+    r2c_odd(fx, in, in_ld, out, out_ld, out_stride, keep, nl, wa, wb, wld, tid, nth);
+    return;
+  }
   int M = fx.M;
   for (int idx = tid; idx < nl * M; idx += nth) {
-    int l = idx >> fx.log2M, k = idx & (M - 1);
+    int l, k;
+    fourier_split(fx, idx, l, k);
     wa[l * wld + k] = c2(in[l * in_ld + 2 * k], in[l * in_ld + 2 * k + 1]);
   }
   __syncthreads();
-  double2* r = fft_pow2(wa, wb, M, fx.log2M, nl, wld, fx.tw, fx.n, false, tid, nth);
+  double2* r = fourier_fft(fx, wa, wb, nl, wld, false, tid, nth);
   for (int idx = tid; idx < nl * keep; idx += nth) {
     int l = idx / keep, k = idx - l * keep;
-    double2 zk = r[l * wld + (k & (M - 1))];
-    double2 zc = conj2(r[l * wld + ((M - k) & (M - 1))]);
+    double2 zk = r[l * wld + (k == M ? 0 : k)];
+    double2 zc = conj2(r[l * wld + (k == 0 ? 0 : M - k)]);
     double2 e = (zk + zc) * 0.5;
     double2 dd = zk - zc;
     double2 o = c2(dd.y * 0.5, -dd.x * 0.5);  // (zk - zc) / (2i)

@@ -2,10 +2,12 @@
 // Fourier transforms and products of the convection term, which the reference
 // computes in FP64 (funspace/src/fourier/r2c.rs:160-226, conv_term.rs:22-42)
 // and the mixed form evaluates in FP32.  Same algorithms as the FP64 lane
-// operations (radix-4/2 Stockham FFT, r2c/c2r through half-length complex
-// FFTs), on float2 data with an FP32 twiddle table.
+// operations (Stockham FFTs, r2c/c2r through half-length complex FFTs for even
+// n), on float2 data with an FP32 twiddle table.
 #pragma once
 #include <cuda_runtime.h>
+
+#include "lane_ops.cuh"
 
 namespace rbc {
 namespace dev {
@@ -64,13 +66,41 @@ __device__ __forceinline__ float2* fft_pow2_f(float2* a, float2* b, int L, int l
   return a;
 }
 
-// c2r: lanes of M+1 complex values (imaginary parts of DC and Nyquist
-// ignored) -> 2M reals, scaled by 1/n.  Lane l reads in[l*in_ld + k*in_stride].
+__device__ __forceinline__ float2* fourier_fft_f(const FourierXformDev& fx, float2* wa, float2* wb, int nl, int wld,
+                                                 bool inv, int tid, int nth) {
+  if (fx.log2M >= 0) return fft_pow2_f(wa, wb, fx.M, fx.log2M, nl, wld, fx.twf, fx.n, inv, tid, nth);
+  return fft_mixed<float2>(wa, wb, fx.M, fx.rad, fx.nrad, nl, wld, fx.twf, fx.n, inv, tid, nth);
+}
+
+// c2r: lanes of n/2+1 complex values (imaginary parts of DC and Nyquist
+// ignored) -> n reals, scaled by 1/n.  Lane l reads in[l*in_ld + k*in_stride].
 __device__ __forceinline__ void c2r_f(const FourierXformDev& fx, const float2* in, int in_ld, int in_stride, float* out,
                                       int out_ld, int nl, float2* wa, float2* wb, int wld, int tid, int nth) {
   const int M = fx.M;
+  const float s = 1.0f / (float)fx.n;
+  if (fx.n & 1) {  // full-length complex FFT
+    const int n = fx.n, h = n / 2;
+    for (int idx = tid; idx < nl * n; idx += nth) {
+      int l, k;
+      fourier_split(fx, idx, l, k);
+      const float2* X = in + l * in_ld;
+      float2 v = k <= h ? X[k * in_stride] : fconj(X[(n - k) * in_stride]);
+      if (k == 0) v.y = 0.f;
+      wa[l * wld + k] = v;
+    }
+    __syncthreads();
+    float2* r = fourier_fft_f(fx, wa, wb, nl, wld, true, tid, nth);
+    for (int idx = tid; idx < nl * n; idx += nth) {
+      int l, k;
+      fourier_split(fx, idx, l, k);
+      out[l * out_ld + k] = r[l * wld + k].x * s;
+    }
+    __syncthreads();
+    return;
+  }
   for (int idx = tid; idx < nl * M; idx += nth) {
-    const int l = idx >> fx.log2M, k = idx & (M - 1);
+    int l, k;
+    fourier_split(fx, idx, l, k);
     const float2* X = in + l * in_ld;
     float2 xk = X[k * in_stride];
     float2 xm = X[(M - k) * in_stride];
@@ -80,10 +110,10 @@ __device__ __forceinline__ void c2r_f(const FourierXformDev& fx, const float2* i
     wa[l * wld + k] = f2(xk.x + xc.x - t.y, xk.y + xc.y + t.x);
   }
   __syncthreads();
-  float2* r = fft_pow2_f(wa, wb, M, fx.log2M, nl, wld, fx.twf, fx.n, true, tid, nth);
-  const float s = 1.0f / (float)fx.n;
+  float2* r = fourier_fft_f(fx, wa, wb, nl, wld, true, tid, nth);
   for (int idx = tid; idx < nl * M; idx += nth) {
-    const int l = idx >> fx.log2M, k = idx & (M - 1);
+    int l, k;
+    fourier_split(fx, idx, l, k);
     const float2 v = r[l * wld + k];
     out[l * out_ld + 2 * k] = v.x * s;
     out[l * out_ld + 2 * k + 1] = v.y * s;
@@ -91,22 +121,39 @@ __device__ __forceinline__ void c2r_f(const FourierXformDev& fx, const float2* i
   __syncthreads();
 }
 
-// r2c: lanes of 2M reals -> first `keep` (<= M+1) complex values; lane l
+// r2c: lanes of n reals -> first `keep` (<= n/2+1) complex values; lane l
 // writes out[l*out_ld + k*out_stride].
 __device__ __forceinline__ void r2c_f(const FourierXformDev& fx, const float* in, int in_ld, float2* out, int out_ld,
                                       int out_stride, int keep, int nl, float2* wa, float2* wb, int wld, int tid,
                                       int nth) {
   const int M = fx.M;
+  if (fx.n & 1) {
+    const int n = fx.n;
+    for (int idx = tid; idx < nl * n; idx += nth) {
+      int l, k;
+      fourier_split(fx, idx, l, k);
+      wa[l * wld + k] = f2(in[l * in_ld + k], 0.f);
+    }
+    __syncthreads();
+    float2* r = fourier_fft_f(fx, wa, wb, nl, wld, false, tid, nth);
+    for (int idx = tid; idx < nl * keep; idx += nth) {
+      const int l = idx / keep, k = idx - l * keep;
+      out[l * out_ld + k * out_stride] = r[l * wld + k];
+    }
+    __syncthreads();
+    return;
+  }
   for (int idx = tid; idx < nl * M; idx += nth) {
-    const int l = idx >> fx.log2M, k = idx & (M - 1);
+    int l, k;
+    fourier_split(fx, idx, l, k);
     wa[l * wld + k] = f2(in[l * in_ld + 2 * k], in[l * in_ld + 2 * k + 1]);
   }
   __syncthreads();
-  float2* r = fft_pow2_f(wa, wb, M, fx.log2M, nl, wld, fx.twf, fx.n, false, tid, nth);
+  float2* r = fourier_fft_f(fx, wa, wb, nl, wld, false, tid, nth);
   for (int idx = tid; idx < nl * keep; idx += nth) {
     const int l = idx / keep, k = idx - l * keep;
-    const float2 zk = r[l * wld + (k & (M - 1))];
-    const float2 zc = fconj(r[l * wld + ((M - k) & (M - 1))]);
+    const float2 zk = r[l * wld + (k == M ? 0 : k)];
+    const float2 zc = fconj(r[l * wld + (k == 0 ? 0 : M - k)]);
     const float2 e = (zk + zc) * 0.5f;
     const float2 dd = zk - zc;
     const float2 o = f2(dd.y * 0.5f, -dd.x * 0.5f);

@@ -137,10 +137,27 @@ ChebXformDev upload_cheb(Arena& a, int n) {
 FourierXformDev upload_fourier(Arena& a, int n) {
   FourierXformDev d;
   std::memset(&d, 0, sizeof d);
-  if (!is_pow2(n) || n < 4) throw std::runtime_error("FourierR2c length must be a power of two >= 4");
+  if (n < 4) throw std::runtime_error("FourierR2c length must be >= 4");
   d.n = n;
-  d.M = n / 2;
-  d.log2M = ilog2(d.M);
+  d.M = (n & 1) ? n : n / 2;
+  if (is_pow2(d.M)) {
+    d.log2M = ilog2(d.M);
+  } else {
+    // mixed-radix stages: radix 4 while it divides, then 2, 3, 5, 7 and the
+    // remaining prime factors
+    d.log2M = -1;
+    int r = d.M;
+    auto push = [&](int p) {
+      if (d.nrad >= 16) throw std::runtime_error("FourierR2c: too many FFT stages");
+      d.rad[d.nrad++] = p;
+      r /= p;
+    };
+    while (r % 4 == 0) push(4);
+    while (r % 2 == 0) push(2);
+    for (int p = 3; p * p <= r; p += 2)
+      while (r % p == 0) push(p);
+    if (r > 1) push(r);
+  }
   std::vector<double> tw = twiddles(n);
   d.tw = reinterpret_cast<const double2*>(a.upload(tw));
   std::vector<float> twf(tw.size());
@@ -428,8 +445,8 @@ __global__ void __launch_bounds__(128) k_pass(const __grid_constant__ PassDesc d
       case P_R2C:
         for (int k = tid; k < len; k += nth) R[k] = A[k].x;
         __syncthreads();
-        r2c(d.fx, R, 0, B, 0, 1, d.fx.M + 1, 1, WA, WB, d.wl, tid, nth);
-        len = d.fx.M + 1;
+        r2c(d.fx, R, 0, B, 0, 1, d.fx.n / 2 + 1, 1, WA, WB, d.wl, tid, nth);
+        len = d.fx.n / 2 + 1;
         { double2* t = A; A = B; B = t; }
         break;
       case P_C2R:

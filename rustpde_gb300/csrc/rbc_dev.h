@@ -63,12 +63,16 @@ struct ChebXformDev {
   const double* bwd;  // dense n x n backward matrix
 };
 
-// Fourier r2c/c2r along x of physical length n (power of two).
+// Fourier r2c/c2r along x of physical length n (any n >= 4).  Even n runs
+// through a complex FFT of half length M = n/2, odd n through one of length
+// M = n.  A power-of-two M uses radix-4/2 Stockham stages (log2M >= 0);
+// any other M the mixed-radix stages rad[0..nrad) (product M).
 struct FourierXformDev {
   int n;        // physical length
-  int M;        // n/2 (half-length complex FFT)
-  int log2M;
-  int pad_;
+  int M;        // complex FFT length: n/2 (even n) or n (odd n)
+  int log2M;    // log2(M) when M is a power of two, else -1
+  int nrad;     // mixed-radix stages (log2M < 0)
+  int rad[16];  // their radices: 4s, then 2, 3, 5, 7 and any larger prime factors
   const double2* tw;  // exp(-2 pi i t / n), t < n
   const float2* twf;  // the same table rounded to FP32 (mixed-precision form)
 };

@@ -30,7 +30,7 @@ def last_error(R):
     (dict(ra=-1.0), "positive"),
     (dict(dt=0.0), "positive"),
     (dict(ny=4), "ny"),
-    (dict(nx=100, kind=2), "power of two"),
+    (dict(nx=6, kind=2), "periodic nx"),
     (dict(nx=4), "nx"),
     (dict(precision=5), "precision"),
 ])

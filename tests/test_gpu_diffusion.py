@@ -32,6 +32,7 @@ SPACES = {
     "cn65xcd64": (O.CN, 65, O.CD, 64),
     "fourier64xcd33": (O.FOURIER, 64, O.CD, 33),
     "fourier128xcn65": (O.FOURIER, 128, O.CN, 65),
+    "fourier96xcd33": (O.FOURIER, 96, O.CD, 33),
 }
 
 

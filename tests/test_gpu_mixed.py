@@ -45,6 +45,9 @@ CASES = {
     "periodic64x33": (O.PERIODIC, 64, 33, 1e5, 1.0, 0.005, 1.0),
     "periodic128x64": (O.PERIODIC, 128, 64, 1e6, 0.7, 2e-3, 1.5),
     "periodic512x257": (O.PERIODIC, 512, 257, 1e7, 1.0, 1e-3, 2.0),
+    # FP32 mixed-radix Fourier transforms (96 = 2 * 48; odd 45)
+    "periodic96x33": (O.PERIODIC, 96, 33, 1e5, 1.0, 0.005, 1.0),
+    "periodic45x33": (O.PERIODIC, 45, 33, 1e5, 1.0, 0.005, 1.0),
 }
 
 

@@ -40,6 +40,13 @@ CASES = {
     "box_cond33": (O.BOX_CONDUCTING, 33, 33, 1e5, 1.0, 0.01, 1.5),
     "periodic64x33": (O.PERIODIC, 64, 33, 1e5, 1.0, 0.005, 1.0),
     "periodic512x257": (O.PERIODIC, 512, 257, 1e7, 1.0, 1e-3, 2.0),
+    # FourierR2c of any length (r2c.rs:45-70): mixed-radix half-length FFTs
+    # (96 = 2 * 48, 80 = 2 * 40), a large prime factor (22 = 2 * 11) and an
+    # odd length (45, full-length FFT)
+    "periodic96x33": (O.PERIODIC, 96, 33, 1e5, 1.0, 5e-3, 1.0),
+    "periodic80x33": (O.PERIODIC, 80, 33, 1e5, 1.0, 5e-3, 1.5),
+    "periodic22x17": (O.PERIODIC, 22, 17, 1e4, 1.0, 1e-2, 1.0),
+    "periodic45x33": (O.PERIODIC, 45, 33, 1e5, 0.7, 5e-3, 1.2),
 }
 # the ensemble's box sizes: the Poisson eigen-decompositions of 126 and 254
 # modes come from the library's own eigensolver on the GPU side and from
@@ -168,6 +175,11 @@ SPACES = [
     (O.FOURIER, 16, O.CD, 17),
     (O.FOURIER, 32, O.CN, 12),
     (O.FOURIER, 8, O.CHEB, 65),
+    (O.FOURIER, 96, O.CD, 17),
+    (O.FOURIER, 80, O.CN, 12),
+    (O.FOURIER, 22, O.CHEB, 9),
+    (O.FOURIER, 45, O.CD, 16),
+    (O.FOURIER, 210, O.CN, 10),
 ]
 
 
