@@ -22,6 +22,9 @@ Workloads (--workload):
                       (see run_extras).
   profile-step        one batched ensemble step between cudaProfilerStart/Stop,
                       for `ncu --profile-from-start off` (see run_profile_step).
+  cpu-table           the CPU restatement of the reference algorithm on the host
+                      cores for configurations 0-3, all threads and one thread
+                      (see run_cpu_table); no GPU work.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload ...]
 
@@ -754,6 +757,79 @@ def run_reference(args, rank, world):
     }
 
 
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+def run_cpu_table(args):
+    """The reference algorithm (the oracle, OpenMP over lanes) on the host
+    cores for configurations 0-3, with all threads and with one, each on a
+    bounded sample: per-step latency percentiles for the single cases, per
+    stage times for the 1-D lanes, and the ensemble case by case."""
+    import numpy as np
+
+    from oracle import oracle as O
+    from rustpde_gb300.ensemble import draw_ensemble
+    O.build()
+    allc = os.cpu_count() or 1
+    rows = []
+
+    def single(name, p, steps):
+        nx, ny = p[0], p[1]
+        o = O.Navier2D(*p)
+        O.standard_ic(o, 1)
+        o.update(1)
+        ts = []
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            o.update(1)
+            ts.append(time.perf_counter() - t0)
+        ts = np.array(ts)
+        return {"config": name, "threads": O.num_threads(), "gp_steps_per_s": nx * ny * steps / ts.sum(),
+                "p50_step_ms": float(np.percentile(ts, 50) * 1e3), "p99_step_ms": float(np.percentile(ts, 99) * 1e3),
+                "sample": f"{steps} steps after 1 warm-up step"}
+
+    for threads in (allc, 1):
+        O.set_threads(threads)
+        rows.append(single("0: box 64^2 Ra 1e5 dt 0.02", (64, 64, 1e5, 1.0, 0.02, 1.0, O.BOX_ADIABATIC),
+                           100))
+        rows.append(single("1: periodic 512x257 Ra 1e7 dt 1e-3", (NX, NY, RA, PR, DT, ASPECT, O.PERIODIC),
+                           20 if threads > 1 else 5))
+        rng = np.random.default_rng(11)
+        for n in (128, 256, 512):
+            m = n - 2
+            spec = rng.standard_normal((4096, m)) * np.exp(-np.arange(m) / 20.0)
+            phys = O.lanes_apply(O.CD, n, 1, spec)
+            ortho = O.lanes_apply(O.CD, n, 2, spec)
+            stage = {}
+            for op, name, x in ((0, "forward", phys), (1, "backward", spec), (2, "to_ortho", spec),
+                                (3, "from_ortho", ortho), (4, "hholtz", ortho)):
+                O.lanes_apply(O.CD, n, op, x, 5e-4)
+                reps = 3
+                t0 = time.perf_counter()
+                for _ in range(reps):
+                    O.lanes_apply(O.CD, n, op, x, 5e-4)
+                stage[name] = (time.perf_counter() - t0) / reps * 1e3
+            rows.append({"config": f"2: 4096 lanes x N={n}, ChebDirichlet", "threads": O.num_threads(),
+                         "ms_per_stage": stage})
+        params = draw_ensemble(args.cases, ENSEMBLE_SEED)
+        steps = 2 if threads > 1 else 1
+        v, secs = cpu_ensemble_sample(O, params, steps, 1)
+        rows.append({"config": "3: 256-case ensemble, case by case", "threads": O.num_threads(),
+                     "gp_steps_per_s": v, "sample": f"all {len(params)} cases x {steps} ensemble steps "
+                                                       f"({secs:.1f} s)"})
+    return {"workload": "cpu-table", "cpu_model": cpu_model(), "host_threads": allc,
+            "what": "oracle/ (C++ restatement of the reference algorithm, FP64, -O3, OpenMP over lanes)",
+            "rows": rows}
+
+
 def run_profile_step(args):
     """The ensemble's batched mixed step for a profiler: the batch (forms from
     the autotuner, or pinned by RBC_BATCH_FORM), W warm-up steps, then ONE step
@@ -788,7 +864,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ensemble",
-                    choices=["ensemble", "periodic512", "serving", "precision", "extras", "profile-step"])
+                    choices=["ensemble", "periodic512", "serving", "precision", "extras", "profile-step",
+                             "cpu-table"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="periodic512: oracle seconds")
     ap.add_argument("--cpu-steps", type=int, default=3, help="ensemble: oracle ensemble steps in cpu_baseline")
     ap.add_argument("--accuracy-steps", type=int, default=505,
@@ -815,6 +892,8 @@ def main():
         line = run_extras(args)
     elif args.workload == "profile-step":
         line = run_profile_step(args)
+    elif args.workload == "cpu-table":
+        line = run_cpu_table(args)
     elif args.workload == "serving":
         from rustpde_gb300 import build
         build.build()

@@ -96,6 +96,7 @@ def lib():
                 "or_adjoint_eval": (D, [P, I]),
                 "or_adjoint_exit": (I, [P]),
                 "or_adjoint_residual": (None, [P, DP]),
+                "or_lanes_apply": (I, [I, I, I, I, D, DP, DP]),
                 "or_space_new": (P, [I, I, I, I]),
                 "or_space_free": (None, [P]),
                 "or_space_sizes": (I, [P, IP]),
@@ -387,6 +388,19 @@ class Space2:
     def average(self, v):
         v = _f64(v, self.phys)
         return lib().or_space_average(self._h, _dp(v))
+
+
+def lanes_apply(kind, n, op, x, c=0.0):
+    """Oracle of the batched 1-D lanes (fs_lanes_apply): op 0 forward, 1
+    backward, 2 to_ortho, 3 from_ortho, 4 HholtzAdi solve (coefficient c) on
+    every row of x (lanes x length), the rows in parallel."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    m = n - 2 if kind in (CD, CN) else n
+    ol = m if op in (0, 3, 4) else n
+    out = np.zeros((x.shape[0], ol))
+    if lib().or_lanes_apply(int(kind), int(n), int(op), x.shape[0], float(c), _dp(x), _dp(out)) != 0:
+        raise RuntimeError(lib().or_last_error().decode())
+    return out
 
 
 class Solver:

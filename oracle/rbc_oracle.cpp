@@ -95,13 +95,22 @@ static Mat matmul(const Mat& a, const Mat& b) {
 }
 
 // ---------------------------------------------------------------------------
-// Mixed-radix complex FFT (recursive decimation in time), any length.
+// Complex FFT of any length: mixed-radix recursive decimation in time, and
+// Bluestein's chirp-z algorithm through a power-of-two FFT when the length has
+// a prime factor above 16 (rustfft, behind the reference's DCT-I and r2c, is
+// O(n log n) for every length too: its Rader and Bluestein algorithms).
 // ---------------------------------------------------------------------------
 struct FFT {
   int n = 0;
   std::vector<int> fac;
   std::vector<cplx> tw;  // tw[t] = exp(-2 pi i t / n)
   int maxp = 1;
+  // Bluestein: chirp[k] = exp(-pi i k^2 / n), the transformed conjugate chirp
+  // of length m (a power of two >= 2n - 1), and the length-m FFT
+  bool blue = false;
+  int m = 0;
+  std::vector<cplx> chirp, bfft;
+  std::unique_ptr<FFT> sub;
   explicit FFT(int n_) : n(n_) {
     int r = n;
     for (int p = 2; p * p <= r; p++)
@@ -112,6 +121,23 @@ struct FFT {
     for (int t = 0; t < n; t++) {
       double ang = 2.0 * PI * (double)t / (double)n;
       tw[t] = cplx(std::cos(ang), -std::sin(ang));
+    }
+    if (maxp > 16) {
+      blue = true;
+      m = 1;
+      while (m < 2 * n - 1) m *= 2;
+      sub.reset(new FFT(m));
+      chirp.resize(n);
+      for (int k = 0; k < n; k++) {
+        const long q = ((long)k * k) % (2L * n);  // k^2 mod 2n keeps the angle exact
+        const double ang = PI * (double)q / (double)n;
+        chirp[k] = cplx(std::cos(ang), -std::sin(ang));
+      }
+      std::vector<cplx> b(m, cplx(0.0, 0.0));
+      b[0] = std::conj(chirp[0]);
+      for (int k = 1; k < n; k++) b[k] = b[m - k] = std::conj(chirp[k]);
+      bfft.resize(m);
+      sub->exec(b.data(), bfft.data(), false);
     }
   }
   inline cplx W(long e, bool inv) const {
@@ -134,6 +160,23 @@ struct FFT {
   }
   // out = sum_j in_j exp(-+ 2 pi i jk/n); unnormalised both ways
   void exec(const cplx* in, cplx* out, bool inv) const {
+    if (blue) {
+      // X_k = chirp_k sum_j (x_j chirp_j) conj(chirp_{k-j}); the inverse is
+      // conj(forward(conj(x)))
+      thread_local std::vector<cplx> a, A;
+      a.assign(m, cplx(0.0, 0.0));
+      A.resize(m);
+      for (int j = 0; j < n; j++) a[j] = (inv ? std::conj(in[j]) : in[j]) * chirp[j];
+      sub->exec(a.data(), A.data(), false);
+      for (int k = 0; k < m; k++) A[k] *= bfft[k];
+      sub->exec(A.data(), a.data(), true);
+      const double s = 1.0 / (double)m;
+      for (int k = 0; k < n; k++) {
+        const cplx v = a[k] * s * chirp[k];
+        out[k] = inv ? std::conj(v) : v;
+      }
+      return;
+    }
     thread_local std::vector<cplx> tmp;
     if ((int)tmp.size() < maxp) tmp.resize(maxp);
     rec(in, 1, out, n, 0, 1, inv, tmp.data());
@@ -1848,6 +1891,42 @@ void or_solver1d(int basekind, int n, int kind, double c, const double* in, doub
   Solver1 s;
   s.build(b, kind, c);
   s.solve(in, out);
+}
+
+// Many lanes of one Chebyshev-family basis (row-major lanes x length), the
+// 1-D axis operations of Space2 (ortho.rs:235-312, composite.rs:156-238) and
+// HholtzAdi::solve along one axis (hholtz_adi.rs:92-131): op 0 forward
+// (n -> m), 1 backward (m -> n), 2 to_ortho (m -> n), 3 from_ortho (n -> m),
+// 4 Helmholtz solve with coefficient c (n -> m).  One basis and one solver
+// serve every lane; lanes run in parallel (OpenMP), as the reference's rayon
+// par_for_each over lanes.
+int or_lanes_apply(int kind, int n, int op, int lanes, double c, const double* in, double* out) {
+  try {
+    Base b(kind, n);
+    if (b.fourier()) throw std::runtime_error("or_lanes_apply: Chebyshev-family bases only");
+    const int m = b.m;
+    const int il = (op == 0 || op == 3 || op == 4) ? n : m;
+    const int ol = (op == 0 || op == 3 || op == 4) ? m : n;
+    Solver1 s;
+    if (op == 4) s.build(b, S_HHOLTZ_ADI, c);
+#pragma omp parallel for schedule(static)
+    for (int l = 0; l < lanes; l++) {
+      const double* x = in + (size_t)l * il;
+      double* y = out + (size_t)l * ol;
+      std::vector<double> o(n);
+      switch (op) {
+        case 0: b.cheb_forward(x, o.data()); b.from_ortho(o.data(), y); break;
+        case 1: b.to_ortho(x, o.data()); b.cheb_backward(o.data(), y); break;
+        case 2: b.to_ortho(x, y); break;
+        case 3: b.from_ortho(x, y); break;
+        default: s.solve(x, y); break;
+      }
+    }
+    return 0;
+  } catch (std::exception& e) {
+    g_err = e.what();
+    return -1;
+  }
 }
 
 // 2-D field solvers (Hholtz / HholtzAdi / Poisson) on a space
