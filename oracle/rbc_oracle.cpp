@@ -97,7 +97,8 @@ static Mat matmul(const Mat& a, const Mat& b) {
 // ---------------------------------------------------------------------------
 // Complex FFT of any length: mixed-radix recursive decimation in time, and
 // Bluestein's chirp-z algorithm through a power-of-two FFT when the length has
-// a prime factor above 16 (rustfft, behind the reference's DCT-I and r2c, is
+// a prime factor above 64, where the direct p-point stage costs more than two
+// power-of-two FFTs (rustfft, behind the reference's DCT-I and r2c, is
 // O(n log n) for every length too: its Rader and Bluestein algorithms).
 // ---------------------------------------------------------------------------
 struct FFT {
@@ -122,7 +123,7 @@ struct FFT {
       double ang = 2.0 * PI * (double)t / (double)n;
       tw[t] = cplx(std::cos(ang), -std::sin(ang));
     }
-    if (maxp > 16) {
+    if (maxp > 64) {
       blue = true;
       m = 1;
       while (m < 2 * n - 1) m *= 2;

@@ -4,7 +4,8 @@
   counterpart of fs_lanes_apply) gives, lane by lane, exactly what the
   oracle's single-lane functions give;
 * the oracle's FFT, with Bluestein's algorithm for lengths that have a prime
-  factor above 16, matches numpy's FFT for r2c and DCT-I lengths of that kind.
+  factor above 64, matches numpy's FFT for such lengths and for the direct
+  prime stages below that.
 """
 import ctypes
 
@@ -44,7 +45,7 @@ def test_lanes_match_single_lane_functions(kind, n):
             assert np.array_equal(got[lane], ref)
 
 
-@pytest.mark.parametrize("n", [22, 94, 194, 202, 254, 1022])
+@pytest.mark.parametrize("n", [22, 94, 194, 202, 254, 510, 1022])
 def test_fft_prime_factor_lengths_match_numpy(n):
     v = np.random.default_rng(n).standard_normal(n)
     out = np.zeros(n // 2 + 1, dtype=np.complex128)
