@@ -427,7 +427,8 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     for (int f = 0; f < 3; f++) h.m_y[f] = A.alloc((size_t)2 * ny * h.mx * 8);
     h.m_q = A.alloc((size_t)3 * ny * std::max(h.kx, 1) * 8);
     h.m_cv = A.alloc((size_t)3 * std::max(h.kx, 1) * h.ky * 16);
-    h.m_s32 = A.alloc((size_t)3 * nstate * (per ? 8 : 4));
+    // FP32 state copy: rows padded to 16 bytes, complex rows as [re | im] (rbc_dev.h)
+    h.m_s32 = A.alloc((size_t)3 * h.mxc * s32_row_floats(h) * 4);
     h.m_bcx = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
     h.m_bcy = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
     c->mops.y1 = upload_op(A, {{&mixed_operator(MOP_BS_CD, ny), 1.0L}, {&mixed_operator(MOP_BDS_CD, ny), 1.0L}});

@@ -205,6 +205,7 @@ struct ATile {
   const T* src[kItems];  // nullptr: lane past the job's end (zeros)
   int es;               // element stride of the lanes (a row length at most)
   int soff0, sstep;     // shared-memory byte offset of item 0, step per item
+  bool vec;             // unit element stride and every item 16-byte aligned: vector loads
 };
 
 __device__ __forceinline__ void item_lane_quad(int q, bool lane_fast, int& l, int& kq) {
@@ -227,6 +228,22 @@ __device__ __forceinline__ void a_setup(ATile<T>& t, const GemmJobDev& J, const 
   }
   // item it+1 is 2 quads further (lanes fast) or 32 lanes further (rows)
   t.sstep = lf ? 2 * (kGemmLanes / 8) * 128 : 4 * 128;
+  // chunk starts are 32 elements apart, so an aligned item stays aligned
+  t.vec = t.es == 1;
+#pragma unroll
+  for (int it = 0; it < kItems; it++)
+    if (t.src[it] != nullptr && (reinterpret_cast<uintptr_t>(t.src[it]) & 15u) != 0) t.vec = false;
+}
+
+// 4 consecutive elements from a 16-byte aligned address
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 x = __ldg(reinterpret_cast<const float4*>(p));
+  v[0] = x.x; v[1] = x.y; v[2] = x.z; v[3] = x.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+  const double2 x = __ldg(reinterpret_cast<const double2*>(p));
+  const double2 y = __ldg(reinterpret_cast<const double2*>(p) + 1);
+  v[0] = x.x; v[1] = x.y; v[2] = y.x; v[3] = y.y;
 }
 
 // loads of chunk k0 .. k0+31; only the job's last chunk checks k < K
@@ -234,11 +251,31 @@ template <class T>
 __device__ __forceinline__ void a_load(AChunk<T>& a, const ATile<T>& t, int k0, int K, bool lane_fast, int tid) {
   const int o = k0 * t.es;
   if (k0 + kGemmKC <= K) {
+    if (t.vec) {
 #pragma unroll
-    for (int it = 0; it < kItems; it++) {
-      const T* p = t.src[it];
+      for (int it = 0; it < kItems; it++) {
+        const T* p = t.src[it];
+        if (p != nullptr) {
+          ld4(p + o, a.v[it]);
+        } else {
 #pragma unroll
-      for (int e = 0; e < 4; e++) a.v[it][e] = p != nullptr ? __ldg(p + o + e * t.es) : T(0);
+          for (int e = 0; e < 4; e++) a.v[it][e] = T(0);
+        }
+      }
+    } else if (t.es == 1) {
+#pragma unroll
+      for (int it = 0; it < kItems; it++) {
+        const T* p = t.src[it] != nullptr ? t.src[it] + o : nullptr;
+#pragma unroll
+        for (int e = 0; e < 4; e++) a.v[it][e] = p != nullptr ? __ldg(p + e) : T(0);
+      }
+    } else {
+#pragma unroll
+      for (int it = 0; it < kItems; it++) {
+        const T* p = t.src[it];
+#pragma unroll
+        for (int e = 0; e < 4; e++) a.v[it][e] = p != nullptr ? __ldg(p + o + e * t.es) : T(0);
+      }
     }
   } else {
 #pragma unroll
@@ -417,31 +454,49 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
       __syncthreads();
       // FP32 outputs of scale 1 are stored as they are (a round trip through
       // FP64 would run at the FP64 rate on this GPU)
+      // A thread's lane (lanes fast) or column (rows) is the same in all 16
+      // iterations, so its addresses advance by a constant: staged element
+      // q = tid + 256 it is (lane l, column n) with
+      //   0: l = tid & 127, n = (tid >> 7) + 2 it
+      //   1: l = (tid >> 5) + 8 it, n = tid & 31
+      //   2: l = 2 (tid >> 6) + (tid & 1) + 8 it, n = (tid >> 1) & 31
+      const long long esz = otype == LT_F64 ? 8 : 4;
       auto store_all = [&](auto store, auto mode) {
         constexpr int M = decltype(mode)::value;
-#pragma unroll 4
-        for (int it = 0; it < 4096 / kGemmThreads; it++) {
-          const int q = tid + kGemmThreads * it;
-          int l, n;
-          if constexpr (M == 0) { l = q & 127; n = q >> 7; }
-          else if constexpr (M == 1) { l = q >> 5; n = q & 31; }
-          else { l = (q >> 6) * 2 + (q & 1); n = (q >> 1) & 31; }
+        if constexpr (M == 0) {
+          const int l = tid & 127, n0 = tid >> 7;
           char* base = ob[l];
-          const int nl = cc + n;
-          if (base != nullptr && nl < nvalid) store(base, (long long)(nbase + nl) * oes, stage[l * 33 + n]);
+          if (base != nullptr) {
+            char* pp = base + (long long)(nbase + cc + n0) * oes * esz;
+            const long long step = 2 * oes * esz;
+            const float* sv = stage + l * 33 + n0;
+#pragma unroll 4
+            for (int it = 0; it < 4096 / kGemmThreads; it++, pp += step)
+              if (cc + n0 + 2 * it < nvalid) store(pp, sv[2 * it]);
+          }
+        } else {
+          const int n = M == 1 ? (tid & 31) : ((tid >> 1) & 31);
+          const int l0 = M == 1 ? (tid >> 5) : 2 * (tid >> 6) + (tid & 1);
+          if (cc + n < nvalid) {
+            const long long off = (long long)(nbase + cc + n) * oes * esz;
+#pragma unroll 4
+            for (int it = 0; it < 4096 / kGemmThreads; it++) {
+              const int l = l0 + 8 * it;
+              char* base = ob[l];
+              if (base != nullptr) store(base + off, stage[l * 33 + n]);
+            }
+          }
         }
       };
       auto store_typed = [&](auto mode) {
         if (otype == LT_F64 && scale == 1.0)  // no FP64 product (the conversion alone runs at the FP64 rate)
-          store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f; }, mode);
+          store_all([&](char* p, float f) { *reinterpret_cast<double*>(p) = (double)f; }, mode);
         else if (otype == LT_F64)
-          store_all([&](char* base, long long o, float f) { reinterpret_cast<double*>(base)[o] = (double)f * scale; },
-                    mode);
+          store_all([&](char* p, float f) { *reinterpret_cast<double*>(p) = (double)f * scale; }, mode);
         else if (scale == 1.0)
-          store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = f; }, mode);
+          store_all([&](char* p, float f) { *reinterpret_cast<float*>(p) = f; }, mode);
         else
-          store_all([&](char* base, long long o, float f) { reinterpret_cast<float*>(base)[o] = (float)((double)f * scale); },
-                    mode);
+          store_all([&](char* p, float f) { *reinterpret_cast<float*>(p) = (float)((double)f * scale); }, mode);
       };
       if (omode == 0) store_typed(std::integral_constant<int, 0>());
       else if (omode == 1) store_typed(std::integral_constant<int, 1>());

@@ -157,9 +157,18 @@ struct CaseDev {
   void* m_ph[8];  // box: FP32 physical fields (nx x ny)
   void* m_p[3];   // box: FP32 products, then their x transforms
   void* m_z;      // box: FP32 pinv_x of the divergence (mxc x ny), then the FP32 Poisson row solutions (mxc x myc)
-  void* m_s32;    // FP32 copy of ux, uy, temp (3 x mxc x myc, interleaved re/im when periodic): the y GEMM's input
+  void* m_s32;    // FP32 copy of ux, uy, temp, the y GEMM's input: 3 x mxc rows of s32_row_floats(), a
+                  // real row padded to a multiple of 4 floats, a complex row as [re | im] parts of that length
   const float* m_bcx;  // FP32 d(fieldbc)/dx, transposed: ny x nx
   const float* m_bcy;  // FP32 d(fieldbc)/dy - m_bcg, transposed: ny x nx
 };
+
+// Row length (floats) of the mixed form's FP32 state copy m_s32 and of the
+// box y GEMM's output rows m_y (mxc values): padded to a multiple of 4 floats
+// so that the lane GEMM reads them with aligned 16-byte loads.
+__host__ __device__ inline int pad4(int n) { return (n + 3) & ~3; }
+__host__ __device__ inline int s32_row_floats(const CaseDev& c) {
+  return c.kind == KIND_PERIODIC ? 2 * pad4(c.myc) : pad4(c.myc);
+}
 
 }  // namespace rbc

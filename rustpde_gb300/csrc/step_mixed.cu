@@ -127,13 +127,20 @@ __global__ void __launch_bounds__(128) k_state_f32(const CaseDev* __restrict__ c
   const CaseDev& c = cases[w.x];
   if (c.gate != nullptr && c.gate[1] == 0) return;
   const int i = w.y;
-  const size_t rl = (size_t)c.myc * (c.kind == KIND_PERIODIC ? 2 : 1);  // doubles per row
-  const size_t fs = (size_t)c.mxc * rl;
+  const int myc = c.myc, mp = pad4(myc);
+  const bool per = c.kind == KIND_PERIODIC;
+  const size_t rl = (size_t)myc * (per ? 2 : 1);  // doubles per state row
+  const size_t ld = (size_t)s32_row_floats(c);    // floats per FP32 row
+  const size_t fs = (size_t)c.mxc * ld;
   const double* src[3] = {static_cast<const double*>(c.ux), static_cast<const double*>(c.uy),
                           static_cast<const double*>(c.temp)};
   float* dst = static_cast<float*>(c.m_s32);
+  // a complex row (re, im interleaved) is split into its [re | im] parts
   for (int f = 0; f < 3; f++)
-    for (size_t k = threadIdx.x; k < rl; k += blockDim.x) dst[f * fs + i * rl + k] = (float)src[f][i * rl + k];
+    for (size_t k = threadIdx.x; k < rl; k += blockDim.x) {
+      const size_t o = per ? (k & 1) * mp + (k >> 1) : k;
+      dst[f * fs + i * ld + o] = (float)src[f][i * rl + k];
+    }
 }
 
 size_t smem_per_x_mixed(const CaseDev& c) {
@@ -186,14 +193,16 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     push(L);
   };
   const int mx = c.mx, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
-  // FP32 copy of the state rows, read by G1
+  // FP32 copy of the state rows, read by G1 (rows of s32_row_floats floats)
+  const int s32ld = s32_row_floats(c);
   void* s32[3];
-  for (int f = 0; f < 3; f++)
-    s32[f] = static_cast<float*>(c.m_s32) + (size_t)f * c.mxc * myc * (c.kind == KIND_PERIODIC ? 2 : 1);
+  for (int f = 0; f < 3; f++) s32[f] = static_cast<float*>(c.m_s32) + (size_t)f * c.mxc * s32ld;
   add(K_STATE_F32, c.mxc, 0);
   if (c.kind == KIND_PERIODIC) {
-    // G1: rows of ux, uy, temp (complex) -> [Y0 | Y1] (FP32), stored transposed
-    LaneSideDev in = lane_rows(s32, 3, mx, myc, myc, LT_F32, true);
+    // G1: rows of ux, uy, temp (complex, [re | im] parts) -> [Y0 | Y1] (FP32), stored transposed
+    LaneSideDev in = lane_rows(s32, 3, mx, myc, s32ld / 2, LT_F32, true);
+    in.elem_stride = 1;
+    in.part_stride = s32ld / 2;
     LaneSideDev out;
     std::memset(&out, 0, sizeof out);
     for (int f = 0; f < 3; f++) out.ptr[f] = c.m_y[f];
@@ -238,11 +247,13 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     return sd;
   };
   auto fptr = [](void* base, size_t off_floats) { return static_cast<void*>(static_cast<float*>(base) + off_floats); };
-  // G1: rows of ux, uy, temp (FP32 copy, mxc x myc) -> [Y0 | Y1] transposed (2 ny x mxc, FP32)
+  // G1: rows of ux, uy, temp (FP32 copy, mxc rows of myc) -> [Y0 | Y1] transposed (2 ny rows of
+  // mxc values, row stride pad4(mxc), FP32)
+  const int myld = pad4(mxc);
   {
     void* yo[3] = {c.m_y[0], c.m_y[1], c.m_y[2]};
-    add_gemm(make_gemm_job(lane_rows(s32, 3, mxc, myc, myc, LT_F32, false),
-                           side(yo, 3, mxc, 2 * ny, 1, mxc, LT_F32, 1), ops.y1, myc, 2 * ny, 1.0, c.status));
+    add_gemm(make_gemm_job(lane_rows(s32, 3, mxc, myc, s32ld, LT_F32, false),
+                           side(yo, 3, mxc, 2 * ny, 1, myld, LT_F32, 1), ops.y1, myc, 2 * ny, 1.0, c.status));
   }
   // GX: x stencils, derivatives and backward transforms -> physical (transposed), one launch of 4 jobs
   {
@@ -251,20 +262,20 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     L.pass = npass++;
     void* a_in[2] = {c.m_y[0], c.m_y[1]};
     void* a_out[2] = {c.m_ph[0], c.m_ph[1]};
-    L.jobs.push_back(make_gemm_job(lane_rows(a_in, 2, ny, mxc, mxc, LT_F32, false),
+    L.jobs.push_back(make_gemm_job(lane_rows(a_in, 2, ny, mxc, myld, LT_F32, false),
                                    lane_rows(a_out, 2, ny, 2 * nx, 2 * nx, LT_F32, false), ops.xa, mxc, 2 * nx, 1.0,
                                    c.status));
-    void* b_in[2] = {fptr(c.m_y[0], (size_t)ny * mxc), fptr(c.m_y[1], (size_t)ny * mxc)};
+    void* b_in[2] = {fptr(c.m_y[0], (size_t)ny * myld), fptr(c.m_y[1], (size_t)ny * myld)};
     void* b_out[2] = {c.m_ph[2], c.m_ph[3]};
-    L.jobs.push_back(make_gemm_job(lane_rows(b_in, 2, ny, mxc, mxc, LT_F32, false),
+    L.jobs.push_back(make_gemm_job(lane_rows(b_in, 2, ny, mxc, myld, LT_F32, false),
                                    lane_rows(b_out, 2, ny, nx, nx, LT_F32, false), ops.xb, mxc, nx, 1.0, c.status));
     void* c_in[1] = {c.m_y[2]};
     void* c_out[1] = {c.m_ph[4]};
-    L.jobs.push_back(make_gemm_job(lane_rows(c_in, 1, ny, mxc, mxc, LT_F32, false),
+    L.jobs.push_back(make_gemm_job(lane_rows(c_in, 1, ny, mxc, myld, LT_F32, false),
                                    lane_rows(c_out, 1, ny, nx, nx, LT_F32, false), ops.xc, mxc, nx, 1.0, c.status));
-    void* d_in[1] = {fptr(c.m_y[2], (size_t)ny * mxc)};
+    void* d_in[1] = {fptr(c.m_y[2], (size_t)ny * myld)};
     void* d_out[1] = {c.m_ph[5]};
-    L.jobs.push_back(make_gemm_job(lane_rows(d_in, 1, ny, mxc, mxc, LT_F32, false),
+    L.jobs.push_back(make_gemm_job(lane_rows(d_in, 1, ny, mxc, myld, LT_F32, false),
                                    lane_rows(d_out, 1, ny, nx, nx, LT_F32, false), ops.xd, mxc, nx, 1.0, c.status));
     size_t sm = 0;
     for (const GemmJobDev& j : L.jobs) sm = std::max(sm, gemm_smem_bytes(j.NT));
