@@ -2131,7 +2131,8 @@ struct RbcServer {
   RbcServerConfig cfg{};
   int device = 0;
   cudaStream_t stream = nullptr;  // steps
-  std::vector<cudaStream_t> branch;
+  std::vector<cudaStream_t> branch;  // low-priority graph branches (one per group)
+  cudaStream_t branch_hi = nullptr;  // the branch of the group with the most work
   std::vector<cudaEvent_t> bev;
   cudaEvent_t fork = nullptr, chunk_done = nullptr;
   std::thread th;
@@ -2363,19 +2364,44 @@ static void server_rebuild(RbcServer* S) {
     bk.d_members = A.upload(bk.members);
   }
   const size_t nb = S->buckets.size();
+  int prio_low = 0, prio_high = 0;
+  cuda_check(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high), "stream priority range");
   while (S->branch.size() < nb) {
     cudaStream_t s;
     cudaEvent_t e;
-    cuda_check(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "stream");
+    cuda_check(cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, prio_low), "stream");
     cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
     S->branch.push_back(s);
     S->bev.push_back(e);
   }
+  if (S->branch_hi == nullptr)
+    cuda_check(cudaStreamCreateWithPriority(&S->branch_hi, cudaStreamNonBlocking, prio_high), "stream");
+  // As in a batch, the group with the most work is the step's critical path
+  // and runs on a high-priority branch, so the other groups fill the SMs it
+  // leaves idle.  The set changes too often to time the groups, so the work
+  // is estimated: grid points times the per-point cost of the kind measured
+  // on the 256-case ensemble (box 0.77 ns, periodic 0.56 ns per grid point in
+  // the mixed form), times 3 for the FP64 form.  Only the schedule depends on
+  // it, not the numbers.
+  size_t critical = 0;
+  double best = -1.0;
+  for (size_t k = 0; k < nb; k++) {
+    double w = 0.0;
+    for (int m : S->buckets[k].members) {
+      const RbcParams& p = S->active[m].r.p;
+      w += (double)p.nx * p.ny * (p.kind == RBC_PERIODIC ? 0.56 : 0.77) * (p.precision == RBC_PREC_FP64 ? 3.0 : 1.0);
+    }
+    if (w > best) {
+      best = w;
+      critical = k;
+    }
+  }
+  const bool use_priority = nb > 1;
   cuda_check(cudaStreamBeginCapture(S->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t le = cudaEventRecord(S->fork, S->stream);
   for (size_t k = 0; k < nb && le == cudaSuccess; k++) {
     auto& bk = S->buckets[k];
-    cudaStream_t s = S->branch[k];
+    cudaStream_t s = (use_priority && k == critical) ? S->branch_hi : S->branch[k];
     le = cudaStreamWaitEvent(s, S->fork, 0);
     if (le == cudaSuccess) le = launch_gate(d_cases, bk.d_members, (int)bk.members.size(), s);
     for (size_t li = 0; li < bk.plan.launches.size() && le == cudaSuccess; li++)
@@ -2388,7 +2414,8 @@ static void server_rebuild(RbcServer* S) {
   cuda_check(le, "server capture");
   cuda_check(ce, "end capture");
   S->graph = g;
-  cuda_check(cudaGraphInstantiate(&S->gexec, g, 0), "graph instantiate");
+  cuda_check(cudaGraphInstantiate(&S->gexec, g, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
+             "graph instantiate");
   S->rebuilds++;
   S->dirty = false;
 }
@@ -2604,6 +2631,7 @@ int rbc_server_destroy(RbcServer* S) {
   S->ready.clear();
   S->plan_arena.reset();
   for (auto s : S->branch) cudaStreamDestroy(s);
+  if (S->branch_hi) cudaStreamDestroy(S->branch_hi);
   for (auto e : S->bev) cudaEventDestroy(e);
   cudaEventDestroy(S->fork);
   cudaEventDestroy(S->chunk_done);
