@@ -48,10 +48,13 @@ __device__ __forceinline__ int cm_off(int r, int k, int R) {
   return ((k >> 2) * (R >> 3) + (r >> 3)) * 128 + (r & 7) * 16 + (k & 3) * 4;
 }
 
+// Round to TF32 (10 mantissa bits), to nearest with ties away from zero:
+// add half a TF32 ulp to the magnitude bits and clear the 13 low bits.  A
+// carry into the exponent is the correct rounding up to the next binade (or
+// to infinity).  For finite values this is the rounding of cvt.rna.tf32.f32,
+// in two integer operations.
 __device__ __forceinline__ float tf32_rna(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r);
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
 
 __device__ __forceinline__ const char* lane_addr(const LaneSideDev& s, int l) {
