@@ -175,6 +175,45 @@ static const float* upload_op(Arena& a, const std::vector<double>& W, int rows, 
   return a.upload(pack_gemm_w(W, rows, cols, gemm_tile_n(rows)));
 }
 
+// Packed operators that depend on the size alone (the y transforms, the box's
+// x forward transform and stencil-transform products, the Poisson eigenbases)
+// are uploaded once per device and read by every case of that size: a batch of
+// many cases of a few sizes then keeps one copy of each in L2 instead of one
+// per case (every lane block of a GEMM re-reads its operator chunk by chunk).
+// They stay allocated until the process exits, a few MB per distinct size, and
+// are not counted against a serving budget.
+static std::mutex g_shared_ops_mu;
+static std::map<std::pair<int, std::string>, const float*> g_shared_ops;
+
+template <class Make>
+static const float* shared_op(const std::string& key, Make make) {
+  int dev = 0;
+  cuda_check(cudaGetDevice(&dev), "get device");
+  std::lock_guard<std::mutex> lk(g_shared_ops_mu);
+  auto it = g_shared_ops.find({dev, key});
+  if (it != g_shared_ops.end()) return it->second;
+  const std::vector<float> pk = make();
+  void* d = nullptr;
+  cuda_check(cudaMalloc(&d, pk.size() * sizeof(float)), "cudaMalloc shared operator");
+  cuda_check(cudaMemcpy(d, pk.data(), pk.size() * sizeof(float), cudaMemcpyHostToDevice), "shared operator");
+  const float* p = static_cast<const float*>(d);
+  g_shared_ops.emplace(std::make_pair(dev, key), p);
+  return p;
+}
+static std::vector<float> pack_blocks(std::initializer_list<std::pair<const LMat*, long double>> blocks) {
+  int rows = 0, cols = -1;
+  for (auto& b : blocks) {
+    rows += b.first->rows;
+    if (cols < 0) cols = b.first->cols;
+    if (cols != b.first->cols) throw std::runtime_error("pack_blocks: column mismatch");
+  }
+  std::vector<double> W((size_t)rows * cols);
+  size_t o = 0;
+  for (auto& b : blocks)
+    for (long double v : b.first->a) W[o++] = (double)(v * b.second);
+  return pack_gemm_w(W, rows, cols, gemm_tile_n(rows));
+}
+
 struct RbcCase {
   RbcParams p{};
   bool periodic = false;
@@ -394,8 +433,10 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     h.pois_bwd = A.upload(bwd);
     if (p.precision == RBC_PREC_MIXED) {
       const int mxc = nx - 2;
-      c->mops.pf = upload_op(A, fwd, mxc, mxc);
-      c->mops.pb = upload_op(A, bwd, mxc, mxc);
+      // the eigenbasis depends on the basis and the size only
+      const std::string k = "pois" + std::to_string(c->sp_p1.hb0.kind) + ":" + std::to_string(mxc);
+      c->mops.pf = shared_op(k + ":fwd", [&] { return pack_gemm_w(fwd, mxc, mxc, gemm_tile_n(mxc)); });
+      c->mops.pb = shared_op(k + ":bwd", [&] { return pack_gemm_w(bwd, mxc, mxc, gemm_tile_n(mxc)); });
     }
   }
   const size_t es = c->spec_elem();
@@ -431,8 +472,11 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     h.m_s32 = A.alloc((size_t)3 * h.mxc * s32_row_floats(h) * 4);
     h.m_bcx = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
     h.m_bcy = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
-    c->mops.y1 = upload_op(A, {{&mixed_operator(MOP_BS_CD, ny), 1.0L}, {&mixed_operator(MOP_BDS_CD, ny), 1.0L}});
-    c->mops.y2 = upload_op(A, {{&mixed_operator(MOP_FWD_23, ny), 1.0L}});
+    c->mops.y1 = shared_op("bs_bds_cd:" + std::to_string(ny), [&] {
+      return pack_blocks({{&mixed_operator(MOP_BS_CD, ny), 1.0L}, {&mixed_operator(MOP_BDS_CD, ny), 1.0L}});
+    });
+    c->mops.y2 = shared_op("fwd23:" + std::to_string(ny),
+                           [&] { return pack_blocks({{&mixed_operator(MOP_FWD_23, ny), 1.0L}}); });
     if (!per) {
       for (int k = 0; k < 6; k++) h.m_ph[k] = A.alloc((size_t)2 * nx * ny * 4);
       for (int k = 0; k < 3; k++) h.m_p[k] = A.alloc((size_t)nx * ny * 4);
@@ -443,11 +487,14 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
       const LMat& bdsu = mixed_operator(MOP_BDS_CD, nx);
       const LMat& bst = mixed_operator(tn ? MOP_BS_CN : MOP_BS_CD, nx);
       const LMat& bdst = mixed_operator(tn ? MOP_BDS_CN : MOP_BDS_CD, nx);
+      // the derivative rows carry the aspect ratio (per case); the rest depends on the size only
       c->mops.xa = upload_op(A, {{&bsu, 1.0L}, {&bdsu, inv_asp}});
-      c->mops.xb = upload_op(A, {{&bsu, 1.0L}});
+      c->mops.xb = shared_op("bs_cd:" + std::to_string(nx), [&] { return pack_blocks({{&bsu, 1.0L}}); });
       c->mops.xc = upload_op(A, {{&bdst, inv_asp}});
-      c->mops.xd = upload_op(A, {{&bst, 1.0L}});
-      c->mops.x2 = upload_op(A, {{&mixed_operator(MOP_FWD_23, nx), 1.0L}});
+      c->mops.xd = shared_op(std::string(tn ? "bs_cn:" : "bs_cd:") + std::to_string(nx),
+                             [&] { return pack_blocks({{&bst, 1.0L}}); });
+      c->mops.x2 = shared_op("fwd23:" + std::to_string(nx),
+                             [&] { return pack_blocks({{&mixed_operator(MOP_FWD_23, nx), 1.0L}}); });
     }
   }
   void* bco = A.alloc((size_t)h.mx * ny * es);
