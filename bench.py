@@ -891,6 +891,13 @@ def main():
         import torch.distributed as dist
         torch.cuda.set_device(local)
         dist.init_process_group("gloo")
+    if args.impl == "ours" and args.workload != "cpu-table":
+        # the library links its own CUDA runtime: select the rank's GPU there too
+        import rustpde_gb300 as R
+        from rustpde_gb300 import build
+        build.build()
+        R.set_device(local)
+        assert R.get_device() == local
     if args.impl == "reference":
         line = run_reference(args, rank, world)
     elif args.workload == "precision":

@@ -332,6 +332,13 @@ int rbc_dev_free(void* ptr);
 int rbc_memcpy_h2d(void* dst, const void* src, size_t bytes);
 int rbc_memcpy_d2h(void* dst, const void* src, size_t bytes);
 int rbc_device_synchronize(void);
+/* The GPU this library's calls run on, for the calling thread (the library
+ * links its own CUDA runtime, so a framework's device selection does not
+ * reach it).  Handles are created on the device current at creation and must
+ * be used with it current; a serving loop keeps the device of its creation.
+ * No reference counterpart (the reference runs on the CPU). */
+int rbc_set_device(int ordinal);
+int rbc_get_device(int* ordinal);
 
 /* ---- funspace primitives on device buffers ---------------------------------
  * Space2::new(base0, base1) (funspace/src/space2.rs:37-50) with bases

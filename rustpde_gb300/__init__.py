@@ -158,6 +158,8 @@ _SIGNATURES = {
     "rbc_memcpy_h2d": (_I, [_P, _P, _SZ]),
     "rbc_memcpy_d2h": (_I, [_P, _P, _SZ]),
     "rbc_device_synchronize": (_I, []),
+    "rbc_set_device": (_I, [_I]),
+    "rbc_get_device": (_I, [_IP]),
     "fs_space_create": (_I, [_I, _I, _I, _I, ctypes.POINTER(_P)]),
     "fs_space_destroy": (_I, [_P]),
     "fs_space_shape": (_I, [_P, _I, _IP, _IP, _IP]),
@@ -1134,6 +1136,19 @@ class Server:
 
 
 MAX_TIMESTEP = 10_000_000
+
+
+def set_device(ordinal: int):
+    """Select the GPU of this thread's library calls (rbc_set_device).  The
+    library links its own CUDA runtime, so torch.cuda.set_device does not
+    select it."""
+    _check(lib().rbc_set_device(int(ordinal)))
+
+
+def get_device() -> int:
+    d = _I()
+    _check(lib().rbc_get_device(ctypes.byref(d)))
+    return d.value
 
 
 def set_gemm_wait_limit(polls: int):

@@ -1686,6 +1686,20 @@ int rbc_device_synchronize(void) {
   cuda_check(cudaDeviceSynchronize(), "cudaDeviceSynchronize");
   API_END
 }
+int rbc_set_device(int ordinal) {
+  API_BEGIN
+  int n = 0;
+  cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+  require(ordinal >= 0 && ordinal < n, "rbc_set_device: ordinal out of range (" + std::to_string(n) + " devices)");
+  cuda_check(cudaSetDevice(ordinal), "cudaSetDevice");
+  API_END
+}
+int rbc_get_device(int* ordinal) {
+  API_BEGIN
+  require(ordinal != nullptr, "null argument");
+  cuda_check(cudaGetDevice(ordinal), "cudaGetDevice");
+  API_END
+}
 
 // ---- funspace primitives
 int fs_space_create(int base0, int n0, int base1, int n1, FsSpace** out) {
