@@ -410,7 +410,7 @@ def run_ensemble(args, rank, world, local):
                    "launches_per_step": launches, "status_nonzero_cases": status_bad},
     })
     if rank == 0 and world == 1:
-        line["serving"] = run_serving(args, args.requests, args.horizon_scale)
+        line["serving"] = run_serving(args, args.requests, args.horizon_scale, args.serving_check)
         line["cpu_baseline"] = cpu_baseline_ensemble(params, steps=args.cpu_steps)
     line["plain_fp64"] = {"value": plain_value, "ms_per_ensemble_step": plain_ms / K,
                           "how": "each case alone through rbc_step, cases one after another"}
@@ -482,7 +482,8 @@ def run_serving(args, n_requests, horizon_scale, n_check=8):
     gp_steps = sum(r["grid_points"] * r["steps"] for r in res)
     span = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
     errs_nu, errs_ke = [], []
-    for r in sorted(res, key=lambda r: r["id"])[:n_check]:
+    # the n_check cheapest results (steps x grid points) are re-run alone in FP64
+    for r in sorted(res, key=lambda r: (r["steps"] * r["grid_points"], r["id"]))[:n_check]:
         rq = ids[r["id"]]
         c = R.Navier2D(*rq.params, precision=R.PREC_FP64, seed=None)
         c.set_velocity(0.2, 1.0, 1.0)
@@ -500,7 +501,8 @@ def run_serving(args, n_requests, horizon_scale, n_check=8):
         "aggregate_grid_pt_steps_per_s": gp_steps / span, "span_s": round(span, 2),
         "graph_rebuilds": st["rebuilds"], "peak_device_gb": round(st["peak_bytes_in_use"] / 1e9, 2),
         "nu_max_rel_vs_fp64": float(max(errs_nu)), "ke_max_rel_vs_fp64": float(max(errs_ke)),
-        "checked": len(errs_nu), "horizon_scale": horizon_scale,
+        "checked": len(errs_nu), "checked_how": "the cheapest results re-run alone in FP64",
+        "horizon_scale": horizon_scale,
     }
 
 
@@ -883,6 +885,8 @@ def main():
                     help="time the batched mixed step only (profiling runs; prints a reduced line)")
     ap.add_argument("--requests", type=int, default=100, help="serving: number of requests")
     ap.add_argument("--horizon-scale", type=float, default=0.1, help="serving: horizon multiplier")
+    ap.add_argument("--serving-check", type=int, default=8,
+                    help="serving: results re-run alone in FP64 for the Nu/KE error")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = 500 if args.workload == "ensemble" else 200
@@ -912,7 +916,8 @@ def main():
     elif args.workload == "serving":
         from rustpde_gb300 import build
         build.build()
-        line = {"metric": METRIC, "workload": "serving", **run_serving(args, args.requests, args.horizon_scale)}
+        line = {"metric": METRIC, "workload": "serving",
+                **run_serving(args, args.requests, args.horizon_scale, args.serving_check)}
     else:
         args.warmup = max(args.warmup, 3)
         line = (run_ensemble if args.workload == "ensemble" else run_periodic512)(args, rank, world, local)

@@ -2413,11 +2413,19 @@ static void server_rebuild(RbcServer* S) {
     }
     S->buckets[found].members.push_back(i);
   }
+  // the forms of the FP64 passes: a CTA per lane by default; RBC_SERVER_FORM=1
+  // or 2 selects the 128-thread or the one-thread-per-sub-lane forms for
+  // every case (a case's arithmetic never depends on the other cases in any
+  // form, so results stay the same alone and in a mix)
+  int form = 0;
+  if (const char* f = std::getenv("RBC_SERVER_FORM"))
+    if (f[0] >= '1' && f[0] <= '2' && f[1] == '\0') form = f[0] - '0';
   for (auto& bk : S->buckets) {
     std::vector<const StepPlan*> plans;
     std::vector<const int*> gates;
     for (int m : bk.members) {
-      plans.push_back(&S->active[m].c->plan);
+      RbcCase* mc = S->active[m].c;
+      plans.push_back(form > 0 && (int)mc->plan_alts.size() >= form ? &mc->plan_alts[form - 1] : &mc->plan);
       gates.push_back(S->active[m].c->gate_mem + 1);
     }
     bk.plan = merge_plans(plans, bk.members, gates);
