@@ -277,7 +277,10 @@ int rbc_diag_series(const RbcCase* c, double* time, double* nu, double* nuvol, d
  * batched steps (continuous batching: requests that arrive while others run
  * join at the next chunk of chunk_steps steps).  Each finished request yields
  * a result (Nu, KE at its horizon, timestamps on the server clock).  A case
- * computes exactly the same numbers alone or in any mix. */
+ * computes exactly the same numbers alone or in any mix.  The FP64 passes run
+ * as a CTA per lane; RBC_SERVER_FORM=1 or 2 (read when the active set changes)
+ * selects the 128-thread or the one-thread-per-sub-lane forms for every case,
+ * which keeps that property. */
 typedef struct RbcServer RbcServer;
 typedef struct RbcServerConfig {
   size_t hbm_budget_bytes; /* admission budget for the cases' device memory */
