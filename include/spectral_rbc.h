@@ -185,8 +185,10 @@ const char* rbc_kernel_name(int kernel);
  * stream, so their state/diagnostic calls are ordered after rbc_batch_step.
  * Mixed-precision batches time the forms of each FP64 pass at creation and
  * keep the fastest (rbc_batch_tuning); the environment variable
- * RBC_BATCH_FORM pins the forms instead (profiling runs): one digit 0|1|2 for
- * every pass, or the list rbc_batch_tuning_forms returns.  The group
+ * RBC_BATCH_FORM pins the forms instead (profiling runs): one digit 0..3 for
+ * every pass, or the list rbc_batch_tuning_forms returns (0 a CTA per lane,
+ * 1 128-thread CTAs, 2 one thread per sub-lane, 3 the same with the periodic
+ * Y2 launches fused into one).  The group
  * whose step takes longest runs on a high-priority branch, so its thread
  * blocks are dispatched first; RBC_BATCH_PRIORITY=0 gives every branch the
  * default priority. */
@@ -223,7 +225,8 @@ int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket
 int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
                      int* n);
 /* The forms kept, one digit per decision of rbc_batch_tuning, comma-separated
- * (0: a CTA per lane, 1: 128-thread CTAs, 2: a thread per sub-lane), NUL-
+ * (0: a CTA per lane, 1: 128-thread CTAs, 2: a thread per sub-lane, 3: the
+ * same with the periodic Y2 launches fused, timed for one-group batches), NUL-
  * terminated in buf (len bytes).  Passed as RBC_BATCH_FORM it makes another
  * batch of the same cases keep the same forms, whatever its own timings say. */
 int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len);
@@ -231,6 +234,16 @@ int rbc_batch_state_bytes(const RbcBatch* b, size_t* bytes);
 int rbc_batch_state_offset(const RbcBatch* b, int i, size_t* offset);
 int rbc_batch_get_state_all(RbcBatch* b, void* host, size_t bytes);
 int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes);
+/* rbc_batch_set_state_all(host_in), rbc_batch_step(nsteps) and
+ * rbc_batch_get_state_all(host_out) in one call, with the same results, the
+ * copies pipelined: each group's cases hold one contiguous range of the state
+ * (rbc_batch_state_offset), which is copied in, stepped by that group's own
+ * graph and copied back on the group's branch, so that one group's copies
+ * overlap the other groups' steps.  Inputs are copied in the order of the
+ * groups' step times, longest first.  host_in and host_out (bytes =
+ * rbc_batch_state_bytes each, page-locked for the copies to be asynchronous)
+ * may be the same buffer; returns when host_out is written. */
+int rbc_batch_step_io(RbcBatch* b, const void* host_in, void* host_out, size_t bytes, int nsteps);
 
 /* ---- snapshots -----------------------------------------------------------------
  * Navier2D::write (navier.rs:975-1013) and Navier2D::read (navier.rs:961-972)
@@ -278,9 +291,9 @@ int rbc_diag_series(const RbcCase* c, double* time, double* nu, double* nuvol, d
  * join at the next chunk of chunk_steps steps).  Each finished request yields
  * a result (Nu, KE at its horizon, timestamps on the server clock).  A case
  * computes exactly the same numbers alone or in any mix.  The FP64 passes run
- * as a CTA per lane; RBC_SERVER_FORM=1 or 2 (read when the active set changes)
- * selects the 128-thread or the one-thread-per-sub-lane forms for every case,
- * which keeps that property. */
+ * as a CTA per lane; RBC_SERVER_FORM=1, 2 or 3 (read when the active set
+ * changes) selects another of the forms above for every case, which keeps
+ * that property. */
 typedef struct RbcServer RbcServer;
 typedef struct RbcServerConfig {
   size_t hbm_budget_bytes; /* admission budget for the cases' device memory */

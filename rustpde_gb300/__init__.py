@@ -151,6 +151,7 @@ _SIGNATURES = {
     "rbc_batch_state_offset": (_I, [_P, _I, ctypes.POINTER(_SZ)]),
     "rbc_batch_get_state_all": (_I, [_P, _P, _SZ]),
     "rbc_batch_set_state_all": (_I, [_P, _P, _SZ]),
+    "rbc_batch_step_io": (_I, [_P, _P, _P, _SZ, _I]),
     "rbc_host_alloc_pinned": (_I, [ctypes.POINTER(_P), _SZ]),
     "rbc_host_free_pinned": (_I, [_P]),
     "rbc_dev_alloc": (_I, [ctypes.POINTER(_P), _SZ]),
@@ -1066,6 +1067,20 @@ class Batch:
 
     def set_state_all(self, host):
         _check(lib().rbc_batch_set_state_all(self._h, host.ctypes.data_as(_P), host.nbytes))
+
+    def state_offset(self, i):
+        n = _SZ()
+        _check(lib().rbc_batch_state_offset(self._h, int(i), ctypes.byref(n)))
+        return n.value
+
+    def step_io(self, host_in, host_out, nsteps=1):
+        """set_state_all(host_in), update(nsteps), get_state_all(host_out) in
+        one call, each group's copies overlapping the other groups' steps
+        (rbc_batch_step_io); returns when host_out is written."""
+        if host_in.nbytes != host_out.nbytes:
+            raise ValueError("step_io: host_in and host_out differ in size")
+        _check(lib().rbc_batch_step_io(self._h, host_in.ctypes.data_as(_P), host_out.ctypes.data_as(_P),
+                                       host_in.nbytes, int(nsteps)))
 
     def __del__(self):
         h = getattr(self, "_h", None)

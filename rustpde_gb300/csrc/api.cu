@@ -591,7 +591,8 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   if (h.mixed) {
     cuda_check(configure_mixed_kernels(), "configure mixed kernels");
     c->plan = build_mixed_plan(h, c->mops, 0);
-    if (!with_graph) c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2)};
+    if (!with_graph)
+      c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2), build_mixed_plan(h, c->mops, 3)};
   } else {
     c->plan = build_step_plan(h);
   }
@@ -1159,12 +1160,17 @@ struct RbcBatch {
     std::vector<int> members;
     StepPlan plan;
     DevPlan dp;
+    size_t state_begin = 0, state_end = 0;  // the members' states: one contiguous range of d_state
+    cudaGraph_t graph = nullptr;             // one step of this group alone (rbc_batch_step_io)
+    cudaGraphExec_t gexec = nullptr;
   };
   std::vector<Bucket> buckets;
+  std::vector<size_t> io_order;  // groups in the order their inputs are copied in: longest step first
+  std::vector<cudaEvent_t> io_events;  // a group's input copy done (rbc_batch_step_io)
   struct Tuned {
     int kernel_cta, kernel_lanes;
     float ms_cta, ms_lanes;
-    int form;  // form kept: 0 CTA per lane, 1 and 2 the other plan variants
+    int form;  // form kept: 0 CTA per lane, 1 to 3 the other plan variants
   };
   std::vector<Tuned> tuning;          // autotuner decisions (rbc_batch_tuning)
   char* d_state = nullptr;            // every case's spectral state, contiguous
@@ -1175,10 +1181,16 @@ struct RbcBatch {
   int launches = 0;
   ~RbcBatch() {
     if (stream) cudaStreamSynchronize(stream);
+    for (auto& s : branch) cudaStreamSynchronize(s);
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
+    for (auto& bk : buckets) {
+      if (bk.gexec) cudaGraphExecDestroy(bk.gexec);
+      if (bk.graph) cudaGraphDestroy(bk.graph);
+    }
     for (RbcCase* c : cases) delete c;
     for (auto e : events) cudaEventDestroy(e);
+    for (auto e : io_events) cudaEventDestroy(e);
     for (auto s : branch) cudaStreamDestroy(s);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -1194,26 +1206,6 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   cuda_check(configure_prim_kernels(), "configure kernels");
   std::unique_ptr<RbcBatch> b(new RbcBatch());
   cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream create");
-  size_t sz[5];
-  for (int i = 0; i < ncases; i++) {
-    b->state_offset.push_back(b->state_bytes);
-    b->state_bytes += state_layout(params[i], sz);
-  }
-  b->d_state = static_cast<char*>(b->arena.alloc(b->state_bytes));
-  for (int i = 0; i < ncases; i++) {
-    std::unique_ptr<RbcCase> c(new RbcCase());
-    c->p = params[i];
-    c->periodic = params[i].kind == RBC_PERIODIC;
-    c->stream = b->stream;
-    c->own_stream = false;
-    c->in_batch = true;
-    build_case(c.get(), false, b->d_state + b->state_offset[i]);
-    b->cases.push_back(c.release());
-  }
-  // device table of all case descriptors
-  std::vector<CaseDev> hd;
-  for (RbcCase* c : b->cases) hd.push_back(c->hd);
-  b->d_cases = b->arena.upload(hd);
   // groups of equal kind (box / periodic) and precision, any size: one launch
   // per pass covers every case of the group
   for (int i = 0; i < ncases; i++) {
@@ -1232,6 +1224,34 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     }
     b->buckets[found].members.push_back(i);
   }
+  // the state of each group's cases is one contiguous range (group by group,
+  // cases in index order within a group), so that rbc_batch_step_io moves a
+  // group's state with one copy each way
+  size_t sz[5];
+  b->state_offset.assign(ncases, 0);
+  for (auto& bk : b->buckets) {
+    bk.state_begin = b->state_bytes;
+    for (int i : bk.members) {
+      b->state_offset[i] = b->state_bytes;
+      b->state_bytes += state_layout(params[i], sz);
+    }
+    bk.state_end = b->state_bytes;
+  }
+  b->d_state = static_cast<char*>(b->arena.alloc(b->state_bytes));
+  for (int i = 0; i < ncases; i++) {
+    std::unique_ptr<RbcCase> c(new RbcCase());
+    c->p = params[i];
+    c->periodic = params[i].kind == RBC_PERIODIC;
+    c->stream = b->stream;
+    c->own_stream = false;
+    c->in_batch = true;
+    build_case(c.get(), false, b->d_state + b->state_offset[i]);
+    b->cases.push_back(c.release());
+  }
+  // device table of all case descriptors
+  std::vector<CaseDev> hd;
+  for (RbcCase* c : b->cases) hd.push_back(c->hd);
+  b->d_cases = b->arena.upload(hd);
   for (auto& bk : b->buckets) {
     std::vector<const StepPlan*> plans;
     for (int m : bk.members) plans.push_back(&b->cases[m]->plan);
@@ -1289,13 +1309,13 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       if (ga[a].size() != gb.size()) throw std::runtime_error("autotune: plan forms of different pass structure");
     }
     // RBC_BATCH_FORM pins the forms instead (profiling runs: a profiler's
-    // per-launch overhead distorts the timings): one digit 0|1|2 for every pass
+    // per-launch overhead distorts the timings): one digit 0..3 for every pass
     // that has forms, or a comma-separated list with one digit per such pass,
     // in the order of rbc_batch_tuning
     std::vector<int> forced_list;
     if (const char* f = std::getenv("RBC_BATCH_FORM"))
       for (const char* q = f; *q; q++)
-        if (*q >= '0' && *q <= '2') forced_list.push_back(*q - '0');
+        if (*q >= '0' && *q <= '3') forced_list.push_back(*q - '0');
     StepPlan tuned;
     for (size_t pi = 0; pi < gb.size(); pi++) {
       auto group_time = [&](const StepPlan& P, const DevPlan& dp, const std::vector<size_t>& g) {
@@ -1307,6 +1327,12 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       float t_base = -1.f, t_best_alt = 1e30f;
       int best = -1, best_alt_kernel = bk.plan.launches[gb[pi][0]].kernel;
       for (size_t a = 0; a < nalt; a++) {
+        // the fused periodic Y2 form (variant 3) holds its registers through
+        // three phases; beside another group it slowed the whole step (256-case
+        // ensemble: 3.34 ms against 3.09 ms) although the pass alone was 5 %
+        // faster, and passes are timed alone here: it is timed for batches of
+        // one group only (RBC_BATCH_FORM still selects it)
+        if (a == 2 && b->buckets.size() > 1) continue;
         const auto ks = kernels_of(alts[a], ga[a][pi]);
         if (std::find(seen.begin(), seen.end(), ks) != seen.end()) continue;
         seen.push_back(ks);
@@ -1404,6 +1430,29 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   b->graph = g;
   cuda_check(cudaGraphInstantiate(&b->gexec, g, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
              "graph instantiate");
+  // rbc_batch_step_io: one graph per group, captured on the group's branch
+  // stream (its priority), and the groups' inputs copied in longest step first
+  for (size_t k = 0; k < nb; k++) {
+    auto& bk = b->buckets[k];
+    cudaStream_t s = b->branch[k];
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = cudaSuccess;
+    for (size_t li = 0; li < bk.plan.launches.size() && e == cudaSuccess; li++)
+      e = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
+    cudaGraph_t bg = nullptr;
+    const cudaError_t be = cudaStreamEndCapture(s, &bg);
+    cuda_check(e, "group capture");
+    cuda_check(be, "end capture");
+    bk.graph = bg;
+    cuda_check(cudaGraphInstantiate(&bk.gexec, bg, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
+               "graph instantiate");
+  }
+  b->io_order.resize(nb);
+  for (size_t k = 0; k < nb; k++) b->io_order[k] = k;
+  std::stable_sort(b->io_order.begin(), b->io_order.end(),
+                   [&](size_t x, size_t y) { return bucket_ms[x] > bucket_ms[y]; });
+  b->io_events.resize(nb);
+  for (auto& e : b->io_events) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
   *out = b.release();
   API_END
 }
@@ -1432,6 +1481,38 @@ int rbc_batch_step(RbcBatch* b, int nsteps) {
     cuda_check(cudaGraphLaunch(b->gexec, b->stream), "graph launch");
     for (RbcCase* c : b->cases) c->time += c->p.dt;
   }
+  API_END
+}
+int rbc_batch_step_io(RbcBatch* b, const void* host_in, void* host_out, size_t bytes, int nsteps) {
+  API_BEGIN
+  require(b && host_in && host_out && nsteps >= 0, "rbc_batch_step_io: invalid argument");
+  require(bytes == b->state_bytes, "rbc_batch_step_io: size mismatch (see rbc_batch_state_bytes)");
+  const size_t nb = b->buckets.size();
+  // after the work already queued on the batch stream; each group: its input
+  // range in (after the previous group's, so the longest step gets the link
+  // first), its steps, its output range back, on its own branch, so that one
+  // group's copies overlap the other groups' steps
+  cuda_check(cudaEventRecord(b->events[nb], b->stream), "event");
+  cudaEvent_t prev = nullptr;
+  for (size_t k : b->io_order) {
+    const auto& bk = b->buckets[k];
+    cudaStream_t s = b->branch[k];
+    const size_t o = bk.state_begin, n = bk.state_end - bk.state_begin;
+    cuda_check(cudaStreamWaitEvent(s, b->events[nb], 0), "stream wait");
+    if (prev != nullptr) cuda_check(cudaStreamWaitEvent(s, prev, 0), "stream wait");
+    cuda_check(cudaMemcpyAsync(b->d_state + o, static_cast<const char*>(host_in) + o, n, cudaMemcpyHostToDevice, s),
+               "state copy h2d");
+    cuda_check(cudaEventRecord(b->io_events[k], s), "event");
+    prev = b->io_events[k];
+    for (int t = 0; t < nsteps; t++) cuda_check(cudaGraphLaunch(bk.gexec, s), "graph launch");
+    cuda_check(cudaMemcpyAsync(static_cast<char*>(host_out) + o, b->d_state + o, n, cudaMemcpyDeviceToHost, s),
+               "state copy d2h");
+    cuda_check(cudaEventRecord(b->events[k], s), "event");
+    cuda_check(cudaStreamWaitEvent(b->stream, b->events[k], 0), "stream wait");
+  }
+  for (int t = 0; t < nsteps; t++)
+    for (RbcCase* c : b->cases) c->time += c->p.dt;
+  cuda_check(cudaStreamSynchronize(b->stream), "stream synchronize");
   API_END
 }
 int rbc_batch_synchronize(RbcBatch* b) {
@@ -2413,13 +2494,14 @@ static void server_rebuild(RbcServer* S) {
     }
     S->buckets[found].members.push_back(i);
   }
-  // the forms of the FP64 passes: a CTA per lane by default; RBC_SERVER_FORM=1
-  // or 2 selects the 128-thread or the one-thread-per-sub-lane forms for
-  // every case (a case's arithmetic never depends on the other cases in any
-  // form, so results stay the same alone and in a mix)
+  // the forms of the FP64 passes: a CTA per lane by default; RBC_SERVER_FORM=1,
+  // 2 or 3 selects the 128-thread, the one-thread-per-sub-lane or that form
+  // with the periodic Y2 launches fused, for every case (a case's arithmetic
+  // never depends on the other cases in any form, so results stay the same
+  // alone and in a mix)
   int form = 0;
   if (const char* f = std::getenv("RBC_SERVER_FORM"))
-    if (f[0] >= '1' && f[0] <= '2' && f[1] == '\0') form = f[0] - '0';
+    if (f[0] >= '1' && f[0] <= '3' && f[1] == '\0') form = f[0] - '0';
   for (auto& bk : S->buckets) {
     std::vector<const StepPlan*> plans;
     std::vector<const int*> gates;

@@ -27,6 +27,8 @@ enum StepKernel {
   K_STATE_F32,
   // the periodic FP32 x pass launched with 128 threads
   K_PER_X_MIXED_T128,
+  // the three periodic Y2 launches as one (a CTA barrier between the phases)
+  K_LP_PER_Y2F,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };

@@ -737,11 +737,11 @@ __global__ void __launch_bounds__(128) k_lp_per_y2(const CaseDev* __restrict__ c
 // the uy right-hand side reads the old temperature; Y2C moves them into the
 // state.  Same operations as k_lp_per_y2 (navier.rs:622-721).
 // ============================================================================
-// Y2A, sub = 2 * field + parity q: right-hand side, pinv rows and the row's
-// banded Helmholtz solve of one field on the columns of parity q
-__global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
-  ROW_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky, f = sub;
+// Y2A, field f, parity q: right-hand side, pinv rows and the row's banded
+// Helmholtz solve of one field on the columns of parity q
+template <int PB = kPBC>
+__device__ __forceinline__ void per_y2a_row(const CaseDev& c, const int i, const int q, const int f) {
+  const int ny = c.ny, myc = c.myc, kx = c.kx, ky = c.ky;
   const double dt = c.dt, inv_asp = 1.0 / c.aspect, kis = (double)i * inv_asp;  // ik/s
   const void* st3[3] = {c.ux, c.uy, c.temp};
   const double2* Fo = static_cast<const double2*>(st3[f]) + (size_t)i * myc;
@@ -754,11 +754,11 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
   double2* out = static_cast<double2*>(c.yw[3 + f]) + (size_t)i * ny;
   const PinvDev& pv = c.pinv_y;
   double2 r2 = c2(0.0, 0.0), r4 = c2(0.0, 0.0), g2 = c2(0.0, 0.0);
-  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPBC) {
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * PB) {
     // the batch's loads first (stencil, convection, pressure, boundary terms)
-    double2 ov[kPBC], cvv[kPBC], pk[kPBC], xv[kPBC];
+    double2 ov[PB], cvv[PB], pk[PB], xv[PB];
 #pragma unroll
-    for (int e = 0; e < kPBC; e++) {
+    for (int e = 0; e < PB; e++) {
       const int k = k0 - 2 * e;
       ov[e] = cvv[e] = pk[e] = xv[e] = c2(0.0, 0.0);
       if (k < 0) continue;
@@ -774,7 +774,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
       }
     }
 #pragma unroll
-    for (int e = 0; e < kPBC; e++) {
+    for (int e = 0; e < PB; e++) {
       const int k = k0 - 2 * e;
       if (k < 0) break;
       const double2 o = ov[e], cvk = cvv[e];
@@ -803,15 +803,19 @@ __global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ 
     }
   }
   const FdmaRow R = fdma_row(f < 2 ? c.hu_y : c.ht_y, i);
-  fdma_fwd_par<double2, kPBC>(R, out, 1, q);
-  fdma_bwd_par<double2, kPBC>(R, out, 1, q);
+  fdma_fwd_par<double2, PB>(R, out, 1, q);
+  fdma_bwd_par<double2, PB>(R, out, 1, q);
+}
+__global__ void __launch_bounds__(256) k_lp_per_y2a(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  per_y2a_row(c, lane, q, sub);
 }
 
-// Y2B, sub = parity q: divergence ik/s Sy ux* + Dy Sy uy* on parity q (from
-// uy* on parity 1 - q), pinv rows and the Poisson row solve -> p1 (p1[0,0] = 0)
-__global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
-  ROW_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc;
+// Y2B, parity q: divergence ik/s Sy ux* + Dy Sy uy* on parity q (from uy* on
+// parity 1 - q), pinv rows and the Poisson row solve -> p1 (p1[0,0] = 0)
+template <int PB = kPBCB>
+__device__ __forceinline__ void per_y2b_row(const CaseDev& c, const int i, const int q) {
+  const int ny = c.ny, myc = c.myc;
   const double inv_asp = 1.0 / c.aspect, kis = (double)i * inv_asp;  // ik/s
   const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
   const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
@@ -819,10 +823,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
   double2* p1 = static_cast<double2*>(c.p1) + (size_t)i * myc;
   const PinvDev& pv = c.pinv_y;
   double2 g2 = c2(0.0, 0.0), w2 = c2(0.0, 0.0), w4 = c2(0.0, 0.0);
-  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * kPBCB) {
-    double2 ov[kPBCB], vv[kPBCB];  // Sy ux* at k, Sy uy* at k + 1
+  for (int k0 = top_par(ny, q); k0 >= 0; k0 -= 2 * PB) {
+    double2 ov[PB], vv[PB];  // Sy ux* at k, Sy uy* at k + 1
 #pragma unroll
-    for (int e = 0; e < kPBCB; e++) {
+    for (int e = 0; e < PB; e++) {
       const int k = k0 - 2 * e;
       ov[e] = vv[e] = c2(0.0, 0.0);
       if (k < 0) continue;
@@ -830,7 +834,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
       if (k < ny - 1) vv[e] = stencil_lane<double2>(c.ycd, V, 1, k + 1);
     }
 #pragma unroll
-    for (int e = 0; e < kPBCB; e++) {
+    for (int e = 0; e < PB; e++) {
       const int k = k0 - 2 * e;
       if (k < 0) break;
       double2 g;
@@ -851,16 +855,20 @@ __global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ 
     }
   }
   const FdmaRow R = fdma_row(c.pois_y, i);
-  fdma_fwd_par<double2, kPBCB>(R, p1, 1, q);
-  fdma_bwd_par<double2, kPBCB>(R, p1, 1, q);
+  fdma_fwd_par<double2, PB>(R, p1, 1, q);
+  fdma_bwd_par<double2, PB>(R, p1, 1, q);
   if (i == 0 && q == 0) p1[0] = c2(0.0, 0.0);
 }
-
-// Y2C, sub = 2 * parity q + part: part 0: O1 = Sy^N p1, dp/dx, pres[0] and
-// ux, temperature on parity q; part 1: dp/dy on parity 1 - q and uy there
-__global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+__global__ void __launch_bounds__(256) k_lp_per_y2b(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   ROW_PROLOGUE
-  const int i = lane, ny = c.ny, myc = c.myc, part = sub;
+  per_y2b_row(c, lane, q);
+}
+
+// Y2C, parity q and part: part 0: O1 = Sy^N p1, dp/dx, pres[0] and ux,
+// temperature on parity q; part 1: dp/dy on parity 1 - q and uy there
+template <int PB = kPBCC>
+__device__ __forceinline__ void per_y2c_row(const CaseDev& c, const int i, const int q, const int part) {
+  const int ny = c.ny, myc = c.myc;
   const double inv_asp = 1.0 / c.aspect, kis = (double)i * inv_asp;  // ik/s
   const double2* p1 = static_cast<const double2*>(c.p1) + (size_t)i * myc;
   bool bad = false;
@@ -868,10 +876,10 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     double2* dpx = static_cast<double2*>(c.yw[1]) + (size_t)i * ny;
     double2* P = static_cast<double2*>(c.p0) + (size_t)i * ny;
     const double2* dvr = static_cast<const double2*>(c.yw[0]) + (size_t)i * ny;
-    for (int k0 = q; k0 < ny; k0 += 2 * kPBCC) {
-      double2 ov[kPBCC], pv0[kPBCC], dv[kPBCC];
+    for (int k0 = q; k0 < ny; k0 += 2 * PB) {
+      double2 ov[PB], pv0[PB], dv[PB];
 #pragma unroll
-      for (int e = 0; e < kPBCC; e++) {
+      for (int e = 0; e < PB; e++) {
         const int k = k0 + 2 * e;
         ov[e] = pv0[e] = dv[e] = c2(0.0, 0.0);
         if (k >= ny) continue;
@@ -880,7 +888,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
         dv[e] = dvr[k];
       }
 #pragma unroll
-      for (int e = 0; e < kPBCC; e++) {
+      for (int e = 0; e < PB; e++) {
         const int k = k0 + 2 * e;
         if (k >= ny) break;
         dpx[k] = mul_ik(ov[e], kis);
@@ -888,7 +896,7 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
         P[k] = fmas(v, ov[e], c.inv_dt);
       }
     }
-    from_ortho_par<double2, kPBCC>(c.ycd, dpx, 1, dpx, 1, q);
+    from_ortho_par<double2, PB>(c.ycd, dpx, 1, dpx, 1, q);
     const double2* U = static_cast<const double2*>(c.yw[3]) + (size_t)i * ny;
     const double2* T = static_cast<const double2*>(c.yw[5]) + (size_t)i * ny;
     double2* ux = static_cast<double2*>(c.ux) + (size_t)i * myc;
@@ -902,9 +910,9 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     }
   } else {
     double2* dpy = static_cast<double2*>(c.yw[2]) + (size_t)i * ny;
-    diff_par<double2, kPBCC>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
+    diff_par<double2, PB>(ny, 1 - q, [&](int k) { return stencil_lane<double2>(c.ycn, p1, 1, k); },
                       [&](int k, double2 d) { dpy[k] = d; });
-    from_ortho_par<double2, kPBCC>(c.ycd, dpy, 1, dpy, 1, 1 - q);
+    from_ortho_par<double2, PB>(c.ycd, dpy, 1, dpy, 1, 1 - q);
     const double2* V = static_cast<const double2*>(c.yw[4]) + (size_t)i * ny;
     double2* uy = static_cast<double2*>(c.uy) + (size_t)i * myc;
     for (int k = 1 - q; k < myc; k += 2) {
@@ -914,6 +922,36 @@ __global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ 
     }
   }
   if (bad) atomicOr(c.status, 1u);
+}
+__global__ void __launch_bounds__(256) k_lp_per_y2c(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
+  ROW_PROLOGUE
+  per_y2c_row(c, lane, q, sub);
+}
+
+// The three phases in one launch: a CTA of three 64-thread groups per work
+// item of up to 32 rows runs Y2A (group = field), then Y2B (group 0), then
+// Y2C (groups 0 and 1 = part), with a CTA barrier between the phases.  Every
+// array a phase reads is a row of this item's, written by the CTA's own
+// threads before the barrier, which makes those writes visible to it; each
+// thread does the arithmetic of the three launches (the elements loaded ahead
+// change only the order of the loads), so the results are the same.  The
+// rows' intermediates are re-read while they are still in L1/L2, and two
+// launch tails go.  Four elements ahead in every phase (128 registers) was
+// the fastest of (2..4, 2..6, 2..8) on the 256-case ensemble: 1.07 ms against
+// 1.13 ms for the three launches.
+__global__ void __launch_bounds__(3 * kLaneBlock) k_lp_per_y2f(const CaseDev* __restrict__ cases,
+                                                               const int4* __restrict__ work) {
+  const int4 w = work[blockIdx.x];
+  const CaseDev& c = cases[w.x];
+  if (c.gate != nullptr && c.gate[1] == 0) return;  // the whole CTA: no barrier is left waiting
+  const int t = (int)(threadIdx.x % kLaneBlock), grp = (int)(threadIdx.x / kLaneBlock);
+  const bool active = (t >> 1) < w.z;
+  const int lane = w.y + (t >> 1), q = t & 1;
+  if (active) per_y2a_row<4>(c, lane, q, grp);
+  __syncthreads();
+  if (active && grp == 0) per_y2b_row<4>(c, lane, q);
+  __syncthreads();
+  if (active && grp < 2) per_y2c_row<4>(c, lane, q, grp);
 }
 
 #undef LANE_PROLOGUE
@@ -936,13 +974,13 @@ int lane_kernel_subs(int kernel) {
 bool lane_kernel_rows(int kernel) {
   switch (kernel) {
     case K_LP_BOX_Y2: case K_LP_BOX_Y3: case K_LP_BOX_Y4: case K_LP_BOX_Y5:
-    case K_LP_PER_Y2A: case K_LP_PER_Y2B: case K_LP_PER_Y2C: return true;
+    case K_LP_PER_Y2A: case K_LP_PER_Y2B: case K_LP_PER_Y2C: case K_LP_PER_Y2F: return true;
     default: return false;
   }
 }
 
 cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const CaseDev* cases, const int4* work) {
-  dim3 g(nblocks, lane_kernel_subs(kernel)), b(kLaneBlock);
+  dim3 g(nblocks, lane_kernel_subs(kernel)), b(kernel == K_LP_PER_Y2F ? 3 * kLaneBlock : kLaneBlock);
   switch (kernel) {
     case K_LP_BOX_GPX: dev::k_lp_box_gpx<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_BOX_X2: dev::k_lp_box_x2<<<g, b, 0, s>>>(cases, work); break;
@@ -956,6 +994,7 @@ cudaError_t launch_lane_kernel(int kernel, int nblocks, cudaStream_t s, const Ca
     case K_LP_PER_Y2A: dev::k_lp_per_y2a<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_PER_Y2B: dev::k_lp_per_y2b<<<g, b, 0, s>>>(cases, work); break;
     case K_LP_PER_Y2C: dev::k_lp_per_y2c<<<g, b, 0, s>>>(cases, work); break;
+    case K_LP_PER_Y2F: dev::k_lp_per_y2f<<<g, b, 0, s>>>(cases, work); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

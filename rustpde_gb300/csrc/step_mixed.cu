@@ -156,7 +156,8 @@ static inline size_t clamp_smem_m(size_t s) { return (s + 127) & ~size_t(127); }
 
 StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   const bool lane_parallel = variant != 0;  // 128-thread or one-thread-per-lane forms
-  const bool lp = variant == 2;             // one-thread-per-lane forms wherever they exist
+  const bool lp = variant >= 2;             // one-thread-per-lane forms wherever they exist
+  const bool fused = variant == 3;          // ... with the periodic Y2 launches fused into one
   StepPlan p;
   // pass ids: one per pass, the same in every variant; `group` >= 0 gives the
   // following launches one shared id (a pass made of several launches)
@@ -223,12 +224,16 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     add_gemm(make_gemm_job(qi, co, ops.y2, ny, ky, 1.0, c.status));
     // Y2: FP64 right-hand sides, banded solves, projection, pressure update:
     // one CTA per row (256 or 128 threads), or three launches of one thread
-    // per (field, parity) sub-lane
+    // per (field, parity) sub-lane, or those three phases in one launch
     if (lp) {
       group = npass++;
-      add_lp(K_LP_PER_Y2A, mx, ny);
-      add_lp(K_LP_PER_Y2B, mx, ny);
-      add_lp(K_LP_PER_Y2C, mx, ny);
+      if (fused) {
+        add_lp(K_LP_PER_Y2F, mx, ny);
+      } else {
+        add_lp(K_LP_PER_Y2A, mx, ny);
+        add_lp(K_LP_PER_Y2B, mx, ny);
+        add_lp(K_LP_PER_Y2C, mx, ny);
+      }
       group = -1;
     } else {
       add(lane_parallel ? K_PER_Y2_PRE_T128 : K_PER_Y2_PRE, mx, dev::smem_per_y2_pre(c));
@@ -307,8 +312,9 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   // Each pass has up to three forms: a CTA per lane (variant 0), the same
   // kernel with 128 threads (variant 1, where it exists; otherwise the lane
   // form) and one thread per (field, parity) sub-lane (variant 2, where it
-  // exists); rbc_batch_create times the forms of every pass on the batch and
-  // keeps the fastest.
+  // exists; variant 3 differs from it in the periodic Y2 pass alone);
+  // rbc_batch_create times the forms of every pass on the batch and keeps the
+  // fastest.
   if (lane_parallel) add_lp(K_LP_BOX_GPX, ny, nx);
   else add(K_BOX_GPX, ny, dev::smem_box_gpx(c));
   if (lp) add_lp(K_LP_BOX_Y2, nx, ny);
@@ -408,6 +414,7 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
       case K_Y1_C: case K_Y1_R: v = 3 * myc * z + 6 * ny * z; break;
       case K_PER_X: v = 6 * mx * z + 2 * nx * 8 + 3 * kx * z; break;
       case K_LP_PER_Y2A:  // the three launches of the periodic Y2 pass move the Y2 arrays once
+      case K_LP_PER_Y2F:
       case K_PER_Y2: case K_PER_Y2_PRE:
         v = (kernel == K_PER_Y2 ? 3 * ny : 3 * ky) * z + 2 * 3 * myc * z + 2 * ny * z + 2 * ny * z + 12 * myc * 8 +
             myc * z;
@@ -447,7 +454,8 @@ const char* step_kernel_name(int kernel) {
                                 "lanes_box_x2", "lanes_box_x3", "lanes_box_x4", "lanes_box_y2", "lanes_box_y3",
                                 "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2", "periodic_y2_pre_t128",
                                 "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128", "lanes_periodic_y2a",
-                                "lanes_periodic_y2b", "lanes_periodic_y2c", "state_f32", "periodic_x_mixed_t128"};
+                                "lanes_periodic_y2b", "lanes_periodic_y2c", "state_f32", "periodic_x_mixed_t128",
+                                "lanes_periodic_y2_fused"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";

@@ -66,3 +66,40 @@ def test_batch_case_handles_are_borrowed(R):
     assert R.lib().rbc_step(b.cases[0]._h, 1) == R.RBC_ERR_INVALID
     assert R.lib().rbc_destroy(b.cases[0]._h) == R.RBC_ERR_INVALID
     assert R.lib().rbc_integrate(b.cases[0]._h, 1.0, 0.0, R.CALLBACK(lambda *a: 0), None, None) == R.RBC_ERR_INVALID
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_step_io_equals_set_step_get(R, precision):
+    # rbc_batch_step_io (each group copied in, stepped and copied back on its
+    # own branch) gives bitwise the state of set_state_all + update + get_state_all
+    prec = R.PREC_FP64 if precision == "fp64" else R.PREC_MIXED
+    bs = [R.Batch(PARAMS, precision=prec) for _ in range(2)]
+    for b in bs:
+        for i in range(len(PARAMS)):
+            R.standard_ic(b.cases[i], seed=30 + i)
+        b.update(1)
+        b.synchronize()
+    n = bs[0].state_bytes()
+    # each group's cases hold one contiguous range; every case has its own range
+    offs = sorted((bs[0].state_offset(i), i) for i in range(len(PARAMS)))
+    assert offs[0][0] == 0 and len({o for o, _ in offs}) == len(PARAMS)
+    kinds = [PARAMS[i][6] == 2 for _, i in offs]
+    assert kinds == sorted(kinds) or kinds == sorted(kinds, reverse=True)
+    start = R.PinnedArray((n,), np.uint8)
+    bs[0].get_state_all(start.array)
+    ref = R.PinnedArray((n,), np.uint8)
+    bs[0].set_state_all(start.array)
+    bs[0].update(3)
+    bs[0].get_state_all(ref.array)
+    out = R.PinnedArray((n,), np.uint8)
+    bs[1].step_io(start.array, out.array, 3)
+    assert np.array_equal(ref.array, out.array)
+    for i in range(len(PARAMS)):
+        assert bs[0].cases[i].get_time() == bs[1].cases[i].get_time()
+        for f in FIELDS:
+            assert np.array_equal(bs[0].cases[i].get(f), bs[1].cases[i].get(f)), (i, f)
+    # in place (host_in is host_out), one step
+    bs[1].step_io(out.array, out.array, 1)
+    bs[0].update(1)
+    bs[0].get_state_all(ref.array)
+    assert np.array_equal(ref.array, out.array)

@@ -140,7 +140,7 @@ def test_mixed_batch_forms_replay(R, monkeypatch):
     # step: bitwise the same numbers
     b1 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     forms = b1.tuning_forms()
-    assert forms and all(ch in "012," for ch in forms), forms
+    assert forms and all(ch in "0123," for ch in forms), forms
     monkeypatch.setenv("RBC_BATCH_FORM", forms)
     b2 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     assert b2.tuning_forms() == forms
@@ -152,6 +152,26 @@ def test_mixed_batch_forms_replay(R, monkeypatch):
     for i in range(len(MIX_PARAMS)):
         for f in FIELDS:
             assert np.array_equal(b1.cases[i].get(f), b2.cases[i].get(f)), (i, f)
+
+
+def test_periodic_y2_fused_form_bitwise(R, monkeypatch):
+    # form 3 is form 2 with the periodic Y2 pass's three launches run as one
+    # (a CTA barrier between the phases): each thread does the same
+    # arithmetic, so the numbers are bitwise the same
+    params = MIX_PARAMS + [(45, 33, 1e5, 1.0, 5e-3, 1.0, O.PERIODIC)]
+    out = []
+    for form in ("2", "3"):
+        monkeypatch.setenv("RBC_BATCH_FORM", form)
+        b = R.Batch(params, precision=R.PREC_MIXED)
+        for i in range(len(params)):
+            R.standard_ic(b.cases[i], seed=80 + i)
+        b.update(4)
+        b.synchronize()
+        assert all(b.cases[i].status() == 0 for i in range(len(params)))
+        out.append([[b.cases[i].get(f) for f in FIELDS] for i in range(len(params))])
+    for i in range(len(params)):
+        for k, f in enumerate(FIELDS):
+            assert np.array_equal(out[0][i][k], out[1][i][k]), (i, f)
 
 
 def test_mixed_batch_one_call_equals_single_steps(R, monkeypatch):

@@ -71,6 +71,22 @@ def test_served_equals_single_case(R):
         assert c.eval(R.NU) == r["nu"] and c.eval(R.KE) == r["ke"]
 
 
+def test_fused_y2_form_served(R, monkeypatch):
+    # RBC_SERVER_FORM=3 runs the periodic Y2 pass as one launch, gated per
+    # case like the three launches of form 2 (the short request finishes while
+    # its group still runs): bitwise the same results
+    reqs = [((128, 65, 1e6, 1.0, 4e-3, 2.0, 2, 1), 0.07, 16), ((64, 33, 1e5, 1.0, 5e-3, 1.0, 2, 1), 0.02, 17),
+            ((64, 64, 1e5, 1.0, 0.02, 1.0, 0, 1), 0.1, 18)]
+    out = {}
+    for form in ("2", "3"):
+        monkeypatch.setenv("RBC_SERVER_FORM", form)
+        out[form], _ = serve(R, reqs)
+    for a, b in zip(out["2"], out["3"]):
+        assert a["status"] == 0 and b["status"] == 0
+        for key in ("nu", "ke", "sim_time"):
+            assert a[key] == b[key], (key, a[key], b[key])
+
+
 def test_budget_rejection(R):
     srv = R.Server(hbm_budget_bytes=1 << 20, max_active=4, chunk_steps=2)
     rid = srv.submit((64, 64, 1e5, 1.0, 0.02, 1.0, 0), 0.1, 1)
