@@ -240,7 +240,7 @@ int rbc_batch_set_state_all(RbcBatch* b, const void* host, size_t bytes);
  * (rbc_batch_state_offset), which is copied in, stepped by that group's own
  * graph and copied back on the group's branch, so that one group's copies
  * overlap the other groups' steps.  Inputs are copied in the order of the
- * groups' step times, longest first.  host_in and host_out (bytes =
+ * groups' step times, shortest first.  host_in and host_out (bytes =
  * rbc_batch_state_bytes each, page-locked for the copies to be asynchronous)
  * may be the same buffer; returns when host_out is written. */
 int rbc_batch_step_io(RbcBatch* b, const void* host_in, void* host_out, size_t bytes, int nsteps);

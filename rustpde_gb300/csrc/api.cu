@@ -1165,7 +1165,7 @@ struct RbcBatch {
     cudaGraphExec_t gexec = nullptr;
   };
   std::vector<Bucket> buckets;
-  std::vector<size_t> io_order;  // groups in the order their inputs are copied in: longest step first
+  std::vector<size_t> io_order;  // groups in the order their inputs are copied in: shortest step first
   std::vector<cudaEvent_t> io_events;  // a group's input copy done (rbc_batch_step_io)
   struct Tuned {
     int kernel_cta, kernel_lanes;
@@ -1431,7 +1431,11 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   cuda_check(cudaGraphInstantiate(&b->gexec, g, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
              "graph instantiate");
   // rbc_batch_step_io: one graph per group, captured on the group's branch
-  // stream (its priority), and the groups' inputs copied in longest step first
+  // stream (its priority), and the groups' inputs copied in shortest step
+  // first: that group computes while the longer group's input arrives, and
+  // its results go back while the longer group still runs (256-case ensemble:
+  // 4.32 ms per step against 4.78 ms longest first, 5.3 ms with the copies
+  // and the step in sequence)
   for (size_t k = 0; k < nb; k++) {
     auto& bk = b->buckets[k];
     cudaStream_t s = b->branch[k];
@@ -1450,7 +1454,7 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   b->io_order.resize(nb);
   for (size_t k = 0; k < nb; k++) b->io_order[k] = k;
   std::stable_sort(b->io_order.begin(), b->io_order.end(),
-                   [&](size_t x, size_t y) { return bucket_ms[x] > bucket_ms[y]; });
+                   [&](size_t x, size_t y) { return bucket_ms[x] < bucket_ms[y]; });
   b->io_events.resize(nb);
   for (auto& e : b->io_events) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
   *out = b.release();
@@ -1489,9 +1493,9 @@ int rbc_batch_step_io(RbcBatch* b, const void* host_in, void* host_out, size_t b
   require(bytes == b->state_bytes, "rbc_batch_step_io: size mismatch (see rbc_batch_state_bytes)");
   const size_t nb = b->buckets.size();
   // after the work already queued on the batch stream; each group: its input
-  // range in (after the previous group's, so the longest step gets the link
-  // first), its steps, its output range back, on its own branch, so that one
-  // group's copies overlap the other groups' steps
+  // range in (after the previous group's: shortest step first), its steps,
+  // its output range back, on its own branch, so that one group's copies
+  // overlap the other groups' steps
   cuda_check(cudaEventRecord(b->events[nb], b->stream), "event");
   cudaEvent_t prev = nullptr;
   for (size_t k : b->io_order) {
