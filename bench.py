@@ -865,6 +865,8 @@ def run_profile_step(args):
     cu.lib.cudaProfilerStart.argtypes = []
     cu.lib.cudaProfilerStop.argtypes = []
     params = draw_ensemble(args.cases, ENSEMBLE_SEED)
+    if args.periodic_only:  # the ensemble's periodic cases alone: a batch of one group
+        params = [p for p in params if p[6] == R.PERIODIC]
     B = R.Batch(params, precision=R.PREC_MIXED)
     for i, c in enumerate(B.cases):
         R.standard_ic(c, seed=1000 + i)
@@ -875,7 +877,8 @@ def run_profile_step(args):
     B.synchronize()
     cu.lib.cudaProfilerStop()
     nb, launches = B.layout()
-    return {"workload": "profile-step", "cases": len(params), "warmup": args.warmup, "launches_in_step": launches,
+    return {"workload": "profile-step" + (" (periodic cases)" if args.periodic_only else ""), "cases": len(params),
+            "warmup": args.warmup, "launches_in_step": launches,
             "autotuner_forms": B.tuning_forms(), "status_max": max(c.status() for c in B.cases)}
 
 
@@ -893,6 +896,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=505,
                     help="ensemble: steps of the mixed-vs-FP64 comparison (the configuration's horizon)")
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
+    ap.add_argument("--periodic-only", action="store_true",
+                    help="profile-step: the ensemble's periodic cases alone (one group)")
     ap.add_argument("--skip-plain", action="store_true",
                     help="time the batched mixed step only (profiling runs; prints a reduced line)")
     ap.add_argument("--requests", type=int, default=100, help="serving: number of requests")
