@@ -79,7 +79,16 @@ const char* rbc_version(void);
 /* ---- case lifecycle ------------------------------------------------------
  * Replaces Navier2D::new (navier.rs:219-307) and Navier2D::new_periodic
  * (navier.rs:384-467).  The state starts at zero; the reference's unseeded
- * random_disturbance(0.1) is available seeded as rbc_random_disturbance. */
+ * random_disturbance(0.1) is available seeded as rbc_random_disturbance.
+ * Sizes: ny in [8, 4097], nx in [8, 4097] (box) or [8, 8192] (periodic), and
+ * within those, what the step's passes can hold: a pass keeps the lanes it
+ * transforms in a block's shared memory.  Where a Chebyshev axis's FFT form
+ * would not fit, the dense transform is used (the same transform as an n x n
+ * product); a case that fits in no form is refused at once with
+ * RBC_ERR_INVALID, naming the pass and the bytes it needs.  On a GB300
+ * (227 KB per block) the FP64 step runs periodic cases up to nx = 1208 and
+ * ny = 631 and boxes up to nx = 906 (ny = 1707); the mixed form periodic
+ * cases up to nx = 2418 and ny = 726, and boxes up to 1707 x 1707. */
 int rbc_create(const RbcParams* params, RbcCase** out);
 int rbc_destroy(RbcCase* c);
 /* nu, ka, ra, pr, dt, scale_x, scale_y (navier.rs:46-55 get_nu/get_ka) */
@@ -373,6 +382,10 @@ int rbc_get_device(int* ordinal);
 #define FS_ORTHO 2
 
 typedef struct FsSpace FsSpace;
+/* Lengths n0, n1 in [4, 8192]; a space whose lanes (with the transforms' work
+ * elements) do not fit a block's shared memory is refused with
+ * RBC_ERR_INVALID (on a GB300: Chebyshev lengths up to 3628, FourierR2c up
+ * to 2902 even and 2419 odd). */
 int fs_space_create(int base0, int n0, int base1, int n1, FsSpace** out);
 int fs_space_destroy(FsSpace* s);
 int fs_space_shape(const FsSpace* s, int which, int* n0, int* n1, int* is_complex);

@@ -61,6 +61,7 @@ def lib():
                 "or_last_error": (ctypes.c_char_p, []),
                 "or_num_threads": (I, []),
                 "or_set_threads": (None, [I]),
+                "or_set_dense_dct": (None, [I]),
                 "or_navier_new": (P, [I, I, D, D, D, D, I]),
                 "or_navier_free": (None, [P]),
                 "or_navier_tensor_pending": (I, [P, IP]),
@@ -155,6 +156,13 @@ def set_threads(n: int) -> None:
 
 def num_threads() -> int:
     return lib().or_num_threads()
+
+
+def set_dense_dct(n: int) -> None:
+    """DCT-I of length n by its defining sum instead of the FFT (-1: none):
+    an exact restatement of the same transform with other rounding, for
+    measuring a case's sensitivity to the transform's rounding."""
+    lib().or_set_dense_dct(int(n))
 
 
 # ---------------------------------------------------------------------------

@@ -26,6 +26,7 @@
 // (LAPACK geev, the same routine ndarray-linalg calls), see or_*_tensor_* below.
 //
 // Build: -O3 -ffp-contract=off (the reference does not contract a*b+c into FMA).
+#include <atomic>
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -192,10 +193,27 @@ static std::shared_ptr<FFT> get_fft(int n) {
   return cache.back();
 }
 
+// Length whose DCT-I runs as its defining sum instead of through the FFT
+// (or_set_dense_dct; -1: none).  Both are exact restatements of the same
+// transform; tests use the pair to measure how much a case's results move
+// with the transform's rounding alone.
+static std::atomic<int> g_dense_dct_n{-1};
+
 // DCT-I (REDFT00, unnormalised): X_k = x_0 + (-1)^k x_N + 2 sum_{j=1}^{N-1} x_j cos(pi j k / N)
 static void dct1(const double* x, double* X, int n) {
   int N = n - 1;
   if (N < 1) { X[0] = x[0]; return; }
+  if (n == g_dense_dct_n.load(std::memory_order_relaxed)) {
+    for (int k = 0; k <= N; k++) {
+      double acc = 0.0;
+      for (int j = 0; j <= N; j++) {
+        const long r = ((long)j * k) % (2L * N);  // the angle pi j k / N reduced exactly
+        acc += ((j == 0 || j == N) ? 1.0 : 2.0) * x[j] * std::cos(M_PI * (double)r / (double)N);
+      }
+      X[k] = acc;
+    }
+    return;
+  }
   auto f = get_fft(2 * N);
   thread_local std::vector<cplx> a, b;
   a.resize(2 * N); b.resize(2 * N);
@@ -1483,6 +1501,7 @@ void or_set_threads(int n) {
   (void)n;
 #endif
 }
+void or_set_dense_dct(int n) { g_dense_dct_n.store(n); }
 
 // ---- Navier2D ------------------------------------------------------------
 // kind: 0 box adiabatic (Navier2D::new, adiabatic=true), 1 box conducting,

@@ -39,6 +39,7 @@ int set_last_error(int code, const std::string& m) { return fail(code, m); }
 #define API_END                                              \
   }                                                          \
   catch (ApiError & e) { return fail(e.code, e.what()); }    \
+  catch (SizeError & e) { return fail(RBC_ERR_INVALID, e.what()); } \
   catch (std::bad_alloc&) { return fail(RBC_ERR_NOMEM, "host allocation failed"); } \
   catch (std::exception & e) {                               \
     std::string w = e.what();                                \
@@ -411,6 +412,35 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     h.pinv_x = upload_pinv(A, nx);
     h.cx = c->sp_u.c0;
   }
+  // Shared memory of the step's CTA passes, before the set-up work (a size
+  // the kernels cannot run is refused at once).  A Chebyshev transform through
+  // an FFT keeps 2(n-1) complex work elements per lane there; where a pass
+  // then exceeds the device's limit, that axis uses the dense transform (an
+  // n x n product per lane), x first (the box x pass holds the most lanes).
+  // Only sizes and transform forms enter those amounts.
+  {
+    CaseDev hs = h;
+    hs.mixed = p.precision == RBC_PREC_MIXED;
+    auto need_of = [&](int* kernel) {
+      if (hs.mixed) return mixed_plan_smem(hs, kernel);
+      size_t m = 0;
+      for (const StepLaunch& L : build_step_plan(hs).launches)
+        if (L.smem > m) { m = L.smem; *kernel = L.kernel; }
+      return m;
+    };
+    int kern = -1;
+    for (int axis = per ? 1 : 0; axis < 2 && need_of(&kern) > smem_limit(); axis++) {
+      ChebXformDev& cx = axis == 0 ? h.cx : h.cy;
+      if (!cx.use_fft) continue;
+      cx = upload_cheb(A, axis == 0 ? nx : ny, false);
+      (axis == 0 ? hs.cx : hs.cy) = cx;
+    }
+    const size_t need = need_of(&kern);
+    if (need > smem_limit())
+      throw SizeError("rbc_create: a " + std::to_string(nx) + " x " + std::to_string(ny) + " case needs " +
+                      std::to_string(need) + " bytes of shared memory per block in its " + step_kernel_name(kern) +
+                      " pass; this device allows " + std::to_string(smem_limit()));
+  }
   const double s0 = std::pow(c->scale[0], 2.0), s1 = std::pow(c->scale[1], 2.0);
   const double cu[2] = {p.dt * c->nu / s0, p.dt * c->nu / s1};
   const double ct[2] = {p.dt * c->ka / s0, p.dt * c->ka / s1};
@@ -588,14 +618,35 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   }
   // ---- step plan, work tables and the CUDA graph of one update()
   cuda_check(configure_step_kernels(), "configure step kernels");
-  if (h.mixed) {
-    cuda_check(configure_mixed_kernels(), "configure mixed kernels");
-    c->plan = build_mixed_plan(h, c->mops, 0);
-    if (!with_graph)
-      c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2), build_mixed_plan(h, c->mops, 3)};
-  } else {
-    c->plan = build_step_plan(h);
-  }
+  if (h.mixed) cuda_check(configure_mixed_kernels(), "configure mixed kernels");
+  auto make_plans = [&]() {
+    if (h.mixed) {
+      c->plan = build_mixed_plan(h, c->mops, 0);
+      if (!with_graph)
+        c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2),
+                        build_mixed_plan(h, c->mops, 3)};
+    } else {
+      c->plan = build_step_plan(h);
+    }
+  };
+  // the largest shared-memory working set of a launch (and its kernel)
+  auto plan_smem = [&](int* kernel) {
+    size_t m = 0;
+    auto scan = [&](const StepPlan& P) {
+      for (const StepLaunch& L : P.launches)
+        if (L.smem > m) { m = L.smem; *kernel = L.kernel; }
+    };
+    scan(c->plan);
+    for (const StepPlan& P : c->plan_alts) scan(P);
+    return m;
+  };
+  make_plans();
+  int kern = -1;
+  const size_t need = plan_smem(&kern);  // checked before the set-up (above); the plans are the same
+  if (need > smem_limit())
+    throw SizeError("rbc_create: a " + std::to_string(nx) + " x " + std::to_string(ny) + " case needs " +
+                    std::to_string(need) + " bytes of shared memory per block in its " + step_kernel_name(kern) +
+                    " pass; this device allows " + std::to_string(smem_limit()));
   if (!with_graph) return;
   capture_graph(c);
 }

@@ -115,13 +115,13 @@ static int ilog2(int v) {
   return r;
 }
 
-ChebXformDev upload_cheb(Arena& a, int n) {
+ChebXformDev upload_cheb(Arena& a, int n, bool allow_fft) {
   ChebXformDev d;
   std::memset(&d, 0, sizeof d);
   d.n = n;
   int N = n - 1;
   d.inv_nm1 = 1.0 / (double)(n - 1);
-  d.use_fft = (N >= 2 && is_pow2(N)) ? 1 : 0;
+  d.use_fft = (allow_fft && N >= 2 && is_pow2(N)) ? 1 : 0;
   if (d.use_fft) {
     d.L = 2 * N;
     d.log2L = ilog2(d.L);
@@ -203,6 +203,8 @@ FdmaDev upload_fdma(Arena& a, const std::vector<Band4>& rows) {
   return d;
 }
 
+static size_t space_pass_smem(const SpaceDev& s);
+
 void build_space(Arena& a, SpaceDev& s, int kind0, int n0, int kind1, int n1) {
   if (kind1 == FOURIER) throw std::runtime_error("FourierR2c is supported along axis 0 only");
   s.hb0 = make_basis(kind0, n0);
@@ -216,6 +218,18 @@ void build_space(Arena& a, SpaceDev& s, int kind0, int n0, int kind1, int n1) {
   s.phys0 = n0; s.phys1 = n1;
   s.spec0 = s.hb0.m; s.spec1 = s.hb1.m;
   s.ortho0 = s.hb0.ortho_len(); s.ortho1 = s.hb1.ortho_len();
+  // a DCT-I through an FFT needs 2(n-1) complex work elements per lane in
+  // shared memory; where a pass would then exceed the device's limit, the
+  // dense form of the transform (an n x n product per lane) is used instead
+  if (space_pass_smem(s) > smem_limit()) {
+    if (!s.cplx && s.c0.use_fft) s.c0 = upload_cheb(a, n0, false);
+    if (s.c1.use_fft) s.c1 = upload_cheb(a, n1, false);
+  }
+  const size_t need = space_pass_smem(s);
+  if (need > smem_limit())
+    throw SizeError("space of lengths " + std::to_string(n0) + " x " + std::to_string(n1) + " needs " +
+                    std::to_string(need) + " bytes of shared memory per block for its lanes; this device allows " +
+                    std::to_string(smem_limit()));
 }
 
 Band4 adi_factor(const HostBasis& b, double c) {
@@ -574,6 +588,9 @@ static void run_pass(PassDesc& d, cudaStream_t st) {
   cuda_check(cudaGetLastError(), "pass kernel launch");
 }
 
+static PassDesc base_desc(const SpaceDev& s);
+static size_t space_pass_smem(const SpaceDev& s) { return pass_smem(base_desc(s)); }
+
 static PassDesc base_desc(const SpaceDev& s) {
   PassDesc d;
   std::memset(&d, 0, sizeof d);
@@ -855,12 +872,20 @@ void diffusion_step(const SolverDev& sv, const SpaceDev& s, void* vhat, const vo
   }
 }
 
+static PassDesc lanes_desc(const LanesDev& L);
+
 void build_lanes(Arena& a, LanesDev& L, int kind, int n) {
   if (kind != CHEB && kind != CD && kind != CN) throw std::runtime_error("lanes: Chebyshev-family bases only");
   L.hb = make_basis(kind, n);
   L.b = upload_basis(a, L.hb);
   L.cx = upload_cheb(a, n);
   L.has_solver = false;
+  // the dense transform where the FFT form's work lanes do not fit (as for spaces)
+  if (pass_smem(lanes_desc(L)) > smem_limit() && L.cx.use_fft) L.cx = upload_cheb(a, n, false);
+  const size_t need = pass_smem(lanes_desc(L));
+  if (need > smem_limit())
+    throw SizeError("lanes of length " + std::to_string(n) + " need " + std::to_string(need) +
+                    " bytes of shared memory per block; this device allows " + std::to_string(smem_limit()));
 }
 
 void lanes_set_hholtz(Arena& a, LanesDev& L, double c) {
@@ -948,10 +973,25 @@ void sum_squares(const double* v, size_t n, double* out, cudaStream_t st) {
   cuda_check(cudaGetLastError(), "sum_squares");
 }
 
+size_t smem_limit() {
+  static size_t lim = 0;
+  if (lim == 0) {
+    int d = 0, v = 0;
+    if (cudaGetDevice(&d) == cudaSuccess &&
+        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, d) == cudaSuccess && v > 0)
+      lim = (size_t)v;
+    else {
+      cudaGetLastError();  // leave no error behind for the next launch check
+      lim = 200 * 1024;
+    }
+  }
+  return lim;
+}
+
 cudaError_t configure_prim_kernels() {
   static bool done = false;
   if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(dev::k_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(dev::k_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit());
   if (e == cudaSuccess) done = true;
   return e;
 }

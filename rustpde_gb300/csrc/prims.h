@@ -8,6 +8,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -47,9 +48,20 @@ class Arena {
 
 void cuda_check(cudaError_t e, const char* what);  // throws std::runtime_error
 
+// A size the kernels cannot run: a lane or a case whose shared-memory working
+// set per block exceeds what the device allows (the C ABI reports it as
+// RBC_ERR_INVALID).
+struct SizeError : std::runtime_error {
+  using std::runtime_error::runtime_error;
+};
+// Dynamic shared memory a block may use on this device (the opt-in maximum,
+// which the library's kernels are configured for), bytes.
+size_t smem_limit();
+
 // Device tables of one basis along one axis.
 BasisDev upload_basis(Arena& a, const HostBasis& b);
-ChebXformDev upload_cheb(Arena& a, int n);
+// allow_fft = false: the dense form even where n - 1 is a power of two
+ChebXformDev upload_cheb(Arena& a, int n, bool allow_fft = true);
 FourierXformDev upload_fourier(Arena& a, int n);
 PinvDev upload_pinv(Arena& a, int n);
 FdmaDev upload_fdma(Arena& a, const std::vector<Band4>& rows);  // swept factors, one per row

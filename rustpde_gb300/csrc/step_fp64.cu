@@ -12,6 +12,7 @@
 // Each launch takes a table of work items (case, first lane, lane count); a
 // batch of cases is the same launch with a longer table.
 #include "lane_ops.cuh"
+#include "prims.h"
 #include "step_fp64.h"
 
 #include <algorithm>
@@ -986,7 +987,7 @@ static inline size_t clamp_smem(size_t s) { return (s + 127) & ~size_t(127); }
 cudaError_t configure_step_kernels() {
   static bool done = false;
   if (done) return cudaSuccess;
-  const int big = 200 * 1024;
+  const int big = (int)smem_limit();
   cudaError_t e;
 #define SET_ATTR(k)                                                                          \
   e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, big);             \

@@ -47,6 +47,8 @@ struct StepPlan {
 
 cudaError_t configure_step_kernels();
 StepPlan build_step_plan(const CaseDev& c);
+// largest dynamic shared memory of a launch of the mixed-precision plan (and its kernel)
+size_t mixed_plan_smem(const CaseDev& c, int* kernel);
 
 // Operators of the mixed-precision step (packed tensor-core operands, device).
 struct MixedOps {

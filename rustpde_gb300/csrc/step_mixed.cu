@@ -14,6 +14,7 @@
 //  periodic:  G1 (y, GEMM) -> X (FP32) -> G2 (y, GEMM) -> Y2 (FP64)
 #include "lane_ops.cuh"
 #include "lane_ops_f32.cuh"
+#include "prims.h"
 #include "step_fp64.h"
 
 #include <algorithm>
@@ -349,10 +350,30 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   return p;
 }
 
+// Largest dynamic shared memory of the CTA passes of build_mixed_plan(c, ops,
+// 0) (its other variants use less), from the sizes and transform forms alone;
+// *kernel receives that pass.  The lane kernels and the GEMMs use none or a
+// fixed amount.
+size_t mixed_plan_smem(const CaseDev& c, int* kernel) {
+  std::vector<std::pair<int, size_t>> k;
+  if (c.kind == KIND_PERIODIC) {
+    k = {{K_PER_X_MIXED, dev::smem_per_x_mixed(c)}, {K_PER_Y2_PRE, dev::smem_per_y2_pre(c)}};
+  } else {
+    k = {{K_BOX_GPX, dev::smem_box_gpx(c)}, {K_BOX_Y2_PRE, dev::smem_box_y2(c)}, {K_BOX_X2, dev::smem_box_x2(c)},
+         {K_BOX_Y3, dev::smem_box_y3(c)},  {K_BOX_X3_MIX, dev::smem_box_x3(c)}, {K_BOX_Y4, dev::smem_box_y4(c)},
+         {K_BOX_X4_MIX, dev::smem_box_x4(c)}, {K_BOX_Y5, dev::smem_box_y5(c)}};
+  }
+  size_t m = 0;
+  for (const auto& e : k)
+    if (clamp_smem_m(e.second) > m) { m = clamp_smem_m(e.second); *kernel = e.first; }
+  return m;
+}
+
 cudaError_t configure_mixed_kernels() {
   static bool done = false;
   if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(dev::k_per_x_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaError_t e = cudaFuncSetAttribute(dev::k_per_x_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem_limit());
   if (e != cudaSuccess) return e;
   e = configure_gemm_kernels();
   if (e == cudaSuccess) done = true;

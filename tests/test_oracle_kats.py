@@ -330,3 +330,22 @@ def test_conv_term_analytic():
                          ((0, 1), np.sin(ax * x)[:, None] * -ay * np.sin(ay * y)[None, :])):
         conv = ux * fsp.backward(tsp.gradient(th, deriv))
         close(conv, exact * ux, 1e-3)
+
+
+@pytest.mark.parametrize("n", [4, 17, 33, 64, 129])
+def test_dense_dct_switch_is_the_same_transform(n):
+    # or_set_dense_dct: DCT-I of length n by its defining sum instead of the
+    # FFT; the two agree to rounding (the switch only measures a case's
+    # sensitivity to the transform's rounding)
+    x = np.random.default_rng(n).standard_normal(n)
+    ref = O.base_forward(O.CHEB, n, x)
+    refb = O.base_backward(O.CHEB, n, x)
+    O.set_dense_dct(n)
+    try:
+        d = O.base_forward(O.CHEB, n, x)
+        db = O.base_backward(O.CHEB, n, x)
+    finally:
+        O.set_dense_dct(-1)
+    close(d, ref, 1e-13 * np.max(np.abs(ref)))
+    close(db, refb, 1e-13 * np.max(np.abs(refb)))
+    assert np.array_equal(O.base_forward(O.CHEB, n, x), ref)
