@@ -1496,9 +1496,9 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       e = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
     cudaGraph_t bg = nullptr;
     const cudaError_t be = cudaStreamEndCapture(s, &bg);
+    bk.graph = bg;  // freed by the destructor whatever follows
     cuda_check(e, "group capture");
     cuda_check(be, "end capture");
-    bk.graph = bg;
     cuda_check(cudaGraphInstantiate(&bk.gexec, bg, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
                "graph instantiate");
   }
