@@ -194,10 +194,13 @@ const char* rbc_kernel_name(int kernel);
  * stream, so their state/diagnostic calls are ordered after rbc_batch_step.
  * Mixed-precision batches time the forms of each FP64 pass at creation and
  * keep the fastest (rbc_batch_tuning); the environment variable
- * RBC_BATCH_FORM pins the forms instead (profiling runs): one digit 0..3 for
- * every pass, or the list rbc_batch_tuning_forms returns (0 a CTA per lane,
- * 1 128-thread CTAs, 2 one thread per sub-lane, 3 the same with the periodic
- * Y2 launches fused into one).  The group
+ * RBC_BATCH_FORM pins the forms instead (profiling runs): the string
+ * rbc_batch_tuning_forms returns, "<FP64 passes>[;<GEMM passes>]", each part
+ * one digit for all its passes or a comma-separated digit per pass.  FP64
+ * passes: 0 a CTA per lane, 1 128-thread CTAs, 2 one thread per sub-lane,
+ * 3 the same with the periodic Y2 launches fused into one.  GEMM passes:
+ * 0 output tiles of up to 64 columns, 4 up to 128 (all 0 without the second
+ * part).  The group
  * whose step takes longest runs on a high-priority branch, so its thread
  * blocks are dispatched first; RBC_BATCH_PRIORITY=0 gives every branch the
  * default priority. */
@@ -233,9 +236,11 @@ int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket
  * rbc_kernel_name). */
 int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
                      int* n);
-/* The forms kept, one digit per decision of rbc_batch_tuning, comma-separated
- * (0: a CTA per lane, 1: 128-thread CTAs, 2: a thread per sub-lane, 3: the
- * same with the periodic Y2 launches fused, timed for one-group batches), NUL-
+/* The forms kept, one digit per decision of rbc_batch_tuning, comma-separated,
+ * the FP64 passes' first and then, after a ';', the GEMM passes' (FP64: 0 a
+ * CTA per lane, 1 128-thread CTAs, 2 a thread per sub-lane, 3 the same with
+ * the periodic Y2 launches fused, timed for one-group batches; GEMM: 0
+ * 64-output tiles, 4 128-output tiles), NUL-
  * terminated in buf (len bytes).  Passed as RBC_BATCH_FORM it makes another
  * batch of the same cases keep the same forms, whatever its own timings say. */
 int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len);
@@ -300,7 +305,7 @@ int rbc_diag_series(const RbcCase* c, double* time, double* nu, double* nuvol, d
  * join at the next chunk of chunk_steps steps).  Each finished request yields
  * a result (Nu, KE at its horizon, timestamps on the server clock).  A case
  * computes exactly the same numbers alone or in any mix.  The FP64 passes run
- * as a CTA per lane; RBC_SERVER_FORM=1, 2 or 3 (read when the active set
+ * as a CTA per lane; RBC_SERVER_FORM=1, 2, 3 or 4 (read when the active set
  * changes) selects another of the forms above for every case, which keeps
  * that property. */
 typedef struct RbcServer RbcServer;

@@ -1050,7 +1050,8 @@ class Batch:
         return out
 
     def tuning_forms(self):
-        """The forms the autotuner kept, as the RBC_BATCH_FORM list ("2,0,...")."""
+        """The forms the autotuner kept, as the RBC_BATCH_FORM string: the FP64
+        passes' digits, then after a ';' the GEMM passes' ("2,0,...;0,0,...")."""
         buf = ctypes.create_string_buffer(256)
         _check(lib().rbc_batch_tuning_forms(self._h, buf, len(buf)))
         return buf.value.decode()

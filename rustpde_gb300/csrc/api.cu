@@ -159,7 +159,8 @@ static const LMat& mixed_operator(int which, int n) {
 }
 
 // Pack rows blocks [A0 * s0 ; A1 * s1 ; ...] (long double) as one split operand.
-static const float* upload_op(Arena& a, std::initializer_list<std::pair<const LMat*, long double>> blocks) {
+static const float* upload_op(Arena& a, std::initializer_list<std::pair<const LMat*, long double>> blocks,
+                              int ntmax = 64) {
   int rows = 0, cols = -1;
   for (auto& b : blocks) {
     rows += b.first->rows;
@@ -170,10 +171,7 @@ static const float* upload_op(Arena& a, std::initializer_list<std::pair<const LM
   size_t o = 0;
   for (auto& b : blocks)
     for (long double v : b.first->a) W[o++] = (double)(v * b.second);
-  return a.upload(pack_gemm_w(W, rows, cols, gemm_tile_n(rows)));
-}
-static const float* upload_op(Arena& a, const std::vector<double>& W, int rows, int cols) {
-  return a.upload(pack_gemm_w(W, rows, cols, gemm_tile_n(rows)));
+  return a.upload(pack_gemm_w(W, rows, cols, gemm_tile_n(rows, ntmax)));
 }
 
 // Packed operators that depend on the size alone (the y transforms, the box's
@@ -201,7 +199,8 @@ static const float* shared_op(const std::string& key, Make make) {
   g_shared_ops.emplace(std::make_pair(dev, key), p);
   return p;
 }
-static std::vector<float> pack_blocks(std::initializer_list<std::pair<const LMat*, long double>> blocks) {
+static std::vector<float> pack_blocks(std::initializer_list<std::pair<const LMat*, long double>> blocks,
+                                      int ntmax = 64) {
   int rows = 0, cols = -1;
   for (auto& b : blocks) {
     rows += b.first->rows;
@@ -212,7 +211,11 @@ static std::vector<float> pack_blocks(std::initializer_list<std::pair<const LMat
   size_t o = 0;
   for (auto& b : blocks)
     for (long double v : b.first->a) W[o++] = (double)(v * b.second);
-  return pack_gemm_w(W, rows, cols, gemm_tile_n(rows));
+  return pack_gemm_w(W, rows, cols, gemm_tile_n(rows, ntmax));
+}
+// shared-operator key of a packing for tiles of at most ntmax outputs
+static std::string op_key(const std::string& k, int ntmax) {
+  return ntmax == 64 ? k : k + ":nt" + std::to_string(ntmax);
 }
 
 struct RbcCase {
@@ -233,9 +236,10 @@ struct RbcCase {
   double* d_red = nullptr;
   cudaStream_t stream = nullptr;
   StepPlan plan;
-  std::vector<StepPlan> plan_alts;  // mixed form in batches: the other forms of the FP64 passes (autotuned)
+  std::vector<StepPlan> plan_alts;  // mixed form in batches: the other forms of the passes (autotuned)
   DevPlan dp;
   MixedOps mops;
+  MixedOps mops_w;  // mixed form in batches: the operators packed for 128-output GEMM tiles (a tuned form)
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   double time = 0.0;
@@ -372,6 +376,11 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   const bool per = c->periodic;
   c->scale[0] = p.aspect;
   c->scale[1] = 1.0;
+  // the packed operators of the mixed form: tiles of at most 64 outputs, and
+  // in batches also 128 (the autotuner times both)
+  c->mops_w.ntmax = 128;
+  std::vector<MixedOps*> mixed_sets{&c->mops};
+  if (!with_graph) mixed_sets.push_back(&c->mops_w);
   c->nu = get_nu(p.ra, p.pr, c->scale[1] * 2.0);
   c->ka = get_ka(p.ra, p.pr, c->scale[1] * 2.0);
   const int xk_u = per ? FOURIER : CD;
@@ -465,8 +474,11 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
       const int mxc = nx - 2;
       // the eigenbasis depends on the basis and the size only
       const std::string k = "pois" + std::to_string(c->sp_p1.hb0.kind) + ":" + std::to_string(mxc);
-      c->mops.pf = shared_op(k + ":fwd", [&] { return pack_gemm_w(fwd, mxc, mxc, gemm_tile_n(mxc)); });
-      c->mops.pb = shared_op(k + ":bwd", [&] { return pack_gemm_w(bwd, mxc, mxc, gemm_tile_n(mxc)); });
+      for (MixedOps* o : mixed_sets) {
+        const int nt = o->ntmax;
+        o->pf = shared_op(op_key(k + ":fwd", nt), [&] { return pack_gemm_w(fwd, mxc, mxc, gemm_tile_n(mxc, nt)); });
+        o->pb = shared_op(op_key(k + ":bwd", nt), [&] { return pack_gemm_w(bwd, mxc, mxc, gemm_tile_n(mxc, nt)); });
+      }
     }
   }
   const size_t es = c->spec_elem();
@@ -502,11 +514,14 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
     h.m_s32 = A.alloc((size_t)3 * h.mxc * s32_row_floats(h) * 4);
     h.m_bcx = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
     h.m_bcy = static_cast<const float*>(A.alloc((size_t)nx * ny * 4));
-    c->mops.y1 = shared_op("bs_bds_cd:" + std::to_string(ny), [&] {
-      return pack_blocks({{&mixed_operator(MOP_BS_CD, ny), 1.0L}, {&mixed_operator(MOP_BDS_CD, ny), 1.0L}});
-    });
-    c->mops.y2 = shared_op("fwd23:" + std::to_string(ny),
-                           [&] { return pack_blocks({{&mixed_operator(MOP_FWD_23, ny), 1.0L}}); });
+    for (MixedOps* o : mixed_sets) {
+      const int nt = o->ntmax;
+      o->y1 = shared_op(op_key("bs_bds_cd:" + std::to_string(ny), nt), [&] {
+        return pack_blocks({{&mixed_operator(MOP_BS_CD, ny), 1.0L}, {&mixed_operator(MOP_BDS_CD, ny), 1.0L}}, nt);
+      });
+      o->y2 = shared_op(op_key("fwd23:" + std::to_string(ny), nt),
+                        [&] { return pack_blocks({{&mixed_operator(MOP_FWD_23, ny), 1.0L}}, nt); });
+    }
     if (!per) {
       for (int k = 0; k < 6; k++) h.m_ph[k] = A.alloc((size_t)2 * nx * ny * 4);
       for (int k = 0; k < 3; k++) h.m_p[k] = A.alloc((size_t)nx * ny * 4);
@@ -518,13 +533,16 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
       const LMat& bst = mixed_operator(tn ? MOP_BS_CN : MOP_BS_CD, nx);
       const LMat& bdst = mixed_operator(tn ? MOP_BDS_CN : MOP_BDS_CD, nx);
       // the derivative rows carry the aspect ratio (per case); the rest depends on the size only
-      c->mops.xa = upload_op(A, {{&bsu, 1.0L}, {&bdsu, inv_asp}});
-      c->mops.xb = shared_op("bs_cd:" + std::to_string(nx), [&] { return pack_blocks({{&bsu, 1.0L}}); });
-      c->mops.xc = upload_op(A, {{&bdst, inv_asp}});
-      c->mops.xd = shared_op(std::string(tn ? "bs_cn:" : "bs_cd:") + std::to_string(nx),
-                             [&] { return pack_blocks({{&bst, 1.0L}}); });
-      c->mops.x2 = shared_op("fwd23:" + std::to_string(nx),
-                             [&] { return pack_blocks({{&mixed_operator(MOP_FWD_23, nx), 1.0L}}); });
+      for (MixedOps* o : mixed_sets) {
+        const int nt = o->ntmax;
+        o->xa = upload_op(A, {{&bsu, 1.0L}, {&bdsu, inv_asp}}, nt);
+        o->xb = shared_op(op_key("bs_cd:" + std::to_string(nx), nt), [&] { return pack_blocks({{&bsu, 1.0L}}, nt); });
+        o->xc = upload_op(A, {{&bdst, inv_asp}}, nt);
+        o->xd = shared_op(op_key(std::string(tn ? "bs_cn:" : "bs_cd:") + std::to_string(nx), nt),
+                          [&] { return pack_blocks({{&bst, 1.0L}}, nt); });
+        o->x2 = shared_op(op_key("fwd23:" + std::to_string(nx), nt),
+                          [&] { return pack_blocks({{&mixed_operator(MOP_FWD_23, nx), 1.0L}}, nt); });
+      }
     }
   }
   void* bco = A.alloc((size_t)h.mx * ny * es);
@@ -622,9 +640,9 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   auto make_plans = [&]() {
     if (h.mixed) {
       c->plan = build_mixed_plan(h, c->mops, 0);
-      if (!with_graph)
+      if (!with_graph)  // forms 1-3 of the FP64 passes; form 4: the GEMMs with 128-output tiles
         c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2),
-                        build_mixed_plan(h, c->mops, 3)};
+                        build_mixed_plan(h, c->mops, 3), build_mixed_plan(h, c->mops_w, 0)};
     } else {
       c->plan = build_step_plan(h);
     }
@@ -1221,7 +1239,8 @@ struct RbcBatch {
   struct Tuned {
     int kernel_cta, kernel_lanes;
     float ms_cta, ms_lanes;
-    int form;  // form kept: 0 CTA per lane, 1 to 3 the other plan variants
+    int form;  // form kept: 0 CTA per lane, 1 to 4 the other plan variants
+    bool gemm;  // a GEMM pass (its forms are tile widths)
   };
   std::vector<Tuned> tuning;          // autotuner decisions (rbc_batch_tuning)
   char* d_state = nullptr;            // every case's spectral state, contiguous
@@ -1348,9 +1367,20 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       }
       return g;
     };
+    // a launch's identity for the comparison of forms: its kernel, and for a
+    // GEMM launch the widest tile of its jobs (forms 0 and 4 differ there only)
     auto kernels_of = [](const StepPlan& P, const std::vector<size_t>& g) {
       std::vector<int> k;
-      for (size_t li : g) k.push_back(P.launches[li].kernel);
+      for (size_t li : g) {
+        const StepLaunch& L = P.launches[li];
+        int id = L.kernel;
+        if (L.kernel == K_GEMM) {
+          int nt = 0;
+          for (const GemmJobDev& j : L.jobs) nt = std::max(nt, j.NT);
+          id = K_GEMM * 1000 + nt;
+        }
+        k.push_back(id);
+      }
       return k;
     };
     const auto gb = passes(bk.plan);
@@ -1360,13 +1390,21 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       if (ga[a].size() != gb.size()) throw std::runtime_error("autotune: plan forms of different pass structure");
     }
     // RBC_BATCH_FORM pins the forms instead (profiling runs: a profiler's
-    // per-launch overhead distorts the timings): one digit 0..3 for every pass
-    // that has forms, or a comma-separated list with one digit per such pass,
-    // in the order of rbc_batch_tuning
-    std::vector<int> forced_list;
-    if (const char* f = std::getenv("RBC_BATCH_FORM"))
-      for (const char* q = f; *q; q++)
-        if (*q >= '0' && *q <= '3') forced_list.push_back(*q - '0');
+    // per-launch overhead distorts the timings): "<passes>[;<gemms>]".  The
+    // first part is one digit 0..3 for every FP64 pass that has forms, or a
+    // comma-separated list with one digit per such pass, in the order of those
+    // passes in rbc_batch_tuning; the second is the same for the GEMM passes
+    // (0: 64-output tiles, 4: 128), all 0 when it is absent
+    const char* fenv = std::getenv("RBC_BATCH_FORM");
+    std::vector<int> forced_fp64, forced_gemm;
+    if (fenv) {
+      bool second = false;
+      for (const char* q = fenv; *q; q++) {
+        if (*q == ';') second = true;
+        else if (*q >= '0' && *q <= '4') (second ? forced_gemm : forced_fp64).push_back(*q - '0');
+      }
+      if (!second) forced_gemm = {0};
+    }
     StepPlan tuned;
     for (size_t pi = 0; pi < gb.size(); pi++) {
       auto group_time = [&](const StepPlan& P, const DevPlan& dp, const std::vector<size_t>& g) {
@@ -1396,12 +1434,16 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
         }
       }
       if (t_base >= 0) {
+        const bool gemm = bk.plan.launches[gb[pi][0]].kernel == K_GEMM;
+        const std::vector<int>& fl = gemm ? forced_gemm : forced_fp64;
+        size_t pos = 0;  // this decision's place among the batch's decisions of its kind
+        for (const auto& t : b->tuning) pos += t.gemm == gemm;
         int forced = -1;
-        if (forced_list.size() == 1) forced = forced_list[0];
-        else if (b->tuning.size() < forced_list.size()) forced = forced_list[b->tuning.size()];
+        if (fl.size() == 1) forced = fl[0];
+        else if (pos < fl.size()) forced = fl[pos];
         if (forced == 0) best = -1;
         else if (forced > 0 && (size_t)forced <= nalt) best = forced - 1;
-        b->tuning.push_back({bk.plan.launches[gb[pi][0]].kernel, best_alt_kernel, t_base, t_best_alt, best + 1});
+        b->tuning.push_back({bk.plan.launches[gb[pi][0]].kernel, best_alt_kernel, t_base, t_best_alt, best + 1, gemm});
       }
       const StepPlan& src = best >= 0 ? alts[best] : bk.plan;
       for (size_t li : (best >= 0 ? ga[best][pi] : gb[pi])) tuned.launches.push_back(src.launches[li]);
@@ -1601,11 +1643,13 @@ int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lane
 int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len) {
   API_BEGIN
   require(b && buf && len > 0, "rbc_batch_tuning_forms: invalid argument");
-  std::string s;
+  std::string s, g;
   for (const auto& t : b->tuning) {
-    if (!s.empty()) s += ',';
-    s += (char)('0' + t.form);
+    std::string& d = t.gemm ? g : s;
+    if (!d.empty()) d += ',';
+    d += (char)('0' + t.form);
   }
+  if (!g.empty()) s += ";" + g;
   require(s.size() < len, "rbc_batch_tuning_forms: buffer too small");
   std::memcpy(buf, s.c_str(), s.size() + 1);
   API_END
@@ -2549,14 +2593,14 @@ static void server_rebuild(RbcServer* S) {
     }
     S->buckets[found].members.push_back(i);
   }
-  // the forms of the FP64 passes: a CTA per lane by default; RBC_SERVER_FORM=1,
-  // 2 or 3 selects the 128-thread, the one-thread-per-sub-lane or that form
-  // with the periodic Y2 launches fused, for every case (a case's arithmetic
-  // never depends on the other cases in any form, so results stay the same
-  // alone and in a mix)
+  // the forms of the passes: a CTA per lane by default; RBC_SERVER_FORM=1, 2,
+  // 3 or 4 selects the 128-thread, the one-thread-per-sub-lane, that form with
+  // the periodic Y2 launches fused, or 128-output GEMM tiles, for every case (a
+  // case's arithmetic never depends on the other cases in any form, so results
+  // stay the same alone and in a mix)
   int form = 0;
   if (const char* f = std::getenv("RBC_SERVER_FORM"))
-    if (f[0] >= '1' && f[0] <= '3' && f[1] == '\0') form = f[0] - '0';
+    if (f[0] >= '1' && f[0] <= '4' && f[1] == '\0') form = f[0] - '0';
   for (auto& bk : S->buckets) {
     std::vector<const StepPlan*> plans;
     std::vector<const int*> gates;

@@ -127,15 +127,16 @@ __device__ __forceinline__ void tmem_ld8_nowait(uint32_t addr, uint32_t (&r)[8])
 
 // running total += chunk partial (or = partial for the first chunk), all 8
 // warps: warp w covers tensor-memory lanes 32 (w % 4) .. + 31 and every other
-// 8-column block (from block w / 4), at most 4 blocks (NT <= 64), in two
-// halves of two blocks: each half issues its loads before one wait (two round
-// trips per flush; all four blocks at once needed registers that spilled).
+// 8-column block (from block w / 4), up to 8 blocks (NT <= 128), in rounds of
+// two blocks: each round issues its loads before one wait (all blocks at once
+// needed registers that spilled).
 __device__ __forceinline__ void tmem_accumulate(uint32_t tmem, uint32_t part, uint32_t total, int NT, bool first,
                                                 int warp) {
   const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
   const int cb0 = (warp >> 2) * 8;
 #pragma unroll
-  for (int h = 0; h < 2; h++) {
+  for (int h = 0; h < 4; h++) {
+    if (32 * h >= NT) break;  // uniform across the CTA
     uint32_t p[2][8], t[2][8];
 #pragma unroll
     for (int b = 0; b < 2; b++) {
@@ -543,13 +544,13 @@ __global__ void __launch_bounds__(kGemmThreads, 2) k_lane_gemm_one(const __grid_
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-int gemm_tile_n(int N) {
-  // at most 64 outputs per tile: 4 NT tensor-memory columns per CTA (two chunk
-  // partials, corrections, total) and two CTAs per SM; wider outputs are split
-  // into equal tiles
+int gemm_tile_n(int N, int ntmax) {
+  // at most ntmax outputs per tile, wider outputs split into equal tiles.
+  // 64: 4 NT tensor-memory columns per CTA (two chunk partials, corrections,
+  // total) leave room for two CTAs per SM; 128: one CTA holds all 512 columns
   auto r16 = [](int v) { return (v + 15) & ~15; };
-  if (N <= 64) return r16(N);
-  int t = (N + 63) / 64;
+  if (N <= ntmax) return r16(N);
+  int t = (N + ntmax - 1) / ntmax;
   return r16((N + t - 1) / t);
 }
 
@@ -609,9 +610,14 @@ size_t gemm_smem_bytes(int NT) {
   const size_t ncols = dev::gemm_tmem_cols(NT);
   // keep (resident CTAs per SM) x (tensor-memory columns) within the 512
   // columns: at most 512 / ncols CTAs fit, so ask for enough shared memory
-  // (of the 228 KB per SM, 1 KB reserved per CTA) that no more become resident
+  // (of the 228 KB per SM, 1 KB reserved per CTA) that no more become resident.
+  // A CTA holding all 512 columns asks for more than what is left beside the
+  // smallest GEMM CTA, so that no CTA of another GEMM launch (its tcgen05.alloc
+  // would wait for columns) shares its SM
+  const size_t sm_total = 228 * 1024;
+  if (ncols >= 512) return std::max(base, sm_total - 2 * 1024 - gemm_smem_bytes(16) + 1);
   const size_t max_ctas = 512 / ncols;
-  const size_t floor_b = (228 * 1024) / (max_ctas + 1) - 1024 + 1;
+  const size_t floor_b = sm_total / (max_ctas + 1) - 1024 + 1;
   return std::max(base, floor_b);
 }
 
@@ -619,10 +625,10 @@ cudaError_t configure_gemm_kernels() {
   static bool done = false;
   if (done) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(dev::k_lane_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)gemm_smem_bytes(64));  // tiles hold at most 64 outputs
+                                       (int)gemm_smem_bytes(128));  // tiles hold at most 128 outputs
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(dev::k_lane_gemm_one, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)gemm_smem_bytes(64));
+                           (int)gemm_smem_bytes(128));
   if (e == cudaSuccess) done = true;
   return e;
 }
@@ -640,7 +646,7 @@ cudaError_t launch_lane_gemm_one(const GemmJobDev& job, cudaStream_t st) {
 }
 
 GemmJobDev make_gemm_job(const LaneSideDev& in, const LaneSideDev& out, const float* w, int K, int N, double scale,
-                         unsigned int* status) {
+                         unsigned int* status, int ntmax) {
   GemmJobDev j;
   std::memset(&j, 0, sizeof j);
   j.in = in;
@@ -648,7 +654,7 @@ GemmJobDev make_gemm_job(const LaneSideDev& in, const LaneSideDev& out, const fl
   j.w = w;
   j.K = K;
   j.N = N;
-  j.NT = gemm_tile_n(N);
+  j.NT = gemm_tile_n(N, ntmax);
   j.kchunks = (K + kGemmKC - 1) / kGemmKC;
   j.ntiles = (N + j.NT - 1) / j.NT;
   j.lanes = in.nf * in.rows * in.parts;

@@ -40,7 +40,7 @@ struct GemmJobDev {
   const int* active;     // when set and 0, the job's tiles do nothing (serving gate)
   double scale;
   int K, N;
-  int NT;       // output columns per tile (multiple of 16, <= 256)
+  int NT;       // output columns per tile (multiple of 16, <= 128)
   int kchunks;  // ceil(K / 32)
   int lanes;    // nf * rows * parts
   int ntiles;   // ceil(N / NT)
@@ -50,8 +50,8 @@ constexpr int kGemmLanes = 128;    // lanes per tile (tcgen05 M)
 constexpr int kGemmThreads = 256;  // threads per CTA (warps 0-3 also read the accumulators)
 constexpr int kGemmKC = 32;      // K elements per staged chunk
 
-// Output tile width for N outputs.
-int gemm_tile_n(int N);
+// Output tile width for N outputs, tiles of at most ntmax (64 or 128) outputs.
+int gemm_tile_n(int N, int ntmax = 64);
 // Split W (N x K row-major, FP64) into TF32 hi / lo parts laid out as the
 // kernel stages them: for tile t and chunk c a block of 2 * NT * 32 floats
 // (hi then lo), each in the K-major core-matrix order of the tcgen05 operand.
@@ -72,8 +72,9 @@ cudaError_t set_gemm_wait_limit(long long polls);
 
 // One job passed by value (no tables): lanes tiled in order.
 cudaError_t launch_lane_gemm_one(const GemmJobDev& job, cudaStream_t st);
+// ntmax: the widest output tile (the operator w must be packed for gemm_tile_n(N, ntmax))
 GemmJobDev make_gemm_job(const LaneSideDev& in, const LaneSideDev& out, const float* w, int K, int N, double scale,
-                         unsigned int* status);
+                         unsigned int* status, int ntmax = 64);
 // Lanes that are rows of row-major (rows x row_len) arrays, real or complex
 // interleaved (each complex row is two lanes, re then im).
 LaneSideDev lane_rows(void* const* ptrs, int nf, int rows, int len, int row_len, int type, bool complex_);

@@ -62,10 +62,12 @@ struct MixedOps {
   const float* x2 = nullptr;  // forward Chebyshev along x, rows < kx: kx x nx
   const float* pf = nullptr;  // Poisson eigenbasis forward: (nx - 2) x (nx - 2)
   const float* pb = nullptr;  // Poisson eigenbasis backward: (nx - 2) x (nx - 2)
+  int ntmax = 64;  // the widest GEMM output tile these operators are packed for (64 or 128)
 };
 // variant 0: a CTA per lane; 1: 128-thread CTAs where that form exists, else
 // one thread per lane; 2: one thread per (field, parity) sub-lane where that
-// form exists, else 128-thread CTAs
+// form exists, else 128-thread CTAs; 3: as 2 with the periodic Y2 launches
+// fused.  The GEMM tiles follow ops.ntmax.
 StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant);
 int lane_kernel_subs(int kernel);
 bool lane_kernel_rows(int kernel);

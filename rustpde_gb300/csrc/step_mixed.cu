@@ -210,7 +210,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     for (int f = 0; f < 3; f++) out.ptr[f] = c.m_y[f];
     out.nf = 3; out.rows = mx; out.parts = 2; out.type = LT_F32;
     out.lane_stride = 2; out.part_stride = 1; out.elem_stride = 2LL * mx; out.len = 2 * ny; out.lane_fast = 1;
-    add_gemm(make_gemm_job(in, out, ops.y1, myc, 2 * ny, 1.0, c.status));
+    add_gemm(make_gemm_job(in, out, ops.y1, myc, 2 * ny, 1.0, c.status, ops.ntmax));
     // X: FP32 convection, one CTA per column (256 threads, or 128 in the batch forms)
     add(lane_parallel ? K_PER_X_MIXED_T128 : K_PER_X_MIXED, ny, dev::smem_per_x_mixed(c));
     // G2: y transform of the x-transformed products (FP32, transposed) -> m_cv (FP64)
@@ -222,7 +222,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     void* cvp[3];
     for (int f = 0; f < 3; f++) cvp[f] = static_cast<double2*>(c.m_cv) + (size_t)f * kx * ky;
     LaneSideDev co = lane_rows(cvp, 3, kx, ky, ky, LT_F64, true);
-    add_gemm(make_gemm_job(qi, co, ops.y2, ny, ky, 1.0, c.status));
+    add_gemm(make_gemm_job(qi, co, ops.y2, ny, ky, 1.0, c.status, ops.ntmax));
     // Y2: FP64 right-hand sides, banded solves, projection, pressure update:
     // one CTA per row (256 or 128 threads), or three launches of one thread
     // per (field, parity) sub-lane, or those three phases in one launch
@@ -259,7 +259,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   {
     void* yo[3] = {c.m_y[0], c.m_y[1], c.m_y[2]};
     add_gemm(make_gemm_job(lane_rows(s32, 3, mxc, myc, s32ld, LT_F32, false),
-                           side(yo, 3, mxc, 2 * ny, 1, myld, LT_F32, 1), ops.y1, myc, 2 * ny, 1.0, c.status));
+                           side(yo, 3, mxc, 2 * ny, 1, myld, LT_F32, 1), ops.y1, myc, 2 * ny, 1.0, c.status, ops.ntmax));
   }
   // GX: x stencils, derivatives and backward transforms -> physical (transposed), one launch of 4 jobs
   {
@@ -270,19 +270,19 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     void* a_out[2] = {c.m_ph[0], c.m_ph[1]};
     L.jobs.push_back(make_gemm_job(lane_rows(a_in, 2, ny, mxc, myld, LT_F32, false),
                                    lane_rows(a_out, 2, ny, 2 * nx, 2 * nx, LT_F32, false), ops.xa, mxc, 2 * nx, 1.0,
-                                   c.status));
+                                   c.status, ops.ntmax));
     void* b_in[2] = {fptr(c.m_y[0], (size_t)ny * myld), fptr(c.m_y[1], (size_t)ny * myld)};
     void* b_out[2] = {c.m_ph[2], c.m_ph[3]};
     L.jobs.push_back(make_gemm_job(lane_rows(b_in, 2, ny, mxc, myld, LT_F32, false),
-                                   lane_rows(b_out, 2, ny, nx, nx, LT_F32, false), ops.xb, mxc, nx, 1.0, c.status));
+                                   lane_rows(b_out, 2, ny, nx, nx, LT_F32, false), ops.xb, mxc, nx, 1.0, c.status, ops.ntmax));
     void* c_in[1] = {c.m_y[2]};
     void* c_out[1] = {c.m_ph[4]};
     L.jobs.push_back(make_gemm_job(lane_rows(c_in, 1, ny, mxc, myld, LT_F32, false),
-                                   lane_rows(c_out, 1, ny, nx, nx, LT_F32, false), ops.xc, mxc, nx, 1.0, c.status));
+                                   lane_rows(c_out, 1, ny, nx, nx, LT_F32, false), ops.xc, mxc, nx, 1.0, c.status, ops.ntmax));
     void* d_in[1] = {fptr(c.m_y[2], (size_t)ny * myld)};
     void* d_out[1] = {c.m_ph[5]};
     L.jobs.push_back(make_gemm_job(lane_rows(d_in, 1, ny, mxc, myld, LT_F32, false),
-                                   lane_rows(d_out, 1, ny, nx, nx, LT_F32, false), ops.xd, mxc, nx, 1.0, c.status));
+                                   lane_rows(d_out, 1, ny, nx, nx, LT_F32, false), ops.xd, mxc, nx, 1.0, c.status, ops.ntmax));
     size_t sm = 0;
     for (const GemmJobDev& j : L.jobs) sm = std::max(sm, gemm_smem_bytes(j.NT));
     L.smem = sm;
@@ -296,7 +296,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     void* gout[3];
     for (int f = 0; f < 3; f++) gout[f] = fptr(c.m_q, (size_t)f * kx * ny);
     add_gemm(make_gemm_job(lane_rows(pin, 3, ny, nx, nx, LT_F32, false), side(gout, 3, ny, kx, 1, ny, LT_F32, 1),
-                           ops.x2, nx, kx, 1.0, c.status));
+                           ops.x2, nx, kx, 1.0, c.status, ops.ntmax));
   }
   // GY2: forward y transform, columns < ky -> m_cv (FP64, kx x ky per field)
   {
@@ -307,7 +307,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
       cvp[f] = static_cast<double*>(c.m_cv) + (size_t)f * kx * ky;
     }
     add_gemm(make_gemm_job(lane_rows(gin, 3, kx, ny, ny, LT_F32, false), lane_rows(cvp, 3, kx, ky, ky, LT_F64, false),
-                           ops.y2, ny, ky, 1.0, c.status));
+                           ops.y2, ny, ky, 1.0, c.status, ops.ntmax));
   }
   // FP64: pressure gradient, Helmholtz (ADI), divergence, Poisson, projection.
   // Each pass has up to three forms: a CTA per lane (variant 0), the same
@@ -333,7 +333,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     void* zi[1] = {c.m_z};
     void* zo[1] = {c.s[6]};
     add_gemm(make_gemm_job(lane_cols(zi, 1, ny, mxc, ny, LT_F32, 0), lane_cols(zo, 1, ny, mxc, ny, LT_F64, 0), ops.pf,
-                           mxc, mxc, 1.0, c.status));
+                           mxc, mxc, 1.0, c.status, ops.ntmax));
   }
   if (lane_parallel) add_lp(K_LP_BOX_Y4, mxc, ny);
   else add(K_BOX_Y4, mxc, dev::smem_box_y4(c));
@@ -341,7 +341,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     void* wi[1] = {c.m_z};
     void* po[1] = {c.p1};
     add_gemm(make_gemm_job(lane_cols(wi, 1, myc, mxc, myc, LT_F32, 0), lane_cols(po, 1, myc, mxc, myc, LT_F64, 0),
-                           ops.pb, mxc, mxc, 1.0, c.status));
+                           ops.pb, mxc, mxc, 1.0, c.status, ops.ntmax));
   }
   if (lane_parallel) add_lp(K_LP_BOX_X4, myc, nx);
   else add(K_BOX_X4_MIX, myc, dev::smem_box_x4(c));

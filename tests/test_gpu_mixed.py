@@ -140,7 +140,7 @@ def test_mixed_batch_forms_replay(R, monkeypatch):
     # step: bitwise the same numbers
     b1 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     forms = b1.tuning_forms()
-    assert forms and all(ch in "0123," for ch in forms), forms
+    assert forms and all(ch in "01234,;" for ch in forms), forms
     monkeypatch.setenv("RBC_BATCH_FORM", forms)
     b2 = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     assert b2.tuning_forms() == forms
@@ -172,6 +172,31 @@ def test_periodic_y2_fused_form_bitwise(R, monkeypatch):
     for i in range(len(params)):
         for k, f in enumerate(FIELDS):
             assert np.array_equal(out[0][i][k], out[1][i][k]), (i, f)
+
+
+def test_wide_gemm_tile_form(R, monkeypatch):
+    # form 4: the tensor-core GEMMs with output tiles of up to 128 columns (one
+    # CTA per SM holding all 512 tensor-memory columns) instead of 64; every
+    # other pass as form 0.  The same products, chunk partials and corrections
+    # per output element
+    params = MIX_PARAMS + [(45, 33, 1e5, 1.0, 5e-3, 1.0, O.PERIODIC)]
+    out = []
+    for form in ("0", "4"):
+        monkeypatch.setenv("RBC_BATCH_FORM", "0;" + form)
+        b = R.Batch(params, precision=R.PREC_MIXED)
+        assert set(b.tuning_forms().replace(",", "").replace(";", "")) <= {form, "0"}
+        for i in range(len(params)):
+            R.standard_ic(b.cases[i], seed=90 + i)
+        b.update(4)
+        b.synchronize()
+        assert all(b.cases[i].status() == 0 for i in range(len(params)))
+        out.append([[b.cases[i].get(f) for f in FIELDS] for i in range(len(params))])
+    same = True
+    for i in range(len(params)):
+        for k, f in enumerate(FIELDS):
+            same &= bool(np.array_equal(out[0][i][k], out[1][i][k]))
+            assert rel(out[1][i][k], out[0][i][k]) < FORMS_TOL, (i, f)
+    print("wide GEMM tiles bitwise equal to 64-column tiles:", same)
 
 
 def test_mixed_batch_one_call_equals_single_steps(R, monkeypatch):
