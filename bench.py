@@ -235,10 +235,15 @@ def step_state_bytes(params):
     return b
 
 
+DETAIL_DIR = None  # --detail-dir: where per-launch detail files go (none written without it)
+
+
 def side_file(name, obj):
-    """Per-launch detail that would crowd the JSON line, next to the run's logs."""
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    with open(os.path.join(ROOT, "gpurun_out", name), "w") as f:
+    """Per-launch detail that would crowd the JSON line, into --detail-dir."""
+    if DETAIL_DIR is None:
+        return
+    os.makedirs(DETAIL_DIR, exist_ok=True)
+    with open(os.path.join(DETAIL_DIR, name), "w") as f:
         json.dump(obj, f, indent=1)
 
 
@@ -896,6 +901,8 @@ def main():
     ap.add_argument("--accuracy-steps", type=int, default=505,
                     help="ensemble: steps of the mixed-vs-FP64 comparison (the configuration's horizon)")
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
+    ap.add_argument("--detail-dir", default=None,
+                    help="directory for the ensemble's per-launch detail file (bench_ensemble_detail.json)")
     ap.add_argument("--periodic-only", action="store_true",
                     help="profile-step: the ensemble's periodic cases alone (one group)")
     ap.add_argument("--skip-plain", action="store_true",
@@ -905,6 +912,8 @@ def main():
     ap.add_argument("--serving-check", type=int, default=8,
                     help="serving: results re-run alone in FP64 for the Nu/KE error")
     args = ap.parse_args()
+    global DETAIL_DIR
+    DETAIL_DIR = args.detail_dir
     if args.steps is None:
         # the reference arm's ensemble step is every case on the CPU (about 1.5 s)
         if args.workload == "ensemble":
