@@ -195,12 +195,16 @@ const char* rbc_kernel_name(int kernel);
  * Mixed-precision batches time the forms of each FP64 pass at creation and
  * keep the fastest (rbc_batch_tuning); the environment variable
  * RBC_BATCH_FORM pins the forms instead (profiling runs): the string
- * rbc_batch_tuning_forms returns, "<FP64 passes>[;<GEMM passes>]", each part
- * one digit for all its passes or a comma-separated digit per pass.  FP64
- * passes: 0 a CTA per lane, 1 128-thread CTAs, 2 one thread per sub-lane,
- * 3 the same with the periodic Y2 launches fused into one.  GEMM passes:
- * 0 output tiles of up to 64 columns, 4 up to 128 (all 0 without the second
- * part).  The group
+ * rbc_batch_tuning_forms returns, "<FP64 passes>[;<GEMM passes>[;<groups>]]",
+ * each part one digit for all its entries or a comma-separated digit per
+ * entry; an empty part is left to the autotuner.  FP64 passes: 0 a CTA per
+ * lane, 1 128-thread CTAs, 2 one thread per sub-lane, 3 the same with the
+ * periodic Y2 launches fused into one.  GEMM passes: 0 output tiles of up to
+ * 64 columns, 4 up to 128 (all 0 when the part is missing).  Groups: mixed-
+ * precision cases whose Chebyshev lengths are all 2^p + 1 are grouped apart,
+ * and each such group runs its transforms as tensor-core GEMMs (0) or as the
+ * FP64 plan's FFT butterflies (1; at least as accurate), whichever its step
+ * measured faster (all 0 when the part is missing).  The group
  * whose step takes longest runs on a high-priority branch, so its thread
  * blocks are dispatched first; RBC_BATCH_PRIORITY=0 gives every branch the
  * default priority. */
@@ -237,10 +241,12 @@ int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket
 int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lanes, double* ms_cta, double* ms_lanes,
                      int* n);
 /* The forms kept, one digit per decision of rbc_batch_tuning, comma-separated,
- * the FP64 passes' first and then, after a ';', the GEMM passes' (FP64: 0 a
- * CTA per lane, 1 128-thread CTAs, 2 a thread per sub-lane, 3 the same with
- * the periodic Y2 launches fused, timed for one-group batches; GEMM: 0
- * 64-output tiles, 4 128-output tiles), NUL-
+ * the FP64 passes' first, then after a ';' the GEMM passes', then after a
+ * second ';' (when the batch has groups of 2^p + 1 sizes) each such group's
+ * transforms (FP64: 0 a CTA per lane, 1 128-thread CTAs, 2 a thread per
+ * sub-lane, 3 the same with the periodic Y2 launches fused, timed for
+ * one-group batches; GEMM: 0 64-output tiles, 4 128-output tiles; groups: 0
+ * tensor-core GEMMs, 1 FP64 butterflies), NUL-
  * terminated in buf (len bytes).  Passed as RBC_BATCH_FORM it makes another
  * batch of the same cases keep the same forms, whatever its own timings say. */
 int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len);

@@ -1243,6 +1243,12 @@ struct RbcBatch {
     bool gemm;  // a GEMM pass (its forms are tile widths)
   };
   std::vector<Tuned> tuning;          // autotuner decisions (rbc_batch_tuning)
+  struct TransformChoice {
+    int bucket;
+    float ms_gemm, ms_butterfly;  // the group's step, launches timed alone
+    bool butterfly;               // kept the butterfly (plain FP64) plan
+  };
+  std::vector<TransformChoice> transforms;  // groups of butterfly sizes (rbc_batch_tuning_forms, third part)
   char* d_state = nullptr;            // every case's spectral state, contiguous
   size_t state_bytes = 0;
   std::vector<size_t> state_offset;   // byte offset of case i in d_state
@@ -1277,10 +1283,15 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   std::unique_ptr<RbcBatch> b(new RbcBatch());
   cuda_check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream create");
   // groups of equal kind (box / periodic) and precision, any size: one launch
-  // per pass covers every case of the group
+  // per pass covers every case of the group.  Mixed-precision cases whose
+  // Chebyshev lengths are all 2^p + 1 (ny, and nx of a box) form groups of
+  // their own (+8): there the transforms also have a butterfly form, and the
+  // autotuner picks between that and the tensor-core GEMMs per group
   for (int i = 0; i < ncases; i++) {
     const RbcParams& p = params[i];
-    int kind = (p.kind == RBC_PERIODIC ? 2 : 0) + 4 * p.precision;
+    const bool bfly = p.precision == RBC_PREC_MIXED && is_pow2(p.ny - 1) &&
+                      (p.kind == RBC_PERIODIC || is_pow2(p.nx - 1));
+    int kind = (p.kind == RBC_PERIODIC ? 2 : 0) + 4 * p.precision + (bfly ? 8 : 0);
     int found = -1;
     for (size_t k = 0; k < b->buckets.size(); k++)
       if (b->buckets[k].kind == kind) found = (int)k;
@@ -1396,14 +1407,16 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     // passes in rbc_batch_tuning; the second is the same for the GEMM passes
     // (0: 64-output tiles, 4: 128), all 0 when it is absent
     const char* fenv = std::getenv("RBC_BATCH_FORM");
-    std::vector<int> forced_fp64, forced_gemm;
+    std::vector<int> forced_fp64, forced_gemm, forced_transform;
     if (fenv) {
-      bool second = false;
+      int part = 0;
       for (const char* q = fenv; *q; q++) {
-        if (*q == ';') second = true;
-        else if (*q >= '0' && *q <= '4') (second ? forced_gemm : forced_fp64).push_back(*q - '0');
+        if (*q == ';') part++;
+        else if (*q >= '0' && *q <= '4')
+          (part == 0 ? forced_fp64 : part == 1 ? forced_gemm : forced_transform).push_back(*q - '0');
       }
-      if (!second) forced_gemm = {0};
+      if (part < 1) forced_gemm = {0};
+      if (part < 2) forced_transform = {0};
     }
     StepPlan tuned;
     for (size_t pi = 0; pi < gb.size(); pi++) {
@@ -1451,6 +1464,42 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     bk.plan = std::move(tuned);
     bk.dp = DevPlan();
     upload_plan(b->arena, bk.plan, bk.dp);
+    // transform-as-GEMM against the butterfly (groups of butterfly sizes, kind
+    // +8): the group's plain plan runs every transform as an FFT butterfly in
+    // FP64 (so at least as accurate), the products in FP64 too.  The whole step
+    // of each plan is timed (its launches alone, as above) and the faster kept;
+    // the third part of RBC_BATCH_FORM pins the choice (0 GEMM, 1 butterfly)
+    if (bk.kind & 8) {
+      std::vector<StepPlan> fp(bk.members.size());
+      std::vector<const StepPlan*> fpp;
+      bool fits = true;
+      for (size_t m = 0; m < bk.members.size(); m++) {
+        fp[m] = build_step_plan(b->cases[bk.members[m]]->hd);
+        for (const StepLaunch& L : fp[m].launches) fits = fits && L.smem <= smem_limit();
+        fpp.push_back(&fp[m]);
+      }
+      if (fits) {
+        StepPlan bp = merge_plans(fpp, bk.members, {});
+        DevPlan bdp;
+        upload_plan(b->arena, bp, bdp);
+        auto whole = [&](const StepPlan& P, const DevPlan& dp) {
+          float t = 0.f;
+          for (size_t li = 0; li < P.launches.size(); li++) t += time_launch(P.launches[li], dp, li);
+          return t;
+        };
+        const float t_gemm = whole(bk.plan, bk.dp), t_bfly = whole(bp, bdp);
+        const size_t pos = b->transforms.size();
+        int forced = -1;
+        if (forced_transform.size() == 1) forced = forced_transform[0];
+        else if (pos < forced_transform.size()) forced = forced_transform[pos];
+        const bool use_bfly = forced >= 0 ? forced == 1 : t_bfly < t_gemm;
+        b->transforms.push_back({(int)(&bk - b->buckets.data()), t_gemm, t_bfly, use_bfly});
+        if (use_bfly) {
+          bk.plan = std::move(bp);
+          bk.dp = bdp;
+        }
+      }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
   }
@@ -1649,7 +1698,13 @@ int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len) {
     if (!d.empty()) d += ',';
     d += (char)('0' + t.form);
   }
-  if (!g.empty()) s += ";" + g;
+  std::string t;
+  for (const auto& x : b->transforms) {
+    if (!t.empty()) t += ',';
+    t += x.butterfly ? '1' : '0';
+  }
+  if (!g.empty() || !t.empty()) s += ";" + g;
+  if (!t.empty()) s += ";" + t;
   require(s.size() < len, "rbc_batch_tuning_forms: buffer too small");
   std::memcpy(buf, s.c_str(), s.size() + 1);
   API_END

@@ -828,6 +828,8 @@ __global__ void __launch_bounds__(256) k_box_x3(const CaseDev* __restrict__ case
 size_t smem_box_x3(const CaseDev& c) { return 8 * (size_t)(c.nx + 1) * 8 + 64; }
 
 // Y4: rows i < mxc.  pinv_y then the Poisson row solve (eigen row i) -> s[7] (mxc x myc)
+// MIX: in FP32 into m_z instead, the input of the eigenbasis GEMM
+template <bool MIX>
 __global__ void __launch_bounds__(256) k_box_y4(const CaseDev* __restrict__ cases, const int4* __restrict__ work) {
   int4 w = work[blockIdx.x];
   const CaseDev& c = cases[w.x];
@@ -844,7 +846,7 @@ __global__ void __launch_bounds__(256) k_box_y4(const CaseDev* __restrict__ case
   __syncthreads();
   matvec_pinv<double>(c.pinv_y, IN, ld, OUT, ld, 1, tid, nth);
   fdma_solve<double>(c.pois_y, OUT, ld, 1, i, 0, tid, nth);
-  if (c.mixed) {  // FP32 into m_z: the input of the eigenbasis GEMM
+  if (MIX) {  // FP32 into m_z: the input of the eigenbasis GEMM
     float* wf = static_cast<float*>(c.m_z);
     for (int k = tid; k < myc; k += nth) wf[(size_t)i * myc + k] = (float)OUT[k];
     return;
@@ -1007,7 +1009,8 @@ cudaError_t configure_step_kernels() {
   SET_ATTR(dev::k_box_y3);
   SET_ATTR(dev::k_box_x3<false>);
   SET_ATTR(dev::k_box_x3<true>);
-  SET_ATTR(dev::k_box_y4);
+  SET_ATTR(dev::k_box_y4<false>);
+  SET_ATTR(dev::k_box_y4<true>);
   SET_ATTR(dev::k_box_x4<false>);
   SET_ATTR(dev::k_box_x4<true>);
   SET_ATTR(dev::k_box_y5);
@@ -1066,7 +1069,8 @@ cudaError_t launch_step_kernel(int kernel, int nblocks, size_t smem, cudaStream_
     case K_BOX_Y3: dev::k_box_y3<<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X3: dev::k_box_x3<false><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X3_MIX: dev::k_box_x3<true><<<g, b, smem, s>>>(cases, work); break;
-    case K_BOX_Y4: dev::k_box_y4<<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y4: dev::k_box_y4<false><<<g, b, smem, s>>>(cases, work); break;
+    case K_BOX_Y4_MIX: dev::k_box_y4<true><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X4: dev::k_box_x4<false><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_X4_MIX: dev::k_box_x4<true><<<g, b, smem, s>>>(cases, work); break;
     case K_BOX_Y5: dev::k_box_y5<<<g, b, smem, s>>>(cases, work); break;

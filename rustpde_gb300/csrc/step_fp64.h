@@ -29,6 +29,8 @@ enum StepKernel {
   K_PER_X_MIXED_T128,
   // the three periodic Y2 launches as one (a CTA barrier between the phases)
   K_LP_PER_Y2F,
+  // box Y4 of the mixed form (FP32 output for the eigenbasis GEMM)
+  K_BOX_Y4_MIX,
   K_NUM_STEP_KERNELS,
   K_GEMM = 100  // tensor-core lane GEMM (jobs instead of work items)
 };

@@ -336,7 +336,7 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
                            mxc, mxc, 1.0, c.status, ops.ntmax));
   }
   if (lane_parallel) add_lp(K_LP_BOX_Y4, mxc, ny);
-  else add(K_BOX_Y4, mxc, dev::smem_box_y4(c));
+  else add(K_BOX_Y4_MIX, mxc, dev::smem_box_y4(c));
   {  // eigenbasis backward along x: p1 = bwd * W (FP32 Poisson row solutions in m_z, columns j < myc)
     void* wi[1] = {c.m_z};
     void* po[1] = {c.p1};
@@ -360,7 +360,7 @@ size_t mixed_plan_smem(const CaseDev& c, int* kernel) {
     k = {{K_PER_X_MIXED, dev::smem_per_x_mixed(c)}, {K_PER_Y2_PRE, dev::smem_per_y2_pre(c)}};
   } else {
     k = {{K_BOX_GPX, dev::smem_box_gpx(c)}, {K_BOX_Y2_PRE, dev::smem_box_y2(c)}, {K_BOX_X2, dev::smem_box_x2(c)},
-         {K_BOX_Y3, dev::smem_box_y3(c)},  {K_BOX_X3_MIX, dev::smem_box_x3(c)}, {K_BOX_Y4, dev::smem_box_y4(c)},
+         {K_BOX_Y3, dev::smem_box_y3(c)},  {K_BOX_X3_MIX, dev::smem_box_x3(c)}, {K_BOX_Y4_MIX, dev::smem_box_y4(c)},
          {K_BOX_X4_MIX, dev::smem_box_x4(c)}, {K_BOX_Y5, dev::smem_box_y5(c)}};
   }
   size_t m = 0;
@@ -420,7 +420,7 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
       case K_LP_BOX_X4: kernel = K_BOX_X4_MIX; break;
       case K_LP_BOX_Y2: kernel = K_BOX_Y2_PRE; break;
       case K_LP_BOX_Y3: kernel = K_BOX_Y3; break;
-      case K_LP_BOX_Y4: kernel = K_BOX_Y4; break;
+      case K_LP_BOX_Y4: case K_BOX_Y4_MIX: kernel = K_BOX_Y4; break;
       case K_LP_BOX_Y5: kernel = K_BOX_Y5; break;
       case K_LP_PER_Y2: kernel = K_PER_Y2_PRE; break;
       case K_PER_Y2_PRE_T128: kernel = K_PER_Y2_PRE; break;
@@ -476,7 +476,7 @@ const char* step_kernel_name(int kernel) {
                                 "lanes_box_y4", "lanes_box_y5", "lanes_periodic_y2", "periodic_y2_pre_t128",
                                 "box_y2_pre_t128", "box_x3_mix_t128", "box_y5_t128", "lanes_periodic_y2a",
                                 "lanes_periodic_y2b", "lanes_periodic_y2c", "state_f32", "periodic_x_mixed_t128",
-                                "lanes_periodic_y2_fused"};
+                                "lanes_periodic_y2_fused", "box_y4_mix"};
   if (kernel == K_GEMM) return "lane_gemm";
   if (kernel >= 0 && kernel < K_NUM_STEP_KERNELS) return names[kernel];
   return "";

@@ -94,11 +94,14 @@ MIX_PARAMS = [(64, 33, 1e5, 1.0, 0.005, 1.0, O.PERIODIC), (128, 64, 1e6, 0.7, 2e
 FORMS_TOL = 1e-7
 
 
-def test_mixed_batch_matches_batch_of_one(R):
+def test_mixed_batch_matches_batch_of_one(R, monkeypatch):
     # batches choose per pass between the forms of the FP64 passes (autotuned
     # on the batch), so a case's numbers match its batch of one up to the
     # roundings of the forms; bitwise identity alone vs in a mix is the
-    # serving loop's guarantee (test_gpu_serving.py)
+    # serving loop's guarantee (test_gpu_serving.py).  The transforms stay
+    # tensor-core GEMMs (";;0"): the butterfly form of a group of 2^p + 1
+    # sizes is the FP64 plan, which differs by the mixed form's own error
+    monkeypatch.setenv("RBC_BATCH_FORM", ";;0")
     b = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     print("autotuner:", b.tuning())
     for i in range(len(MIX_PARAMS)):
@@ -115,9 +118,11 @@ def test_mixed_batch_matches_batch_of_one(R):
             assert e < FORMS_TOL, (i, f, e)
 
 
-def test_mixed_batch_matches_single_case(R):
+def test_mixed_batch_matches_single_case(R, monkeypatch):
     # a single case runs the FP64 passes one CTA per lane (scans): same
-    # arithmetic up to the order of the recurrences' roundings
+    # arithmetic up to the order of the recurrences' roundings (transforms
+    # pinned to the GEMMs, as above)
+    monkeypatch.setenv("RBC_BATCH_FORM", ";;0")
     b = R.Batch(MIX_PARAMS, precision=R.PREC_MIXED)
     singles = []
     for i, p in enumerate(MIX_PARAMS):
@@ -172,6 +177,34 @@ def test_periodic_y2_fused_form_bitwise(R, monkeypatch):
     for i in range(len(params)):
         for k, f in enumerate(FIELDS):
             assert np.array_equal(out[0][i][k], out[1][i][k]), (i, f)
+
+
+BFLY = [(128, 129, 1e5, 1.0, 5e-3, 1.0, O.PERIODIC), (65, 65, 1e5, 1.0, 1e-2, 1.0, O.BOX_ADIABATIC),
+        (129, 129, 1e6, 0.7, 4e-3, 1.5, O.BOX_CONDUCTING), (64, 33, 1e5, 1.0, 5e-3, 1.0, O.PERIODIC)]
+
+
+def test_transform_gemm_or_butterfly(R, monkeypatch):
+    # mixed cases whose Chebyshev lengths are all 2^p + 1 form groups of their
+    # own, where the autotuner times the tensor-core GEMM transforms against
+    # the butterfly (the group's plain FP64 plan) and keeps the faster: one
+    # decision per such group, after the second ';' of the forms
+    b = R.Batch(BFLY + [(96, 40, 1e5, 1.0, 5e-3, 1.0, O.PERIODIC)], precision=R.PREC_MIXED)
+    parts = b.tuning_forms().split(";")
+    assert len(parts) == 3 and len(parts[2].split(",")) == 2, parts  # periodic and box groups
+    # pinned to the butterfly, the groups run the FP64 plan: bitwise an FP64 batch
+    monkeypatch.setenv("RBC_BATCH_FORM", ";;1")
+    bm = R.Batch(BFLY, precision=R.PREC_MIXED)
+    assert bm.tuning_forms().split(";")[2] == "1,1"
+    bf = R.Batch(BFLY, precision=R.PREC_FP64)
+    for bb in (bm, bf):
+        for i in range(len(BFLY)):
+            R.standard_ic(bb.cases[i], seed=70 + i)
+        bb.update(3)
+        bb.synchronize()
+    for i in range(len(BFLY)):
+        assert bm.cases[i].status() == 0
+        for f in FIELDS:
+            assert np.array_equal(bm.cases[i].get(f), bf.cases[i].get(f)), (i, f)
 
 
 def test_wide_gemm_tile_form(R, monkeypatch):
