@@ -22,6 +22,7 @@
 // the stores, drains its MMA in flight (again bounded), frees its tensor memory
 // and returns.
 #include "lane_gemm.h"
+#include "per_device.h"
 
 #include <algorithm>
 #include <cstring>
@@ -622,14 +623,14 @@ size_t gemm_smem_bytes(int NT) {
 }
 
 cudaError_t configure_gemm_kernels() {
-  static bool done = false;
-  if (done) return cudaSuccess;
+  static PerDeviceFlag done;
+  if (done.test()) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(dev::k_lane_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)gemm_smem_bytes(128));  // tiles hold at most 128 outputs
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(dev::k_lane_gemm_one, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)gemm_smem_bytes(128));
-  if (e == cudaSuccess) done = true;
+  if (e == cudaSuccess) done.set();
   return e;
 }
 

@@ -5,6 +5,7 @@
 #include <stdexcept>
 
 #include "lane_ops.cuh"
+#include "per_device.h"
 #include "prims.h"
 
 #include <map>
@@ -974,25 +975,27 @@ void sum_squares(const double* v, size_t n, double* out, cudaStream_t st) {
 }
 
 size_t smem_limit() {
-  static size_t lim = 0;
-  if (lim == 0) {
-    int d = 0, v = 0;
-    if (cudaGetDevice(&d) == cudaSuccess &&
-        cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, d) == cudaSuccess && v > 0)
-      lim = (size_t)v;
-    else {
+  static std::atomic<size_t> lim[64];
+  const int d = current_device();
+  size_t v = d < 64 ? lim[d].load() : 0;
+  if (v == 0) {
+    int a = 0;
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrMaxSharedMemoryPerBlockOptin, d) == cudaSuccess && a > 0) {
+      v = (size_t)a;
+    } else {
       cudaGetLastError();  // leave no error behind for the next launch check
-      lim = 200 * 1024;
+      v = 200 * 1024;
     }
+    if (d < 64) lim[d].store(v);
   }
-  return lim;
+  return v;
 }
 
 cudaError_t configure_prim_kernels() {
-  static bool done = false;
-  if (done) return cudaSuccess;
+  static PerDeviceFlag done;
+  if (done.test()) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(dev::k_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_limit());
-  if (e == cudaSuccess) done = true;
+  if (e == cudaSuccess) done.set();
   return e;
 }
 

@@ -12,6 +12,7 @@
 // Each launch takes a table of work items (case, first lane, lane count); a
 // batch of cases is the same launch with a longer table.
 #include "lane_ops.cuh"
+#include "per_device.h"
 #include "prims.h"
 #include "step_fp64.h"
 
@@ -987,8 +988,8 @@ size_t smem_box_y5(const CaseDev& c) { return 12 * (size_t)(c.ny + 1) * 8 + 64; 
 static inline size_t clamp_smem(size_t s) { return (s + 127) & ~size_t(127); }
 
 cudaError_t configure_step_kernels() {
-  static bool done = false;
-  if (done) return cudaSuccess;
+  static PerDeviceFlag done;
+  if (done.test()) return cudaSuccess;
   const int big = (int)smem_limit();
   cudaError_t e;
 #define SET_ATTR(k)                                                                          \
@@ -1015,7 +1016,7 @@ cudaError_t configure_step_kernels() {
   SET_ATTR(dev::k_box_x4<true>);
   SET_ATTR(dev::k_box_y5);
 #undef SET_ATTR
-  done = true;
+  done.set();
   return cudaSuccess;
 }
 

@@ -14,6 +14,7 @@
 //  periodic:  G1 (y, GEMM) -> X (FP32) -> G2 (y, GEMM) -> Y2 (FP64)
 #include "lane_ops.cuh"
 #include "lane_ops_f32.cuh"
+#include "per_device.h"
 #include "prims.h"
 #include "step_fp64.h"
 
@@ -370,13 +371,13 @@ size_t mixed_plan_smem(const CaseDev& c, int* kernel) {
 }
 
 cudaError_t configure_mixed_kernels() {
-  static bool done = false;
-  if (done) return cudaSuccess;
+  static PerDeviceFlag done;
+  if (done.test()) return cudaSuccess;
   cudaError_t e = cudaFuncSetAttribute(dev::k_per_x_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem_limit());
   if (e != cudaSuccess) return e;
   e = configure_gemm_kernels();
-  if (e == cudaSuccess) done = true;
+  if (e == cudaSuccess) done.set();
   return e;
 }
 
