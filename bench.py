@@ -493,6 +493,12 @@ def run_serving(args, n_requests, horizon_scale, n_check=8):
     ok = srv.wait_idle(1800.0)
     res = srv.poll(len(reqs) + 8)
     st = srv.stats()
+    if DETAIL_DIR is not None:  # one JSON line per request
+        os.makedirs(DETAIL_DIR, exist_ok=True)
+        path = os.path.join(DETAIL_DIR, "serving_requests.jsonl")
+        if os.path.exists(path):
+            os.remove(path)
+        srv.write_records(path, res)
     srv.close()
     lat = np.array([r["t_done"] - r["t_submit"] for r in res])
     setup = np.array([r["t_admit"] - r["t_submit"] for r in res])

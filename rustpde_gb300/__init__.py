@@ -1102,6 +1102,7 @@ class Server:
         h = _P()
         _check(lib().rbc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
+        self._requests = {}  # id -> (params, horizon, seed), for the result records
 
     def submit(self, params, horizon, seed, precision=PREC_FP64):
         nx, ny, ra, pr, dt, asp, kind = params[:7]
@@ -1109,7 +1110,28 @@ class Server:
         p = RbcParams(int(nx), int(ny), float(ra), float(pr), float(dt), float(asp), int(kind), int(prec))
         rid = ctypes.c_longlong()
         _check(lib().rbc_server_submit(self._h, ctypes.byref(p), float(horizon), int(seed), ctypes.byref(rid)))
+        self._requests[rid.value] = ((int(nx), int(ny), float(ra), float(pr), float(dt), float(asp), int(kind),
+                                      int(prec)), float(horizon), int(seed))
         return rid.value
+
+    def record(self, result):
+        """One request's record for a JSON-lines log: id, sizes and parameters,
+        horizon, seed, status, steps, simulated time, wall time from submission
+        to result (and the part spent queued and in set-up), Nu and KE."""
+        p, horizon, seed = self._requests.get(result["id"], ((None,) * 8, None, None))
+        keys = ("nx", "ny", "ra", "pr", "dt", "aspect", "kind", "precision")
+        rec = {"id": result["id"], **dict(zip(keys, p)), "horizon": horizon, "seed": seed,
+               "status": result["status"], "steps": result["steps"], "sim_time": result["sim_time"],
+               "wall_s": result["t_done"] - result["t_submit"], "queue_and_setup_s": result["t_admit"] - result["t_submit"],
+               "nu": result["nu"], "ke": result["ke"]}
+        return rec
+
+    def write_records(self, path, results):
+        """Append the results' records to `path`, one JSON object per line."""
+        import json
+        with open(path, "a") as f:
+            for r in results:
+                f.write(json.dumps(self.record(r)) + "\n")
 
     def cancel(self, rid):
         """Cancel request `rid`; True if it had not finished.  Its result

@@ -16,6 +16,7 @@
 #include "host_ops.h"
 #include "lane_gemm.h"
 #include "prims.h"
+#include "trace.h"
 #include "solid_masks.h"
 #include "spectral_rbc.h"
 #include "step_fp64.h"
@@ -852,6 +853,7 @@ static void validate_params(const RbcParams& p) {
 
 int rbc_create(const RbcParams* params, RbcCase** out) {
   API_BEGIN
+  TraceRange tr("rbc_create");
   require(params != nullptr && out != nullptr, "rbc_create: null argument");
   *out = nullptr;
   const RbcParams& p = *params;
@@ -929,6 +931,7 @@ int rbc_random_disturbance(RbcCase* c, double amp, uint64_t seed) {
 
 int rbc_step(RbcCase* c, int nsteps) {
   API_BEGIN
+  TraceRange tr("rbc_step");
   require(c != nullptr && nsteps >= 0, "rbc_step: invalid argument");
   require(c->gexec != nullptr, "rbc_step: the case belongs to a batch (use rbc_batch_step)");
   for (int s = 0; s < nsteps; s++) {
@@ -1276,6 +1279,7 @@ extern "C" {
 
 int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
   API_BEGIN
+  TraceRange tr("rbc_batch_create");
   require(params != nullptr && out != nullptr && ncases > 0, "rbc_batch_create: invalid argument");
   *out = nullptr;
   for (int i = 0; i < ncases; i++) validate_params(params[i]);
@@ -1622,6 +1626,7 @@ int rbc_batch_case(RbcBatch* b, int i, RbcCase** c) {
 }
 int rbc_batch_step(RbcBatch* b, int nsteps) {
   API_BEGIN
+  TraceRange tr("rbc_batch_step");
   require(b && nsteps >= 0, "rbc_batch_step: invalid argument");
   for (int s = 0; s < nsteps; s++) {
     cuda_check(cudaGraphLaunch(b->gexec, b->stream), "graph launch");
@@ -1631,6 +1636,7 @@ int rbc_batch_step(RbcBatch* b, int nsteps) {
 }
 int rbc_batch_step_io(RbcBatch* b, const void* host_in, void* host_out, size_t bytes, int nsteps) {
   API_BEGIN
+  TraceRange tr("rbc_batch_step_io");
   require(b && host_in && host_out && nsteps >= 0, "rbc_batch_step_io: invalid argument");
   require(bytes == b->state_bytes, "rbc_batch_step_io: size mismatch (see rbc_batch_state_bytes)");
   const size_t nb = b->buckets.size();
@@ -1646,6 +1652,7 @@ int rbc_batch_step_io(RbcBatch* b, const void* host_in, void* host_out, size_t b
     const size_t o = bk.state_begin, n = bk.state_end - bk.state_begin;
     cuda_check(cudaStreamWaitEvent(s, b->events[nb], 0), "stream wait");
     if (prev != nullptr) cuda_check(cudaStreamWaitEvent(s, prev, 0), "stream wait");
+    TraceRange tg("group: copy in, steps, copy out");
     cuda_check(cudaMemcpyAsync(b->d_state + o, static_cast<const char*>(host_in) + o, n, cudaMemcpyHostToDevice, s),
                "state copy h2d");
     cuda_check(cudaEventRecord(b->io_events[k], s), "event");
@@ -1758,6 +1765,7 @@ int rbc_profile_step(RbcCase* c, int nsteps, double* stage_ms, int max_stages, i
   for (int s = 0; s < nsteps; s++) {
     cuda_check(cudaEventRecord(ev[0], c->stream), "event record");
     for (int k = 0; k < ns; k++) {
+      TraceRange ts(step_kernel_name(c->plan.launches[k].kernel));
       cuda_check(launch_entry(c->plan.launches[k], c->dp, k, c->stream, c->d_case),
                  "stage launch");
       cuda_check(cudaEventRecord(ev[k + 1], c->stream), "event record");
@@ -1808,6 +1816,7 @@ int rbc_batch_profile_step(RbcBatch* b, int nsteps, double* stage_ms, double* st
   for (int s = 0; s < nsteps; s++) {
     for (auto& bk : b->buckets)
       for (size_t li = 0; li < bk.plan.launches.size(); li++) {
+        TraceRange ts(step_kernel_name(bk.plan.launches[li].kernel));
         cuda_check(cudaEventRecord(e0, b->stream), "event record");
         cuda_check(launch_entry(bk.plan.launches[li], bk.dp, li, b->stream, b->d_cases), "stage launch");
         cuda_check(cudaEventRecord(e1, b->stream), "event record");
@@ -1857,6 +1866,7 @@ int rbc_batch_profile_launches(RbcBatch* b, int nsteps, int* kernel, int* bucket
     int idx = 0;
     for (auto& bk : b->buckets)
       for (size_t li = 0; li < bk.plan.launches.size(); li++, idx++) {
+        TraceRange ts(step_kernel_name(bk.plan.launches[li].kernel));
         cuda_check(cudaEventRecord(e0, b->stream), "event record");
         cuda_check(launch_entry(bk.plan.launches[li], bk.dp, li, b->stream, b->d_cases), "stage launch");
         cuda_check(cudaEventRecord(e1, b->stream), "event record");
@@ -2774,8 +2784,12 @@ static void server_main(RbcServer* S) {
           continue;
         }
       }
-      if (S->dirty) server_rebuild(S);
+      if (S->dirty) {
+        TraceRange tr("server: rebuild the batched step");
+        server_rebuild(S);
+      }
       const int n = S->cfg.chunk_steps;
+      TraceRange tc("server: chunk");
       for (int k = 0; k < n; k++) cuda_check(cudaGraphLaunch(S->gexec, S->stream), "graph launch");
       cuda_check(cudaEventRecord(S->chunk_done, S->stream), "event record");
       {

@@ -115,3 +115,22 @@ def test_admission_under_memory_pressure(R):
         assert r["status"] == 0 and r["steps"] == 5
         alone, _ = serve(R, [reqs[k]])
         assert alone[0]["nu"] == r["nu"] and alone[0]["ke"] == r["ke"]
+
+
+def test_request_records(R, tmp_path):
+    # one JSON line per request: its sizes and parameters, steps, wall time, Nu, KE, status
+    import json
+    srv = R.Server(hbm_budget_bytes=8 * 10**9, max_active=8, chunk_steps=4)
+    ids = [srv.submit(p, h, seed) for p, h, seed in REQS[:3]]
+    assert srv.wait_idle(120.0)
+    res = srv.poll()
+    path = tmp_path / "requests.jsonl"
+    srv.write_records(str(path), res)
+    srv.close()
+    lines = [json.loads(x) for x in path.read_text().splitlines()]
+    assert sorted(r["id"] for r in lines) == sorted(ids)
+    for rec in lines:
+        p, h, seed = REQS[ids.index(rec["id"])]
+        assert (rec["nx"], rec["ny"], rec["kind"]) == (p[0], p[1], p[6]) and rec["seed"] == seed
+        assert rec["status"] == 0 and rec["steps"] == max(1, round(h / p[4])) and rec["wall_s"] > 0
+        assert np.isfinite(rec["nu"]) and np.isfinite(rec["ke"])
