@@ -200,7 +200,8 @@ const char* rbc_kernel_name(int kernel);
  * entry; an empty part is left to the autotuner.  FP64 passes: 0 a CTA per
  * lane, 1 128-thread CTAs, 2 one thread per sub-lane, 3 the same with the
  * periodic Y2 launches fused into one.  GEMM passes: 0 output tiles of up to
- * 64 columns, 4 up to 128 (all 0 when the part is missing).  Groups: mixed-
+ * 64 columns, 4 up to 128, 5 64 in the warp-specialised form (producer, MMA
+ * and flush warps; all 0 when the part is missing).  Groups: mixed-
  * precision cases whose Chebyshev lengths are all 2^p + 1 are grouped apart,
  * and each such group runs its transforms as tensor-core GEMMs (0) or as the
  * FP64 plan's FFT butterflies (1; at least as accurate), whichever its step
@@ -245,8 +246,8 @@ int rbc_batch_tuning(const RbcBatch* b, int k, int* kernel_cta, int* kernel_lane
  * second ';' (when the batch has groups of 2^p + 1 sizes) each such group's
  * transforms (FP64: 0 a CTA per lane, 1 128-thread CTAs, 2 a thread per
  * sub-lane, 3 the same with the periodic Y2 launches fused, timed for
- * one-group batches; GEMM: 0 64-output tiles, 4 128-output tiles; groups: 0
- * tensor-core GEMMs, 1 FP64 butterflies), NUL-
+ * one-group batches; GEMM: 0 64-output tiles, 4 128-output tiles, 5
+ * warp-specialised; groups: 0 tensor-core GEMMs, 1 FP64 butterflies), NUL-
  * terminated in buf (len bytes).  Passed as RBC_BATCH_FORM it makes another
  * batch of the same cases keep the same forms, whatever its own timings say. */
 int rbc_batch_tuning_forms(const RbcBatch* b, char* buf, size_t len);
@@ -311,7 +312,7 @@ int rbc_diag_series(const RbcCase* c, double* time, double* nu, double* nuvol, d
  * join at the next chunk of chunk_steps steps).  Each finished request yields
  * a result (Nu, KE at its horizon, timestamps on the server clock).  A case
  * computes exactly the same numbers alone or in any mix.  The FP64 passes run
- * as a CTA per lane; RBC_SERVER_FORM=1, 2, 3 or 4 (read when the active set
+ * as a CTA per lane; RBC_SERVER_FORM=1 to 5 (read when the active set
  * changes) selects another of the forms above for every case, which keeps
  * that property. */
 typedef struct RbcServer RbcServer;

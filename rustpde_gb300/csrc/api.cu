@@ -96,7 +96,8 @@ static void upload_plan(Arena& A, const StepPlan& plan, DevPlan& dp) {
 
 static cudaError_t launch_entry(const StepLaunch& L, const DevPlan& dp, size_t k, cudaStream_t st,
                                 const CaseDev* cases) {
-  if (L.kernel == K_GEMM) return launch_lane_gemm(dp.jobs[k], dp.tiles[k], dp.ntiles[k], dp.max_nt[k], st);
+  if (L.kernel == K_GEMM)
+    return launch_lane_gemm(dp.jobs[k], dp.tiles[k], dp.ntiles[k], dp.max_nt[k], st, L.gemm_ws != 0);
   return launch_step_kernel(L.kernel, (int)L.items.size(), L.smem, st, cases, dp.work[k]);
 }
 
@@ -641,9 +642,13 @@ void build_case(RbcCase* c, bool with_graph = true, char* state_region = nullptr
   auto make_plans = [&]() {
     if (h.mixed) {
       c->plan = build_mixed_plan(h, c->mops, 0);
-      if (!with_graph)  // forms 1-3 of the FP64 passes; form 4: the GEMMs with 128-output tiles
+      if (!with_graph) {  // forms 1-3 of the FP64 passes; GEMM forms 4 (128-output tiles), 5 (warp-specialised)
+        MixedOps ws = c->mops;
+        ws.ws = 1;
         c->plan_alts = {build_mixed_plan(h, c->mops, 1), build_mixed_plan(h, c->mops, 2),
-                        build_mixed_plan(h, c->mops, 3), build_mixed_plan(h, c->mops_w, 0)};
+                        build_mixed_plan(h, c->mops, 3), build_mixed_plan(h, c->mops_w, 0),
+                        build_mixed_plan(h, ws, 0)};
+      }
     } else {
       c->plan = build_step_plan(h);
     }
@@ -1383,7 +1388,8 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       return g;
     };
     // a launch's identity for the comparison of forms: its kernel, and for a
-    // GEMM launch the widest tile of its jobs (forms 0 and 4 differ there only)
+    // GEMM launch the widest tile of its jobs and its form (forms 0, 4 and 5
+    // differ there only)
     auto kernels_of = [](const StepPlan& P, const std::vector<size_t>& g) {
       std::vector<int> k;
       for (size_t li : g) {
@@ -1392,7 +1398,7 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
         if (L.kernel == K_GEMM) {
           int nt = 0;
           for (const GemmJobDev& j : L.jobs) nt = std::max(nt, j.NT);
-          id = K_GEMM * 1000 + nt;
+          id = K_GEMM * 1000 + nt + (L.gemm_ws ? 500 : 0);
         }
         k.push_back(id);
       }
@@ -1416,7 +1422,7 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
       int part = 0;
       for (const char* q = fenv; *q; q++) {
         if (*q == ';') part++;
-        else if (*q >= '0' && *q <= '4')
+        else if (*q >= '0' && *q <= '5')
           (part == 0 ? forced_fp64 : part == 1 ? forced_gemm : forced_transform).push_back(*q - '0');
       }
       if (part < 1) forced_gemm = {0};
@@ -2665,7 +2671,7 @@ static void server_rebuild(RbcServer* S) {
   // stay the same alone and in a mix)
   int form = 0;
   if (const char* f = std::getenv("RBC_SERVER_FORM"))
-    if (f[0] >= '1' && f[0] <= '4' && f[1] == '\0') form = f[0] - '0';
+    if (f[0] >= '1' && f[0] <= '5' && f[1] == '\0') form = f[0] - '0';
   for (auto& bk : S->buckets) {
     std::vector<const StepPlan*> plans;
     std::vector<const int*> gates;

@@ -192,22 +192,22 @@ __device__ __forceinline__ bool mma_wait(uint64_t* mbar, uint32_t parity, long l
 }
 
 // Input chunk of a tile held in registers between its global loads and its
-// conversion: item (lane l, quad kq) -> 4 consecutive k of one lane.
-constexpr int kItems = 1024 / kGemmThreads;  // (lane, 4-k quad) items per thread per chunk
-
-template <class T>
+// conversion: item (lane l, quad kq) -> 4 consecutive k of one lane.  NTHR
+// threads stage a chunk (the whole CTA, or the producer warps of the
+// warp-specialised form), 1024 / NTHR (lane, 4-k quad) items each.
+template <class T, int NTHR = kGemmThreads>
 struct AChunk {
-  T v[kItems][4];
+  T v[1024 / NTHR][4];
 };
 
 // A thread's items are the same in every chunk of a tile: item it of thread
-// tid is q = tid + 256 it, lane l and quad kq as below.  With lanes fast in
-// memory (columns) a thread keeps one lane and steps kq by 2; with rows it
-// keeps kq and steps the lane by 32.  The lane addresses (element 4 kq of each
-// item's lane) are formed once per tile.
-template <class T>
+// tid is q = tid + NTHR it, lane l and quad kq as below.  With lanes fast in
+// memory (columns) a thread keeps one lane and steps kq by NTHR / 128; with
+// rows it keeps kq and steps the lane by NTHR / 8.  The lane addresses
+// (element 4 kq of each item's lane) are formed once per tile.
+template <class T, int NTHR = kGemmThreads>
 struct ATile {
-  const T* src[kItems];  // nullptr: lane past the job's end (zeros)
+  const T* src[1024 / NTHR];  // nullptr: lane past the job's end (zeros)
   int es;               // element stride of the lanes (a row length at most)
   int soff0, sstep;     // shared-memory byte offset of item 0, step per item
   bool vec;             // unit element stride and every item 16-byte aligned: vector loads
@@ -219,20 +219,21 @@ __device__ __forceinline__ void item_lane_quad(int q, bool lane_fast, int& l, in
   kq = lane_fast ? r >> 4 : r & 7;
 }
 
-template <class T>
-__device__ __forceinline__ void a_setup(ATile<T>& t, const GemmJobDev& J, const char* const* ib, int tid) {
+template <class T, int NTHR = kGemmThreads>
+__device__ __forceinline__ void a_setup(ATile<T, NTHR>& t, const GemmJobDev& J, const char* const* ib, int tid) {
+  constexpr int kItems = 1024 / NTHR;
   const bool lf = J.in.lane_fast != 0;
   t.es = (int)J.in.elem_stride;
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
     int l, kq;
-    item_lane_quad(tid + kGemmThreads * it, lf, l, kq);
+    item_lane_quad(tid + NTHR * it, lf, l, kq);
     const T* b = reinterpret_cast<const T*>(ib[l]);
     t.src[it] = b != nullptr ? b + (long long)(kq * 4) * t.es : nullptr;
     if (it == 0) t.soff0 = cm_off(l, kq * 4, kGemmLanes);
   }
-  // item it+1 is 2 quads further (lanes fast) or 32 lanes further (rows)
-  t.sstep = lf ? 2 * (kGemmLanes / 8) * 128 : 4 * 128;
+  // item it+1 is NTHR / 128 quads further (lanes fast) or NTHR / 8 lanes further (rows)
+  t.sstep = lf ? (NTHR / 128) * (kGemmLanes / 8) * 128 : (NTHR / 64) * 128;
   // chunk starts are 32 elements apart, so an aligned item stays aligned
   t.vec = t.es == 1;
 #pragma unroll
@@ -252,8 +253,10 @@ __device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
 }
 
 // loads of chunk k0 .. k0+31; only the job's last chunk checks k < K
-template <class T>
-__device__ __forceinline__ void a_load(AChunk<T>& a, const ATile<T>& t, int k0, int K, bool lane_fast, int tid) {
+template <class T, int NTHR = kGemmThreads>
+__device__ __forceinline__ void a_load(AChunk<T, NTHR>& a, const ATile<T, NTHR>& t, int k0, int K, bool lane_fast,
+                                       int tid) {
+  constexpr int kItems = 1024 / NTHR;
   const int o = k0 * t.es;
   if (k0 + kGemmKC <= K) {
     if (t.vec) {
@@ -286,7 +289,7 @@ __device__ __forceinline__ void a_load(AChunk<T>& a, const ATile<T>& t, int k0, 
 #pragma unroll
     for (int it = 0; it < kItems; it++) {
       int l, kq;
-      item_lane_quad(tid + kGemmThreads * it, lane_fast, l, kq);
+      item_lane_quad(tid + NTHR * it, lane_fast, l, kq);
       const T* p = t.src[it];
 #pragma unroll
       for (int e = 0; e < 4; e++) {
@@ -297,9 +300,10 @@ __device__ __forceinline__ void a_load(AChunk<T>& a, const ATile<T>& t, int k0, 
   }
 }
 
-template <class T>
-__device__ __forceinline__ void a_store(const AChunk<T>& a, const ATile<T>& t, unsigned char* Ahi,
+template <class T, int NTHR = kGemmThreads>
+__device__ __forceinline__ void a_store(const AChunk<T, NTHR>& a, const ATile<T, NTHR>& t, unsigned char* Ahi,
                                         unsigned char* Alo) {
+  constexpr int kItems = 1024 / NTHR;
 #pragma unroll
   for (int it = 0; it < kItems; it++) {
     float4 hi, lo;
@@ -316,11 +320,92 @@ __device__ __forceinline__ void a_store(const AChunk<T>& a, const ATile<T>& t, u
   }
 }
 
-// issue the asynchronous copy of operator chunk c (hi block then lo block)
-__device__ __forceinline__ void w_issue(const float* wsrc, int c, int NT, unsigned char* wbuf, int tid) {
+// issue the asynchronous copy of operator chunk c (hi block then lo block),
+// nthr threads
+__device__ __forceinline__ void w_issue(const float* wsrc, int c, int NT, unsigned char* wbuf, int tid,
+                                        int nthr = kGemmThreads) {
   const char* g = reinterpret_cast<const char*>(wsrc + (size_t)c * 2 * NT * kGemmKC);
   const uint32_t sb = smem_u32(wbuf);
-  for (int i = tid; i < NT * 16; i += kGemmThreads) cp_async16(sb + i * 16, g + (size_t)i * 16);
+  for (int i = tid; i < NT * 16; i += nthr) cp_async16(sb + i * 16, g + (size_t)i * 16);
+}
+
+// Output of a tile: total + corrections read back from tensor memory (warps
+// 0-3, 32 columns at a time), staged through shared memory, stored coalesced.
+// Every thread of the CTA takes part (two CTA barriers per 32 columns).
+__device__ __forceinline__ void gemm_epilogue(const GemmJobDev& J, uint32_t tmem, uint32_t total, uint32_t corr,
+                                              int NT, int tile_n, char* const* ob, float* stage, int tid, int warp,
+                                              int wl) {
+  // output mapping of staged element q = tid + 256 it -> (lane l, column n):
+  // 0: lanes fast in memory (columns); 1: real rows; 2: complex rows (re, im
+  // lanes of one row interleaved)
+  const int omode = J.out.lane_fast ? 0 : (J.out.parts == 2 ? 2 : 1);
+  const long long oes = J.out.elem_stride;
+  const int otype = J.out.type;
+  const double scale = J.scale;
+  const int nbase = tile_n * NT;
+  const int nvalid = min(NT, J.N - nbase);  // valid columns of this tile
+  for (int cc = 0; cc < NT; cc += 32) {
+    if (warp < 4) {  // warp w reads accumulator lanes 32w .. 32w+31
+      uint32_t r[32], q[32];
+      tmem_ld32_nowait(tmem + ((uint32_t)(warp * 32) << 16) + total + (uint32_t)cc, r);
+      tmem_ld32_nowait(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < 32; j++)
+        stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
+    }
+    __syncthreads();
+    // FP32 outputs of scale 1 are stored as they are (a round trip through
+    // FP64 would run at the FP64 rate on this GPU)
+    // A thread's lane (lanes fast) or column (rows) is the same in all 16
+    // iterations, so its addresses advance by a constant: staged element
+    // q = tid + 256 it is (lane l, column n) with
+    //   0: l = tid & 127, n = (tid >> 7) + 2 it
+    //   1: l = (tid >> 5) + 8 it, n = tid & 31
+    //   2: l = 2 (tid >> 6) + (tid & 1) + 8 it, n = (tid >> 1) & 31
+    const long long esz = otype == LT_F64 ? 8 : 4;
+    auto store_all = [&](auto store, auto mode) {
+      constexpr int M = decltype(mode)::value;
+      if constexpr (M == 0) {
+        const int l = tid & 127, n0 = tid >> 7;
+        char* base = ob[l];
+        if (base != nullptr) {
+          char* pp = base + (long long)(nbase + cc + n0) * oes * esz;
+          const long long step = 2 * oes * esz;
+          const float* sv = stage + l * 33 + n0;
+#pragma unroll 4
+          for (int it = 0; it < 4096 / kGemmThreads; it++, pp += step)
+            if (cc + n0 + 2 * it < nvalid) store(pp, sv[2 * it]);
+        }
+      } else {
+        const int n = M == 1 ? (tid & 31) : ((tid >> 1) & 31);
+        const int l0 = M == 1 ? (tid >> 5) : 2 * (tid >> 6) + (tid & 1);
+        if (cc + n < nvalid) {
+          const long long off = (long long)(nbase + cc + n) * oes * esz;
+#pragma unroll 4
+          for (int it = 0; it < 4096 / kGemmThreads; it++) {
+            const int l = l0 + 8 * it;
+            char* base = ob[l];
+            if (base != nullptr) store(base + off, stage[l * 33 + n]);
+          }
+        }
+      }
+    };
+    auto store_typed = [&](auto mode) {
+      if (otype == LT_F64 && scale == 1.0)  // no FP64 product (the conversion alone runs at the FP64 rate)
+        store_all([&](char* p, float f) { *reinterpret_cast<double*>(p) = (double)f; }, mode);
+      else if (otype == LT_F64)
+        store_all([&](char* p, float f) { *reinterpret_cast<double*>(p) = (double)f * scale; }, mode);
+      else if (scale == 1.0)
+        store_all([&](char* p, float f) { *reinterpret_cast<float*>(p) = f; }, mode);
+      else
+        store_all([&](char* p, float f) { *reinterpret_cast<float*>(p) = (float)((double)f * scale); }, mode);
+    };
+    if (omode == 0) store_typed(std::integral_constant<int, 0>());
+    else if (omode == 1) store_typed(std::integral_constant<int, 1>());
+    else store_typed(std::integral_constant<int, 2>());
+    __syncthreads();
+  }
 }
 
 template <class T>
@@ -437,83 +522,243 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
   asm volatile("cp.async.wait_all;" ::: "memory");
 
   if (ok) {
-    // output mapping of staged element q = tid + 256 it -> (lane l, column n):
-    // 0: lanes fast in memory (columns); 1: real rows; 2: complex rows (re, im
-    // lanes of one row interleaved)
-    const int omode = J.out.lane_fast ? 0 : (J.out.parts == 2 ? 2 : 1);
-    const long long oes = J.out.elem_stride;
-    const int otype = J.out.type;
-    const double scale = J.scale;
-    const int nbase = tile_n * NT;
-    const int nvalid = min(NT, J.N - nbase);  // valid columns of this tile
-    for (int cc = 0; cc < NT; cc += 32) {
-      if (warp < 4) {  // warp w reads accumulator lanes 32w .. 32w+31
-        uint32_t r[32], q[32];
-        tmem_ld32_nowait(tmem + ((uint32_t)(warp * 32) << 16) + total + (uint32_t)cc, r);
-        tmem_ld32_nowait(tmem + ((uint32_t)(warp * 32) << 16) + corr + (uint32_t)cc, q);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int j = 0; j < 32; j++)
-          stage[(warp * 32 + wl) * 33 + j] = __fadd_rn(__uint_as_float(r[j]), __uint_as_float(q[j]));
-      }
-      __syncthreads();
-      // FP32 outputs of scale 1 are stored as they are (a round trip through
-      // FP64 would run at the FP64 rate on this GPU)
-      // A thread's lane (lanes fast) or column (rows) is the same in all 16
-      // iterations, so its addresses advance by a constant: staged element
-      // q = tid + 256 it is (lane l, column n) with
-      //   0: l = tid & 127, n = (tid >> 7) + 2 it
-      //   1: l = (tid >> 5) + 8 it, n = tid & 31
-      //   2: l = 2 (tid >> 6) + (tid & 1) + 8 it, n = (tid >> 1) & 31
-      const long long esz = otype == LT_F64 ? 8 : 4;
-      auto store_all = [&](auto store, auto mode) {
-        constexpr int M = decltype(mode)::value;
-        if constexpr (M == 0) {
-          const int l = tid & 127, n0 = tid >> 7;
-          char* base = ob[l];
-          if (base != nullptr) {
-            char* pp = base + (long long)(nbase + cc + n0) * oes * esz;
-            const long long step = 2 * oes * esz;
-            const float* sv = stage + l * 33 + n0;
-#pragma unroll 4
-            for (int it = 0; it < 4096 / kGemmThreads; it++, pp += step)
-              if (cc + n0 + 2 * it < nvalid) store(pp, sv[2 * it]);
-          }
-        } else {
-          const int n = M == 1 ? (tid & 31) : ((tid >> 1) & 31);
-          const int l0 = M == 1 ? (tid >> 5) : 2 * (tid >> 6) + (tid & 1);
-          if (cc + n < nvalid) {
-            const long long off = (long long)(nbase + cc + n) * oes * esz;
-#pragma unroll 4
-            for (int it = 0; it < 4096 / kGemmThreads; it++) {
-              const int l = l0 + 8 * it;
-              char* base = ob[l];
-              if (base != nullptr) store(base + off, stage[l * 33 + n]);
-            }
-          }
-        }
-      };
-      auto store_typed = [&](auto mode) {
-        if (otype == LT_F64 && scale == 1.0)  // no FP64 product (the conversion alone runs at the FP64 rate)
-          store_all([&](char* p, float f) { *reinterpret_cast<double*>(p) = (double)f; }, mode);
-        else if (otype == LT_F64)
-          store_all([&](char* p, float f) { *reinterpret_cast<double*>(p) = (double)f * scale; }, mode);
-        else if (scale == 1.0)
-          store_all([&](char* p, float f) { *reinterpret_cast<float*>(p) = f; }, mode);
-        else
-          store_all([&](char* p, float f) { *reinterpret_cast<float*>(p) = (float)((double)f * scale); }, mode);
-      };
-      if (omode == 0) store_typed(std::integral_constant<int, 0>());
-      else if (omode == 1) store_typed(std::integral_constant<int, 1>());
-      else store_typed(std::integral_constant<int, 2>());
-      __syncthreads();
-    }
+    gemm_epilogue(J, tmem, total, corr, NT, tile_n, ob, stage, tid, warp, wl);
   } else {
     if (tid == 0 && J.status != nullptr) atomicOr(J.status, kStatusGemmTimeout);
     // the MMAs of the commit that was not seen to complete may still read
     // shared memory and write tensor memory: wait for them (bounded) before
     // the shared memory and the columns are given back
     mma_wait(mbar, pending, kWaitLimit);
+    tc_fence_after();
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised form (a tuned GEMM form): the same products, partials,
+// corrections and epilogue, with the per-chunk sequence split over roles that
+// hand chunks on through mbarriers instead of CTA barriers:
+//   * warps 0-3 (producers) stage chunk c (input converted to hi/lo TF32 and
+//     the operator chunk by cp.async) into buffer c % 2 and arrive on full;
+//   * warp 4, lane 0 waits for full (and for the flush of the chunk that last
+//     used the same partial columns), issues the chunk's 12 MMAs and commits
+//     to mdone;
+//   * warps 4-7 (one tensor-memory lane quadrant each) wait for mdone and add
+//     the chunk's partial into the running total, then arrive on flushed.
+// So staging chunk c+1, the MMAs of chunk c and the flush of chunk c-1 overlap.
+// Buffers and partials are double-buffered; each barrier's phases alternate
+// per use, and no role gets more than one phase ahead of another.  Every wait
+// is bounded: a warp that gives up sets the tile's abort flag, the others give
+// up at their next check, and the tile then drains its committed MMAs, sets
+// kStatusGemmTimeout and frees its tensor memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_arrive(uint64_t* m) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(m)) : "memory");
+}
+
+// bounded wait of one warp for phase `parity` of an mbarrier: lane 0 polls
+// (giving up early once the tile is aborted), the outcome goes to all lanes
+__device__ __forceinline__ bool warp_mbar_wait(uint64_t* m, uint32_t parity, long long limit,
+                                               volatile int* abort_flag) {
+  int ok = 0;
+  if ((threadIdx.x & 31) == 0) {
+    for (long long i = 0; i < limit; i++) {
+      if (mbar_try(m, parity)) {
+        ok = 1;
+        break;
+      }
+      if ((i & 1023) == 1023 && *abort_flag) break;
+    }
+    if (!ok) *abort_flag = 1;
+  }
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// running total += chunk partial (or = partial for the first chunk) for one
+// warp's 32 tensor-memory lanes (quadrant q) and all NT <= 64 columns, in
+// rounds of two 8-column blocks
+__device__ __forceinline__ void tmem_accumulate_warp(uint32_t tmem, uint32_t part, uint32_t total, int NT,
+                                                     bool first, int q) {
+  const uint32_t lane_base = (uint32_t)(q * 32) << 16;
+#pragma unroll
+  for (int h = 0; h < 4; h++) {
+    const int cb = 16 * h;
+    if (cb >= NT) break;  // NT is a multiple of 16: both blocks of a round are valid
+    uint32_t p[2][8], t[2][8];
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      tmem_ld8_nowait(tmem + lane_base + part + (uint32_t)(cb + 8 * b), p[b]);
+      if (!first) tmem_ld8_nowait(tmem + lane_base + total + (uint32_t)(cb + 8 * b), t[b]);
+    }
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      float v[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++)
+        v[j] = first ? __uint_as_float(p[b][j]) : __fadd_rn(__uint_as_float(t[b][j]), __uint_as_float(p[b][j]));
+      tmem_st8(tmem + lane_base + total + (uint32_t)(cb + 8 * b), v);
+    }
+  }
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+// shared memory of the warp-specialised form: two input chunks (hi, lo), two
+// operator chunks, six barriers and three words, the lane bases
+__host__ __device__ inline size_t gemm_ws_smem_base(int NT) {
+  return 65536 + (size_t)4 * NT * 128 + 64 + 2 * kGemmLanes * 8;
+}
+
+template <class T>
+__device__ __forceinline__ void gemm_tile_ws_t(const GemmJobDev& J, const int lane0, const int tile_n) {
+  const int NT = J.NT;  // <= 64
+  const int tid = threadIdx.x, warp = tid >> 5, wl = tid & 31;
+  extern __shared__ __align__(128) unsigned char sm[];
+  unsigned char* Ab[2] = {sm, sm + 32768};
+  unsigned char* Wb[2] = {sm + 65536, sm + 65536 + 2 * NT * 128};
+  unsigned char* tail = sm + 65536 + 4 * NT * 128;
+  uint64_t* full = reinterpret_cast<uint64_t*>(tail);  // [2]
+  uint64_t* mdone = full + 2;                          // [2]
+  uint64_t* flushed = full + 4;                        // [2]
+  uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 48);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tail + 52);
+  volatile int* issued = reinterpret_cast<volatile int*>(tail + 56);  // chunks whose MMAs were committed
+  const char** ib = reinterpret_cast<const char**>(tail + 64);
+  char** ob = reinterpret_cast<char**>(tail + 64 + kGemmLanes * 8);
+  float* stage = reinterpret_cast<float*>(sm);  // epilogue staging, after the last MMA
+
+  if (tid < kGemmLanes) {
+    const int l = lane0 + tid;
+    const char* ip = nullptr;
+    char* op = nullptr;
+    if (l < J.lanes) {
+      ip = lane_addr(J.in, l);
+      op = const_cast<char*>(lane_addr(J.out, l));
+    }
+    ib[tid] = ip;
+    ob[tid] = op;
+  }
+  const float* wsrc = J.w + (size_t)tile_n * J.kchunks * 2 * NT * kGemmKC;
+  const uint32_t ncols = gemm_tmem_cols(NT);
+  const uint32_t corr = 2u * (uint32_t)NT, total = 3u * (uint32_t)NT;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < 2; s++) {
+      mbar_init(&full[s], 128);
+      mbar_init(&mdone[s], 1);
+      mbar_init(&flushed[s], 128);
+    }
+    *abort_flag = 0;
+    *issued = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NT >> 3) << 17) | ((128u >> 4) << 24);
+  const uint32_t a_lbo = (kGemmLanes / 8) * 128, w_lbo = (uint32_t)(NT / 8) * 128;
+  const long long wait_limit = g_gemm_wait_limit;
+  const int K = J.K, kchunks = J.kchunks;
+
+  if (warp < 4) {
+    // producers: stage chunk c into buffer c % 2 once the MMAs of chunk c-2 are done with it
+    const bool in_lf = J.in.lane_fast != 0;
+    ATile<T, 128> at;
+    a_setup<T, 128>(at, J, ib, tid);
+    AChunk<T, 128> a;
+    a_load<T, 128>(a, at, 0, K, in_lf, tid);
+    for (int c = 0; c < kchunks; c++) {
+      const int s = c & 1;
+      if (c >= 2 && !warp_mbar_wait(&mdone[s], (uint32_t)(((c >> 1) - 1) & 1), wait_limit, abort_flag)) break;
+      w_issue(wsrc, c, NT, Wb[s], tid, 128);
+      cp_async_commit();
+      a_store<T, 128>(a, at, Ab[s], Ab[s] + 16384);
+      if (c + 1 < kchunks) a_load<T, 128>(a, at, (c + 1) * kGemmKC, K, in_lf, tid);
+      asm volatile("cp.async.wait_all;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(&full[s]);
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+  } else {
+    // MMA issue (warp 4, lane 0) and the flush of the previous chunk (warps 4-7)
+    const int quad = warp - 4;
+    for (int c = 0; c <= kchunks; c++) {
+      if (c < kchunks && warp == 4) {
+        int ok = 1;
+        if (wl == 0) {
+          const int s = c & 1;
+          ok = 0;
+          for (long long i = 0; i < wait_limit && !ok; i++) {
+            ok = mbar_try(&full[s], (uint32_t)((c >> 1) & 1)) ? 1 : 0;
+            if (!ok && (i & 1023) == 1023 && *abort_flag) break;
+          }
+          if (ok && c >= 2) {
+            ok = 0;
+            for (long long i = 0; i < wait_limit && !ok; i++) {
+              ok = mbar_try(&flushed[s], (uint32_t)(((c >> 1) - 1) & 1)) ? 1 : 0;
+              if (!ok && (i & 1023) == 1023 && *abort_flag) break;
+            }
+          }
+          if (ok) {
+            tc_fence_after();
+            unsigned char* Ahi = Ab[s];
+            unsigned char* Alo = Ab[s] + 16384;
+            unsigned char* Whi = Wb[s];
+            unsigned char* Wlo = Whi + NT * 128;
+            const uint32_t part = (uint32_t)(s * NT);
+#pragma unroll
+            for (int ks = 0; ks < kGemmKC / 8; ks++) {
+              const uint64_t ah = umma_desc(smem_u32(Ahi) + ks * 2 * a_lbo, a_lbo, 128);
+              const uint64_t al = umma_desc(smem_u32(Alo) + ks * 2 * a_lbo, a_lbo, 128);
+              const uint64_t wh = umma_desc(smem_u32(Whi) + ks * 2 * w_lbo, w_lbo, 128);
+              const uint64_t wlo = umma_desc(smem_u32(Wlo) + ks * 2 * w_lbo, w_lbo, 128);
+              const uint32_t acc = (c > 0 || ks > 0) ? 1u : 0u;
+              mma_tf32(tmem + corr, al, wh, idesc, acc);
+              mma_tf32(tmem + corr, ah, wlo, idesc, 1u);
+              mma_tf32(tmem + part, ah, wh, idesc, ks > 0 ? 1u : 0u);  // fresh partial per chunk
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_u32(&mdone[s]))
+                         : "memory");
+            *issued = c + 1;
+          } else {
+            *abort_flag = 1;
+          }
+        }
+        if (__shfl_sync(0xffffffffu, ok, 0) == 0) break;
+      }
+      if (c >= 1) {
+        const int c1 = c - 1, s1 = c1 & 1;
+        if (!warp_mbar_wait(&mdone[s1], (uint32_t)((c1 >> 1) & 1), wait_limit, abort_flag)) break;
+        tc_fence_after();
+        tmem_accumulate_warp(tmem, (uint32_t)(s1 * NT), total, NT, c1 == 0, quad);
+        tc_fence_before();
+        mbar_arrive(&flushed[s1]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const bool ok = *abort_flag == 0;
+  if (ok) {
+    gemm_epilogue(J, tmem, total, corr, NT, tile_n, ob, stage, tid, warp, wl);
+  } else {
+    if (tid == 0) {
+      if (J.status != nullptr) atomicOr(J.status, kStatusGemmTimeout);
+      // the last commit on each buffer may still be in flight: wait for it
+      // (bounded) before the shared memory and the columns are given back
+      const int n = *issued;
+      for (int c = n - 2 < 0 ? 0 : n - 2; c < n; c++)
+        for (long long i = 0; i < kWaitLimit; i++)
+          if (mbar_try(&mdone[c & 1], (uint32_t)((c >> 1) & 1))) break;
+    }
     tc_fence_after();
   }
   tc_fence_before();
@@ -532,6 +777,16 @@ __global__ void __launch_bounds__(kGemmThreads, 2) k_lane_gemm(const GemmJobDev*
                                                                 const int4* __restrict__ tiles) {
   const int4 tl = tiles[blockIdx.x];
   gemm_tile(jobs[tl.x], tl.y, tl.z);
+}
+
+// the same tiles in the warp-specialised form (output tiles of at most 64 columns)
+__global__ void __launch_bounds__(kGemmThreads, 2) k_lane_gemm_ws(const GemmJobDev* __restrict__ jobs,
+                                                                   const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  const GemmJobDev& J = jobs[tl.x];
+  if (J.active != nullptr && *J.active == 0) return;
+  if (J.in.type == LT_F64) gemm_tile_ws_t<double>(J, tl.y, tl.z);
+  else gemm_tile_ws_t<float>(J, tl.y, tl.z);
 }
 
 // single job passed by value: block b -> lanes (b / ntiles) * 128, output tile b % ntiles
@@ -622,6 +877,11 @@ size_t gemm_smem_bytes(int NT) {
   return std::max(base, floor_b);
 }
 
+size_t gemm_ws_smem_bytes(int NT) {
+  // as gemm_smem_bytes: no more CTAs per SM than the tensor-memory columns allow
+  return std::max(dev::gemm_ws_smem_base(NT), gemm_smem_bytes(NT));
+}
+
 cudaError_t configure_gemm_kernels() {
   static PerDeviceFlag done;
   if (done.test()) return cudaSuccess;
@@ -630,6 +890,9 @@ cudaError_t configure_gemm_kernels() {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(dev::k_lane_gemm_one, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)gemm_smem_bytes(128));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(dev::k_lane_gemm_ws, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)gemm_ws_smem_bytes(64));
   if (e == cudaSuccess) done.set();
   return e;
 }
@@ -698,9 +961,14 @@ LaneSideDev lane_cols(void* const* ptrs, int nf, int cols, int len, int row_len,
 }
 
 cudaError_t launch_lane_gemm(const GemmJobDev* jobs, const int4* tiles, int ntiles_total, int max_nt,
-                             cudaStream_t st) {
+                             cudaStream_t st, bool ws) {
   if (ntiles_total <= 0) return cudaSuccess;
-  dev::k_lane_gemm<<<ntiles_total, kGemmThreads, gemm_smem_bytes(max_nt), st>>>(jobs, tiles);
+  if (ws) {
+    if (max_nt > 64) return cudaErrorInvalidValue;
+    dev::k_lane_gemm_ws<<<ntiles_total, kGemmThreads, gemm_ws_smem_bytes(max_nt), st>>>(jobs, tiles);
+  } else {
+    dev::k_lane_gemm<<<ntiles_total, kGemmThreads, gemm_smem_bytes(max_nt), st>>>(jobs, tiles);
+  }
   return cudaGetLastError();
 }
 

@@ -59,10 +59,13 @@ std::vector<float> pack_gemm_w(const std::vector<double>& W, int N, int K, int N
 // Tiles (job, first lane, output tile, 0) of a job list.
 void gemm_tiles(const std::vector<GemmJobDev>& jobs, std::vector<int4>& tiles);
 size_t gemm_smem_bytes(int NT);
+// the warp-specialised form's (NT <= 64): two input and two operator chunk buffers
+size_t gemm_ws_smem_bytes(int NT);
 cudaError_t configure_gemm_kernels();
-// jobs and tiles are device arrays; max_nt = largest NT among the jobs.
+// jobs and tiles are device arrays; max_nt = largest NT among the jobs.  ws:
+// the warp-specialised form (producer, MMA and flush warps; max_nt <= 64).
 cudaError_t launch_lane_gemm(const GemmJobDev* jobs, const int4* tiles, int ntiles_total, int max_nt,
-                             cudaStream_t st);
+                             cudaStream_t st, bool ws = false);
 
 // Poll limit of the kernel's bounded completion waits on the current device
 // (negative: the default, 2^22 polls).  A small limit makes the waits run out

@@ -37,6 +37,7 @@ enum StepKernel {
 
 struct StepLaunch {
   int kernel;
+  int gemm_ws = 0;  // K_GEMM: 1 for the warp-specialised form
   int pass = -1;  // launches of one pass share the id (the autotuner swaps whole passes)
   size_t smem;
   std::vector<int4> items;       // (case index, first lane, lane count, 0)
@@ -65,6 +66,7 @@ struct MixedOps {
   const float* pf = nullptr;  // Poisson eigenbasis forward: (nx - 2) x (nx - 2)
   const float* pb = nullptr;  // Poisson eigenbasis backward: (nx - 2) x (nx - 2)
   int ntmax = 64;  // the widest GEMM output tile these operators are packed for (64 or 128)
+  int ws = 0;      // 1: the GEMMs in the warp-specialised form (ntmax 64)
 };
 // variant 0: a CTA per lane; 1: 128-thread CTAs where that form exists, else
 // one thread per lane; 2: one thread per (field, parity) sub-lane where that

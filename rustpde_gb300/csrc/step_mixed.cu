@@ -191,7 +191,8 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
   auto add_gemm = [&](const GemmJobDev& j) {
     StepLaunch L;
     L.kernel = K_GEMM;
-    L.smem = gemm_smem_bytes(j.NT);
+    L.gemm_ws = ops.ws;
+    L.smem = ops.ws ? gemm_ws_smem_bytes(j.NT) : gemm_smem_bytes(j.NT);
     L.jobs.push_back(j);
     push(L);
   };
@@ -285,8 +286,9 @@ StepPlan build_mixed_plan(const CaseDev& c, const MixedOps& ops, int variant) {
     L.jobs.push_back(make_gemm_job(lane_rows(d_in, 1, ny, mxc, myld, LT_F32, false),
                                    lane_rows(d_out, 1, ny, nx, nx, LT_F32, false), ops.xd, mxc, nx, 1.0, c.status, ops.ntmax));
     size_t sm = 0;
-    for (const GemmJobDev& j : L.jobs) sm = std::max(sm, gemm_smem_bytes(j.NT));
+    for (const GemmJobDev& j : L.jobs) sm = std::max(sm, ops.ws ? gemm_ws_smem_bytes(j.NT) : gemm_smem_bytes(j.NT));
     L.smem = sm;
+    L.gemm_ws = ops.ws;
     p.launches.push_back(L);
   }
   // products (FP32)

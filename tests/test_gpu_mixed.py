@@ -207,14 +207,16 @@ def test_transform_gemm_or_butterfly(R, monkeypatch):
             assert np.array_equal(bm.cases[i].get(f), bf.cases[i].get(f)), (i, f)
 
 
-def test_wide_gemm_tile_form(R, monkeypatch):
-    # form 4: the tensor-core GEMMs with output tiles of up to 128 columns (one
-    # CTA per SM holding all 512 tensor-memory columns) instead of 64; every
-    # other pass as form 0.  The same products, chunk partials and corrections
-    # per output element
+@pytest.mark.parametrize("gemm_form", ["4", "5"])
+def test_wide_gemm_tile_form(R, monkeypatch, gemm_form):
+    # GEMM form 4: output tiles of up to 128 columns (one CTA per SM holding all
+    # 512 tensor-memory columns) instead of 64; form 5: 64-column tiles in the
+    # warp-specialised kernel (producer, MMA and flush warps).  Every other
+    # pass as form 0.  The same products, chunk partials and corrections per
+    # output element, in the same order: bitwise the same numbers
     params = MIX_PARAMS + [(45, 33, 1e5, 1.0, 5e-3, 1.0, O.PERIODIC)]
     out = []
-    for form in ("0", "4"):
+    for form in ("0", gemm_form):
         monkeypatch.setenv("RBC_BATCH_FORM", "0;" + form)
         b = R.Batch(params, precision=R.PREC_MIXED)
         assert set(b.tuning_forms().replace(",", "").replace(";", "")) <= {form, "0"}
@@ -229,7 +231,7 @@ def test_wide_gemm_tile_form(R, monkeypatch):
         for k, f in enumerate(FIELDS):
             same &= bool(np.array_equal(out[0][i][k], out[1][i][k]))
             assert rel(out[1][i][k], out[0][i][k]) < FORMS_TOL, (i, f)
-    print("wide GEMM tiles bitwise equal to 64-column tiles:", same)
+    assert same
 
 
 def test_mixed_batch_one_call_equals_single_steps(R, monkeypatch):
