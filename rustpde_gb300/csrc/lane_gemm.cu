@@ -540,8 +540,9 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
 // Warp-specialised form (a tuned GEMM form): the same products, partials,
 // corrections and epilogue, with the per-chunk sequence split over roles that
 // hand chunks on through mbarriers instead of CTA barriers:
-//   * warps 0-3 (producers) stage chunk c (input converted to hi/lo TF32 and
-//     the operator chunk by cp.async) into buffer c % 2 and arrive on full;
+//   * warps 0-3 (producers) stage chunk c (input converted to hi/lo TF32; the
+//     operator chunk as one bulk copy whose bytes the same barrier counts)
+//     into buffer c % 2 and arrive on full;
 //   * warp 4, lane 0 waits for full (and for the flush of the chunk that last
 //     used the same partial columns), issues the chunk's 12 MMAs and commits
 //     to mdone;
@@ -556,6 +557,21 @@ __device__ __forceinline__ void gemm_tile_t(const GemmJobDev& J, const int lane0
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void mbar_arrive(uint64_t* m) {
   asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_u32(m)) : "memory");
+}
+// one arrival that also announces `bytes` of asynchronous transfer to come
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* m, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                   smem_u32(m)),
+               "r"(bytes)
+               : "memory");
+}
+// bulk copy global -> shared (16-byte aligned, size a multiple of 16), its
+// completion counted on the mbarrier's transaction count
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* m) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(m))
+               : "memory");
 }
 
 // bounded wait of one warp for phase `parity` of an mbarrier: lane 0 polls
@@ -624,7 +640,8 @@ __device__ __forceinline__ void gemm_tile_ws_t(const GemmJobDev& J, const int la
   uint64_t* flushed = full + 4;                        // [2]
   uint32_t* slot = reinterpret_cast<uint32_t*>(tail + 48);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tail + 52);
-  volatile int* issued = reinterpret_cast<volatile int*>(tail + 56);  // chunks whose MMAs were committed
+  volatile int* issued = reinterpret_cast<volatile int*>(tail + 56);   // chunks whose MMAs were committed
+  volatile int* wissued = reinterpret_cast<volatile int*>(tail + 60);  // chunks whose operator copy was issued
   const char** ib = reinterpret_cast<const char**>(tail + 64);
   char** ob = reinterpret_cast<char**>(tail + 64 + kGemmLanes * 8);
   float* stage = reinterpret_cast<float*>(sm);  // epilogue staging, after the last MMA
@@ -650,12 +667,13 @@ __device__ __forceinline__ void gemm_tile_ws_t(const GemmJobDev& J, const int la
   }
   if (tid == 0) {
     for (int s = 0; s < 2; s++) {
-      mbar_init(&full[s], 128);
+      mbar_init(&full[s], 129);  // the producers, and the arrival that announces the operator chunk's bytes
       mbar_init(&mdone[s], 1);
       mbar_init(&flushed[s], 128);
     }
     *abort_flag = 0;
     *issued = 0;
+    *wissued = 0;
   }
   tc_fence_before();
   __syncthreads();
@@ -676,15 +694,19 @@ __device__ __forceinline__ void gemm_tile_ws_t(const GemmJobDev& J, const int la
     for (int c = 0; c < kchunks; c++) {
       const int s = c & 1;
       if (c >= 2 && !warp_mbar_wait(&mdone[s], (uint32_t)(((c >> 1) - 1) & 1), wait_limit, abort_flag)) break;
-      w_issue(wsrc, c, NT, Wb[s], tid, 128);
-      cp_async_commit();
+      if (tid == 0) {
+        const uint32_t wbytes = (uint32_t)(2 * NT * kGemmKC * 4);
+        mbar_arrive_expect_tx(&full[s], wbytes);
+        bulk_g2s(Wb[s], wsrc + (size_t)c * 2 * NT * kGemmKC, wbytes, &full[s]);
+        *wissued = c + 1;
+      }
+      // no exit between the copy's issue and this chunk's arrival: every issued
+      // copy completes its phase of full, which an aborted tile waits for
       a_store<T, 128>(a, at, Ab[s], Ab[s] + 16384);
       if (c + 1 < kchunks) a_load<T, 128>(a, at, (c + 1) * kGemmKC, K, in_lf, tid);
-      asm volatile("cp.async.wait_all;" ::: "memory");
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(&full[s]);
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
   } else {
     // MMA issue (warp 4, lane 0) and the flush of the previous chunk (warps 4-7)
     const int quad = warp - 4;
@@ -752,9 +774,13 @@ __device__ __forceinline__ void gemm_tile_ws_t(const GemmJobDev& J, const int la
   } else {
     if (tid == 0) {
       if (J.status != nullptr) atomicOr(J.status, kStatusGemmTimeout);
-      // the last commit on each buffer may still be in flight: wait for it
-      // (bounded) before the shared memory and the columns are given back
-      const int n = *issued;
+      // operator copies not consumed by an MMA, and the last commit on each
+      // buffer, may still be in flight: wait for them (bounded) before the
+      // shared memory and the columns are given back
+      const int n = *issued, nw = *wissued;
+      for (int c = n; c < nw; c++)
+        for (long long i = 0; i < kWaitLimit; i++)
+          if (mbar_try(&full[c & 1], (uint32_t)((c >> 1) & 1))) break;
       for (int c = n - 2 < 0 ? 0 : n - 2; c < n; c++)
         for (long long i = 0; i < kWaitLimit; i++)
           if (mbar_try(&mdone[c & 1], (uint32_t)((c >> 1) & 1))) break;
