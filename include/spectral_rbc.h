@@ -108,8 +108,10 @@ int rbc_set_temperature_noise(RbcCase* c, double amp, uint64_t seed);
  * 189-190): conv_ux, conv_uy and conv_temp subtract (-1/eta) mask w with
  * eta = 1e-2 and w = ux, uy, T + T_bc - value (navier.rs:551-560, 579-584,
  * 603-608).  mask, value: physical nx*ny arrays on the temperature grid
- * (value NULL = 0); mask NULL removes the solid.  FP64 cases stepped on their
- * own only (RBC_ERR_UNSUPPORTED for batch members and RBC_PREC_MIXED). */
+ * (value NULL = 0); mask NULL removes the solid.  FP64 cases, stepped on
+ * their own or in a batch (the batch rebuilds the case's group plan and its
+ * graphs; a batch case then steps bitwise as it does alone);
+ * RBC_ERR_UNSUPPORTED for RBC_PREC_MIXED. */
 int rbc_set_solid(RbcCase* c, const double* mask, const double* value, size_t n_doubles);
 /* present = 1 with the mask and value (either may be NULL) when a solid is set */
 int rbc_get_solid(const RbcCase* c, int* present, double* mask, double* value, size_t n_doubles);

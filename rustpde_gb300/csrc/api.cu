@@ -258,6 +258,8 @@ struct RbcCase {
   // device arrays [(-1/eta) mask | value] the x pass reads
   std::vector<double> solid_host[2];
   double* solid_mem = nullptr;
+  struct RbcBatch* batch = nullptr;  // the batch a batch case belongs to (its descriptor is batch->d_cases[batch_index])
+  int batch_index = -1;
   ~RbcCase() {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
@@ -946,13 +948,17 @@ int rbc_step(RbcCase* c, int nsteps) {
   API_END
 }
 
+// a batch case's solid mask changed (defined with the batch)
+static void batch_solid_changed(RbcCase* c);
+
 // navier.rs:189-190 (`navier.solid = Some([mask, value])`) with the damping of
 // conv_ux / conv_uy / conv_temp (navier.rs:551-560, 579-584, 603-608).
 int rbc_set_solid(RbcCase* c, const double* mask, const double* value, size_t n_doubles) {
   API_BEGIN
   require(c != nullptr, "rbc_set_solid: null case");
-  if (c->in_batch) throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_set_solid: set solid masks on cases stepped on their own");
   if (c->hd.mixed) throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_set_solid: solid masks need RBC_PREC_FP64");
+  if (c->in_batch && c->batch == nullptr)
+    throw ApiError(RBC_ERR_UNSUPPORTED, "rbc_set_solid: the case belongs to a serving loop");
   const size_t np = (size_t)c->p.nx * c->p.ny;
   c->sync();
   if (mask == nullptr) {
@@ -979,7 +985,8 @@ int rbc_set_solid(RbcCase* c, const double* mask, const double* value, size_t n_
   cuda_check(cudaMemcpy(c->d_case, &c->hd, sizeof(CaseDev), cudaMemcpyHostToDevice), "copy case descriptor");
   // the x pass's lane count (and shared memory) depends on the solid
   c->plan = build_step_plan(c->hd);
-  capture_graph(c);
+  if (c->batch != nullptr) batch_solid_changed(c);
+  else capture_graph(c);
   API_END
 }
 
@@ -1242,6 +1249,7 @@ struct RbcBatch {
     cudaGraphExec_t gexec = nullptr;
   };
   std::vector<Bucket> buckets;
+  bool use_priority = false;      // the critical group's branch captured at high priority
   std::vector<size_t> io_order;  // groups in the order their inputs are copied in: shortest step first
   std::vector<cudaEvent_t> io_events;  // a group's input copy done (rbc_batch_step_io)
   struct Tuned {
@@ -1279,6 +1287,88 @@ struct RbcBatch {
     if (stream) cudaStreamDestroy(stream);
   }
 };
+
+// The batch step as CUDA graphs: one graph with a branch per group (the
+// critical group's branch at high priority), and one graph per group for
+// rbc_batch_step_io.  Earlier graphs are replaced.
+static void batch_capture_graphs(RbcBatch* b) {
+  const size_t nb = b->buckets.size();
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->gexec = nullptr;
+  b->graph = nullptr;
+  for (auto& bk : b->buckets) {
+    if (bk.gexec) cudaGraphExecDestroy(bk.gexec);
+    if (bk.graph) cudaGraphDestroy(bk.graph);
+    bk.gexec = nullptr;
+    bk.graph = nullptr;
+  }
+  b->launches = 0;
+  cuda_check(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+  cudaError_t le = cudaEventRecord(b->events[nb], b->stream);
+  for (size_t k = 0; k < nb && le == cudaSuccess; k++) {
+    auto& bk = b->buckets[k];
+    cudaStream_t s = b->branch[k];
+    le = cudaStreamWaitEvent(s, b->events[nb], 0);
+    for (size_t li = 0; li < bk.plan.launches.size() && le == cudaSuccess; li++) {
+      le = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
+      b->launches++;
+    }
+    if (le == cudaSuccess) le = cudaEventRecord(b->events[k], s);
+    if (le == cudaSuccess) le = cudaStreamWaitEvent(b->stream, b->events[k], 0);
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+  cuda_check(le, "batch capture");
+  cuda_check(ce, "end capture");
+  b->graph = g;
+  cuda_check(cudaGraphInstantiate(&b->gexec, g, b->use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
+             "graph instantiate");
+  // rbc_batch_step_io: one graph per group, captured on the group's branch
+  // stream (its priority), and the groups' inputs copied in shortest step
+  // first: that group computes while the longer group's input arrives, and
+  // its results go back while the longer group still runs (256-case ensemble:
+  // 4.32 ms per step against 4.78 ms longest first, 5.3 ms with the copies
+  // and the step in sequence)
+  for (size_t k = 0; k < nb; k++) {
+    auto& bk = b->buckets[k];
+    cudaStream_t s = b->branch[k];
+    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t e = cudaSuccess;
+    for (size_t li = 0; li < bk.plan.launches.size() && e == cudaSuccess; li++)
+      e = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
+    cudaGraph_t bg = nullptr;
+    const cudaError_t be = cudaStreamEndCapture(s, &bg);
+    bk.graph = bg;  // freed by the destructor whatever follows
+    cuda_check(e, "group capture");
+    cuda_check(be, "end capture");
+    cuda_check(cudaGraphInstantiate(&bk.gexec, bg, b->use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
+               "graph instantiate");
+  }
+}
+
+// A batch case's solid mask changed: its descriptor in the batch's table, its
+// group's plan (the x pass's lanes and shared memory follow the mask) and the
+// batch's graphs are rebuilt (FP64 groups; the mixed form has no solid lane).
+static void batch_solid_changed(RbcCase* c) {
+  RbcBatch* b = c->batch;
+  cuda_check(cudaStreamSynchronize(b->stream), "stream synchronize");
+  for (auto s : b->branch) cuda_check(cudaStreamSynchronize(s), "stream synchronize");
+  cuda_check(cudaMemcpy(b->d_cases + c->batch_index, &c->hd, sizeof(CaseDev), cudaMemcpyHostToDevice),
+             "copy case descriptor");
+  for (auto& bk : b->buckets) {
+    if (std::find(bk.members.begin(), bk.members.end(), c->batch_index) == bk.members.end()) continue;
+    std::vector<const StepPlan*> plans;
+    for (int m : bk.members) {
+      b->cases[m]->plan = build_step_plan(b->cases[m]->hd);
+      plans.push_back(&b->cases[m]->plan);
+    }
+    bk.plan = merge_plans(plans, bk.members, {});
+    bk.dp = DevPlan();
+    upload_plan(b->arena, bk.plan, bk.dp);
+  }
+  batch_capture_graphs(b);
+}
 
 extern "C" {
 
@@ -1335,6 +1425,8 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     c->stream = b->stream;
     c->own_stream = false;
     c->in_batch = true;
+    c->batch = b.get();
+    c->batch_index = i;
     build_case(c.get(), false, b->d_state + b->state_offset[i]);
     b->cases.push_back(c.release());
   }
@@ -1562,47 +1654,8 @@ int rbc_batch_create(const RbcParams* params, int ncases, RbcBatch** out) {
     cuda_check(cudaStreamCreateWithPriority(&b->branch[k], cudaStreamNonBlocking, prio), "stream");
   }
   for (auto& e : b->events) cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
-  cuda_check(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
-  cudaError_t le = cudaEventRecord(b->events[nb], b->stream);
-  for (size_t k = 0; k < nb && le == cudaSuccess; k++) {
-    auto& bk = b->buckets[k];
-    cudaStream_t s = b->branch[k];
-    le = cudaStreamWaitEvent(s, b->events[nb], 0);
-    for (size_t li = 0; li < bk.plan.launches.size() && le == cudaSuccess; li++) {
-      le = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
-      b->launches++;
-    }
-    if (le == cudaSuccess) le = cudaEventRecord(b->events[k], s);
-    if (le == cudaSuccess) le = cudaStreamWaitEvent(b->stream, b->events[k], 0);
-  }
-  cudaGraph_t g = nullptr;
-  cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
-  cuda_check(le, "batch capture");
-  cuda_check(ce, "end capture");
-  b->graph = g;
-  cuda_check(cudaGraphInstantiate(&b->gexec, g, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
-             "graph instantiate");
-  // rbc_batch_step_io: one graph per group, captured on the group's branch
-  // stream (its priority), and the groups' inputs copied in shortest step
-  // first: that group computes while the longer group's input arrives, and
-  // its results go back while the longer group still runs (256-case ensemble:
-  // 4.32 ms per step against 4.78 ms longest first, 5.3 ms with the copies
-  // and the step in sequence)
-  for (size_t k = 0; k < nb; k++) {
-    auto& bk = b->buckets[k];
-    cudaStream_t s = b->branch[k];
-    cuda_check(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
-    cudaError_t e = cudaSuccess;
-    for (size_t li = 0; li < bk.plan.launches.size() && e == cudaSuccess; li++)
-      e = launch_entry(bk.plan.launches[li], bk.dp, li, s, b->d_cases);
-    cudaGraph_t bg = nullptr;
-    const cudaError_t be = cudaStreamEndCapture(s, &bg);
-    bk.graph = bg;  // freed by the destructor whatever follows
-    cuda_check(e, "group capture");
-    cuda_check(be, "end capture");
-    cuda_check(cudaGraphInstantiate(&bk.gexec, bg, use_priority ? cudaGraphInstantiateFlagUseNodePriority : 0),
-               "graph instantiate");
-  }
+  b->use_priority = use_priority;
+  batch_capture_graphs(b.get());
   b->io_order.resize(nb);
   for (size_t k = 0; k < nb; k++) b->io_order[k] = k;
   std::stable_sort(b->io_order.begin(), b->io_order.end(),
