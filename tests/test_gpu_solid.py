@@ -97,8 +97,9 @@ def test_solid_changes_the_flow(R):
 
 
 def test_solid_unsupported_forms(R):
+    # the mixed form has no solid lane, in a batch or alone (FP64 batches take masks)
     params = [(32, 17, 1e5, 1.0, 0.005, 1.0, R.PERIODIC)] * 2
-    b = R.Batch(params)
+    b = R.Batch(params, precision=R.PREC_MIXED)
     m = np.zeros((32, 17))
     with pytest.raises(R.RbcError) as e:
         b.cases[0].solid = [m, m]
