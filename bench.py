@@ -58,7 +58,7 @@ METRIC = "grid-pt-steps/s"
 NX, NY, RA, PR, DT, ASPECT = 512, 257, 1e7, 1.0, 1e-3, 2.0
 WORKLOAD_512 = "Navier2D::new_periodic 512x257 Ra=1e7 Pr=1 dt=1e-3 aspect=2 (FourierR2c x ChebDirichlet), plain FP64"
 ENSEMBLE_N, ENSEMBLE_SEED = 256, 2024
-WORKLOAD_ENS = ("256-case RBC ensemble of uneven size (nx,ny in {64,128,256}^2, box/periodic 50/50, "
+WORKLOAD_ENS = ("{n}-case RBC ensemble of uneven size (nx,ny in {64,128,256}^2, box/periodic 50/50, "
                 "Ra log-U[1e4,1e8], Pr {0.7,1,7}, aspect U[1,2], dt=min(0.02,2/sqrt(Ra)), seed 2024), "
                 "batched mixed precision")
 
@@ -203,10 +203,11 @@ def barrier(world):
 # ---------------------------------------------------------------------------
 def ensemble_config(params):
     """The workload's `config`, shared by both arms (what is run, not how)."""
-    return {"workload": WORKLOAD_ENS, "cases": len(params), "grid_points": sum(p[0] * p[1] for p in params),
+    return {"workload": WORKLOAD_ENS.replace("{n}", str(len(params))), "cases": len(params),
+            "grid_points": sum(p[0] * p[1] for p in params),
             "seeds": "ensemble 2024, initial fields 1000 + case index",
             "l2": "GPU: flushed before the timed call (256 MiB memset outside the events); the state "
-                  "(221 MB) exceeds L2"}
+                  "(221 MB for 256 cases) exceeds L2"}
 
 
 def transform_flops(params):
