@@ -171,7 +171,7 @@ int rbc_get_coords(const RbcCase* c, int field, double* x, double* y);
 /* diagnostics: RBC_NU, RBC_NUVOL, RBC_RE, RBC_KE, RBC_DIV_NORM */
 int rbc_eval(RbcCase* c, int what, double* out);
 int rbc_get_stream(RbcCase* c, void** stream);
-/* device bytes held by the case (state, scratch, operators) */
+/* device bytes held by the case (state, scratch, operators, step tables, solid mask) */
 int rbc_device_bytes(const RbcCase* c, size_t* bytes);
 
 /* Time the kernels of the step individually: runs nsteps steps launching each

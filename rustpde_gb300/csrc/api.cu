@@ -61,12 +61,15 @@ static double get_ka(double ra, double pr, double h) { return std::sqrt(1.0 / ((
 using namespace rbc;
 
 // Device copies of a step plan: work tables of the lane kernels, job and tile
-// tables of the tensor-core GEMM launches.
+// tables of the tensor-core GEMM launches.  own: the tables' memory when the
+// plan holds it itself (plans rebuilt during a case's life, on a solid mask
+// change); replacing such a plan frees the old tables.
 struct DevPlan {
   std::vector<int4*> work;
   std::vector<GemmJobDev*> jobs;
   std::vector<int4*> tiles;
   std::vector<int> ntiles, max_nt;
+  std::shared_ptr<Arena> own;
 };
 
 static void upload_plan(Arena& A, const StepPlan& plan, DevPlan& dp) {
@@ -92,6 +95,18 @@ static void upload_plan(Arena& A, const StepPlan& plan, DevPlan& dp) {
     dp.ntiles.push_back(nt);
     dp.max_nt.push_back(mnt);
   }
+}
+
+// Upload a plan into memory of its own, replacing dp (and freeing the tables
+// dp held itself).  No launch may still use dp's tables: the caller has
+// synchronised the streams that ran them, and replaces the graphs that name
+// them before the next step.
+static void upload_plan_owned(const StepPlan& plan, DevPlan& dp) {
+  auto mem = std::make_shared<Arena>();
+  DevPlan fresh;
+  upload_plan(*mem, plan, fresh);
+  fresh.own = std::move(mem);
+  dp = std::move(fresh);
 }
 
 static cudaError_t launch_entry(const StepLaunch& L, const DevPlan& dp, size_t k, cudaStream_t st,
@@ -685,7 +700,7 @@ void capture_graph(RbcCase* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   c->gexec = nullptr;
   c->graph = nullptr;
-  upload_plan(c->arena, c->plan, c->dp);
+  upload_plan_owned(c->plan, c->dp);
   cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
   cudaError_t le = cudaSuccess;
   for (size_t k = 0; k < c->plan.launches.size(); k++) {
@@ -1225,7 +1240,10 @@ int rbc_get_stream(RbcCase* c, void** stream) {
 int rbc_device_bytes(const RbcCase* c, size_t* bytes) {
   API_BEGIN
   require(c && bytes, "null argument");
-  *bytes = c->arena.bytes();
+  size_t n = c->arena.bytes();
+  if (c->dp.own) n += c->dp.own->bytes();
+  if (c->solid_mem) n += 2 * (size_t)c->p.nx * c->p.ny * sizeof(double);
+  *bytes = n;
   API_END
 }
 
@@ -1364,8 +1382,7 @@ static void batch_solid_changed(RbcCase* c) {
       plans.push_back(&b->cases[m]->plan);
     }
     bk.plan = merge_plans(plans, bk.members, {});
-    bk.dp = DevPlan();
-    upload_plan(b->arena, bk.plan, bk.dp);
+    upload_plan_owned(bk.plan, bk.dp);
   }
   batch_capture_graphs(b);
 }
