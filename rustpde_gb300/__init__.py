@@ -1102,7 +1102,9 @@ class Server:
         h = _P()
         _check(lib().rbc_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h
-        self._requests = {}  # id -> (params, horizon, seed), for the result records
+        # id -> (params, horizon, seed) of the requests whose results poll()
+        # has not returned yet; poll() moves them into the results
+        self._requests = {}
 
     def submit(self, params, horizon, seed, precision=PREC_FP64):
         nx, ny, ra, pr, dt, asp, kind = params[:7]
@@ -1118,7 +1120,8 @@ class Server:
         """One request's record for a JSON-lines log: id, sizes and parameters,
         horizon, seed, status, steps, simulated time, wall time from submission
         to result (and the part spent queued and in set-up), Nu and KE."""
-        p, horizon, seed = self._requests.get(result["id"], ((None,) * 8, None, None))
+        req = result.get("request") or self._requests.get(result["id"], ((None,) * 8, None, None))
+        p, horizon, seed = req
         keys = ("nx", "ny", "ra", "pr", "dt", "aspect", "kind", "precision")
         rec = {"id": result["id"], **dict(zip(keys, p)), "horizon": horizon, "seed": seed,
                "status": result["status"], "steps": result["steps"], "sim_time": result["sim_time"],
@@ -1147,7 +1150,11 @@ class Server:
         out = []
         for k in range(n.value):
             r = buf[k]
-            out.append({f: getattr(r, f) for f, _ in RbcRequestResult._fields_})
+            d = {f: getattr(r, f) for f, _ in RbcRequestResult._fields_}
+            # a result is delivered once: its request leaves the table with it
+            # (the table holds the requests in flight only)
+            d["request"] = self._requests.pop(d["id"], None)
+            out.append(d)
         return out
 
     def wait_idle(self, timeout=60.0):

@@ -124,6 +124,7 @@ def test_request_records(R, tmp_path):
     ids = [srv.submit(p, h, seed) for p, h, seed in REQS[:3]]
     assert srv.wait_idle(120.0)
     res = srv.poll()
+    assert not srv._requests  # delivered requests leave the table: it holds those in flight only
     path = tmp_path / "requests.jsonl"
     srv.write_records(str(path), res)
     srv.close()
