@@ -416,6 +416,9 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
     const double lanes = it.z > 0 ? it.z : 1;
     double v = 0;
     int kernel = L.kernel;
+    // box y4 of the mixed form also writes the solution's FP32 copy (the
+    // eigenbasis GEMM's input)
+    if (kernel == K_LP_BOX_Y4 || kernel == K_BOX_Y4_MIX) v += myc * 4;
     switch (kernel) {  // the one-thread-per-lane kernels move the same arrays
       case K_LP_BOX_GPX: kernel = K_BOX_GPX; break;
       case K_LP_BOX_X2: kernel = K_BOX_X2; break;
@@ -452,7 +455,9 @@ double launch_algorithmic_bytes(const StepLaunch& L, const CaseDev* cases) {
       case K_BOX_X2: v = 3 * nx * 8 + 3 * mxc * 8; break;
       case K_BOX_Y3: v = 6 * myc * 8 + 2 * ny * 8; break;
       case K_BOX_X3: case K_BOX_X3_MIX: v = 2 * mxc * 8 + nx * 8 + mxc * 8; break;
-      case K_BOX_Y4: v = ny * 8 + myc * 8; break;
+      // the row's own Poisson factors (four arrays of myc: the y operator
+      // depends on the row's x eigenvalue), its right-hand side in, its solution out
+      case K_BOX_Y4: v += ny * 8 + myc * 8 + 4 * myc * 8; break;
       case K_BOX_X4: case K_BOX_X4_MIX: v = mxc * 8 + nx * 8 + 3 * mxc * 8; break;
       case K_BOX_Y5: v = 7 * myc * 8 + 3 * ny * 8; break;
       case K_BOX_PROD_MIXED: v = 13 * nx * 4; break;
