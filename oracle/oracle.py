@@ -78,6 +78,7 @@ def lib():
                 "or_navier_zero_pressure": (None, [P]),
                 "or_navier_set_solid": (None, [P, DP, DP]),
                 "or_navier_update": (I, [P, I]),
+                "or_navier_update_many": (I, [ctypes.POINTER(P), I, I]),
                 "or_navier_time": (D, [P]),
                 "or_navier_set_time": (None, [P, D]),
                 "or_navier_eval": (D, [P, I]),
@@ -312,6 +313,14 @@ class Navier2D:
 
     def state(self):
         return {f: self.get(f) for f in (TEMP, UX, UY, PRES0, PRES1)}
+
+
+def update_many(navs, nsteps: int = 1) -> None:
+    """Advance independent cases by `nsteps` each, in parallel: one case per
+    host thread at a time, in the order given (put the largest first)."""
+    arr = (ctypes.c_void_p * len(navs))(*[n._h for n in navs])
+    if lib().or_navier_update_many(arr, len(navs), int(nsteps)) != 0:
+        raise RuntimeError(lib().or_last_error().decode())
 
 
 def standard_ic(nav: Navier2D, seed: int = 1, vel_amp: float = 0.2, temp_amp: float = 1e-3):

@@ -96,92 +96,204 @@ static Mat matmul(const Mat& a, const Mat& b) {
 }
 
 // ---------------------------------------------------------------------------
-// Complex FFT of any length: mixed-radix recursive decimation in time, and
-// Bluestein's chirp-z algorithm through a power-of-two FFT when the length has
-// a prime factor above 64, where the direct p-point stage costs more than two
-// power-of-two FFTs (rustfft, behind the reference's DCT-I and r2c, is
-// O(n log n) for every length too: its Rader and Bluestein algorithms).
+// Complex FFT of any length: self-sorting (Stockham) mixed-radix stages of
+// radix 4, 2, 3 and any other prime up to 64, and Bluestein's chirp-z
+// algorithm through a power-of-two FFT when the length has a prime factor
+// above 64 (rustfft, behind the reference's DCT-I and r2c, is O(n log n) for
+// every length too: its Rader and Bluestein algorithms).
+//
+// A stage of radix p on sub-length L with stride s (L = n, s = 1 first): for
+// j < L/p and t < s, the p inputs x[t + s (j + r L/p)], r < p, go through a
+// p-point DFT; output u is multiplied by exp(-2 pi i j u / L) and written to
+// y[t + s (p j + u)].  That splits a length-L DFT into p DFTs of length L/p
+// (X[u + p k] = DFT_{L/p}(y^u)[k]); the next stage takes L/p and stride s p,
+// and after the last one the outputs are in natural order.
 // ---------------------------------------------------------------------------
 struct FFT {
   int n = 0;
-  std::vector<int> fac;
-  std::vector<cplx> tw;  // tw[t] = exp(-2 pi i t / n)
-  int maxp = 1;
-  // Bluestein: chirp[k] = exp(-pi i k^2 / n), the transformed conjugate chirp
-  // of length m (a power of two >= 2n - 1), and the length-m FFT
+  struct Stage {
+    int p = 0, L = 0;
+    std::vector<cplx> tw;     // tw[j (p - 1) + u - 1] = exp(-2 pi i j u / L), j < L/p, 0 < u < p
+    std::vector<cplx> roots;  // exp(-2 pi i k / p), k < p (radices other than 2, 3, 4)
+  };
+  std::vector<Stage> stages;
+  // Bluestein: chirp[k] = exp(-pi i k^2 / n), and the length-m FFT (m a power
+  // of two >= 2n - 1) of the conjugate chirp wrapped around
   bool blue = false;
   int m = 0;
   std::vector<cplx> chirp, bfft;
   std::unique_ptr<FFT> sub;
+
+  static cplx expi(long e, long d) {  // exp(-2 pi i e / d), the angle reduced exactly
+    e %= d;
+    if (e < 0) e += d;
+    const double ang = 2.0 * PI * (double)e / (double)d;
+    return cplx(std::cos(ang), -std::sin(ang));
+  }
+
   explicit FFT(int n_) : n(n_) {
+    std::vector<int> fac;
     int r = n;
-    for (int p = 2; p * p <= r; p++)
+    while (r % 4 == 0) { fac.push_back(4); r /= 4; }
+    if (r % 2 == 0) { fac.push_back(2); r /= 2; }
+    for (int p = 3; p * p <= r; p += 2)
       while (r % p == 0) { fac.push_back(p); r /= p; }
     if (r > 1) fac.push_back(r);
+    int maxp = 1;
     for (int p : fac) maxp = std::max(maxp, p);
-    tw.resize(n);
-    for (int t = 0; t < n; t++) {
-      double ang = 2.0 * PI * (double)t / (double)n;
-      tw[t] = cplx(std::cos(ang), -std::sin(ang));
-    }
     if (maxp > 64) {
       blue = true;
       m = 1;
       while (m < 2 * n - 1) m *= 2;
       sub.reset(new FFT(m));
       chirp.resize(n);
-      for (int k = 0; k < n; k++) {
-        const long q = ((long)k * k) % (2L * n);  // k^2 mod 2n keeps the angle exact
-        const double ang = PI * (double)q / (double)n;
-        chirp[k] = cplx(std::cos(ang), -std::sin(ang));
-      }
+      for (int k = 0; k < n; k++) chirp[k] = expi((long)k * k, 2L * n);  // exp(-pi i k^2 / n)
       std::vector<cplx> b(m, cplx(0.0, 0.0));
       b[0] = std::conj(chirp[0]);
       for (int k = 1; k < n; k++) b[k] = b[m - k] = std::conj(chirp[k]);
       bfft.resize(m);
       sub->exec(b.data(), bfft.data(), false);
+      return;
+    }
+    int L = n;
+    for (int p : fac) {
+      Stage st;
+      st.p = p;
+      st.L = L;
+      const int q = L / p;
+      st.tw.resize((size_t)q * (p - 1));
+      for (int j = 0; j < q; j++)
+        for (int u = 1; u < p; u++) st.tw[(size_t)j * (p - 1) + u - 1] = expi((long)j * u, L);
+      if (p != 2 && p != 3 && p != 4) {
+        st.roots.resize(p);
+        for (int k = 0; k < p; k++) st.roots[k] = expi(k, p);
+      }
+      stages.push_back(std::move(st));
+      L = q;
     }
   }
-  inline cplx W(long e, bool inv) const {
-    cplx w = tw[(size_t)(e % n)];
-    return inv ? std::conj(w) : w;
+
+  static inline cplx mul(cplx a, cplx b) {
+    return cplx(a.real() * b.real() - a.imag() * b.imag(), a.real() * b.imag() + a.imag() * b.real());
   }
-  void rec(const cplx* in, int is, cplx* out, int len, int fi, int step, bool inv, cplx* tmp) const {
-    if (len == 1) { out[0] = in[0]; return; }
-    int p = fac[fi], m = len / p;
-    for (int q = 0; q < p; q++) rec(in + (size_t)q * is, is * p, out + (size_t)q * m, m, fi + 1, step * p, inv, tmp);
-    int pstep = n / p;
-    for (int k = 0; k < m; k++) {
-      for (int q = 0; q < p; q++) tmp[q] = cmul(out[(size_t)q * m + k], W((long)q * k * step, inv));
-      for (int r = 0; r < p; r++) {
-        cplx s(0.0, 0.0);
-        for (int q = 0; q < p; q++) s += cmul(tmp[q], W((long)((q * r) % p) * pstep, inv));
-        out[(size_t)r * m + k] = s;
+
+  // one stage: x (sub-length L, stride s) -> y
+  static void stage(const Stage& st, int s, const cplx* x, cplx* y) {
+    const int p = st.p, q = st.L / p;
+    const cplx* tw = st.tw.data();
+    if (p == 2) {
+      for (int j = 0; j < q; j++) {
+        const cplx w = tw[j];
+        for (int t = 0; t < s; t++) {
+          const cplx a0 = x[t + (size_t)s * j], a1 = x[t + (size_t)s * (j + q)];
+          y[t + (size_t)s * (2 * j)] = a0 + a1;
+          y[t + (size_t)s * (2 * j + 1)] = mul(a0 - a1, w);
+        }
+      }
+    } else if (p == 4) {
+      for (int j = 0; j < q; j++) {
+        const cplx w1 = tw[3 * j], w2 = tw[3 * j + 1], w3 = tw[3 * j + 2];
+        for (int t = 0; t < s; t++) {
+          const cplx a0 = x[t + (size_t)s * j], a1 = x[t + (size_t)s * (j + q)];
+          const cplx a2 = x[t + (size_t)s * (j + 2 * q)], a3 = x[t + (size_t)s * (j + 3 * q)];
+          const cplx t0 = a0 + a2, t1 = a0 - a2, t2 = a1 + a3, t3 = a1 - a3;
+          const cplx mit3(t3.imag(), -t3.real());  // -i t3
+          cplx* o = y + t + (size_t)s * (4 * j);
+          o[0] = t0 + t2;
+          o[s] = mul(t1 + mit3, w1);
+          o[2 * (size_t)s] = mul(t0 - t2, w2);
+          o[3 * (size_t)s] = mul(t1 - mit3, w3);
+        }
+      }
+    } else if (p == 3) {
+      const double h = 0.86602540378443864676372317075293618;  // sin(2 pi / 3)
+      for (int j = 0; j < q; j++) {
+        const cplx w1 = tw[2 * j], w2 = tw[2 * j + 1];
+        for (int t = 0; t < s; t++) {
+          const cplx a0 = x[t + (size_t)s * j], a1 = x[t + (size_t)s * (j + q)];
+          const cplx a2 = x[t + (size_t)s * (j + 2 * q)];
+          const cplx sm = a1 + a2, df = a1 - a2;
+          const cplx mid = a0 - 0.5 * sm;
+          const cplx rot(h * df.imag(), -h * df.real());  // -i sin(2 pi / 3) (a1 - a2)
+          cplx* o = y + t + (size_t)s * (3 * j);
+          o[0] = a0 + sm;
+          o[s] = mul(mid + rot, w1);
+          o[2 * (size_t)s] = mul(mid - rot, w2);
+        }
+      }
+    } else {
+      // odd prime p: inputs r and p - r pair up, sum s_r and difference d_r;
+      // outputs u and p - u share c = a_0 + sum s_r cos(2 pi r u / p) and
+      // v = sum d_r sin(2 pi r u / p): b_u = c - i v, b_{p-u} = c + i v
+      const cplx* rt = st.roots.data();  // cos + i(-sin) of 2 pi k / p
+      const int hp = (p - 1) / 2;
+      thread_local std::vector<cplx> sm, df;
+      sm.resize(hp + 1);
+      df.resize(hp + 1);
+      for (int j = 0; j < q; j++) {
+        for (int t = 0; t < s; t++) {
+          const cplx a0 = x[t + (size_t)s * j];
+          cplx b0 = a0;
+          for (int r = 1; r <= hp; r++) {
+            const cplx ar = x[t + (size_t)s * (j + (size_t)r * q)], ap = x[t + (size_t)s * (j + (size_t)(p - r) * q)];
+            sm[r] = ar + ap;
+            df[r] = ar - ap;
+            b0 += sm[r];
+          }
+          cplx* o = y + t + (size_t)s * ((size_t)p * j);
+          o[0] = b0;
+          for (int u = 1; u <= hp; u++) {
+            double cr = a0.real(), ci = a0.imag(), vr = 0.0, vi = 0.0;
+            int e = 0;
+            for (int r = 1; r <= hp; r++) {
+              e += u;
+              if (e >= p) e -= p;
+              const double cs = rt[e].real(), sn = -rt[e].imag();
+              cr += sm[r].real() * cs;
+              ci += sm[r].imag() * cs;
+              vr += df[r].real() * sn;
+              vi += df[r].imag() * sn;
+            }
+            // -i v = (vi, -vr), +i v = (-vi, vr)
+            o[(size_t)s * u] = mul(cplx(cr + vi, ci - vr), tw[(size_t)j * (p - 1) + u - 1]);
+            o[(size_t)s * (p - u)] = mul(cplx(cr - vi, ci + vr), tw[(size_t)j * (p - 1) + p - u - 1]);
+          }
+        }
       }
     }
   }
-  // out = sum_j in_j exp(-+ 2 pi i jk/n); unnormalised both ways
+
+  // out = sum_j in_j exp(-+ 2 pi i jk/n); unnormalised both ways (the inverse
+  // is conj(forward(conj(x)))); in and out may be the same array
   void exec(const cplx* in, cplx* out, bool inv) const {
     if (blue) {
-      // X_k = chirp_k sum_j (x_j chirp_j) conj(chirp_{k-j}); the inverse is
-      // conj(forward(conj(x)))
+      // X_k = chirp_k sum_j (x_j chirp_j) conj(chirp_{k-j})
       thread_local std::vector<cplx> a, A;
       a.assign(m, cplx(0.0, 0.0));
       A.resize(m);
-      for (int j = 0; j < n; j++) a[j] = (inv ? std::conj(in[j]) : in[j]) * chirp[j];
+      for (int j = 0; j < n; j++) a[j] = mul(inv ? std::conj(in[j]) : in[j], chirp[j]);
       sub->exec(a.data(), A.data(), false);
-      for (int k = 0; k < m; k++) A[k] *= bfft[k];
+      for (int k = 0; k < m; k++) A[k] = mul(A[k], bfft[k]);
       sub->exec(A.data(), a.data(), true);
       const double s = 1.0 / (double)m;
       for (int k = 0; k < n; k++) {
-        const cplx v = a[k] * s * chirp[k];
+        const cplx v = mul(a[k] * s, chirp[k]);
         out[k] = inv ? std::conj(v) : v;
       }
       return;
     }
-    thread_local std::vector<cplx> tmp;
-    if ((int)tmp.size() < maxp) tmp.resize(maxp);
-    rec(in, 1, out, n, 0, 1, inv, tmp.data());
+    thread_local std::vector<cplx> b0, b1;
+    if ((int)b0.size() < n) { b0.resize(n); b1.resize(n); }
+    cplx* x = b0.data();
+    cplx* y = b1.data();
+    for (int j = 0; j < n; j++) x[j] = inv ? std::conj(in[j]) : in[j];
+    int s = 1;
+    for (const Stage& st : stages) {
+      stage(st, s, x, y);
+      std::swap(x, y);
+      s *= st.p;
+    }
+    for (int k = 0; k < n; k++) out[k] = inv ? std::conj(x[k]) : x[k];
   }
 };
 
@@ -199,7 +311,76 @@ static std::shared_ptr<FFT> get_fft(int n) {
 // with the transform's rounding alone.
 static std::atomic<int> g_dense_dct_n{-1};
 
-// DCT-I (REDFT00, unnormalised): X_k = x_0 + (-1)^k x_N + 2 sum_{j=1}^{N-1} x_j cos(pi j k / N)
+// real -> complex, unnormalised, m = n/2+1 outputs (ndfft_r2c).  Even n: the
+// n/2-point complex FFT of z_j = x_2j + i x_2j+1 gives the DFTs E and O of
+// the even and odd samples, and X_k = E_k + exp(-2 pi i k/n) O_k.
+static void rfft(const double* x, cplx* X, int n) {
+  if (n % 2 != 0 || n < 4) {
+    auto f = get_fft(n);
+    thread_local std::vector<cplx> a;
+    a.resize(n);
+    for (int j = 0; j < n; j++) a[j] = cplx(x[j], 0.0);
+    f->exec(a.data(), a.data(), false);
+    for (int k = 0; k <= n / 2; k++) X[k] = a[k];
+    return;
+  }
+  const int h = n / 2;
+  auto f = get_fft(h);
+  thread_local std::vector<cplx> z;
+  z.resize(h);
+  for (int j = 0; j < h; j++) z[j] = cplx(x[2 * j], x[2 * j + 1]);
+  f->exec(z.data(), z.data(), false);
+  X[0] = cplx(z[0].real() + z[0].imag(), 0.0);
+  X[h] = cplx(z[0].real() - z[0].imag(), 0.0);
+  for (int k = 1; k < h; k++) {
+    const cplx zk = z[k], zc = std::conj(z[h - k]);
+    const cplx e = 0.5 * (zk + zc);
+    const cplx d = 0.5 * (zk - zc);
+    const cplx o(d.imag(), -d.real());  // (zk - zc) / (2 i)
+    X[k] = e + FFT::mul(FFT::expi(k, n), o);
+  }
+}
+
+// complex -> real with 1/n (ndifft_r2c); imaginary parts of DC (and Nyquist
+// for even n) are ignored, Hermitian symmetry assumed.  Even n: one n/2-point
+// inverse FFT of Z_k = (a_k + conj a_{h-k}) + i (a_k - conj a_{h-k}) exp(2 pi i k/n)
+// gives x_2j + i x_2j+1 (h = n/2).
+static void irfft(const cplx* X, double* x, int n) {
+  const double s = 1.0 / (double)n;
+  if (n % 2 != 0 || n < 4) {
+    auto f = get_fft(n);
+    thread_local std::vector<cplx> a;
+    a.resize(n);
+    const int m = n / 2 + 1;
+    a[0] = cplx(X[0].real(), 0.0);
+    for (int k = 1; k < m; k++) a[k] = X[k];
+    if (n % 2 == 0) a[n / 2] = cplx(X[n / 2].real(), 0.0);
+    for (int k = 1; k < m; k++)
+      if (n - k != k) a[n - k] = std::conj(X[k]);
+    f->exec(a.data(), a.data(), true);
+    for (int j = 0; j < n; j++) x[j] = a[j].real() * s;
+    return;
+  }
+  const int h = n / 2;
+  auto f = get_fft(h);
+  thread_local std::vector<cplx> z;
+  z.resize(h);
+  for (int k = 0; k < h; k++) {
+    const cplx ak = k == 0 ? cplx(X[0].real(), 0.0) : X[k];
+    const cplx ah = (h - k == h) ? cplx(X[h].real(), 0.0) : X[h - k];  // a_{h-k}; k = 0: the Nyquist bin
+    const cplx ac = std::conj(ah);
+    const cplx d = FFT::mul(ak - ac, std::conj(FFT::expi(k, n)));  // (a_k - conj a_{h-k}) exp(2 pi i k/n)
+    z[k] = (ak + ac) + cplx(-d.imag(), d.real());
+  }
+  f->exec(z.data(), z.data(), true);
+  for (int j = 0; j < h; j++) {
+    x[2 * j] = z[j].real() * s;
+    x[2 * j + 1] = z[j].imag() * s;
+  }
+}
+
+// DCT-I (REDFT00, unnormalised): X_k = x_0 + (-1)^k x_N + 2 sum_{j=1}^{N-1} x_j cos(pi j k / N),
+// the real parts of the 2N-point DFT of the even extension
 static void dct1(const double* x, double* X, int n) {
   int N = n - 1;
   if (N < 1) { X[0] = x[0]; return; }
@@ -214,41 +395,14 @@ static void dct1(const double* x, double* X, int n) {
     }
     return;
   }
-  auto f = get_fft(2 * N);
-  thread_local std::vector<cplx> a, b;
-  a.resize(2 * N); b.resize(2 * N);
-  for (int j = 0; j <= N; j++) a[j] = cplx(x[j], 0.0);
-  for (int j = 1; j < N; j++) a[2 * N - j] = cplx(x[j], 0.0);
-  f->exec(a.data(), b.data(), false);
+  thread_local std::vector<double> a;
+  thread_local std::vector<cplx> b;
+  a.resize(2 * N);
+  b.resize(N + 1);
+  for (int j = 0; j <= N; j++) a[j] = x[j];
+  for (int j = 1; j < N; j++) a[2 * N - j] = x[j];
+  rfft(a.data(), b.data(), 2 * N);
   for (int k = 0; k <= N; k++) X[k] = b[k].real();
-}
-
-// real -> complex, unnormalised, m = n/2+1 outputs (ndfft_r2c)
-static void rfft(const double* x, cplx* X, int n) {
-  auto f = get_fft(n);
-  thread_local std::vector<cplx> a, b;
-  a.resize(n); b.resize(n);
-  for (int j = 0; j < n; j++) a[j] = cplx(x[j], 0.0);
-  f->exec(a.data(), b.data(), false);
-  int m = n / 2 + 1;
-  for (int k = 0; k < m; k++) X[k] = b[k];
-}
-
-// complex -> real with 1/n (ndifft_r2c); imaginary parts of DC (and Nyquist
-// for even n) are ignored, Hermitian symmetry assumed.
-static void irfft(const cplx* X, double* x, int n) {
-  auto f = get_fft(n);
-  thread_local std::vector<cplx> a, b;
-  a.resize(n); b.resize(n);
-  int m = n / 2 + 1;
-  a[0] = cplx(X[0].real(), 0.0);
-  for (int k = 1; k < m; k++) a[k] = X[k];
-  if (n % 2 == 0) a[n / 2] = cplx(X[n / 2].real(), 0.0);
-  for (int k = 1; k < m; k++)
-    if (n - k != k) a[n - k] = std::conj(X[k]);
-  f->exec(a.data(), b.data(), true);
-  double s = 1.0 / (double)n;
-  for (int j = 0; j < n; j++) x[j] = b[j].real() * s;
 }
 
 // ---------------------------------------------------------------------------
@@ -1622,6 +1776,33 @@ int or_navier_update(void* p, int nsteps) {
     g_err = e.what();
     return -1;
   }
+}
+// Independent cases advanced together: one case per thread at a time (the
+// order given, dynamically scheduled), each case's own loops on that thread
+// alone.  The way an ensemble of independent solves fills a many-core host.
+int or_navier_update_many(void** hs, int n, int nsteps) {
+  int bad = 0;
+  std::string err;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int i = 0; i < n; i++) {
+    try {
+      auto* h = (OrNavier*)hs[i];
+      for (int s = 0; s < nsteps; s++) {
+        if (h->periodic) h->per.update(); else h->box.update();
+      }
+    } catch (std::exception& e) {
+#pragma omp critical(or_update_many_err)
+      {
+        bad = 1;
+        err = e.what();
+      }
+    }
+  }
+  if (bad) {
+    g_err = err;
+    return -1;
+  }
+  return 0;
 }
 // Navier2D::solid = Some([mask, value]) (navier.rs:189-190); mask == NULL clears it.
 // mask, value: physical nx x ny arrays (value NULL = zeros)

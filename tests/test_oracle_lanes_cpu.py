@@ -52,3 +52,34 @@ def test_fft_prime_factor_lengths_match_numpy(n):
     O.lib().or_base_forward(O.FOURIER, n, _dp(v), out.ctypes.data_as(DP))
     ref = np.fft.rfft(v)
     assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+# every stage the FFT builds: radix 4, 2, 3, odd primes up to 64 (paired
+# butterflies), Bluestein (prime factors above 64), and the odd-length and
+# packed even-length real transforms
+FFT_LENGTHS = list(range(1, 70)) + [96, 105, 126, 127, 128, 134, 255, 256, 257, 289, 510, 512, 513, 1021, 1024, 2046]
+
+
+def test_r2c_c2r_all_stage_kinds_match_numpy():
+    rng = np.random.default_rng(5)
+    for n in FFT_LENGTHS:
+        v = rng.standard_normal(n)
+        out = np.zeros(n // 2 + 1, dtype=np.complex128)
+        O.lib().or_base_forward(O.FOURIER, n, _dp(v), out.ctypes.data_as(DP))
+        ref = np.fft.rfft(v)
+        assert np.max(np.abs(out - ref)) <= 1e-13 * np.max(np.abs(ref)), n
+        back = O.base_backward(O.FOURIER, n, ref)
+        assert np.max(np.abs(back - np.fft.irfft(ref, n))) <= 1e-13 * np.max(np.abs(v)), n
+
+
+def test_dct1_fft_equals_defining_sum():
+    rng = np.random.default_rng(6)
+    for n in [2, 3, 4, 5, 9, 17, 33, 64, 65, 128, 129, 130, 256, 257, 512, 513]:
+        x = rng.standard_normal(n)
+        a = O.base_forward(O.CHEB, n, x)
+        O.set_dense_dct(n)
+        try:
+            b = O.base_forward(O.CHEB, n, x)
+        finally:
+            O.set_dense_dct(-1)
+        assert np.max(np.abs(a - b)) <= 1e-13 * np.max(np.abs(b)), n
