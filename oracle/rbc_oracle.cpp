@@ -367,7 +367,7 @@ static void irfft(const cplx* X, double* x, int n) {
   z.resize(h);
   for (int k = 0; k < h; k++) {
     const cplx ak = k == 0 ? cplx(X[0].real(), 0.0) : X[k];
-    const cplx ah = (h - k == h) ? cplx(X[h].real(), 0.0) : X[h - k];  // a_{h-k}; k = 0: the Nyquist bin
+    const cplx ah = k == 0 ? cplx(X[h].real(), 0.0) : X[h - k];  // a_{h-k}; k = 0: the Nyquist bin
     const cplx ac = std::conj(ah);
     const cplx d = FFT::mul(ak - ac, std::conj(FFT::expi(k, n)));  // (a_k - conj a_{h-k}) exp(2 pi i k/n)
     z[k] = (ak + ac) + cplx(-d.imag(), d.real());
