@@ -311,6 +311,26 @@ static std::shared_ptr<FFT> get_fft(int n) {
 // with the transform's rounding alone.
 static std::atomic<int> g_dense_dct_n{-1};
 
+// Even-length real transforms: the n/2-point complex FFT and the factors
+// exp(-2 pi i k / n), k < n/2, of the split into even and odd samples
+struct RealFFT {
+  int n = 0;
+  std::shared_ptr<FFT> half;
+  std::vector<cplx> w;
+};
+static const RealFFT& get_real_fft(int n) {
+  thread_local std::vector<std::unique_ptr<RealFFT>> cache;
+  for (auto& r : cache)
+    if (r->n == n) return *r;
+  auto r = std::make_unique<RealFFT>();
+  r->n = n;
+  r->half = get_fft(n / 2);
+  r->w.resize(n / 2);
+  for (int k = 0; k < n / 2; k++) r->w[k] = FFT::expi(k, n);
+  cache.push_back(std::move(r));
+  return *cache.back();
+}
+
 // real -> complex, unnormalised, m = n/2+1 outputs (ndfft_r2c).  Even n: the
 // n/2-point complex FFT of z_j = x_2j + i x_2j+1 gives the DFTs E and O of
 // the even and odd samples, and X_k = E_k + exp(-2 pi i k/n) O_k.
@@ -325,11 +345,11 @@ static void rfft(const double* x, cplx* X, int n) {
     return;
   }
   const int h = n / 2;
-  auto f = get_fft(h);
+  const RealFFT& rf = get_real_fft(n);
   thread_local std::vector<cplx> z;
   z.resize(h);
   for (int j = 0; j < h; j++) z[j] = cplx(x[2 * j], x[2 * j + 1]);
-  f->exec(z.data(), z.data(), false);
+  rf.half->exec(z.data(), z.data(), false);
   X[0] = cplx(z[0].real() + z[0].imag(), 0.0);
   X[h] = cplx(z[0].real() - z[0].imag(), 0.0);
   for (int k = 1; k < h; k++) {
@@ -337,7 +357,7 @@ static void rfft(const double* x, cplx* X, int n) {
     const cplx e = 0.5 * (zk + zc);
     const cplx d = 0.5 * (zk - zc);
     const cplx o(d.imag(), -d.real());  // (zk - zc) / (2 i)
-    X[k] = e + FFT::mul(FFT::expi(k, n), o);
+    X[k] = e + FFT::mul(rf.w[k], o);
   }
 }
 
@@ -362,17 +382,17 @@ static void irfft(const cplx* X, double* x, int n) {
     return;
   }
   const int h = n / 2;
-  auto f = get_fft(h);
+  const RealFFT& rf = get_real_fft(n);
   thread_local std::vector<cplx> z;
   z.resize(h);
   for (int k = 0; k < h; k++) {
     const cplx ak = k == 0 ? cplx(X[0].real(), 0.0) : X[k];
     const cplx ah = k == 0 ? cplx(X[h].real(), 0.0) : X[h - k];  // a_{h-k}; k = 0: the Nyquist bin
     const cplx ac = std::conj(ah);
-    const cplx d = FFT::mul(ak - ac, std::conj(FFT::expi(k, n)));  // (a_k - conj a_{h-k}) exp(2 pi i k/n)
+    const cplx d = FFT::mul(ak - ac, std::conj(rf.w[k]));  // (a_k - conj a_{h-k}) exp(2 pi i k/n)
     z[k] = (ak + ac) + cplx(-d.imag(), d.real());
   }
-  f->exec(z.data(), z.data(), true);
+  rf.half->exec(z.data(), z.data(), true);
   for (int j = 0; j < h; j++) {
     x[2 * j] = z[j].real() * s;
     x[2 * j + 1] = z[j].imag() * s;
