@@ -461,7 +461,7 @@ def cpu_ensemble_sample(O, params, steps, warmup):
     return gp * steps / secs, secs
 
 
-def cpu_baseline_ensemble(params, steps=40):
+def cpu_baseline_ensemble(params, steps=60):
     from oracle import oracle as O
     O.build()
     O.set_threads(os.cpu_count() or 1)
@@ -910,7 +910,7 @@ def main():
                     choices=["ensemble", "periodic512", "serving", "precision", "extras", "profile-step",
                              "cpu-table"])
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="periodic512: oracle seconds")
-    ap.add_argument("--cpu-steps", type=int, default=40, help="ensemble: oracle ensemble steps in cpu_baseline")
+    ap.add_argument("--cpu-steps", type=int, default=60, help="ensemble: oracle ensemble steps in cpu_baseline")
     ap.add_argument("--accuracy-steps", type=int, default=505,
                     help="ensemble: steps of the mixed-vs-FP64 comparison (the configuration's horizon)")
     ap.add_argument("--cases", type=int, default=ENSEMBLE_N, help="ensemble size (default 256)")
